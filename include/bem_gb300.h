@@ -1,0 +1,174 @@
+/* bem_gb300.h - C ABI of the GB300 traditional-BEM library.
+ *
+ * Boundary-element solver for exterior/interior Helmholtz problems in
+ * Burton-Miller form with constant (one unknown per element) triangular and
+ * quadrilateral elements, the method of Mesh2HRTF's NumCalc when it runs its
+ * traditional BEM (methodBEM = 0).  The reference has no library API: its only
+ * interface is the NumCalc process.  Each entry point below takes over one
+ * phase of NumCalc's per-frequency loop (mesh2hrtf/NumCalc/src/NC_Main.cpp:
+ * 370-963); the file:line after each declaration names the reference routine
+ * it replaces.  The drop-in NumCalc executable of this project is the main
+ * caller; Python tooling binds the same symbols through ctypes.
+ *
+ * Conventions (as in NumCalc): time factor e^{-i w t} (time_factor = +1) or
+ * e^{+i w t} (-1); Green's function e^{i k r}/(4 pi r); unknown = velocity
+ * potential phi for velocity/admittance elements and normal velocity for
+ * pressure elements; pressure = i rho w phi.  Complex numbers are two
+ * doubles (re, im).  All host pointers are read during the call only.
+ * Every call returns a bem_status; bem_last_error() gives a message for the
+ * calling thread.  One bem_solver_t must not be used by two threads at once.
+ */
+#ifndef BEM_GB300_H
+#define BEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    BEM_OK = 0,
+    BEM_ERR_INVALID = 1,        /* bad argument or unsupported input          */
+    BEM_ERR_OUT_OF_HBM = 2,     /* admission refused: footprint above budget   */
+    BEM_ERR_NOT_CONVERGED = 3,  /* Krylov solver hit its iteration limit       */
+    BEM_ERR_DEVICE_TIMEOUT = 4, /* a bounded device wait gave up               */
+    BEM_ERR_CUDA = 5,           /* CUDA runtime error                          */
+    BEM_ERR_SUBDIVISION = 6     /* element subdivision limit exceeded (NumCalc
+                                   stops with the same condition)              */
+} bem_status;
+
+typedef enum {
+    BEM_PREC_FP64 = 0,   /* FP64 assembly, complex128 matrix, FP64 GMRES        */
+    BEM_PREC_MIXED = 1   /* FP32 regular/near assembly, FP64 singular terms,     */
+                         /* complex64 matrix, compensated FP32 matvec inside a   */
+                         /* restarted GMRES with FP64 Arnoldi and an FP64 outer  */
+                         /* residual (iterative refinement)                      */
+} bem_precision;
+
+typedef struct bem_mesh_s *bem_mesh_t;
+typedef struct bem_solver_s *bem_solver_t;
+
+/* Boundary mesh.  Element order defines the unknown order (NumCalc's jelist,
+ * NC_Addresses.cpp:179-184).  centers/normals/areas may be NULL, in which case
+ * they are computed with NumCalc's formulas (NC_Input.cpp:522-602); the
+ * drop-in passes the values its parser computed so that both agree bit for
+ * bit. */
+typedef struct {
+    int32_t n_elem;
+    int32_t n_nodes;
+    const double *nodes;     /* [n_nodes][3]                                  */
+    const int32_t *conn;     /* [n_elem][4] node indices, -1 past nvert       */
+    const int32_t *nvert;    /* [n_elem] 3 or 4                               */
+    const double *centers;   /* [n_elem][3] or NULL                           */
+    const double *normals;   /* [n_elem][3] unit normal at the centre or NULL */
+    const double *areas;     /* [n_elem] or NULL                              */
+} bem_mesh_desc;
+
+/* Per-frequency data: NumCalc's state after NC_UpdateFreqCurves
+ * (NC_EquationSystem.cpp:1815-1961). */
+typedef struct {
+    double wave_number;        /* k = 2 pi f / c                               */
+    double time_factor;        /* +1 or -1                                     */
+    double tao;                /* +1 exterior, -1 interior problem             */
+    const int32_t *bc_type;    /* [n_elem] 0 velocity, 1 pressure,
+                                  2 velocity + surface admittance; NULL = 0    */
+    const double *bc_value;    /* [n_elem][4] complex nodal values (zbval0),
+                                  potential units; NULL = 0                    */
+    const double *admittance;  /* [n_elem] complex (zbval1, already scaled by
+                                  i k time_factor); NULL = 0                   */
+    int32_t n_point;           /* point sources                                */
+    const double *point_xyz;   /* [n_point][3]                                 */
+    const double *point_amp;   /* [n_point] complex: NC.inp amplitude/(i rho w)*/
+    int32_t n_plane;           /* plane waves                                  */
+    const double *plane_dir;   /* [n_plane][3] unit direction                  */
+    const double *plane_amp;   /* [n_plane] complex: amplitude/(i rho w)       */
+} bem_frequency_desc;
+
+typedef struct {
+    int32_t precision;         /* bem_precision                                */
+    int32_t restart;           /* GMRES restart length (0 = default 60)        */
+    int32_t max_iter;          /* total inner iterations (0 = default 1000)    */
+    double tol;                /* relative residual target (0 = 1e-9)          */
+    double hbm_budget_bytes;   /* admission budget for this solver (0 = all
+                                  free device memory minus a reserve)          */
+} bem_solver_params;
+
+typedef struct {
+    int32_t iterations;        /* Krylov iterations (matrix-vector products)   */
+    int32_t restarts;          /* outer cycles (explicit residuals)            */
+    double rel_residual;       /* final ||b - A x|| / ||b||                    */
+    double assemble_ms;        /* device time of the last bem_assemble         */
+    double solve_ms;           /* device time of the last bem_solve            */
+    double project_ms;         /* device time of the last bem_project          */
+    int64_t n_near_pairs;      /* element pairs that needed subdivision        */
+} bem_solve_info;
+
+/* Library / device ------------------------------------------------------- */
+const char *bem_last_error(void);
+const char *bem_version(void);
+/* Select the CUDA device for this thread's subsequent calls. */
+bem_status bem_set_device(int32_t device);
+/* Bytes a solver for n_elem unknowns holds on the device (matrix, Krylov
+ * basis, work vectors) at the given precision and restart length: the HBM
+ * admission footprint (NumCalc's host RAM estimate, NC_Main.cpp:524-541,
+ * counts (N + N^2) * 16 bytes for the same data). */
+double bem_footprint_bytes(int32_t n_elem, int32_t precision, int32_t restart);
+
+/* Mesh: upload and precompute element tables.
+ * Replaces NC_ReadMesh's geometry part (NC_Input.cpp:522-602) and the per-pair
+ * element gather NC_ComputeElementData (NC_3dFunctions.cpp:245-354). */
+bem_status bem_mesh_create(const bem_mesh_desc *desc, bem_mesh_t *out);
+bem_status bem_mesh_destroy(bem_mesh_t mesh);
+
+/* Solver workspace on the device (matrix + Krylov state), admitted against
+ * params->hbm_budget_bytes.  Replaces the per-frequency allocations of
+ * NC_Main.cpp:744-757 and NC_Addresses.cpp:236-238. */
+bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *params,
+                             bem_solver_t *out);
+bem_status bem_solver_destroy(bem_solver_t solver);
+
+/* Assemble A and b for one frequency.
+ * Replaces NC_SetupEquationSystem / NC_BuildSystemTBEM /
+ * NC_ComputeEntriesForTBEM / NC_AssembleTBEM / NC_SingularIntegration /
+ * NC_RegularIntegration / NC_IncidentWaveRHS
+ * (NC_EquationSystem.cpp:79-302,1408-1812) and NC_GenerateSubelements
+ * (NC_3dFunctions.cpp:575-783). */
+bem_status bem_assemble(bem_solver_t solver, const bem_frequency_desc *freq);
+
+/* Solve A x = b.  Replaces NC_IterativeSolverCGS with its preconditioners
+ * and direct fallback (NC_CommonFunctions.cpp:1066-1208,1322-1721) by a
+ * restarted GMRES (see bem_precision). */
+bem_status bem_solve(bem_solver_t solver, bem_solve_info *info);
+
+/* Copy the solution (complex, n_elem) to host memory. */
+bem_status bem_get_solution(bem_solver_t solver, double *x_host);
+
+/* Copy the assembled matrix rows [row0, row1) (complex, row-major, n_elem
+ * columns, converted to FP64) and the right-hand side to host memory; NULL
+ * skips either.  For tests and diagnostics. */
+bem_status bem_get_system(bem_solver_t solver, int32_t row0, int32_t row1,
+                          double *a_host, double *b_host);
+
+/* Potential and its gradient at n_pts field points (host arrays), from the
+ * boundary data of the last solve plus the incident field.
+ * Replaces the TBEM branch of NC_WriteResultsEvaluationGrid with
+ * NC_ContributionTBEM / NC_IntegrationTBEM / NC_ContributionIncidentWaves
+ * (NC_PostProcessing.cpp:581-773,776-975,1217-1322).  pot_out: [n_pts]
+ * complex; grad_out: [n_pts][3] complex (may be NULL). */
+bem_status bem_project(bem_solver_t solver, int32_t n_pts, const double *pts,
+                       double *pot_out, double *grad_out);
+
+/* One complete frequency step through host buffers: assemble, solve, copy
+ * the unknowns to x_out (may be NULL) and project onto n_pts points.
+ * The sequence NC_Main.cpp:744-907 runs per frequency. */
+bem_status bem_solve_frequency(bem_solver_t solver, const bem_frequency_desc *freq,
+                               int32_t n_pts, const double *pts, double *x_out,
+                               double *pot_out, double *grad_out,
+                               bem_solve_info *info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BEM_GB300_H */

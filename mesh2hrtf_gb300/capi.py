@@ -1,0 +1,236 @@
+"""ctypes binding of the C ABI in include/bem_gb300.h (libbem_gb300.so).
+
+This is the Python face of the GPU library: tests, the bench and the serving
+loop drive the solver through exactly the entry points the drop-in NumCalc
+executable uses.  There is no fallback: if the library or a CUDA device is
+missing, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+BEM_OK = 0
+BEM_ERR_INVALID = 1
+BEM_ERR_OUT_OF_HBM = 2
+BEM_ERR_NOT_CONVERGED = 3
+BEM_ERR_DEVICE_TIMEOUT = 4
+BEM_ERR_CUDA = 5
+BEM_ERR_SUBDIVISION = 6
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+EXPORTED = [
+    "bem_last_error", "bem_version", "bem_set_device", "bem_footprint_bytes",
+    "bem_mesh_create", "bem_mesh_destroy", "bem_solver_create", "bem_solver_destroy",
+    "bem_assemble", "bem_solve", "bem_get_solution", "bem_get_system", "bem_project",
+    "bem_solve_frequency",
+]
+
+
+class BemError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("bem status %d: %s" % (status, msg))
+        self.status = status
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("n_elem", C.c_int32), ("n_nodes", C.c_int32), ("nodes", C.c_void_p),
+                ("conn", C.c_void_p), ("nvert", C.c_void_p), ("centers", C.c_void_p),
+                ("normals", C.c_void_p), ("areas", C.c_void_p)]
+
+
+class FreqDesc(C.Structure):
+    _fields_ = [("wave_number", C.c_double), ("time_factor", C.c_double), ("tao", C.c_double),
+                ("bc_type", C.c_void_p), ("bc_value", C.c_void_p), ("admittance", C.c_void_p),
+                ("n_point", C.c_int32), ("point_xyz", C.c_void_p), ("point_amp", C.c_void_p),
+                ("n_plane", C.c_int32), ("plane_dir", C.c_void_p), ("plane_amp", C.c_void_p)]
+
+
+class SolverParams(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("restart", C.c_int32), ("max_iter", C.c_int32),
+                ("tol", C.c_double), ("hbm_budget_bytes", C.c_double)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("restarts", C.c_int32), ("rel_residual", C.c_double),
+                ("assemble_ms", C.c_double), ("solve_ms", C.c_double), ("project_ms", C.c_double),
+                ("n_near_pairs", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Load libbem_gb300.so (building it first when absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise OSError("libbem_gb300.so not built: " + LIB_PATH)
+        _build.build_library()
+    lib = C.CDLL(LIB_PATH)
+    vp, i32, dp = C.c_void_p, C.c_int32, C.POINTER(C.c_double)
+    lib.bem_last_error.restype = C.c_char_p
+    lib.bem_version.restype = C.c_char_p
+    lib.bem_set_device.argtypes = [i32]
+    lib.bem_footprint_bytes.argtypes = [i32, i32, i32]
+    lib.bem_footprint_bytes.restype = C.c_double
+    lib.bem_mesh_create.argtypes = [C.POINTER(MeshDesc), C.POINTER(vp)]
+    lib.bem_mesh_destroy.argtypes = [vp]
+    lib.bem_solver_create.argtypes = [vp, C.POINTER(SolverParams), C.POINTER(vp)]
+    lib.bem_solver_destroy.argtypes = [vp]
+    lib.bem_assemble.argtypes = [vp, C.POINTER(FreqDesc)]
+    lib.bem_solve.argtypes = [vp, C.POINTER(SolveInfo)]
+    lib.bem_get_solution.argtypes = [vp, vp]
+    lib.bem_get_system.argtypes = [vp, i32, i32, vp, vp]
+    lib.bem_project.argtypes = [vp, i32, vp, vp, vp]
+    lib.bem_solve_frequency.argtypes = [vp, C.POINTER(FreqDesc), i32, vp, vp, vp, vp, C.POINTER(SolveInfo)]
+    for name in EXPORTED:
+        if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes"):
+            getattr(lib, name).restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def _check(rc, allow=()):
+    if rc != BEM_OK and rc not in allow:
+        raise BemError(rc, load().bem_last_error().decode())
+    return rc
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class Mesh:
+    """Device-resident boundary mesh (bem_mesh_create)."""
+
+    def __init__(self, nodes, elems, centers=None, normals=None, areas=None, device=0):
+        lib = load()
+        _check(lib.bem_set_device(device))
+        elems = np.asarray(elems)
+        n = len(elems)
+        self.n = n
+        self.nodes = np.ascontiguousarray(nodes, np.float64)
+        self.conn = -np.ones((n, 4), np.int32)
+        self.conn[:, : elems.shape[1]] = elems
+        self.nvert = np.full(n, elems.shape[1], np.int32)
+        if elems.shape[1] == 4:
+            self.nvert[elems[:, 3] < 0] = 3
+        keep = [self.nodes, self.conn, self.nvert]
+        cen = None if centers is None else np.ascontiguousarray(centers, np.float64)
+        nor = None if normals is None else np.ascontiguousarray(normals, np.float64)
+        ar = None if areas is None else np.ascontiguousarray(areas, np.float64)
+        keep += [cen, nor, ar]
+        d = MeshDesc(n, len(self.nodes), _ptr(self.nodes), _ptr(self.conn), _ptr(self.nvert),
+                     _ptr(cen), _ptr(nor), _ptr(ar))
+        h = C.c_void_p()
+        _check(lib.bem_mesh_create(C.byref(d), C.byref(h)))
+        self.handle = h
+        self._keep = keep
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().bem_mesh_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Frequency:
+    """Per-frequency data (bem_frequency_desc); arrays are kept alive here."""
+
+    def __init__(self, k, n_elem, bc_type=None, bc_value=None, admittance=None, point_sources=(),
+                 point_amps=(), plane_dirs=(), plane_amps=(), time_factor=1.0, tao=1.0):
+        self.bct = None if bc_type is None else np.ascontiguousarray(bc_type, np.int32)
+        self.bcv = None if bc_value is None else np.ascontiguousarray(
+            np.asarray(bc_value, np.complex128).reshape(n_elem, 4))
+        self.adm = None if admittance is None else np.ascontiguousarray(admittance, np.complex128)
+        self.ps = np.ascontiguousarray(np.reshape(point_sources, (-1, 3)), np.float64)
+        self.psa = np.ascontiguousarray(np.asarray(point_amps, np.complex128).reshape(-1))
+        self.pw = np.ascontiguousarray(np.reshape(plane_dirs, (-1, 3)), np.float64)
+        self.pwa = np.ascontiguousarray(np.asarray(plane_amps, np.complex128).reshape(-1))
+        self.desc = FreqDesc(k, time_factor, tao, _ptr(self.bct), _ptr(self.bcv), _ptr(self.adm),
+                             len(self.ps), _ptr(self.ps), _ptr(self.psa), len(self.pw), _ptr(self.pw),
+                             _ptr(self.pwa))
+
+
+class Solver:
+    """bem_solver_t: matrix + Krylov workspace for one mesh on the device."""
+
+    def __init__(self, mesh: Mesh, precision=PREC_FP64, restart=0, max_iter=0, tol=0.0, hbm_budget=0.0):
+        lib = load()
+        self.mesh = mesh
+        self.n = mesh.n
+        p = SolverParams(precision, restart, max_iter, tol, hbm_budget)
+        h = C.c_void_p()
+        _check(lib.bem_solver_create(mesh.handle, C.byref(p), C.byref(h)))
+        self.handle = h
+        self.info = SolveInfo()
+
+    def assemble(self, freq: Frequency):
+        _check(load().bem_assemble(self.handle, C.byref(freq.desc)))
+
+    def solve(self, allow_not_converged=False):
+        allow = (BEM_ERR_NOT_CONVERGED,) if allow_not_converged else ()
+        _check(load().bem_solve(self.handle, C.byref(self.info)), allow)
+        return self.info.as_dict()
+
+    def solution(self):
+        x = np.zeros(self.n, np.complex128)
+        _check(load().bem_get_solution(self.handle, _ptr(x)))
+        return x
+
+    def system(self, rows=None, with_matrix=True):
+        r0, r1 = (0, self.n) if rows is None else rows
+        A = np.zeros((r1 - r0, self.n), np.complex128) if with_matrix else None
+        b = np.zeros(self.n, np.complex128)
+        _check(load().bem_get_system(self.handle, r0, r1, _ptr(A), _ptr(b)))
+        return A, b
+
+    def project(self, pts, with_grad=True):
+        pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+        pot = np.zeros(len(pts), np.complex128)
+        grad = np.zeros((len(pts), 3), np.complex128) if with_grad else None
+        _check(load().bem_project(self.handle, len(pts), _ptr(pts), _ptr(pot), _ptr(grad)))
+        return pot, grad
+
+    def solve_frequency(self, freq: Frequency, pts, with_grad=True, allow_not_converged=False):
+        pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+        x = np.zeros(self.n, np.complex128)
+        pot = np.zeros(len(pts), np.complex128)
+        grad = np.zeros((len(pts), 3), np.complex128) if with_grad else None
+        allow = (BEM_ERR_NOT_CONVERGED,) if allow_not_converged else ()
+        _check(load().bem_solve_frequency(self.handle, C.byref(freq.desc), len(pts), _ptr(pts), _ptr(x),
+                                          _ptr(pot), _ptr(grad), C.byref(self.info)), allow)
+        return x, pot, grad
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().bem_solver_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def footprint_bytes(n_elem, precision=PREC_MIXED, restart=0):
+    return load().bem_footprint_bytes(n_elem, precision, restart)

@@ -1,0 +1,643 @@
+// bem_api.cu - the C ABI of include/bem_gb300.h: handles, device memory,
+// HBM admission, the restarted GMRES driver and the per-frequency sequence.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/bem_gb300.h"
+#include "bem_internal.h"
+
+using cd = std::complex<double>;
+
+namespace {
+
+thread_local std::string g_err;
+
+bem_status fail(bem_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return st;
+}
+
+#define CU(call)                                                                                 \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return fail(BEM_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+std::mutex g_init_mu;
+bool g_init_done[64];
+
+bem_status ensure_device_init() {
+    int dev = 0;
+    CU(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (dev < 0 || dev >= 64) return fail(BEM_ERR_INVALID, "device index %d out of range", dev);
+    if (!g_init_done[dev]) {
+        CU(bem::init_device_tables());
+        g_init_done[dev] = true;
+    }
+    return BEM_OK;
+}
+
+template <typename T> cudaError_t dalloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void **)p, count * sizeof(T));
+}
+
+size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+// ------------------------------------------------------------------ mesh
+struct bem_mesh_s {
+    int device = 0;
+    int n = 0;
+    std::vector<int> nvert;
+    // device buffers
+    int *d_nvert = nullptr;
+    double *d_v64 = nullptr, *d_c64 = nullptr, *d_n64 = nullptr, *d_area = nullptr, *d_sqa = nullptr;
+    float *d_chi = nullptr, *d_clo = nullptr, *d_t32 = nullptr, *d_q32 = nullptr, *d_isqa = nullptr;
+    bem::DevMeshView view() const {
+        bem::DevMeshView v;
+        v.n = n; v.nvert = d_nvert; v.v64 = d_v64; v.c64 = d_c64; v.n64 = d_n64; v.area64 = d_area;
+        v.sqa64 = d_sqa; v.chi = d_chi; v.clo = d_clo; v.t32 = d_t32; v.q32 = d_q32; v.isqa32 = d_isqa;
+        return v;
+    }
+    ~bem_mesh_s() {
+        cudaFree(d_nvert); cudaFree(d_v64); cudaFree(d_c64); cudaFree(d_n64); cudaFree(d_area);
+        cudaFree(d_sqa); cudaFree(d_chi); cudaFree(d_clo); cudaFree(d_t32); cudaFree(d_q32); cudaFree(d_isqa);
+    }
+};
+
+namespace {
+
+// Centre, unit normal at the centre and area with NumCalc's formulas
+// (NC_Input.cpp:522-602 with NC_3dFunctions.cpp:95-178).  This translation
+// unit's host code is compiled with -ffp-contract=off so that the products
+// and sums round as in the reference's x86 build.
+void element_geometry(int nv, const double p[4][3], double c[3], double nrm[3], double *area) {
+    double s, t, are0, sh[4], ds[4], dt[4];
+    if (nv == 3) {
+        s = t = 1.0 / 3.0; are0 = 0.5;
+        sh[0] = s; sh[1] = t; sh[2] = 1.0 - s - t;
+        ds[0] = 1.0; ds[1] = 0.0; ds[2] = -1.0;
+        dt[0] = 0.0; dt[1] = 1.0; dt[2] = -1.0;
+    } else {
+        s = t = 0.0; are0 = 4.0;
+        double s1 = 0.25 * (s + 1.0), s2 = 0.25 * (s - 1.0), t1 = t + 1.0, t2 = t - 1.0;
+        sh[0] = s1 * t1; sh[1] = -s2 * t1; sh[2] = s2 * t2; sh[3] = -s1 * t2;
+        ds[0] = 0.25 * (t + 1.0); ds[2] = 0.25 * (t - 1.0); ds[1] = -ds[0]; ds[3] = -ds[2];
+        dt[0] = 0.25 * (s + 1.0); dt[2] = 0.25 * (s - 1.0); dt[1] = -dt[2]; dt[3] = -dt[0];
+    }
+    double dxs[3], dxt[3];
+    for (int k = 0; k < 3; ++k) {
+        c[k] = 0.0; dxs[k] = 0.0; dxt[k] = 0.0;
+        for (int a = 0; a < nv; ++a) {
+            c[k] += sh[a] * p[a][k];
+            dxs[k] += ds[a] * p[a][k];
+            dxt[k] += dt[a] * p[a][k];
+        }
+    }
+    double n0 = dxs[1] * dxt[2] - dxt[1] * dxs[2];
+    double n1 = dxs[2] * dxt[0] - dxt[2] * dxs[0];
+    double n2 = dxs[0] * dxt[1] - dxt[0] * dxs[1];
+    double len = std::sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+    nrm[0] = n0 / len; nrm[1] = n1 / len; nrm[2] = n2 / len;
+    *area = len * are0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- solver
+struct bem_solver_s {
+    bem_mesh_t mesh = nullptr;
+    int n = 0;
+    int prec = 0;
+    int restart = 60;
+    int max_iter = 1000;
+    double tol = 1e-9;
+    size_t lda = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[6] = {};
+    void *A = nullptr;
+    double *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *V = nullptr;
+    double *hd = nullptr, *hsum = nullptr, *nrm = nullptr, *ydev = nullptr;
+    void *xf = nullptr;
+    int *status = nullptr;
+    unsigned long long *n_near = nullptr;
+    // per-frequency device data
+    int *f_bct = nullptr, *f_cols = nullptr;
+    double *f_bcv = nullptr, *f_adm = nullptr, *f_src = nullptr;
+    bem::DevFreq freq{};
+    bool have_freq = false;
+    bool solved = false;
+    // fields and projection
+    double *phi = nullptr, *vel = nullptr;
+    int *ivi = nullptr;
+    double *pts = nullptr, *pot = nullptr, *grad = nullptr;
+    int pts_cap = 0;
+    // pinned staging
+    double *h_pin = nullptr;
+    bem_solve_info info{};
+    ~bem_solver_s() {
+        if (st) cudaStreamSynchronize(st);
+        cudaFree(A); cudaFree(b); cudaFree(x); cudaFree(r); cudaFree(w); cudaFree(V); cudaFree(hd);
+        cudaFree(hsum); cudaFree(nrm); cudaFree(ydev); cudaFree(xf); cudaFree(status); cudaFree(n_near);
+        cudaFree(f_bct); cudaFree(f_cols); cudaFree(f_bcv); cudaFree(f_adm); cudaFree(f_src);
+        cudaFree(phi); cudaFree(vel); cudaFree(ivi); cudaFree(pts); cudaFree(pot); cudaFree(grad);
+        if (h_pin) cudaFreeHost(h_pin);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+extern "C" {
+
+const char *bem_last_error(void) { return g_err.c_str(); }
+
+const char *bem_version(void) { return "mesh2hrtf_gb300 1.0 (sm_103a)"; }
+
+bem_status bem_set_device(int32_t device) {
+    CU(cudaSetDevice(device));
+    return ensure_device_init();
+}
+
+double bem_footprint_bytes(int32_t n_elem, int32_t precision, int32_t restart) {
+    const double n = (double)n_elem;
+    const double lda = (double)round_up((size_t)std::max(n_elem, 1), 32);
+    const double esz = precision == BEM_PREC_FP64 ? 16.0 : 8.0;
+    const int m = restart > 0 ? restart : 60;
+    // matrix + Krylov basis + 4 work vectors + split x + fields (phi, 4 vel)
+    return n * lda * esz + (m + 1) * n * 16.0 + 4 * n * 16.0 + n * 16.0 + 5 * n * 16.0 + n * 64.0;
+}
+
+bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
+    if (!d || !out) return fail(BEM_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (d->n_elem <= 0 || d->n_nodes <= 0 || !d->nodes || !d->conn || !d->nvert)
+        return fail(BEM_ERR_INVALID, "mesh needs elements, nodes, connectivity and vertex counts");
+    bem_status s = ensure_device_init();
+    if (s != BEM_OK) return s;
+    const int n = d->n_elem;
+    std::vector<double> v64(12 * (size_t)n, 0.0), c64(3 * (size_t)n), n64(3 * (size_t)n), area(n), sqa(n);
+    std::vector<float> chi(3 * (size_t)n), clo(3 * (size_t)n), t32(10 * (size_t)n, 0.f), q32(12 * (size_t)n, 0.f),
+        isqa(n);
+    std::vector<int> nvert(n);
+    for (int j = 0; j < n; ++j) {
+        const int nv = d->nvert[j];
+        if (nv != 3 && nv != 4) return fail(BEM_ERR_INVALID, "element %d has %d vertices (3 or 4 allowed)", j, nv);
+        nvert[j] = nv;
+        double p[4][3] = {{0}};
+        for (int a = 0; a < nv; ++a) {
+            const int node = d->conn[4 * (size_t)j + a];
+            if (node < 0 || node >= d->n_nodes) return fail(BEM_ERR_INVALID, "element %d: node index %d", j, node);
+            for (int k = 0; k < 3; ++k) {
+                p[a][k] = d->nodes[3 * (size_t)node + k];
+                v64[(3 * a + k) * (size_t)n + j] = p[a][k];
+            }
+        }
+        double c[3], nr[3], ar;
+        element_geometry(nv, p, c, nr, &ar);
+        if (d->centers) for (int k = 0; k < 3; ++k) c[k] = d->centers[3 * (size_t)j + k];
+        if (d->normals) for (int k = 0; k < 3; ++k) nr[k] = d->normals[3 * (size_t)j + k];
+        if (d->areas) ar = d->areas[j];
+        if (!(ar > 0.0)) return fail(BEM_ERR_INVALID, "element %d has area %g", j, ar);
+        for (int k = 0; k < 3; ++k) {
+            c64[k * (size_t)n + j] = c[k];
+            n64[k * (size_t)n + j] = nr[k];
+            const float h = (float)c[k];
+            chi[k * (size_t)n + j] = h;
+            clo[k * (size_t)n + j] = (float)(c[k] - (double)h);
+        }
+        area[j] = ar;
+        sqa[j] = std::sqrt(ar);
+        isqa[j] = (float)(1.0 / sqa[j]);
+        if (nv == 3) {
+            for (int k = 0; k < 3; ++k) {
+                t32[k * (size_t)n + j] = (float)(p[0][k] - p[2][k]);
+                t32[(3 + k) * (size_t)n + j] = (float)(p[1][k] - p[2][k]);
+                t32[(6 + k) * (size_t)n + j] = (float)nr[k];
+            }
+            t32[9 * (size_t)n + j] = (float)(2.0 * ar);
+        } else {
+            for (int a = 0; a < 4; ++a)
+                for (int k = 0; k < 3; ++k) q32[(3 * a + k) * (size_t)n + j] = (float)(p[a][k] - c[k]);
+        }
+    }
+    bem_mesh_s *m = new bem_mesh_s();
+    cudaGetDevice(&m->device);
+    m->n = n;
+    m->nvert = nvert;
+    auto up = [&](auto **dst, const auto &src) -> cudaError_t {
+        cudaError_t e = dalloc(dst, src.size());
+        if (e != cudaSuccess) return e;
+        return cudaMemcpy(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice);
+    };
+    cudaError_t e = up(&m->d_nvert, nvert);
+    if (e == cudaSuccess) e = up(&m->d_v64, v64);
+    if (e == cudaSuccess) e = up(&m->d_c64, c64);
+    if (e == cudaSuccess) e = up(&m->d_n64, n64);
+    if (e == cudaSuccess) e = up(&m->d_area, area);
+    if (e == cudaSuccess) e = up(&m->d_sqa, sqa);
+    if (e == cudaSuccess) e = up(&m->d_chi, chi);
+    if (e == cudaSuccess) e = up(&m->d_clo, clo);
+    if (e == cudaSuccess) e = up(&m->d_t32, t32);
+    if (e == cudaSuccess) e = up(&m->d_q32, q32);
+    if (e == cudaSuccess) e = up(&m->d_isqa, isqa);
+    if (e != cudaSuccess) {
+        delete m;
+        return fail(e == cudaErrorMemoryAllocation ? BEM_ERR_OUT_OF_HBM : BEM_ERR_CUDA, "mesh upload: %s",
+                    cudaGetErrorString(e));
+    }
+    *out = m;
+    return BEM_OK;
+}
+
+bem_status bem_mesh_destroy(bem_mesh_t mesh) {
+    delete mesh;
+    return BEM_OK;
+}
+
+bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_solver_t *out) {
+    if (!mesh || !out) return fail(BEM_ERR_INVALID, "null argument");
+    *out = nullptr;
+    bem_solver_params prm{};
+    if (p) prm = *p;
+    if (prm.precision != BEM_PREC_FP64 && prm.precision != BEM_PREC_MIXED)
+        return fail(BEM_ERR_INVALID, "unknown precision %d", prm.precision);
+    const int n = mesh->n;
+    const int m = prm.restart > 0 ? prm.restart : 60;
+    const double need = bem_footprint_bytes(n, prm.precision, m);
+    size_t free_b = 0, total_b = 0;
+    CU(cudaMemGetInfo(&free_b, &total_b));
+    double budget = prm.hbm_budget_bytes > 0 ? prm.hbm_budget_bytes : (double)free_b - 1.0e9;
+    if (need > budget)
+        return fail(BEM_ERR_OUT_OF_HBM, "solver for %d unknowns needs %.3f GB, budget %.3f GB", n, need / 1e9,
+                    budget / 1e9);
+    bem_solver_s *s = new bem_solver_s();
+    s->mesh = mesh;
+    s->n = n;
+    s->prec = prm.precision;
+    s->restart = m;
+    s->max_iter = prm.max_iter > 0 ? prm.max_iter : 1000;
+    s->tol = prm.tol > 0 ? prm.tol : 1e-9;
+    s->lda = round_up((size_t)n, 32);
+    const size_t esz = s->prec == BEM_PREC_FP64 ? 16 : 8;
+    auto cleanup = [&](cudaError_t e) {
+        delete s;
+        return fail(e == cudaErrorMemoryAllocation ? BEM_ERR_OUT_OF_HBM : BEM_ERR_CUDA, "solver allocation: %s",
+                    cudaGetErrorString(e));
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    for (auto &ev : s->ev)
+        if (e == cudaSuccess) e = cudaEventCreate(&ev);
+    if (e == cudaSuccess) e = cudaMalloc(&s->A, (size_t)n * s->lda * esz);
+    if (e == cudaSuccess) e = dalloc(&s->b, 2 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&s->x, 2 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&s->r, 2 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&s->w, 2 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&s->V, 2 * (size_t)n * (m + 1));
+    if (e == cudaSuccess) e = dalloc(&s->hd, 2 * (size_t)(m + 2));
+    if (e == cudaSuccess) e = dalloc(&s->hsum, 2 * (size_t)(m + 2));
+    if (e == cudaSuccess) e = dalloc(&s->nrm, 4);
+    if (e == cudaSuccess) e = dalloc(&s->ydev, 2 * (size_t)(m + 2));
+    if (e == cudaSuccess) e = cudaMalloc(&s->xf, 16 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&s->status, 1);
+    if (e == cudaSuccess) e = dalloc(&s->n_near, 1);
+    if (e == cudaSuccess) e = dalloc(&s->phi, 2 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&s->vel, 8 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&s->ivi, (size_t)n);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_pin, sizeof(double) * (2 * (size_t)(m + 4) + 8));
+    if (e != cudaSuccess) return cleanup(e);
+    *out = s;
+    return BEM_OK;
+}
+
+bem_status bem_solver_destroy(bem_solver_t s) {
+    delete s;
+    return BEM_OK;
+}
+
+static bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f) {
+    const int n = s->n;
+    if (!(f->wave_number > 0.0)) return fail(BEM_ERR_INVALID, "wave number must be > 0");
+    if (f->n_point < 0 || f->n_plane < 0) return fail(BEM_ERR_INVALID, "negative source count");
+    if ((f->n_point && (!f->point_xyz || !f->point_amp)) || (f->n_plane && (!f->plane_dir || !f->plane_amp)))
+        return fail(BEM_ERR_INVALID, "source arrays missing");
+    bem::DevFreq &F = s->freq;
+    F = bem::DevFreq{};
+    const double htf = f->time_factor == -1.0 ? -1.0 : 1.0;
+    const double tao = f->tao == -1.0 ? -1.0 : 1.0;
+    F.k = f->wave_number;
+    F.wr = htf * f->wave_number;
+    F.tao = tao;
+    F.beta_im = tao < 0 ? 0.0 : htf / f->wave_number;   // NC_EquationSystem.cpp:85-86
+    cudaFree(s->f_bct); cudaFree(s->f_cols); cudaFree(s->f_bcv); cudaFree(s->f_adm); cudaFree(s->f_src);
+    s->f_bct = s->f_cols = nullptr;
+    s->f_bcv = s->f_adm = s->f_src = nullptr;
+    std::vector<int> cols;
+    if (f->bc_type) {
+        for (int j = 0; j < n; ++j)
+            if (f->bc_type[j] < 0 || f->bc_type[j] > 2)
+                return fail(BEM_ERR_INVALID, "element %d: boundary condition type %d unsupported", j, f->bc_type[j]);
+        CU(dalloc(&s->f_bct, (size_t)n));
+        CU(cudaMemcpyAsync(s->f_bct, f->bc_type, sizeof(int) * n, cudaMemcpyHostToDevice, s->st));
+        F.bc_type = s->f_bct;
+    }
+    if (f->bc_value) {
+        std::vector<double> t(8 * (size_t)n);
+        for (int j = 0; j < n; ++j) {
+            bool nz = false;
+            for (int a = 0; a < 4; ++a) {
+                const double re = f->bc_value[8 * (size_t)j + 2 * a], im = f->bc_value[8 * (size_t)j + 2 * a + 1];
+                t[2 * ((size_t)a * n + j)] = re;
+                t[2 * ((size_t)a * n + j) + 1] = im;
+                // NumCalc's test: |value| > EPSY on the element's nodes (NC_EquationSystem.cpp:264-275)
+                if (a < s->mesh->nvert[j] && std::sqrt(re * re + im * im) > 1.0e-14) nz = true;
+            }
+            if (nz) cols.push_back(j);
+        }
+        CU(dalloc(&s->f_bcv, t.size()));
+        CU(cudaMemcpyAsync(s->f_bcv, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, s->st));
+        CU(cudaStreamSynchronize(s->st));
+        F.bc_val = s->f_bcv;
+    }
+    if (f->admittance) {
+        CU(dalloc(&s->f_adm, 2 * (size_t)n));
+        CU(cudaMemcpyAsync(s->f_adm, f->admittance, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, s->st));
+        F.adm = s->f_adm;
+    }
+    if (!cols.empty()) {
+        CU(dalloc(&s->f_cols, cols.size()));
+        CU(cudaMemcpyAsync(s->f_cols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, s->st));
+        F.bc_cols = s->f_cols;
+        F.n_bc_cols = (int)cols.size();
+    }
+    const size_t nsrc = 5 * (size_t)f->n_point + 5 * (size_t)f->n_plane;
+    if (nsrc) {
+        // complex amplitudes first so that they start on 16-byte boundaries
+        // (the kernels read them as double2), coordinates after them
+        std::vector<double> src;
+        src.reserve(nsrc);
+        for (int i = 0; i < 2 * f->n_point; ++i) src.push_back(f->point_amp[i]);
+        for (int i = 0; i < 2 * f->n_plane; ++i) src.push_back(f->plane_amp[i]);
+        for (int i = 0; i < 3 * f->n_point; ++i) src.push_back(f->point_xyz[i]);
+        for (int i = 0; i < 3 * f->n_plane; ++i) src.push_back(f->plane_dir[i]);
+        CU(dalloc(&s->f_src, src.size()));
+        CU(cudaMemcpyAsync(s->f_src, src.data(), sizeof(double) * src.size(), cudaMemcpyHostToDevice, s->st));
+        CU(cudaStreamSynchronize(s->st));
+        F.n_point = f->n_point;
+        F.n_plane = f->n_plane;
+        F.ps_amp = s->f_src;
+        F.pw_amp = s->f_src + 2 * (size_t)f->n_point;
+        F.ps_xyz = s->f_src + 2 * (size_t)f->n_point + 2 * (size_t)f->n_plane;
+        F.pw_dir = F.ps_xyz + 3 * (size_t)f->n_point;
+    }
+    return BEM_OK;
+}
+
+bem_status bem_assemble(bem_solver_t s, const bem_frequency_desc *f) {
+    if (!s || !f) return fail(BEM_ERR_INVALID, "null argument");
+    bem_status rc = upload_freq(s, f);
+    if (rc != BEM_OK) return rc;
+    CU(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+    CU(cudaMemsetAsync(s->n_near, 0, sizeof(unsigned long long), s->st));
+    CU(cudaEventRecord(s->ev[0], s->st));
+    CU(bem::launch_assemble(s->mesh->view(), s->freq, s->prec, s->A, s->lda, s->status, s->n_near, s->st));
+    CU(bem::launch_rhs(s->mesh->view(), s->freq, s->b, s->status, s->st));
+    CU(cudaEventRecord(s->ev[1], s->st));
+    int st_h = 0;
+    unsigned long long nn = 0;
+    CU(cudaMemcpyAsync(&st_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CU(cudaMemcpyAsync(&nn, s->n_near, sizeof(nn), cudaMemcpyDeviceToHost, s->st));
+    CU(cudaStreamSynchronize(s->st));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]));
+    s->info.assemble_ms = ms;
+    s->info.n_near_pairs = (int64_t)nn;
+    s->have_freq = true;
+    s->solved = false;
+    if (st_h != 0)
+        return fail(BEM_ERR_SUBDIVISION,
+                    st_h == 1 ? "number of subelements which are subdivided in a loop must <= 15"
+                              : "number of subelements must be < 220");
+    return BEM_OK;
+}
+
+namespace {
+
+// host copy of a device complex vector
+bem_status fetch(bem_solver_t s, const double *dsrc, double *hdst, size_t ndoubles) {
+    CU(cudaMemcpyAsync(hdst, dsrc, ndoubles * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    CU(cudaStreamSynchronize(s->st));
+    return BEM_OK;
+}
+
+}  // namespace
+
+// Restarted GMRES.  Each cycle starts from the explicitly computed residual
+// r = b - A x, so with BEM_PREC_MIXED every cycle is one step of iterative
+// refinement: the inner Arnoldi process (FP64 vectors, CGS with one
+// re-orthogonalisation, FP64 inner products) works with the fast FP32
+// matrix-vector product and stops once it has gained five digits, and the
+// outer residual is evaluated with the error-free-transformation product.
+bem_status bem_solve(bem_solver_t s, bem_solve_info *info) {
+    if (!s) return fail(BEM_ERR_INVALID, "null solver");
+    if (!s->have_freq) return fail(BEM_ERR_INVALID, "bem_solve before bem_assemble");
+    const int n = s->n, m = s->restart;
+    const size_t ldv = 2 * (size_t)n;
+    CU(cudaEventRecord(s->ev[2], s->st));
+    CU(cudaMemsetAsync(s->x, 0, sizeof(double) * 2 * n, s->st));
+    CU(bem::launch_norm2(s->b, n, s->nrm, s->st));
+    double *hp = s->h_pin;
+    bem_status rc = fetch(s, s->nrm, hp, 1);
+    if (rc) return rc;
+    const double bnorm = std::sqrt(hp[0]);
+    int iters = 0, cycles = 0;
+    double rel = 0.0;
+    bool converged = false;
+    if (bnorm == 0.0 || !std::isfinite(bnorm)) {
+        converged = bnorm == 0.0;
+        if (!converged) return fail(BEM_ERR_INVALID, "right-hand side is not finite");
+    } else {
+        CU(cudaMemcpyAsync(s->r, s->b, sizeof(double) * 2 * n, cudaMemcpyDeviceToDevice, s->st));
+        CU(cudaMemcpyAsync(s->nrm + 1, s->nrm, sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+        double beta = bnorm, prev_beta = 0.0;
+        std::vector<cd> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+        while (true) {
+            ++cycles;
+            CU(bem::launch_scale_inv(s->r, s->nrm + 1, s->V, n, s->st));
+            std::fill(H.begin(), H.end(), cd(0.0));
+            std::fill(g.begin(), g.end(), cd(0.0));
+            g[0] = beta;
+            const double inner_floor = s->prec == BEM_PREC_MIXED ? 1e-5 * beta : 0.0;
+            int kk = 0;
+            for (int k = 0; k < m && iters < s->max_iter; ++k) {
+                double *vk = s->V + (size_t)k * ldv;
+                CU(bem::launch_matvec(s->prec, false, s->A, n, s->lda, vk, nullptr, s->w, s->xf, s->st));
+                CU(cudaMemsetAsync(s->hsum, 0, sizeof(double) * 2 * (k + 1), s->st));
+                for (int pass = 0; pass < 2; ++pass) {
+                    CU(bem::launch_multi_dot(s->V, (int)ldv / 2, k + 1, s->w, n, s->hd, s->st));
+                    CU(bem::launch_multi_axpy(s->V, (int)ldv / 2, k + 1, s->hd, s->hsum, s->w, n, s->st));
+                }
+                CU(bem::launch_norm2(s->w, n, s->nrm, s->st));
+                CU(bem::launch_scale_inv(s->w, s->nrm, s->V + (size_t)(k + 1) * ldv, n, s->st));
+                CU(cudaMemcpyAsync(hp, s->hsum, sizeof(double) * 2 * (k + 1), cudaMemcpyDeviceToHost, s->st));
+                CU(cudaMemcpyAsync(hp + 2 * (k + 1), s->nrm, sizeof(double), cudaMemcpyDeviceToHost, s->st));
+                CU(cudaStreamSynchronize(s->st));
+                ++iters;
+                for (int l = 0; l <= k; ++l) H[(size_t)l * m + k] = cd(hp[2 * l], hp[2 * l + 1]);
+                const double hn = std::sqrt(hp[2 * (k + 1)]);
+                // previous rotations
+                for (int l = 0; l < k; ++l) {
+                    const cd a = H[(size_t)l * m + k], b2 = H[(size_t)(l + 1) * m + k];
+                    H[(size_t)l * m + k] = std::conj(cs[l]) * a + std::conj(sn[l]) * b2;
+                    H[(size_t)(l + 1) * m + k] = -sn[l] * a + cs[l] * b2;
+                }
+                // new rotation zeroing the subdiagonal hn
+                const cd a = H[(size_t)k * m + k];
+                const double den = std::sqrt(std::norm(a) + hn * hn);
+                if (den == 0.0) { cs[k] = 1.0; sn[k] = 0.0; }
+                else { cs[k] = a / den; sn[k] = cd(hn / den, 0.0); }
+                H[(size_t)k * m + k] = std::conj(cs[k]) * a + std::conj(sn[k]) * hn;
+                g[k + 1] = -sn[k] * g[k];
+                g[k] = std::conj(cs[k]) * g[k];
+                kk = k + 1;
+                const double res = std::abs(g[k + 1]);
+                if (!std::isfinite(res)) return fail(BEM_ERR_NOT_CONVERGED, "GMRES breakdown (non-finite residual)");
+                if (res <= s->tol * bnorm || res <= inner_floor || hn == 0.0) break;
+            }
+            // y = H^{-1} g (upper triangular kk x kk)
+            for (int i2 = kk - 1; i2 >= 0; --i2) {
+                cd acc = g[i2];
+                for (int l = i2 + 1; l < kk; ++l) acc -= H[(size_t)i2 * m + l] * y[l];
+                y[i2] = acc / H[(size_t)i2 * m + i2];
+            }
+            for (int l = 0; l < kk; ++l) { hp[2 * l] = y[l].real(); hp[2 * l + 1] = y[l].imag(); }
+            CU(cudaMemcpyAsync(s->ydev, hp, sizeof(double) * 2 * kk, cudaMemcpyHostToDevice, s->st));
+            CU(bem::launch_update_x(s->V, (int)ldv / 2, kk, s->ydev, s->x, n, s->st));
+            // explicit residual (the refinement step)
+            CU(bem::launch_matvec(s->prec, true, s->A, n, s->lda, s->x, s->b, s->r, s->xf, s->st));
+            CU(bem::launch_norm2(s->r, n, s->nrm + 1, s->st));
+            rc = fetch(s, s->nrm + 1, hp, 1);
+            if (rc) return rc;
+            prev_beta = beta;
+            beta = std::sqrt(hp[0]);
+            rel = beta / bnorm;
+            if (!std::isfinite(rel)) return fail(BEM_ERR_NOT_CONVERGED, "GMRES breakdown (non-finite residual)");
+            if (rel <= s->tol) { converged = true; break; }
+            if (iters >= s->max_iter) break;
+            if (cycles > 2 && beta > 0.9 * prev_beta && s->prec == BEM_PREC_MIXED) break;  // refinement stagnates
+        }
+    }
+    CU(cudaEventRecord(s->ev[3], s->st));
+    CU(cudaEventSynchronize(s->ev[3]));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, s->ev[2], s->ev[3]));
+    s->info.solve_ms = ms;
+    s->info.iterations = iters;
+    s->info.restarts = cycles;
+    s->info.rel_residual = rel;
+    s->solved = true;
+    if (info) *info = s->info;
+    if (!converged)
+        return fail(BEM_ERR_NOT_CONVERGED, "GMRES reached %d iterations, relative residual %.3e", iters, rel);
+    return BEM_OK;
+}
+
+bem_status bem_get_solution(bem_solver_t s, double *x_host) {
+    if (!s || !x_host) return fail(BEM_ERR_INVALID, "null argument");
+    return fetch(s, s->x, x_host, 2 * (size_t)s->n);
+}
+
+bem_status bem_get_system(bem_solver_t s, int32_t row0, int32_t row1, double *a_host, double *b_host) {
+    if (!s) return fail(BEM_ERR_INVALID, "null solver");
+    if (row0 < 0 || row1 > s->n || row0 > row1) return fail(BEM_ERR_INVALID, "bad row range");
+    const int n = s->n;
+    if (a_host && row1 > row0) {
+        if (s->prec == BEM_PREC_FP64) {
+            CU(cudaMemcpy2DAsync(a_host, sizeof(double) * 2 * n, (const char *)s->A + (size_t)row0 * s->lda * 16,
+                                 s->lda * 16, sizeof(double) * 2 * n, row1 - row0, cudaMemcpyDeviceToHost, s->st));
+            CU(cudaStreamSynchronize(s->st));
+        } else {
+            std::vector<float> tmp(2 * (size_t)n * (row1 - row0));
+            CU(cudaMemcpy2DAsync(tmp.data(), sizeof(float) * 2 * n, (const char *)s->A + (size_t)row0 * s->lda * 8,
+                                 s->lda * 8, sizeof(float) * 2 * n, row1 - row0, cudaMemcpyDeviceToHost, s->st));
+            CU(cudaStreamSynchronize(s->st));
+            for (size_t i = 0; i < tmp.size(); ++i) a_host[i] = tmp[i];
+        }
+    }
+    if (b_host) return fetch(s, s->b, b_host, 2 * (size_t)n);
+    return BEM_OK;
+}
+
+bem_status bem_project(bem_solver_t s, int32_t n_pts, const double *pts, double *pot_out, double *grad_out) {
+    if (!s) return fail(BEM_ERR_INVALID, "null solver");
+    if (!s->solved) return fail(BEM_ERR_INVALID, "bem_project before bem_solve");
+    if (n_pts < 0 || (n_pts > 0 && (!pts || !pot_out))) return fail(BEM_ERR_INVALID, "bad point arrays");
+    if (n_pts > s->pts_cap) {
+        cudaFree(s->pts); cudaFree(s->pot); cudaFree(s->grad);
+        s->pts = s->pot = s->grad = nullptr;
+        s->pts_cap = 0;
+        CU(dalloc(&s->pts, 3 * (size_t)n_pts));
+        CU(dalloc(&s->pot, 2 * (size_t)n_pts));
+        CU(dalloc(&s->grad, 6 * (size_t)n_pts));
+        s->pts_cap = n_pts;
+    }
+    CU(cudaEventRecord(s->ev[4], s->st));
+    CU(bem::launch_fields(s->mesh->view(), s->freq, s->x, s->phi, s->vel, s->ivi, s->st));
+    if (n_pts > 0) {
+        CU(cudaMemcpyAsync(s->pts, pts, sizeof(double) * 3 * n_pts, cudaMemcpyHostToDevice, s->st));
+        CU(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+        CU(bem::launch_project(s->mesh->view(), s->freq, s->prec, s->phi, s->vel, s->ivi, n_pts, s->pts, s->pot,
+                               s->grad, s->status, s->st));
+        CU(cudaMemcpyAsync(pot_out, s->pot, sizeof(double) * 2 * n_pts, cudaMemcpyDeviceToHost, s->st));
+        if (grad_out)
+            CU(cudaMemcpyAsync(grad_out, s->grad, sizeof(double) * 6 * n_pts, cudaMemcpyDeviceToHost, s->st));
+    }
+    CU(cudaEventRecord(s->ev[5], s->st));
+    int st_h = 0;
+    CU(cudaMemcpyAsync(&st_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CU(cudaStreamSynchronize(s->st));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, s->ev[4], s->ev[5]));
+    s->info.project_ms = ms;
+    if (st_h != 0)
+        return fail(BEM_ERR_SUBDIVISION, "evaluation point too close to the boundary: subdivision limit");
+    return BEM_OK;
+}
+
+bem_status bem_solve_frequency(bem_solver_t s, const bem_frequency_desc *f, int32_t n_pts, const double *pts,
+                               double *x_out, double *pot_out, double *grad_out, bem_solve_info *info) {
+    bem_status rc = bem_assemble(s, f);
+    if (rc != BEM_OK) return rc;
+    rc = bem_solve(s, info);
+    if (rc != BEM_OK && rc != BEM_ERR_NOT_CONVERGED) return rc;
+    bem_status solve_rc = rc;
+    if (x_out) {
+        rc = bem_get_solution(s, x_out);
+        if (rc != BEM_OK) return rc;
+    }
+    rc = bem_project(s, n_pts, pts, pot_out, grad_out);
+    if (rc != BEM_OK) return rc;
+    if (info) *info = s->info;
+    return solve_rc;
+}
+
+}  // extern "C"

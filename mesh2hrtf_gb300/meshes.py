@@ -237,3 +237,12 @@ def grid_triangles(points):
 
     hull = ConvexHull(points)
     return np.asarray(hull.simplices, dtype=np.int64)
+
+
+def shells_triangles(shells):
+    """Evaluation elements for several concentric point shells, one hull each."""
+    tris, off = [], 0
+    for pts in shells:
+        tris.append(grid_triangles(np.asarray(pts)) + off)
+        off += len(pts)
+    return np.vstack(tris)
