@@ -103,11 +103,17 @@ typedef struct {
     double solve_ms;           /* device time of the last bem_solve            */
     double project_ms;         /* device time of the last bem_project          */
     int64_t n_near_pairs;      /* element pairs that needed subdivision        */
+    double matvec_ms;          /* device time of the matrix-vector products of
+                                  the last bem_solve (inner and residual)      */
+    int32_t n_matvec;          /* number of those products                     */
 } bem_solve_info;
 
 /* Library / device ------------------------------------------------------- */
 const char *bem_last_error(void);
 const char *bem_version(void);
+/* Number of CUDA kernels this library has launched in this process (all
+ * devices).  Diagnostic with no counterpart in the reference. */
+int64_t bem_kernel_launches(void);
 /* Select the CUDA device for this thread's subsequent calls. */
 bem_status bem_set_device(int32_t device);
 /* Bytes a solver for n_elem unknowns holds on the device (matrix, Krylov
@@ -128,6 +134,11 @@ bem_status bem_mesh_destroy(bem_mesh_t mesh);
 bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *params,
                              bem_solver_t *out);
 bem_status bem_solver_destroy(bem_solver_t solver);
+/* Change the tolerance and the iteration limit of an existing solver (the
+ * precision and restart length are fixed at creation); fields <= 0 keep
+ * their value.  NumCalc's -nitermax option (NC_Main.cpp:171-175) sets the
+ * CGS limit the same way. */
+bem_status bem_solver_set_params(bem_solver_t solver, const bem_solver_params *params);
 
 /* Assemble A and b for one frequency.
  * Replaces NC_SetupEquationSystem / NC_BuildSystemTBEM /

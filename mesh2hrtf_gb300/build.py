@@ -18,6 +18,7 @@ OBJDIR = os.path.join(PKG, "lib", "obj")
 LIB = os.path.join(LIBDIR, "libbem_gb300.so")
 NUMCALC_DIR = os.path.join(PKG, "numcalc")
 NUMCALC_BIN = os.path.join(NUMCALC_DIR, "bin", "NumCalc")
+NUMCALC_SRC = os.path.join(NUMCALC_DIR, "src")
 
 CU_SOURCES = ["bem_api.cu", "bem_kernels.cu", "bem_krylov.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -68,16 +69,13 @@ def build_library(verbose: bool = False, force: bool = False) -> str:
 
 def build_numcalc() -> str:
     """Build the drop-in NumCalc executable (links libbem_gb300.so by rpath)."""
-    mk = os.path.join(NUMCALC_DIR, "Makefile")
-    if os.path.exists(mk):
-        _run(["make", "-s", "-C", NUMCALC_DIR, "-j4"])
+    _run(["make", "-s", "-C", NUMCALC_SRC])
     return NUMCALC_BIN
 
 
 def build_all(verbose: bool = False):
     build_library(verbose)
-    if os.path.exists(os.path.join(NUMCALC_DIR, "Makefile")):
-        build_numcalc()
+    build_numcalc()
 
 
 if __name__ == "__main__":

@@ -27,8 +27,8 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 
 EXPORTED = [
-    "bem_last_error", "bem_version", "bem_set_device", "bem_footprint_bytes",
-    "bem_mesh_create", "bem_mesh_destroy", "bem_solver_create", "bem_solver_destroy",
+    "bem_last_error", "bem_version", "bem_kernel_launches", "bem_set_device", "bem_footprint_bytes",
+    "bem_mesh_create", "bem_mesh_destroy", "bem_solver_create", "bem_solver_destroy", "bem_solver_set_params",
     "bem_assemble", "bem_solve", "bem_get_solution", "bem_get_system", "bem_project",
     "bem_solve_frequency",
 ]
@@ -61,7 +61,7 @@ class SolverParams(C.Structure):
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("restarts", C.c_int32), ("rel_residual", C.c_double),
                 ("assemble_ms", C.c_double), ("solve_ms", C.c_double), ("project_ms", C.c_double),
-                ("n_near_pairs", C.c_int64)]
+                ("n_near_pairs", C.c_int64), ("matvec_ms", C.c_double), ("n_matvec", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -83,6 +83,7 @@ def load(build_if_missing: bool = True):
     vp, i32, dp = C.c_void_p, C.c_int32, C.POINTER(C.c_double)
     lib.bem_last_error.restype = C.c_char_p
     lib.bem_version.restype = C.c_char_p
+    lib.bem_kernel_launches.restype = C.c_int64
     lib.bem_set_device.argtypes = [i32]
     lib.bem_footprint_bytes.argtypes = [i32, i32, i32]
     lib.bem_footprint_bytes.restype = C.c_double
@@ -90,6 +91,7 @@ def load(build_if_missing: bool = True):
     lib.bem_mesh_destroy.argtypes = [vp]
     lib.bem_solver_create.argtypes = [vp, C.POINTER(SolverParams), C.POINTER(vp)]
     lib.bem_solver_destroy.argtypes = [vp]
+    lib.bem_solver_set_params.argtypes = [vp, C.POINTER(SolverParams)]
     lib.bem_assemble.argtypes = [vp, C.POINTER(FreqDesc)]
     lib.bem_solve.argtypes = [vp, C.POINTER(SolveInfo)]
     lib.bem_get_solution.argtypes = [vp, vp]
@@ -97,7 +99,7 @@ def load(build_if_missing: bool = True):
     lib.bem_project.argtypes = [vp, i32, vp, vp, vp]
     lib.bem_solve_frequency.argtypes = [vp, C.POINTER(FreqDesc), i32, vp, vp, vp, vp, C.POINTER(SolveInfo)]
     for name in EXPORTED:
-        if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes"):
+        if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes", "bem_kernel_launches"):
             getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -182,6 +184,10 @@ class Solver:
         _check(lib.bem_solver_create(mesh.handle, C.byref(p), C.byref(h)))
         self.handle = h
         self.info = SolveInfo()
+
+    def set_params(self, max_iter=0, tol=0.0):
+        p = SolverParams(0, 0, max_iter, tol, 0.0)
+        _check(load().bem_solver_set_params(self.handle, C.byref(p)))
 
     def assemble(self, freq: Frequency):
         _check(load().bem_assemble(self.handle, C.byref(freq.desc)))

@@ -133,7 +133,7 @@ struct bem_solver_s {
     double tol = 1e-9;
     size_t lda = 0;
     cudaStream_t st = nullptr;
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[8] = {};
     void *A = nullptr;
     double *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *V = nullptr;
     double *hd = nullptr, *hsum = nullptr, *nrm = nullptr, *ydev = nullptr;
@@ -172,6 +172,8 @@ extern "C" {
 const char *bem_last_error(void) { return g_err.c_str(); }
 
 const char *bem_version(void) { return "mesh2hrtf_gb300 1.0 (sm_103a)"; }
+
+int64_t bem_kernel_launches(void) { return (int64_t)bem::launches(); }
 
 bem_status bem_set_device(int32_t device) {
     CU(cudaSetDevice(device));
@@ -334,6 +336,13 @@ bem_status bem_solver_destroy(bem_solver_t s) {
     return BEM_OK;
 }
 
+bem_status bem_solver_set_params(bem_solver_t s, const bem_solver_params *p) {
+    if (!s || !p) return fail(BEM_ERR_INVALID, "null argument");
+    if (p->max_iter > 0) s->max_iter = p->max_iter;
+    if (p->tol > 0) s->tol = p->tol;
+    return BEM_OK;
+}
+
 static bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f) {
     const int n = s->n;
     if (!(f->wave_number > 0.0)) return fail(BEM_ERR_INVALID, "wave number must be > 0");
@@ -469,8 +478,8 @@ bem_status bem_solve(bem_solver_t s, bem_solve_info *info) {
     bem_status rc = fetch(s, s->nrm, hp, 1);
     if (rc) return rc;
     const double bnorm = std::sqrt(hp[0]);
-    int iters = 0, cycles = 0;
-    double rel = 0.0;
+    int iters = 0, cycles = 0, n_mv = 0;
+    double rel = 0.0, mv_ms = 0.0;
     bool converged = false;
     if (bnorm == 0.0 || !std::isfinite(bnorm)) {
         converged = bnorm == 0.0;
@@ -490,7 +499,9 @@ bem_status bem_solve(bem_solver_t s, bem_solve_info *info) {
             int kk = 0;
             for (int k = 0; k < m && iters < s->max_iter; ++k) {
                 double *vk = s->V + (size_t)k * ldv;
+                CU(cudaEventRecord(s->ev[6], s->st));
                 CU(bem::launch_matvec(s->prec, false, s->A, n, s->lda, vk, nullptr, s->w, s->xf, s->st));
+                CU(cudaEventRecord(s->ev[7], s->st));
                 CU(cudaMemsetAsync(s->hsum, 0, sizeof(double) * 2 * (k + 1), s->st));
                 for (int pass = 0; pass < 2; ++pass) {
                     CU(bem::launch_multi_dot(s->V, (int)ldv / 2, k + 1, s->w, n, s->hd, s->st));
@@ -501,6 +512,12 @@ bem_status bem_solve(bem_solver_t s, bem_solve_info *info) {
                 CU(cudaMemcpyAsync(hp, s->hsum, sizeof(double) * 2 * (k + 1), cudaMemcpyDeviceToHost, s->st));
                 CU(cudaMemcpyAsync(hp + 2 * (k + 1), s->nrm, sizeof(double), cudaMemcpyDeviceToHost, s->st));
                 CU(cudaStreamSynchronize(s->st));
+                {
+                    float mv = 0.f;
+                    CU(cudaEventElapsedTime(&mv, s->ev[6], s->ev[7]));
+                    mv_ms += mv;
+                    ++n_mv;
+                }
                 ++iters;
                 for (int l = 0; l <= k; ++l) H[(size_t)l * m + k] = cd(hp[2 * l], hp[2 * l + 1]);
                 const double hn = std::sqrt(hp[2 * (k + 1)]);
@@ -533,10 +550,18 @@ bem_status bem_solve(bem_solver_t s, bem_solve_info *info) {
             CU(cudaMemcpyAsync(s->ydev, hp, sizeof(double) * 2 * kk, cudaMemcpyHostToDevice, s->st));
             CU(bem::launch_update_x(s->V, (int)ldv / 2, kk, s->ydev, s->x, n, s->st));
             // explicit residual (the refinement step)
+            CU(cudaEventRecord(s->ev[6], s->st));
             CU(bem::launch_matvec(s->prec, true, s->A, n, s->lda, s->x, s->b, s->r, s->xf, s->st));
+            CU(cudaEventRecord(s->ev[7], s->st));
             CU(bem::launch_norm2(s->r, n, s->nrm + 1, s->st));
             rc = fetch(s, s->nrm + 1, hp, 1);
             if (rc) return rc;
+            {
+                float mv = 0.f;
+                CU(cudaEventElapsedTime(&mv, s->ev[6], s->ev[7]));
+                mv_ms += mv;
+                ++n_mv;
+            }
             prev_beta = beta;
             beta = std::sqrt(hp[0]);
             rel = beta / bnorm;
@@ -554,6 +579,8 @@ bem_status bem_solve(bem_solver_t s, bem_solve_info *info) {
     s->info.iterations = iters;
     s->info.restarts = cycles;
     s->info.rel_residual = rel;
+    s->info.matvec_ms = mv_ms;
+    s->info.n_matvec = n_mv;
     s->solved = true;
     if (info) *info = s->info;
     if (!converged)

@@ -30,6 +30,10 @@ struct DevFreq {
     const double *pw_amp;      // [n_plane] complex
 };
 
+// Process-wide count of kernel launches issued by the launch_* functions.
+void count_launches(int k);
+long long launches();
+
 // Copies the quadrature tables into constant memory of the current device.
 cudaError_t init_device_tables();
 

@@ -602,6 +602,7 @@ cudaError_t init_device_tables() {
 cudaError_t launch_assemble(const DevMeshView &m, const DevFreq &f, int prec, void *A, size_t lda, int *status,
                             unsigned long long *n_near, cudaStream_t st) {
     dim3 block(32, 8), grid((m.n + 31) / 32, (m.n + 7) / 8);
+    count_launches(1);
     if (prec == 0)
         k_assemble<double><<<grid, block, 0, st>>>(m, f, (double2 *)A, lda, status, n_near);
     else
@@ -611,12 +612,14 @@ cudaError_t launch_assemble(const DevMeshView &m, const DevFreq &f, int prec, vo
 
 cudaError_t launch_rhs(const DevMeshView &m, const DevFreq &f, double *b, int *status, cudaStream_t st) {
     dim3 block(32, 8), grid((m.n + 7) / 8);
+    count_launches(1);
     k_rhs<<<grid, block, 0, st>>>(m, f, (double2 *)b, status);
     return cudaGetLastError();
 }
 
 cudaError_t launch_fields(const DevMeshView &m, const DevFreq &f, const double *x, double *phi, double *vel,
                           int *ivi, cudaStream_t st) {
+    count_launches(1);
     k_fields<<<(m.n + 255) / 256, 256, 0, st>>>(m, f, (const double2 *)x, (double2 *)phi, (double2 *)vel, ivi);
     return cudaGetLastError();
 }
@@ -626,6 +629,7 @@ cudaError_t launch_project(const DevMeshView &m, const DevFreq &f, int prec, con
                            cudaStream_t st) {
     if (npts <= 0) return cudaSuccess;
     dim3 block(32, 8), grid((npts + 7) / 8);
+    count_launches(1);
     if (prec == 0)
         k_project<double><<<grid, block, 0, st>>>(m, f, (const double2 *)phi, (const double2 *)vel, ivi, npts, pts,
                                                   (double2 *)pot, (double2 *)grad, status);

@@ -10,6 +10,8 @@
 // in registers and are reduced across the warp in FP64 at the end.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "bem_internal.h"
 
 namespace bem {
@@ -265,11 +267,17 @@ __global__ void k_update_x(const double2 *__restrict__ V, int ldv, int nv, const
     x[i] = acc;
 }
 
+std::atomic<long long> g_launches{0};
+
 }  // namespace
+
+void count_launches(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+long long launches() { return g_launches.load(std::memory_order_relaxed); }
 
 cudaError_t launch_matvec(int prec, bool exact, const void *A, int n, size_t lda, const double *x,
                           const double *r_in, double *y, void *xf, cudaStream_t st) {
     const int grid = (n + kRowsPerBlock - 1) / kRowsPerBlock;
+    count_launches(prec == 0 ? 1 : 2);
     if (prec == 0) {
         k_matvec64<<<grid, 256, 0, st>>>((const double2 *)A, n, lda, (const double2 *)x, (const double2 *)r_in,
                                          (double2 *)y);
@@ -286,12 +294,14 @@ cudaError_t launch_matvec(int prec, bool exact, const void *A, int n, size_t lda
 }
 
 cudaError_t launch_multi_dot(const double *V, int ldv, int nv, const double *w, int n, double *h, cudaStream_t st) {
+    count_launches(1);
     k_multi_dot<<<nv, 512, 0, st>>>((const double2 *)V, ldv, (const double2 *)w, n, (double2 *)h);
     return cudaGetLastError();
 }
 
 cudaError_t launch_multi_axpy(const double *V, int ldv, int nv, const double *h, double *hacc, double *w, int n,
                               cudaStream_t st) {
+    count_launches(1);
     k_multi_axpy<<<(n + 255) / 256, 256, nv * sizeof(double2), st>>>((const double2 *)V, ldv, nv,
                                                                      (const double2 *)h, (double2 *)hacc,
                                                                      (double2 *)w, n);
@@ -299,16 +309,19 @@ cudaError_t launch_multi_axpy(const double *V, int ldv, int nv, const double *h,
 }
 
 cudaError_t launch_norm2(const double *w, int n, double *out, cudaStream_t st) {
+    count_launches(1);
     k_norm2<<<1, 512, 0, st>>>((const double2 *)w, n, out);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scale_inv(const double *w, const double *nrm2, double *v, int n, cudaStream_t st) {
+    count_launches(1);
     k_scale_inv<<<(n + 255) / 256, 256, 0, st>>>((const double2 *)w, nrm2, (double2 *)v, n);
     return cudaGetLastError();
 }
 
 cudaError_t launch_update_x(const double *V, int ldv, int nv, const double *y, double *x, int n, cudaStream_t st) {
+    count_launches(1);
     k_update_x<<<(n + 255) / 256, 256, nv * sizeof(double2), st>>>((const double2 *)V, ldv, nv,
                                                                     (const double2 *)y, (double2 *)x, n);
     return cudaGetLastError();

@@ -1,0 +1,76 @@
+"""The drop-in NumCalc end to end on the GPU: same files and numbers as the
+reference NumCalc on the same project (reference results from
+tests/golden/sphere80.npz, printed there with 17 digits, here with NumCalc's
+7-digit format)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from mesh2hrtf_gb300 import build, meshes, project
+from tests import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def numcalc():
+    build.build_all()
+    return build.NUMCALC_BIN
+
+
+def _project(tmp_path):
+    c = gc.load("sphere80")
+    ps = c["point_sources"]
+    sh = [c.pts[:24], c.pts[24:]]
+    p = project.Project(root=str(tmp_path / "p"), nodes=c.nodes, elems=c.elems, eval_points=c.pts,
+                        eval_elems=meshes.shells_triangles(sh), freqs=list(c.freqs),
+                        point_sources=[tuple(ps[0])], boundary=["ELEM 0 TO 79 VELO 0.0 -1 0.0 -1"])
+    return c, project.write_project(p)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 2e-6), ("mixed", 1e-5)])
+def test_be_out_matches_reference(numcalc, tmp_path, precision, tol):
+    c, wd = _project(tmp_path)
+    env = dict(os.environ, NUMCALC_GB300_PRECISION=precision)
+    r = subprocess.run([numcalc], cwd=wd, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:]
+    out = open(os.path.join(wd, "NC.out")).read()
+    assert out.count(">> S T E P   N U M B E R   A N D   F R E Q U E N C Y <<") == 2
+    assert "CGS solver: number of iterations = " in out and "End time:" in out
+    assert "Assembling the equation system         : " in out
+    for s in (1, 2):
+        for f in ("pBoundary", "vBoundary", "pEvalGrid", "vEvalGrid"):
+            ids, vals = project.read_result(os.path.join(wd, "be.out", "be.%d" % s, f))
+            assert np.array_equal(ids, c["s%d_%s_ids" % (s, f)])
+            ref = c["s%d_%s" % (s, f)]
+            if np.abs(ref).max() == 0:
+                assert np.abs(vals).max() == 0
+            else:
+                assert gc.rel_err(vals, ref) < tol, (s, f, gc.rel_err(vals, ref))
+
+
+@pytest.mark.parametrize("nitermax", [0, 1, 2])
+def test_nitermax_reports_limit(numcalc, tmp_path, nitermax):
+    c, wd = _project(tmp_path)
+    r = subprocess.run([numcalc, "-nitermax", str(nitermax)], cwd=wd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:]
+    out = open(os.path.join(wd, "NC.out")).read()
+    assert "CGS solver: number of iterations = %d" % nitermax in out
+    assert "Warning: Maximum number of iterations is reached!" in out
+    # the step still ends with a converged solution
+    ids, vals = project.read_result(os.path.join(wd, "be.out", "be.1", "pEvalGrid"))
+    assert gc.rel_err(vals, c["s1_pEvalGrid"]) < 1e-5
+
+
+def test_istart_iend_keeps_other_steps(numcalc, tmp_path):
+    c, wd = _project(tmp_path)
+    assert subprocess.run([numcalc, "-istart", "2", "-iend", "2"], cwd=wd, capture_output=True).returncode == 0
+    assert os.path.exists(os.path.join(wd, "NC2-2.out"))
+    assert os.path.exists(os.path.join(wd, "be.out", "be.2", "pEvalGrid"))
+    assert not os.path.exists(os.path.join(wd, "be.out", "be.1"))
+    assert subprocess.run([numcalc, "-istart", "1", "-iend", "1"], cwd=wd, capture_output=True).returncode == 0
+    assert os.path.exists(os.path.join(wd, "be.out", "be.2", "pEvalGrid"))
+    out = open(os.path.join(wd, "NC1-1.out")).read()
+    assert "Step 1," in out and "Step 2," not in out
