@@ -273,7 +273,7 @@ def main():
     e2e_val, h2d, d2h = None, 0, 0
     t0 = time.perf_counter()
     e2e_steps = max(1, min(args.steps, 2))
-    for s in range(e2e_steps):
+    for s in range(args.warmup, args.warmup + e2e_steps):
         m2 = capi.Mesh(v, f, device=dev)
         s2 = capi.Solver(m2, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000)
         for fr in batch_freqs(s):

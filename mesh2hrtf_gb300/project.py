@@ -109,7 +109,7 @@ def write_project(p: Project, source_dir: str = "source_1") -> str:
         "0 0 0 0",
         "##",
         "## 4. Main Parameters IV",
-        "%s %se+00 1.0 0.0e+00 0.0 e+00 0.0e+00 0.0e+00" % (repr(p.speed_of_sound), repr(p.density)),
+        "%s %se+00 1.0 0.0e+00 0.0 e+00 0.0e+00 0.0e+00" % (repr(float(p.speed_of_sound)), repr(float(p.density))),
         "##",
         "NODES",
         "../../ObjectMeshes/Reference/Nodes.txt",
@@ -129,12 +129,12 @@ def write_project(p: Project, source_dir: str = "source_1") -> str:
     if p.plane_waves:
         lines.append("PLANE WAVES")
         for i, (dx, dy, dz, ar, ai) in enumerate(p.plane_waves):
-            lines.append("%d %s %s %s %s -1 %s -1" % (i, _fmt(dx), _fmt(dy), _fmt(dz), repr(ar), repr(ai)))
+            lines.append("%d %s %s %s %s -1 %s -1" % (i, _fmt(dx), _fmt(dy), _fmt(dz), repr(float(ar)), repr(float(ai))))
         lines.append("##")
     if p.point_sources:
         lines.append("POINT SOURCES")
         for i, (x, y, z, ar, ai) in enumerate(p.point_sources):
-            lines.append("%d %s %s %s %s -1 %s -1" % (i, _fmt(x), _fmt(y), _fmt(z), repr(ar), repr(ai)))
+            lines.append("%d %s %s %s %s -1 %s -1" % (i, _fmt(x), _fmt(y), _fmt(z), repr(float(ar)), repr(float(ai))))
         lines.append("##")
     if p.curves:
         lines.append("CURVES")
