@@ -171,6 +171,35 @@ bem_status bem_get_system(bem_solver_t solver, int32_t row0, int32_t row1,
 bem_status bem_project(bem_solver_t solver, int32_t n_pts, const double *pts,
                        double *pot_out, double *grad_out);
 
+/* Field projection that allocates nothing.
+ *
+ * Same result as bem_project, but points and outputs are device pointers the
+ * caller owns and the call makes no device allocation (no cudaMalloc,
+ * cudaFree or allocating library routine): its scratch lives in a fixed
+ * device array inside the library.  It is meant for callers that must not
+ * allocate once they are running, for example a real-time renderer or audio
+ * plug-in host that evaluates the solved field at new listener positions on
+ * every processing block (an allocation there can block or synchronize the
+ * device), or code that manages all device memory through its own pool.
+ * No counterpart in the reference (NumCalc only projects onto the grids of
+ * NC.inp, NC_PostProcessing.cpp:581-773).
+ *
+ * Limits and rules:
+ *  - at most BEM_STATIC_MAX_ELEMENTS boundary elements (larger solvers get
+ *    BEM_ERR_INVALID); the scratch array (about 2.8 MB) is held on every
+ *    device that loads the library until the process exits;
+ *  - the first call on a device looks up the array's device address; make
+ *    that first call before any stream capture;
+ *  - all calls share the one array, so calls that overlap on the GPU (other
+ *    streams, other threads) race: serialize them;
+ *  - the call runs on `stream` (a cudaStream_t, NULL for the legacy default
+ *    stream) and returns after it has finished;
+ *  - pts_dev [n_pts][3] FP64, pot_dev [n_pts] complex, grad_dev [n_pts][3]
+ *    complex or NULL, all device memory. */
+#define BEM_STATIC_MAX_ELEMENTS 32768
+bem_status bem_project_static(bem_solver_t solver, int32_t n_pts, const double *pts_dev,
+                              double *pot_dev, double *grad_dev, void *stream);
+
 /* One complete frequency step through host buffers: assemble, solve, copy
  * the unknowns to x_out (may be NULL) and project onto n_pts points.
  * The sequence NC_Main.cpp:744-907 runs per frequency. */

@@ -30,8 +30,9 @@ EXPORTED = [
     "bem_last_error", "bem_version", "bem_kernel_launches", "bem_set_device", "bem_footprint_bytes",
     "bem_mesh_create", "bem_mesh_destroy", "bem_solver_create", "bem_solver_destroy", "bem_solver_set_params",
     "bem_assemble", "bem_solve", "bem_get_solution", "bem_get_system", "bem_project",
-    "bem_solve_frequency",
+    "bem_solve_frequency", "bem_project_static",
 ]
+STATIC_MAX_ELEMENTS = 32768
 
 
 class BemError(RuntimeError):
@@ -98,6 +99,7 @@ def load(build_if_missing: bool = True):
     lib.bem_get_system.argtypes = [vp, i32, i32, vp, vp]
     lib.bem_project.argtypes = [vp, i32, vp, vp, vp]
     lib.bem_solve_frequency.argtypes = [vp, C.POINTER(FreqDesc), i32, vp, vp, vp, vp, C.POINTER(SolveInfo)]
+    lib.bem_project_static.argtypes = [vp, i32, vp, vp, vp, vp]
     for name in EXPORTED:
         if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes", "bem_kernel_launches"):
             getattr(lib, name).restype = C.c_int
@@ -215,6 +217,10 @@ class Solver:
         grad = np.zeros((len(pts), 3), np.complex128) if with_grad else None
         _check(load().bem_project(self.handle, len(pts), _ptr(pts), _ptr(pot), _ptr(grad)))
         return pot, grad
+
+    def project_static(self, n_pts, pts_dev, pot_dev, grad_dev=None, stream=None):
+        """bem_project_static: device pointers in and out, no allocation."""
+        return _check(load().bem_project_static(self.handle, n_pts, pts_dev, pot_dev, grad_dev, stream))
 
     def solve_frequency(self, freq: Frequency, pts, with_grad=True, allow_not_converged=False):
         pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)

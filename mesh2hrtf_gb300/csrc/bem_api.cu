@@ -668,3 +668,30 @@ bem_status bem_solve_frequency(bem_solver_t s, const bem_frequency_desc *f, int3
 }
 
 }  // extern "C"
+
+namespace bem {
+
+// Inputs of the projection kernels held by a solved solver (for
+// bem_project_static in bem_static.cu).
+bool solver_projection_inputs(bem_solver_t s, int max_elem, DevMeshView *m, DevFreq *f, int *prec,
+                              const double **x, int *n) {
+    if (!s) { g_err = "null solver"; return false; }
+    if (s->n > max_elem) {
+        char buf[160];
+        snprintf(buf, sizeof(buf), "bem_project_static: %d boundary elements, limit BEM_STATIC_MAX_ELEMENTS = %d",
+                 s->n, max_elem);
+        g_err = buf;
+        return false;
+    }
+    if (!s->solved) { g_err = "bem_project_static before bem_solve"; return false; }
+    *m = s->mesh->view();
+    *f = s->freq;
+    *prec = s->prec;
+    *x = s->x;
+    *n = s->n;
+    return true;
+}
+
+void set_error(const char *msg) { g_err = msg; }
+
+}  // namespace bem
