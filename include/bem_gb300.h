@@ -93,6 +93,8 @@ typedef struct {
     double tol;                /* relative residual target (0 = 1e-9)          */
     double hbm_budget_bytes;   /* admission budget for this solver (0 = all
                                   free device memory minus a reserve)          */
+    int32_t no_precond;        /* 0: block-Jacobi preconditioner (default),
+                                  1: none                                      */
 } bem_solver_params;
 
 typedef struct {
@@ -117,7 +119,8 @@ int64_t bem_kernel_launches(void);
 /* Select the CUDA device for this thread's subsequent calls. */
 bem_status bem_set_device(int32_t device);
 /* Bytes a solver for n_elem unknowns holds on the device (matrix, Krylov
- * basis, work vectors) at the given precision and restart length: the HBM
+ * basis, preconditioner, work vectors) at the given precision and restart
+ * length: the HBM
  * admission footprint (NumCalc's host RAM estimate, NC_Main.cpp:524-541,
  * counts (N + N^2) * 16 bytes for the same data). */
 double bem_footprint_bytes(int32_t n_elem, int32_t precision, int32_t restart);

@@ -47,8 +47,39 @@ template <typename T> __device__ __forceinline__ cplx<T> warp_sum(cplx<T> v) {
     return {warp_sum(v.re), warp_sum(v.im)};
 }
 
+// sin and cos of a float phase k*r: Cody & Waite argument reduction by pi/2
+// (FMA variant, pi/2 split into three floats), then the Taylor polynomials of
+// sin (through r^9) and cos (through r^10) on |r| <= pi/4, whose truncation
+// error (< 3e-9) is below float rounding.  Phases in this library stay below
+// ~10^3, where the reduction is accurate to a few float ulps.
+//
+// The quadrant is rounded with the 1.5*2^23 shifter instead of rintf/F2I: on
+// GB300 conversion instructions share the narrow FP64 pipe, while the shifter
+// needs only FP32 adds and integer bit operations.
+__device__ __forceinline__ void phase_sincos(float x, float *s, float *c) {
+    const float sh = fmaf(x, 0.636619772f, 12582912.0f);   // 1.5 * 2^23
+    const int qi = __float_as_int(sh);                      // low bits: round(x 2/pi)
+    const float q = sh - 12582912.0f;
+    float r = fmaf(q, -1.57079637050628662f, x);
+    r = fmaf(q, 4.37113882867379e-08f, r);
+    r = fmaf(q, 1.71512451000588e-15f, r);
+    const float r2 = r * r;
+    float ps = fmaf(r2, 2.755731922e-6f, -1.984126984e-4f);
+    ps = fmaf(ps, r2, 8.333333333e-3f);
+    ps = fmaf(ps, r2, -0.1666666667f);
+    const float sn = fmaf(ps * r2, r, r);
+    float pc = fmaf(r2, -2.755731922e-7f, 2.480158730e-5f);
+    pc = fmaf(pc, r2, -1.388888889e-3f);
+    pc = fmaf(pc, r2, 4.166666667e-2f);
+    pc = fmaf(pc, r2, -0.5f);
+    const float cs = fmaf(pc, r2, 1.0f);
+    float so = (qi & 1) ? cs : sn, co = (qi & 1) ? sn : cs;
+    *s = (qi & 2) ? -so : so;
+    *c = ((qi + 1) & 2) ? -co : co;
+}
+
 __device__ __forceinline__ void sincos_t(double x, double *s, double *c) { sincos(x, s, c); }
-__device__ __forceinline__ void sincos_t(float x, float *s, float *c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_t(float x, float *s, float *c) { phase_sincos(x, s, c); }
 __device__ __forceinline__ double sqrt_t(double x) { return sqrt(x); }
 __device__ __forceinline__ float sqrt_t(float x) { return sqrtf(x); }
 
@@ -129,6 +160,7 @@ struct DevMesh {
     const float *t32;       // 10 rows (triangles): a = P0-P2, b = P1-P2, n, J
     const float *q32;       // 12 rows (quads): vertex offsets from the centre
     const float *isqa32;    // 1 / sqrt(areael) in float (approximate ratios)
+    const float *n32;       // 3 rows: centre normal in float
 };
 
 // One element in registers (FP64), for decisions and the FP64 arithmetic.
@@ -187,6 +219,7 @@ __device__ __forceinline__ double ratio0_exact(const DevMesh &m, int j, const do
 template <typename T> struct QPoint {
     T d[3];    // y - x
     T r;       // |y - x|
+    T ir;      // 1 / r
     T ny[3];   // unit normal at y
     T wj;      // weight * Jacobian
     T sh[4];   // shape functions at y (for interpolating nodal data)
@@ -225,6 +258,7 @@ __device__ __forceinline__ void map_point(const Elem64 &e, double s, double t, c
 #pragma unroll
     for (int k = 0; k < 3; ++k) q.d[k] = y[k] - x[k];
     q.r = sqrt(q.d[0] * q.d[0] + q.d[1] * q.d[1] + q.d[2] * q.d[2]);
+    q.ir = 1.0 / q.r;
 #pragma unroll
     for (int a = 0; a < 4; ++a) q.sh[a] = sh[a];
 }
@@ -302,7 +336,9 @@ __device__ __forceinline__ void map_point(const Elem32 &e, float s, float t, flo
 #pragma unroll
         for (int a = 0; a < 4; ++a) q.sh[a] = sh[a];
     }
-    q.r = sqrtf(q.d[0] * q.d[0] + q.d[1] * q.d[1] + q.d[2] * q.d[2]);
+    const float r2 = q.d[0] * q.d[0] + q.d[1] * q.d[1] + q.d[2] * q.d[2];
+    q.ir = rsqrtf(r2);
+    q.r = r2 * q.ir;
 }
 
 // Kernel values of one quadrature point for a collocation point with normal
@@ -315,7 +351,7 @@ template <typename T> struct KVals { cplx<T> G, H, HT, E; };
 
 template <typename T>
 __device__ __forceinline__ KVals<T> kernel_values(const QPoint<T> &q, const T nx[3], T k, T wr) {
-    T r = q.r, ir = T(1) / r;
+    const T r = q.r, ir = q.ir;
     T s, c;
     sincos_t(wr * r, &s, &c);
     T amp = q.wj * T(1.0 / kPI4) * ir;

@@ -12,12 +12,13 @@ struct DevMeshView {
     int n;
     const int *nvert;
     const double *v64, *c64, *n64, *area64, *sqa64;
-    const float *chi, *clo, *t32, *q32, *isqa32;
+    const float *chi, *clo, *t32, *q32, *isqa32, *n32;
 };
 
 // One frequency's data on the device.
 struct DevFreq {
     double k, wr, tao, beta_im;
+    float kf, wrf, taof, beta_imf;   // the same in float
     const int *bc_type;        // [n] or nullptr (all velocity)
     const double *bc_val;      // [4][n] complex (row a = node a), or nullptr
     const double *adm;         // [n] complex, or nullptr
@@ -30,6 +31,9 @@ struct DevFreq {
     const double *pw_amp;      // [n_plane] complex
 };
 
+// Unknowns per diagonal block of the block-Jacobi preconditioner.
+constexpr int kBlock = 128;
+
 // Process-wide count of kernel launches issued by the launch_* functions.
 void count_launches(int k);
 long long launches();
@@ -37,11 +41,14 @@ long long launches();
 // Copies the quadrature tables into constant memory of the current device.
 cudaError_t init_device_tables();
 
+// Pairs integrated with subdivision plus self pairs, (row, column);
+// list == nullptr only counts.
+cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long *count, cudaStream_t st);
 // A = assembled TBEM matrix, row-major n x n with leading dimension lda,
-// complex128 (prec 0) or complex64 (prec 1).  status: device int receiving
-// subdivision errors.
-cudaError_t launch_assemble(const DevMeshView &m, const DevFreq &f, int prec, void *A, size_t lda, int *status,
-                            unsigned long long *n_near, cudaStream_t st);
+// complex128 (prec 0) or complex64 (prec 1): regular pairs, then the near
+// list.  status: device int receiving subdivision errors.
+cudaError_t launch_assemble(const DevMeshView &m, const DevFreq &f, int prec, void *A, size_t lda,
+                            const int2 *near_list, long long n_near, int *status, cudaStream_t st);
 // b = free terms + incident waves + columns with prescribed values (FP64).
 cudaError_t launch_rhs(const DevMeshView &m, const DevFreq &f, double *b, int *status, cudaStream_t st);
 // Element potentials and nodal normal velocities from the unknowns x.
@@ -53,6 +60,16 @@ cudaError_t launch_project(const DevMeshView &m, const DevFreq &f, int prec, con
                            double *pot, double *grad, int *status, cudaStream_t st);
 
 // ---- Krylov building blocks (bem_krylov.cu); vectors are complex128 ----
+// Device-side control word of one GMRES cycle.  Kernels given `done` return
+// at once when it is set, so the host can queue several Arnoldi steps ahead
+// and check convergence once per batch.
+struct GmresCtrl {
+    int done;     // residual estimate reached thr (or breakdown)
+    int kdone;    // Arnoldi steps completed in this cycle
+    double res;   // |g[k+1]| after the last step
+    double thr;   // absolute residual target of the cycle
+};
+
 // y = A x for a row-major n x n matrix with leading dimension lda
 // (r_in != nullptr: y = r_in - A x).
 // prec 0: complex128 A, FP64 arithmetic.
@@ -63,19 +80,39 @@ cudaError_t launch_project(const DevMeshView &m, const DevFreq &f, int prec, con
 //   accuracy (the refinement residual).
 // xf: scratch of 2 * n float2 for the split of x.
 cudaError_t launch_matvec(int prec, bool exact, const void *A, int n, size_t lda, const double *x,
-                          const double *r_in, double *y, void *xf, cudaStream_t st);
-// h[l] = <V[l], w> (conjugated in V) for l < nv; V has leading dimension ldv.
-cudaError_t launch_multi_dot(const double *V, int ldv, int nv, const double *w, int n, double *h,
-                             cudaStream_t st);
-// w -= sum_l h[l] V[l];  optionally hacc[l] += h[l].
-cudaError_t launch_multi_axpy(const double *V, int ldv, int nv, const double *h, double *hacc, double *w,
-                              int n, cudaStream_t st);
+                          const double *r_in, double *y, void *xf, cudaStream_t st, const int *done = nullptr);
+// Blocks of partial sums used by launch_multi_dot.
+int dot_blocks(int n);
+// h[l] = <V[l], w> (conjugated in V) for l < nv, V with leading dimension
+// ldv (complex entries); hsum[l] += h[l] if hsum != nullptr.  partial: nv *
+// dot_blocks(n) complex scratch.
+cudaError_t launch_multi_dot(const double *V, size_t ldv, int nv, const double *w, int n, double *partial,
+                             double *h, double *hsum, cudaStream_t st, const int *done = nullptr);
+// w -= sum_l h[l] V[l]
+cudaError_t launch_multi_axpy(const double *V, size_t ldv, int nv, const double *h, double *w, int n,
+                              cudaStream_t st, const int *done = nullptr);
 // out[0] = ||w||^2
 cudaError_t launch_norm2(const double *w, int n, double *out, cudaStream_t st);
 // v = w * (1 / sqrt(nrm2[0]))
-cudaError_t launch_scale_inv(const double *w, const double *nrm2, double *v, int n, cudaStream_t st);
+cudaError_t launch_scale_inv(const double *w, const double *nrm2, double *v, int n, cudaStream_t st,
+                             const int *done = nullptr);
+// Givens step k of the cycle on the device (see GmresCtrl).
+cudaError_t launch_givens(int k, int m, double *hsum, const double *wnorm2, double *H, double *cs, double *sn,
+                          double *g, GmresCtrl *ctrl, cudaStream_t st);
 // x += sum_l y[l] V[l]  (y complex on the device)
 cudaError_t launch_update_x(const double *V, int ldv, int nv, const double *y, double *x, int n,
                             cudaStream_t st);
+
+// ---- block-Jacobi preconditioner (bem_precond.cu) ----
+size_t precond_bytes(int n, int prec);
+// Inverts the kBlock x kBlock diagonal blocks of A into Minv (transposed
+// blocks); FP64 uses `work` (same size as Minv) as inversion workspace.
+cudaError_t launch_block_inverse(int prec, const void *A, size_t lda, int n, void *Minv, void *work, int *status,
+                                 cudaStream_t st);
+// z = M^{-1} v
+cudaError_t launch_block_apply(int prec, const void *Minv, int n, const double *v, double *z, cudaStream_t st,
+                               const int *done = nullptr);
+// x += z
+cudaError_t launch_axpy(const double *z, double *x, int n, cudaStream_t st);
 
 }  // namespace bem

@@ -25,7 +25,7 @@ __device__ __forceinline__ DevMesh to_dev(const DevMeshView &v) {
     DevMesh m;
     m.n = v.n; m.nvert = v.nvert; m.v64 = v.v64; m.c64 = v.c64; m.n64 = v.n64;
     m.area64 = v.area64; m.sqa64 = v.sqa64; m.chi = v.chi; m.clo = v.clo; m.t32 = v.t32;
-    m.q32 = v.q32; m.isqa32 = v.isqa32;
+    m.q32 = v.q32; m.isqa32 = v.isqa32; m.n32 = v.n32;
     return m;
 }
 
@@ -112,109 +112,161 @@ __device__ __forceinline__ cplx<T> col_adm(const DevFreq &f, int j, int bc) {
     return {(T)a.re, (T)a.im};
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_assemble(DevMeshView mv, DevFreq f,
-                                                  typename Vec2<T>::type *__restrict__ A, size_t lda,
-                                                  int *status, unsigned long long *n_near) {
-    __shared__ WarpScratch ws_all[8];
+// ------------------------------------------------------------ near list
+// Pairs (row i, column j) that NumCalc integrates with subdivision (level-0
+// ratio distance/sqrt(area) < 1.3, exact FP64 test) plus the self pairs.
+// Depends on the geometry only, so it is built once per mesh.  Pass 1
+// (list == nullptr) counts, pass 2 fills; warp-aggregated atomics.
+__global__ void __launch_bounds__(256) k_near_list(DevMeshView mv, int2 *list, unsigned long long *count) {
     const DevMesh m = to_dev(mv);
-    const int lane = threadIdx.x, w = threadIdx.y;
-    const int n = m.n;
-    const int i = blockIdx.y * 8 + w;
+    const int lane = threadIdx.x, n = m.n;
+    const int i = blockIdx.y * 8 + threadIdx.y;
     const int j = blockIdx.x * 32 + lane;
-    if (i >= n) return;  // uniform per warp
-    WarpScratch &ws = ws_all[w];
-    const bool valid = j < n;
-
-    const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
-    const double nx64[3] = {m.n64[i], m.n64[n + i], m.n64[2 * n + i]};
-    const float xhi[3] = {m.chi[i], m.chi[n + i], m.chi[2 * n + i]};
-    const float xlo[3] = {m.clo[i], m.clo[n + i], m.clo[2 * n + i]};
-    const float nx32[3] = {(float)nx64[0], (float)nx64[1], (float)nx64[2]};
-    Phys<double> P{f.k, f.wr, f.tao, f.beta_im};
-    Phys<T> PT{(T)f.k, (T)f.wr, (T)f.tao, (T)f.beta_im};
-
-    const int bcj = (valid && f.bc_type) ? f.bc_type[j] : 0;
+    if (i >= n) return;
     bool near = false;
-    int order = 2;
-    cplx<T> val = {T(0), T(0)};
-    if (valid && j != i) {
-        if constexpr (std::is_same<T, double>::value) {
-            const double rd = ratio0_exact(m, j, x64);
-            near = rd < kTolf;
-            if (!near) order = gauss_order(rd);
-            if (!near) {
-                Elem64 e;
-                load_elem64(m, j, e);
-                KVals<double> v = FarPair<double>::run(e, x64, nx64, order, f.k, f.wr);
-                val = combine_entry(v, bcj, col_adm<double>(f, j, bcj), PT);
+    if (j < n) {
+        if (j == i) near = true;
+        else {
+            const float d0 = (m.chi[j] - m.chi[i]) + (m.clo[j] - m.clo[i]);
+            const float d1 = (m.chi[n + j] - m.chi[n + i]) + (m.clo[n + j] - m.clo[n + i]);
+            const float d2 = (m.chi[2 * n + j] - m.chi[2 * n + i]) + (m.clo[2 * n + j] - m.clo[2 * n + i]);
+            const float rf = sqrtf(d0 * d0 + d1 * d1 + d2 * d2) * m.isqa32[j];
+            if (rf <= 1.3f * (1.0f + 1e-4f)) {
+                const double x[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
+                near = ratio0_exact(m, j, x) < kTolf;
             }
-        } else {
-            Elem32 e;
-            load_elem32(m, j, xhi, xlo, e);
-            const float dist = sqrtf(e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]);
-            const float rf = dist * m.isqa32[j];
+        }
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, near);
+    if (!mask) return;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (near && list) list[base + __popc(mask & ((1u << lane) - 1u))] = make_int2(i, j);
+}
+
+// ------------------------------------------------------------ regular pairs
+// Regular (not subdivided) pairs: block of 8 warps, every warp 4 rows x 32
+// columns, one column per lane.  The column element is loaded once per lane
+// and reused for its 4 rows; entries go out as coalesced row segments.  Near
+// and self pairs are skipped here and written by k_near.
+constexpr int kRowsPerThread = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(256, 3) k_far(DevMeshView mv, DevFreq f, typename Vec2<T>::type *__restrict__ A,
+                                             size_t lda) {
+    const DevMesh m = to_dev(mv);
+    const int lane = threadIdx.x, n = m.n;
+    const int i0 = (blockIdx.y * 8 + threadIdx.y) * kRowsPerThread;
+    const int j = blockIdx.x * 32 + lane;
+    if (i0 >= n || j >= n) return;
+    Phys<T> PT;
+    if constexpr (std::is_same<T, double>::value) PT = {f.k, f.wr, f.tao, f.beta_im};
+    else PT = {f.kf, f.wrf, f.taof, f.beta_imf};
+    const int bcj = f.bc_type ? f.bc_type[j] : 0;
+    const cplx<T> admj = col_adm<T>(f, j, bcj);
+    if constexpr (std::is_same<T, double>::value) {
+        Elem64 e;
+        load_elem64(m, j, e);
+        for (int r = 0; r < kRowsPerThread; ++r) {
+            const int i = i0 + r;
+            if (i >= n) break;
+            if (i == j) continue;
+            const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
+            const double rd = ratio0_exact(m, j, x64);
+            if (rd < kTolf) continue;
+            const double nx64[3] = {m.n64[i], m.n64[n + i], m.n64[2 * n + i]};
+            KVals<double> v = FarPair<double>::run(e, x64, nx64, gauss_order(rd), f.k, f.wr);
+            const cplx<double> val = combine_entry(v, bcj, admj, PT);
+            A[(size_t)i * lda + j] = make_double2(val.re, val.im);
+        }
+    } else {
+        Elem32 e;
+        const float zero[3] = {0.f, 0.f, 0.f};
+        load_elem32(m, j, zero, zero, e);
+        const float cjh[3] = {m.chi[j], m.chi[n + j], m.chi[2 * n + j]};
+        const float cjl[3] = {m.clo[j], m.clo[n + j], m.clo[2 * n + j]};
+        const float isq = m.isqa32[j];
+        for (int r = 0; r < kRowsPerThread; ++r) {
+            const int i = i0 + r;
+            if (i >= n) break;
+            if (i == j) continue;
+            for (int k = 0; k < 3; ++k) e.D[k] = (cjh[k] - m.chi[k * n + i]) + (cjl[k] - m.clo[k * n + i]);
+            const float rf = sqrtf(e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * isq;
+            bool near = false;
+            int order = 2;
             if (!classify_fast(rf, near, order)) {
+                const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
                 const double rd = ratio0_exact(m, j, x64);
                 near = rd < kTolf;
                 if (!near) order = gauss_order(rd);
             }
-            if (!near) {
-                KVals<float> v = FarPair<float>::run(e, nx32, order, PT.k, PT.wr);
-                val = combine_entry(v, bcj, col_adm<float>(f, j, bcj), PT);
-            }
+            if (near) continue;
+            const float nx[3] = {m.n32[i], m.n32[n + i], m.n32[2 * n + i]};
+            KVals<float> v = FarPair<float>::run(e, nx, order, PT.k, PT.wr);
+            const cplx<float> val = combine_entry(v, bcj, admj, PT);
+            A[(size_t)i * lda + j] = make_float2(val.re, val.im);
         }
     }
+}
 
-    // pairs that need the whole warp: subdivided ones and the self element
-    const unsigned near_mask = __ballot_sync(0xffffffffu, valid && near);
-    unsigned todo = __ballot_sync(0xffffffffu, valid && (near || j == i));
+// ------------------------------------------------------------ near pairs
+// One warp per entry of the near list: the self pair by warp_singular (FP64,
+// plus NumCalc's free term), subdivided pairs by warp_subdivide with the
+// kernel arithmetic in T.
+template <typename T>
+__global__ void __launch_bounds__(256) k_near(DevMeshView mv, DevFreq f, const int2 *__restrict__ list, long long count,
+                                              typename Vec2<T>::type *__restrict__ A, size_t lda, int *status) {
+    __shared__ WarpScratch ws_all[8];
+    const DevMesh m = to_dev(mv);
+    const int lane = threadIdx.x, n = m.n;
+    const long long idx = (long long)blockIdx.x * 8 + threadIdx.y;
+    if (idx >= count) return;
+    WarpScratch &ws = ws_all[threadIdx.y];
+    const int2 ij = list[idx];
+    const int i = ij.x, j = ij.y;
+    const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
+    const double nx64[3] = {m.n64[i], m.n64[n + i], m.n64[2 * n + i]};
+    Phys<double> P{f.k, f.wr, f.tao, f.beta_im};
+    Phys<T> PT{(T)f.k, (T)f.wr, (T)f.tao, (T)f.beta_im};
+    const int bcj = f.bc_type ? f.bc_type[j] : 0;
+    Elem64 e;
+    load_elem64(m, j, e);
+    cplx<T> entry;
     int err = kDevOk;
-    while (todo) {
-        const int L = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const int jl = __shfl_sync(0xffffffffu, j, L);
-        const int bcl = __shfl_sync(0xffffffffu, bcj, L);
-        Elem64 e;
-        load_elem64(m, jl, e);
-        cplx<T> entry;
-        if (jl == i) {
-            SingOut so = warp_singular(e, x64, nx64, P, 0, nullptr);
-            cplx<double> a = combine_entry(so.v, bcl, col_adm<double>(f, jl, bcl), P);
-            // free term, NC_EquationSystem.cpp:220-231
-            const cplx<double> beta = {0.0, P.beta_im};
-            if (bcl == 1) a += beta * (-(0.5 * P.tao));
-            else a += (col_adm<double>(f, jl, bcl) * beta - cplx<double>{1.0, 0.0}) * 0.5;
-            entry = {(T)a.re, (T)a.im};
-        } else if constexpr (std::is_same<T, double>::value) {
-            AsmSink<double> sink;
-            sink.e = &e; sink.x = x64; sink.nx = nx64; sink.k = f.k; sink.wr = f.wr;
-            sink.init();
-            const int rc = warp_subdivide(e, m.area64[jl], x64, ws, sink);
-            if (rc != kDevOk) err = rc;
-            KVals<double> v = sink.reduce();
-            entry = combine_entry(v, bcl, col_adm<double>(f, jl, bcl), PT);
-        } else {
-            Elem32 e32;
-            load_elem32(m, jl, xhi, xlo, e32);
-            AsmSink<float> sink;
-            sink.e = &e32; sink.nx = nx32; sink.k = PT.k; sink.wr = PT.wr;
-            sink.init();
-            const int rc = warp_subdivide(e, m.area64[jl], x64, ws, sink);
-            if (rc != kDevOk) err = rc;
-            KVals<float> v = sink.reduce();
-            entry = combine_entry(v, bcl, col_adm<float>(f, jl, bcl), PT);
-        }
-        if (lane == L) val = entry;
-    }
-    if (valid) {
-        typename Vec2<T>::type o;
-        o.x = val.re;
-        o.y = val.im;
-        A[(size_t)i * lda + j] = o;
+    if (i == j) {
+        SingOut so = warp_singular(e, x64, nx64, P, 0, nullptr);
+        cplx<double> a = combine_entry(so.v, bcj, col_adm<double>(f, j, bcj), P);
+        // free term, NC_EquationSystem.cpp:220-231
+        const cplx<double> beta = {0.0, P.beta_im};
+        if (bcj == 1) a += beta * (-(0.5 * P.tao));
+        else a += (col_adm<double>(f, j, bcj) * beta - cplx<double>{1.0, 0.0}) * 0.5;
+        entry = {(T)a.re, (T)a.im};
+    } else if constexpr (std::is_same<T, double>::value) {
+        AsmSink<double> sink;
+        sink.e = &e; sink.x = x64; sink.nx = nx64; sink.k = f.k; sink.wr = f.wr;
+        sink.init();
+        err = warp_subdivide(e, m.area64[j], x64, ws, sink);
+        KVals<double> v = sink.reduce();
+        entry = combine_entry(v, bcj, col_adm<double>(f, j, bcj), PT);
+    } else {
+        const float xhi[3] = {m.chi[i], m.chi[n + i], m.chi[2 * n + i]};
+        const float xlo[3] = {m.clo[i], m.clo[n + i], m.clo[2 * n + i]};
+        const float nx32[3] = {(float)nx64[0], (float)nx64[1], (float)nx64[2]};
+        Elem32 e32;
+        load_elem32(m, j, xhi, xlo, e32);
+        AsmSink<float> sink;
+        sink.e = &e32; sink.nx = nx32; sink.k = PT.k; sink.wr = PT.wr;
+        sink.init();
+        err = warp_subdivide(e, m.area64[j], x64, ws, sink);
+        KVals<float> v = sink.reduce();
+        entry = combine_entry(v, bcj, col_adm<float>(f, j, bcj), PT);
     }
     if (lane == 0) {
-        if (near_mask) atomicAdd(n_near, (unsigned long long)__popc(near_mask));
+        typename Vec2<T>::type o;
+        o.x = entry.re;
+        o.y = entry.im;
+        A[(size_t)i * lda + j] = o;
         if (err != kDevOk) atomicMax(status, err);
     }
 }
@@ -599,14 +651,25 @@ cudaError_t init_device_tables() {
     return e;
 }
 
-cudaError_t launch_assemble(const DevMeshView &m, const DevFreq &f, int prec, void *A, size_t lda, int *status,
-                            unsigned long long *n_near, cudaStream_t st) {
+cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long *count, cudaStream_t st) {
     dim3 block(32, 8), grid((m.n + 31) / 32, (m.n + 7) / 8);
     count_launches(1);
-    if (prec == 0)
-        k_assemble<double><<<grid, block, 0, st>>>(m, f, (double2 *)A, lda, status, n_near);
-    else
-        k_assemble<float><<<grid, block, 0, st>>>(m, f, (float2 *)A, lda, status, n_near);
+    k_near_list<<<grid, block, 0, st>>>(m, list, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble(const DevMeshView &m, const DevFreq &f, int prec, void *A, size_t lda,
+                            const int2 *near_list, long long n_near, int *status, cudaStream_t st) {
+    dim3 block(32, 8), grid((m.n + 31) / 32, (m.n + 8 * kRowsPerThread - 1) / (8 * kRowsPerThread));
+    const int nblk = (int)((n_near + 7) / 8);
+    count_launches(2);
+    if (prec == 0) {
+        k_far<double><<<grid, block, 0, st>>>(m, f, (double2 *)A, lda);
+        if (nblk) k_near<double><<<nblk, block, 0, st>>>(m, f, near_list, n_near, (double2 *)A, lda, status);
+    } else {
+        k_far<float><<<grid, block, 0, st>>>(m, f, (float2 *)A, lda);
+        if (nblk) k_near<float><<<nblk, block, 0, st>>>(m, f, near_list, n_near, (float2 *)A, lda, status);
+    }
     return cudaGetLastError();
 }
 

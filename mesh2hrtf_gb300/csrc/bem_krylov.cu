@@ -38,8 +38,10 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 // FP64: y = r_in - A x or A x
 __global__ void __launch_bounds__(256) k_matvec64(const double2 *__restrict__ A, int n, size_t lda,
                                                   const double2 *__restrict__ x,
-                                                  const double2 *__restrict__ r_in, double2 *__restrict__ y) {
+                                                  const double2 *__restrict__ r_in, double2 *__restrict__ y,
+                                                  const int *done) {
     __shared__ double2 xs[kTile];
+    if (done && *done) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int row0 = blockIdx.x * kRowsPerBlock + warp * kRowsPerWarp;
     double re[kRowsPerWarp] = {0.0, 0.0}, im[kRowsPerWarp] = {0.0, 0.0};
@@ -77,9 +79,9 @@ __global__ void __launch_bounds__(256) k_matvec64(const double2 *__restrict__ A,
 }
 
 // split x (complex128) into x_hi + x_lo (complex64 each)
-__global__ void k_split(const double2 *__restrict__ x, float4 *__restrict__ xf, int n) {
+__global__ void k_split(const double2 *__restrict__ x, float4 *__restrict__ xf, int n, const int *done) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (done && *done)) return;
     const double2 v = x[i];
     const float hr = (float)v.x, hi = (float)v.y;
     xf[i] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
@@ -89,8 +91,10 @@ __global__ void k_split(const double2 *__restrict__ x, float4 *__restrict__ xf, 
 // EXACT = true: two-product/two-sum accumulation of A x_hi plus FP32 A x_lo.
 template <bool EXACT>
 __global__ void __launch_bounds__(256) k_matvec32(const float2 *__restrict__ A, int n, size_t lda, const float4 *__restrict__ xf,
-                                                  const double2 *__restrict__ r_in, double2 *__restrict__ y) {
+                                                  const double2 *__restrict__ r_in, double2 *__restrict__ y,
+                                                  const int *done) {
     __shared__ float4 xs[kTile];
+    if (done && *done) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int row0 = blockIdx.x * kRowsPerBlock + warp * kRowsPerWarp;
     float sr[kRowsPerWarp] = {0.f, 0.f}, si[kRowsPerWarp] = {0.f, 0.f};
@@ -175,44 +179,77 @@ __global__ void __launch_bounds__(256) k_matvec32(const float2 *__restrict__ A, 
     }
 }
 
-// h[l] = sum_i conj(V_l[i]) w[i]   (one block per l)
-__global__ void __launch_bounds__(512) k_multi_dot(const double2 *__restrict__ V, int ldv, const double2 *__restrict__ w,
-                                                   int n, double2 *__restrict__ h) {
-    __shared__ double sre[16], sim[16];
-    const int l = blockIdx.x;
-    const double2 *v = V + (size_t)l * ldv;
-    double re = 0.0, im = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double2 a = v[i], b = w[i];
-        re = fma(a.x, b.x, re); re = fma(a.y, b.y, re);
-        im = fma(a.x, b.y, im); im = fma(-a.y, b.x, im);
+// ---- inner products: partial sums per chunk of rows, then a final pass
+// h[l] = sum_i conj(V_l[i]) w[i] for l < nv.  Grid (row chunks, groups of
+// kDotVec vectors): a block owns kDotChunk rows (one per thread) for kDotVec
+// vectors and writes one partial sum per vector: partial[l * nblk + b].
+constexpr int kDotChunk = 256;
+constexpr int kDotVec = 8;
+
+__global__ void __launch_bounds__(kDotChunk) k_dot_partial(const double2 *__restrict__ V, size_t ldv, int nv,
+                                                           const double2 *__restrict__ w, int n,
+                                                           double2 *__restrict__ partial, const int *done) {
+    __shared__ double red[kDotChunk / 32][2 * kDotVec];
+    if (done && *done) return;
+    const int b = blockIdx.x, nblk = gridDim.x, l0 = blockIdx.y * kDotVec;
+    const int i = b * kDotChunk + threadIdx.x;
+    const double2 wv = i < n ? w[i] : make_double2(0.0, 0.0);
+    double acc[2 * kDotVec];
+#pragma unroll
+    for (int q = 0; q < kDotVec; ++q) {
+        double re = 0.0, im = 0.0;
+        if (i < n && l0 + q < nv) {
+            const double2 a = V[(size_t)(l0 + q) * ldv + i];
+            re = fma(a.x, wv.x, a.y * wv.y);
+            im = fma(a.x, wv.y, -a.y * wv.x);
+        }
+        acc[2 * q] = warp_sum_d(re);
+        acc[2 * q + 1] = warp_sum_d(im);
     }
-    re = warp_sum_d(re);
-    im = warp_sum_d(im);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { sre[wid] = re; sim[wid] = im; }
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 2 * kDotVec; ++q) red[wid][q] = acc[q];
     __syncthreads();
-    if (wid == 0) {
-        const int nw = blockDim.x >> 5;
-        re = lane < nw ? sre[lane] : 0.0;
-        im = lane < nw ? sim[lane] : 0.0;
-        re = warp_sum_d(re);
-        im = warp_sum_d(im);
-        if (lane == 0) h[l] = make_double2(re, im);
+    if (threadIdx.x < 2 * kDotVec) {
+        double t = 0.0;
+#pragma unroll
+        for (int ww = 0; ww < kDotChunk / 32; ++ww) t += red[ww][threadIdx.x];
+        const int q = threadIdx.x >> 1;
+        if (l0 + q < nv) {
+            double *dst = reinterpret_cast<double *>(partial + (size_t)(l0 + q) * nblk + b);
+            dst[threadIdx.x & 1] = t;
+        }
     }
 }
 
-// w -= sum_l h[l] V_l ; hacc += h
-__global__ void k_multi_axpy(const double2 *__restrict__ V, int ldv, int nv, const double2 *__restrict__ h,
-                             double2 *__restrict__ hacc, double2 *__restrict__ w, int n) {
+// h[l] = sum_b partial[l][b]; optionally hsum[l] += h[l]; warp l per vector
+__global__ void k_dot_final(const double2 *__restrict__ partial, int nblk, int nv, double2 *__restrict__ h,
+                            double2 *__restrict__ hsum, const int *done) {
+    if (done && *done) return;
+    const int l = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (l >= nv) return;
+    double re = 0.0, im = 0.0;
+    for (int b = lane; b < nblk; b += 32) {
+        const double2 p = partial[(size_t)l * nblk + b];
+        re += p.x;
+        im += p.y;
+    }
+    re = warp_sum_d(re);
+    im = warp_sum_d(im);
+    if (lane == 0) {
+        h[l] = make_double2(re, im);
+        if (hsum) { hsum[l].x += re; hsum[l].y += im; }
+    }
+}
+
+// w -= sum_l h[l] V_l
+__global__ void k_multi_axpy(const double2 *__restrict__ V, size_t ldv, int nv, const double2 *__restrict__ h,
+                             double2 *__restrict__ w, int n, const int *done) {
     extern __shared__ double2 hs[];
+    if (done && *done) return;
     for (int l = threadIdx.x; l < nv; l += blockDim.x) hs[l] = h[l];
     __syncthreads();
-    if (hacc && blockIdx.x == 0)
-        for (int l = threadIdx.x; l < nv; l += blockDim.x) {
-            hacc[l].x += hs[l].x;
-            hacc[l].y += hs[l].y;
-        }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double2 acc = w[i];
@@ -243,12 +280,64 @@ __global__ void __launch_bounds__(512) k_norm2(const double2 *__restrict__ w, in
     }
 }
 
-__global__ void k_scale_inv(const double2 *__restrict__ w, const double *nrm2, double2 *__restrict__ v, int n) {
+// v = w / sqrt(nrm2.re) where nrm2 is the complex <w, w>
+__global__ void k_scale_inv(const double2 *__restrict__ w, const double *nrm2, double2 *__restrict__ v, int n,
+                            const int *done) {
+    if (done && *done) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double s = 1.0 / sqrt(nrm2[0]);
     const double2 a = w[i];
     v[i] = make_double2(a.x * s, a.y * s);
+}
+
+// One Arnoldi step's Givens work on the device (one thread): column k of H
+// from hsum[0..k] and |w|^2, previous rotations, the new rotation, the
+// residual estimate |g[k+1]|; sets ctrl->done when it is below the target.
+// Clears hsum for the next step.
+__global__ void k_givens(int k, int m, double2 *__restrict__ hsum, const double *__restrict__ wnorm2,
+                         double2 *__restrict__ H, double2 *__restrict__ cs, double2 *__restrict__ sn,
+                         double2 *__restrict__ g, GmresCtrl *ctrl) {
+    if (threadIdx.x != 0 || ctrl->done) return;
+    for (int l = 0; l <= k; ++l) {
+        H[(size_t)l * m + k] = hsum[l];
+        hsum[l] = make_double2(0.0, 0.0);
+    }
+    const double hn = sqrt(wnorm2[0]);
+    // previous rotations: [a; b] <- [[conj(c), conj(s)], [-s, c]] [a; b]
+    for (int l = 0; l < k; ++l) {
+        const double2 a = H[(size_t)l * m + k], b = H[(size_t)(l + 1) * m + k];
+        const double2 c = cs[l], s = sn[l];
+        H[(size_t)l * m + k] = make_double2(c.x * a.x + c.y * a.y + s.x * b.x + s.y * b.y,
+                                            c.x * a.y - c.y * a.x + s.x * b.y - s.y * b.x);
+        H[(size_t)(l + 1) * m + k] = make_double2(-(s.x * a.x - s.y * a.y) + c.x * b.x - c.y * b.y,
+                                                  -(s.x * a.y + s.y * a.x) + c.x * b.y + c.y * b.x);
+    }
+    const double2 a = H[(size_t)k * m + k];
+    const double den = sqrt(a.x * a.x + a.y * a.y + hn * hn);
+    double2 c, s;
+    if (den == 0.0) { c = make_double2(1.0, 0.0); s = make_double2(0.0, 0.0); }
+    else { c = make_double2(a.x / den, a.y / den); s = make_double2(hn / den, 0.0); }
+    cs[k] = c;
+    sn[k] = s;
+    H[(size_t)k * m + k] = make_double2(c.x * a.x + c.y * a.y + s.x * hn, c.x * a.y - c.y * a.x + s.y * hn);
+    const double2 gk = g[k];
+    g[k + 1] = make_double2(-(s.x * gk.x - s.y * gk.y), -(s.x * gk.y + s.y * gk.x));
+    g[k] = make_double2(c.x * gk.x + c.y * gk.y, c.x * gk.y - c.y * gk.x);
+    const double res = sqrt(g[k + 1].x * g[k + 1].x + g[k + 1].y * g[k + 1].y);
+    ctrl->kdone = k + 1;
+    ctrl->res = res;
+    if (!(res > ctrl->thr) || hn == 0.0 || !isfinite(res)) ctrl->done = 1;
+}
+
+__global__ void k_axpy(const double2 *__restrict__ z, double2 *__restrict__ x, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double2 a = z[i];
+    double2 b = x[i];
+    b.x += a.x;
+    b.y += a.y;
+    x[i] = b;
 }
 
 __global__ void k_update_x(const double2 *__restrict__ V, int ldv, int nv, const double2 *__restrict__ y,
@@ -275,36 +364,42 @@ void count_launches(int k) { g_launches.fetch_add(k, std::memory_order_relaxed);
 long long launches() { return g_launches.load(std::memory_order_relaxed); }
 
 cudaError_t launch_matvec(int prec, bool exact, const void *A, int n, size_t lda, const double *x,
-                          const double *r_in, double *y, void *xf, cudaStream_t st) {
+                          const double *r_in, double *y, void *xf, cudaStream_t st, const int *done) {
     const int grid = (n + kRowsPerBlock - 1) / kRowsPerBlock;
     count_launches(prec == 0 ? 1 : 2);
     if (prec == 0) {
         k_matvec64<<<grid, 256, 0, st>>>((const double2 *)A, n, lda, (const double2 *)x, (const double2 *)r_in,
-                                         (double2 *)y);
+                                         (double2 *)y, done);
     } else {
-        k_split<<<(n + 255) / 256, 256, 0, st>>>((const double2 *)x, (float4 *)xf, n);
+        k_split<<<(n + 255) / 256, 256, 0, st>>>((const double2 *)x, (float4 *)xf, n, done);
         if (exact)
             k_matvec32<true><<<grid, 256, 0, st>>>((const float2 *)A, n, lda, (const float4 *)xf,
-                                                   (const double2 *)r_in, (double2 *)y);
+                                                   (const double2 *)r_in, (double2 *)y, done);
         else
             k_matvec32<false><<<grid, 256, 0, st>>>((const float2 *)A, n, lda, (const float4 *)xf,
-                                                    (const double2 *)r_in, (double2 *)y);
+                                                    (const double2 *)r_in, (double2 *)y, done);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_multi_dot(const double *V, int ldv, int nv, const double *w, int n, double *h, cudaStream_t st) {
-    count_launches(1);
-    k_multi_dot<<<nv, 512, 0, st>>>((const double2 *)V, ldv, (const double2 *)w, n, (double2 *)h);
+int dot_blocks(int n) { return (n + kDotChunk - 1) / kDotChunk; }
+
+cudaError_t launch_multi_dot(const double *V, size_t ldv, int nv, const double *w, int n, double *partial,
+                             double *h, double *hsum, cudaStream_t st, const int *done) {
+    const int nb = dot_blocks(n);
+    count_launches(2);
+    dim3 grid(nb, (nv + kDotVec - 1) / kDotVec);
+    k_dot_partial<<<grid, kDotChunk, 0, st>>>((const double2 *)V, ldv, nv, (const double2 *)w, n, (double2 *)partial,
+                                              done);
+    k_dot_final<<<(nv + 7) / 8, 256, 0, st>>>((const double2 *)partial, nb, nv, (double2 *)h, (double2 *)hsum, done);
     return cudaGetLastError();
 }
 
-cudaError_t launch_multi_axpy(const double *V, int ldv, int nv, const double *h, double *hacc, double *w, int n,
-                              cudaStream_t st) {
+cudaError_t launch_multi_axpy(const double *V, size_t ldv, int nv, const double *h, double *w, int n,
+                              cudaStream_t st, const int *done) {
     count_launches(1);
     k_multi_axpy<<<(n + 255) / 256, 256, nv * sizeof(double2), st>>>((const double2 *)V, ldv, nv,
-                                                                     (const double2 *)h, (double2 *)hacc,
-                                                                     (double2 *)w, n);
+                                                                     (const double2 *)h, (double2 *)w, n, done);
     return cudaGetLastError();
 }
 
@@ -314,9 +409,24 @@ cudaError_t launch_norm2(const double *w, int n, double *out, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_scale_inv(const double *w, const double *nrm2, double *v, int n, cudaStream_t st) {
+cudaError_t launch_scale_inv(const double *w, const double *nrm2, double *v, int n, cudaStream_t st,
+                             const int *done) {
     count_launches(1);
-    k_scale_inv<<<(n + 255) / 256, 256, 0, st>>>((const double2 *)w, nrm2, (double2 *)v, n);
+    k_scale_inv<<<(n + 255) / 256, 256, 0, st>>>((const double2 *)w, nrm2, (double2 *)v, n, done);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_givens(int k, int m, double *hsum, const double *wnorm2, double *H, double *cs, double *sn,
+                          double *g, GmresCtrl *ctrl, cudaStream_t st) {
+    count_launches(1);
+    k_givens<<<1, 32, 0, st>>>(k, m, (double2 *)hsum, wnorm2, (double2 *)H, (double2 *)cs, (double2 *)sn,
+                               (double2 *)g, ctrl);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_axpy(const double *z, double *x, int n, cudaStream_t st) {
+    count_launches(1);
+    k_axpy<<<(n + 255) / 256, 256, 0, st>>>((const double2 *)z, (double2 *)x, n);
     return cudaGetLastError();
 }
 

@@ -89,7 +89,7 @@ template <typename T> struct ProjAcc { cplx<T> p, g[3]; };
 template <typename T>
 __device__ __forceinline__ void proj_point(const QPoint<T> &q, cplx<T> phi, const cplx<T> *vel, int nv,
                                            bool ivi, T k, T wr, ProjAcc<T> &a) {
-    T r = q.r, ir = T(1) / r;
+    const T r = q.r, ir = q.ir;
     T dh[3] = {q.d[0] * ir, q.d[1] * ir, q.d[2] * ir};
     T s, c;
     sincos_t(wr * r, &s, &c);

@@ -1,0 +1,223 @@
+// bem_precond.cu - block-Jacobi preconditioner for the GMRES of bem_solve.
+//
+// The library numbers the unknowns along a Morton (Z-order) curve of the
+// element centres, so consecutive unknowns are spatial neighbours and the
+// diagonal blocks of A hold the strongest (near-field) couplings.  The
+// preconditioner is the block diagonal of A with blocks of kBlock unknowns,
+// inverted once per frequency; NumCalc's own preconditioner is a threshold
+// ILU on the same near-field entries (NC_CommonFunctions.cpp:1357-1721).
+//
+// Inversion: one CTA per block, in-place Gauss-Jordan with partial pivoting.
+// complex64 blocks live in shared memory (128 KB); complex128 blocks are
+// inverted in a global workspace (L2 resident).  Inverses are stored
+// transposed so that the application reads them coalesced.
+#include <cuda_runtime.h>
+
+#include "bem_internal.h"
+
+namespace bem {
+namespace {
+
+template <typename T> struct C2;
+template <> struct C2<float> { using t = float2; };
+template <> struct C2<double> { using t = double2; };
+
+template <typename V> __device__ __forceinline__ V cmul2(V a, V b) {
+    V r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename V> __device__ __forceinline__ V cinv2(V a) {
+    // 1/a, scaled to avoid overflow
+    auto s = fabs(a.x) > fabs(a.y) ? fabs(a.x) : fabs(a.y);
+    decltype(s) ar = a.x / s, ai = a.y / s, d = ar * ar + ai * ai;
+    V r;
+    r.x = ar / (d * s);
+    r.y = -ai / (d * s);
+    return r;
+}
+
+// In-place Gauss-Jordan on the nb x nb block W (row-major, leading dim ld),
+// executed by one CTA.  colk: nb scratch, piv: nb ints.
+template <typename T>
+__device__ void gauss_jordan(typename C2<T>::t *W, int ld, int nb, typename C2<T>::t *colk, int *piv,
+                             int *pivrow, int *singular) {
+    using V = typename C2<T>::t;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int k = 0; k < nb; ++k) {
+        // pivot search by warp 0
+        if (tid < 32) {
+            T best = -1;
+            int bi = k;
+            for (int i = k + tid; i < nb; i += 32) {
+                V a = W[(size_t)i * ld + k];
+                T m = a.x * a.x + a.y * a.y;
+                if (m > best) { best = m; bi = i; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                T ob = __shfl_down_sync(0xffffffffu, best, o);
+                int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (tid == 0) {
+                *pivrow = bi;
+                piv[k] = bi;
+                if (!(best > 0)) *singular = 1;
+            }
+        }
+        __syncthreads();
+        const int p = *pivrow;
+        if (p != k)
+            for (int j = tid; j < nb; j += nt) {
+                V t = W[(size_t)k * ld + j];
+                W[(size_t)k * ld + j] = W[(size_t)p * ld + j];
+                W[(size_t)p * ld + j] = t;
+            }
+        __syncthreads();
+        const V inv = cinv2(W[(size_t)k * ld + k]);
+        for (int i = tid; i < nb; i += nt) colk[i] = W[(size_t)i * ld + k];
+        __syncthreads();
+        for (int j = tid; j < nb; j += nt) {
+            V a = j == k ? V{1, 0} : W[(size_t)k * ld + j];
+            W[(size_t)k * ld + j] = cmul2(a, inv);
+        }
+        __syncthreads();
+        for (int e = tid; e < nb * nb; e += nt) {
+            const int i = e / nb, j = e - i * nb;
+            if (i == k) continue;
+            const V f = colk[i];
+            V a = j == k ? V{0, 0} : W[(size_t)i * ld + j];
+            const V r = W[(size_t)k * ld + j];
+            a.x -= f.x * r.x - f.y * r.y;
+            a.y -= f.x * r.y + f.y * r.x;
+            W[(size_t)i * ld + j] = a;
+        }
+        __syncthreads();
+    }
+    // undo the row interchanges as column interchanges, last first
+    for (int k = nb - 1; k >= 0; --k) {
+        const int p = piv[k];
+        if (p != k)
+            for (int i = tid; i < nb; i += nt) {
+                V t = W[(size_t)i * ld + k];
+                W[(size_t)i * ld + k] = W[(size_t)i * ld + p];
+                W[(size_t)i * ld + p] = t;
+            }
+        __syncthreads();
+    }
+}
+
+// complex64: block in shared memory
+__global__ void __launch_bounds__(512) k_binv32(const float2 *__restrict__ A, size_t lda, int n, float2 *__restrict__ Minv,
+                                                int *status) {
+    extern __shared__ float2 smem[];
+    __shared__ float2 colk[kBlock];
+    __shared__ int piv[kBlock];
+    __shared__ int pivrow, singular;
+    const int b = blockIdx.x, r0 = b * kBlock;
+    const int nb = min(kBlock, n - r0);
+    if (threadIdx.x == 0) singular = 0;
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+        const int i = e / nb, j = e - i * nb;
+        smem[i * kBlock + j] = A[(size_t)(r0 + i) * lda + r0 + j];
+    }
+    __syncthreads();
+    gauss_jordan<float>(smem, kBlock, nb, colk, piv, &pivrow, &singular);
+    // store transposed: Minv[b][c][r] = inv[r][c]
+    float2 *out = Minv + (size_t)b * kBlock * kBlock;
+    for (int e = threadIdx.x; e < kBlock * kBlock; e += blockDim.x) {
+        const int c = e / kBlock, r = e - c * kBlock;
+        out[e] = (r < nb && c < nb) ? smem[r * kBlock + c] : make_float2(0.f, 0.f);
+    }
+    if (threadIdx.x == 0 && singular) atomicMax(status, 1);
+}
+
+// complex128: block in a global workspace
+__global__ void __launch_bounds__(512) k_binv64(const double2 *__restrict__ A, size_t lda, int n, double2 *__restrict__ W,
+                                                double2 *__restrict__ Minv, int *status) {
+    __shared__ double2 colk[kBlock];
+    __shared__ int piv[kBlock];
+    __shared__ int pivrow, singular;
+    const int b = blockIdx.x, r0 = b * kBlock;
+    const int nb = min(kBlock, n - r0);
+    double2 *w = W + (size_t)b * kBlock * kBlock;
+    if (threadIdx.x == 0) singular = 0;
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+        const int i = e / nb, j = e - i * nb;
+        w[i * kBlock + j] = A[(size_t)(r0 + i) * lda + r0 + j];
+    }
+    __syncthreads();
+    gauss_jordan<double>(w, kBlock, nb, colk, piv, &pivrow, &singular);
+    double2 *out = Minv + (size_t)b * kBlock * kBlock;
+    for (int e = threadIdx.x; e < kBlock * kBlock; e += blockDim.x) {
+        const int c = e / kBlock, r = e - c * kBlock;
+        out[e] = (r < nb && c < nb) ? w[r * kBlock + c] : make_double2(0.0, 0.0);
+    }
+    if (threadIdx.x == 0 && singular) atomicMax(status, 1);
+}
+
+// z = M^{-1} v, one CTA of kBlock threads per block; thread r owns row r.
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_bapply(const V *__restrict__ Minv, int n, const double2 *__restrict__ v,
+                                                   double2 *__restrict__ z, const int *done) {
+    __shared__ double2 xs[kBlock];
+    if (done && *done) return;
+    const int b = blockIdx.x, r0 = b * kBlock, r = threadIdx.x;
+    const int nb = min(kBlock, n - r0);
+    xs[r] = r < nb ? v[r0 + r] : make_double2(0.0, 0.0);
+    __syncthreads();
+    if (r >= nb) return;
+    const V *M = Minv + (size_t)b * kBlock * kBlock;
+    double sr = 0.0, si = 0.0;
+    // float blocks: FP32 products, FP64 accumulation in chunks of 16
+    for (int c0 = 0; c0 < nb; c0 += 16) {
+        decltype(M[0].x) ar = 0, ai = 0;
+        const int ce = min(c0 + 16, nb);
+        for (int c = c0; c < ce; ++c) {
+            const V m = M[(size_t)c * kBlock + r];
+            const decltype(m.x) xr = (decltype(m.x))xs[c].x, xi = (decltype(m.x))xs[c].y;
+            ar += m.x * xr - m.y * xi;
+            ai += m.x * xi + m.y * xr;
+        }
+        sr += (double)ar;
+        si += (double)ai;
+    }
+    z[r0 + r] = make_double2(sr, si);
+}
+
+}  // namespace
+
+size_t precond_bytes(int n, int prec) {
+    const size_t nb = (size_t)(n + kBlock - 1) / kBlock;
+    const size_t per = (size_t)kBlock * kBlock * (prec == 0 ? 16 : 8);
+    return nb * per * (prec == 0 ? 2 : 1);   // FP64 needs the inversion workspace too
+}
+
+cudaError_t launch_block_inverse(int prec, const void *A, size_t lda, int n, void *Minv, void *work, int *status,
+                                 cudaStream_t st) {
+    const int nb = (n + kBlock - 1) / kBlock;
+    count_launches(1);
+    if (prec == 0) {
+        k_binv64<<<nb, 512, 0, st>>>((const double2 *)A, lda, n, (double2 *)work, (double2 *)Minv, status);
+    } else {
+        const int smem = kBlock * kBlock * sizeof(float2);
+        cudaError_t e = cudaFuncSetAttribute(k_binv32, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_binv32<<<nb, 512, smem, st>>>((const float2 *)A, lda, n, (float2 *)Minv, status);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_block_apply(int prec, const void *Minv, int n, const double *v, double *z, cudaStream_t st,
+                               const int *done) {
+    const int nb = (n + kBlock - 1) / kBlock;
+    count_launches(1);
+    if (prec == 0)
+        k_bapply<double2><<<nb, kBlock, 0, st>>>((const double2 *)Minv, n, (const double2 *)v, (double2 *)z, done);
+    else
+        k_bapply<float2><<<nb, kBlock, 0, st>>>((const float2 *)Minv, n, (const double2 *)v, (double2 *)z, done);
+    return cudaGetLastError();
+}
+
+}  // namespace bem
