@@ -8,15 +8,21 @@ assemble A(k) and b, GMRES to a relative residual of 1e-9, project onto the
 1730 points.  A step is one batch of --batch frequencies (default 8) taken
 from a seeded permutation of the 200, so K steps sample the whole band.
 
-value     mixed-precision solves/s with the mesh resident on the device.
-e2e       the same through the C ABI with host buffers: every step uploads the
-          mesh and evaluation points, creates the solver, solves its batch
-          with bem_solve_frequency and copies unknowns and fields back.
-fp64      the plain FP64 GPU path on one batch of the same frequencies, with
-          the mixed path's relative L2 boundary-pressure error against it.
+value     mixed-precision solves/s with the mesh resident on the device; a
+          step is one bem_solve_batch call over its frequencies (one solver
+          per frequency on the shared mesh).
+latency   p50/p99 of the same frequencies solved one at a time
+          (bem_solve_frequency).
+e2e       the same as value through the C ABI with host buffers: every step
+          uploads the mesh and evaluation points, creates the solvers, runs
+          bem_solve_batch and copies unknowns and fields back.
+fp64      the plain FP64 GPU path on one batch of the same frequencies (also
+          batched), with the mixed path's relative L2 boundary-pressure error
+          against it.
 roofline  the dominant kernel (the complex64 matrix-vector product of the
-          solve), algorithmic bytes N^2*8 + 2*N*16 per product over its
-          average CUDA-event time, against the measured HBM copy bandwidth.
+          solve), algorithmic bytes N^2*8 + 2*N*16 per product and system over
+          the CUDA-event time of the product launches, against the measured
+          HBM copy bandwidth.
 cpu_baseline  the FP64 C restatement of the reference path (oracle/, the
           "port") on the host cores, on a bounded sample: 2048 rows of the
           assembly, the dense matrix-vector product of those rows and 256
@@ -211,24 +217,24 @@ def main():
     torch.cuda.set_device(dev)
     lib = capi.load()
     mesh = capi.Mesh(v, f, device=dev)
-    solver = capi.Solver(mesh, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000)
     B = args.batch
+    # one solver per frequency of a step, all on the resident mesh; a step is
+    # one bem_solve_batch call (assembly, lockstep GMRES and projection of the
+    # B frequencies together)
+    solvers = [capi.Solver(mesh, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000) for _ in range(B)]
+
     # each rank takes its own slice of the permuted frequency list
     def batch_freqs(step):
         base = (step * world + rank) * B
         return [float(freqs[(base + b) % len(freqs)]) for b in range(B)]
 
-    lat, infos = [], []
+    infos, batch_ms = [], []
 
     def run_step(step, record):
-        for fr in batch_freqs(step):
-            F = freq_desc(capi, n, fr, src)
-            t0 = time.perf_counter()
-            solver.solve_frequency(F, pts)
-            dt = time.perf_counter() - t0
-            if record:
-                lat.append(dt)
-                infos.append(solver.info.as_dict())
+        Fs = [freq_desc(capi, n, fr, src) for fr in batch_freqs(step)]
+        res = capi.solve_batch(solvers, Fs, [pts] * B)
+        if record:
+            infos.append([r[3] for r in res])
 
     for s in range(args.warmup):
         run_step(s, False)
@@ -254,31 +260,50 @@ def main():
     total_solves = args.steps * B * world
     value = total_solves / elapsed
 
-    # roofline of the dominant kernel: complex64 matvec
-    mv_ms = sum(i["matvec_ms"] for i in infos)
-    n_mv = sum(i["n_matvec"] for i in infos)
-    asm_ms = sum(i["assemble_ms"] for i in infos)
-    solve_ms = sum(i["solve_ms"] for i in infos)
-    proj_ms = sum(i["project_ms"] for i in infos)
-    bytes_mv = n * n * 8.0 + 2 * n * 16.0
-    achieved = bytes_mv / (mv_ms / n_mv / 1000.0) / 1e9 if n_mv else None
+    # roofline of the dominant kernel: the complex64 matvec.  Each launch of
+    # the batched product covers every system still iterating; its bytes are
+    # counted per system and product (N^2*8 + 2*N*16), its time is the
+    # CUDA-event time of the launches inside the iteration bodies.
+    bytes_one = n * n * 8.0 + 2 * n * 16.0
+    mv_ms = sum(step[0]["matvec_ms"] for step in infos)
+    n_mv = sum(i["n_matvec"] for step in infos for i in step)
+    achieved = bytes_one * n_mv / (mv_ms / 1000.0) / 1e9 if mv_ms > 0 else None
+    asm_ms = sum(step[0]["assemble_ms"] for step in infos)
+    solve_ms = sum(step[0]["solve_ms"] for step in infos)
+    proj_ms = sum(step[0]["project_ms"] for step in infos)
+    n_solves = len(infos) * B
+    iters = [i["iterations"] for step in infos for i in step]
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except OSError:
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
+    for sv in solvers:
+        sv.close()
 
-    # end to end through the C ABI with host buffers
-    e2e_val, h2d, d2h = None, 0, 0
+    # latency: the same frequencies solved one at a time (bem_solve_frequency)
+    lat = []
+    single = capi.Solver(mesh, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000)
+    for s in range(args.warmup, args.warmup + args.steps):
+        for fr in batch_freqs(s):
+            F = freq_desc(capi, n, fr, src)
+            t1 = time.perf_counter()
+            single.solve_frequency(F, pts)
+            lat.append(time.perf_counter() - t1)
+    single.close()
+
+    # end to end through the C ABI with host buffers: per step the mesh and
+    # the evaluation points go up, B solvers are created, bem_solve_batch
+    # runs, unknowns and fields come back
     t0 = time.perf_counter()
     e2e_steps = max(1, min(args.steps, 2))
     for s in range(args.warmup, args.warmup + e2e_steps):
         m2 = capi.Mesh(v, f, device=dev)
-        s2 = capi.Solver(m2, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000)
-        for fr in batch_freqs(s):
-            s2.solve_frequency(freq_desc(capi, n, fr, src), pts)
-        s2.close()
+        s2 = [capi.Solver(m2, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000) for _ in range(B)]
+        capi.solve_batch(s2, [freq_desc(capi, n, fr, src) for fr in batch_freqs(s)], [pts] * B)
+        for sv in s2:
+            sv.close()
         m2.close()
     torch.cuda.synchronize()
     e2e_val = e2e_steps * B / (time.perf_counter() - t0)
@@ -288,36 +313,41 @@ def main():
     h2d = n * (20 * 8 + 30 * 4) + B * (pts.nbytes + 16 + 24)
     d2h = B * (n * 16 + len(pts) * 16 * 4)
 
-    # FP64 GPU path on one batch, and the mixed path's error against it
-    fp64 = capi.Solver(mesh, precision=capi.PREC_FP64, tol=1e-9, max_iter=3000)
-    mixed_check = capi.Solver(mesh, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000)
-    errs, t64 = [], 0.0
-    for fr in batch_freqs(args.warmup):
-        F = freq_desc(capi, n, fr, src)
-        t1 = time.perf_counter()
-        x64, p64, _ = fp64.solve_frequency(F, pts)
-        t64 += time.perf_counter() - t1
-        xm, pm, _ = mixed_check.solve_frequency(F, pts)
-        errs.append(float(np.linalg.norm(xm - x64) / np.linalg.norm(x64)))
+    # FP64 GPU path on one batch (also batched), and the mixed path's error
+    # against it
+    frs = batch_freqs(args.warmup)
+    Fs = [freq_desc(capi, n, fr, src) for fr in frs]
+    s64 = [capi.Solver(mesh, precision=capi.PREC_FP64, tol=1e-9, max_iter=3000) for _ in range(B)]
+    capi.solve_batch(s64[:1], Fs[:1], [pts])   # warm-up of the FP64 engine
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    r64 = capi.solve_batch(s64, Fs, [pts] * B)
+    t64 = time.perf_counter() - t1
+    for sv in s64:
+        sv.close()
+    smx = [capi.Solver(mesh, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000) for _ in range(B)]
+    rmx = capi.solve_batch(smx, Fs, [pts] * B)
+    for sv in smx:
+        sv.close()
+    errs = [float(np.linalg.norm(a[0] - b[0]) / np.linalg.norm(b[0])) for a, b in zip(rmx, r64)]
     fp64_val = B / t64
-    fp64.close()
-    mixed_check.close()
 
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1000.0, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP32 assembly/matvec, FP64 singular + refinement)",
         "data": "synthetic", "config": cfg,
-        "latency_ms": {"p50": float(np.percentile(lat, 50) * 1000), "p99": float(np.percentile(lat, 99) * 1000)},
-        "fp64_gpu": {"value": fp64_val, "unit": "solves/s", "frequencies": batch_freqs(args.warmup),
+        "latency_ms": {"p50": float(np.percentile(lat, 50) * 1000), "p99": float(np.percentile(lat, 99) * 1000),
+                       "mode": "one solve at a time (bem_solve_frequency), same frequencies"},
+        "fp64_gpu": {"value": fp64_val, "unit": "solves/s", "frequencies": frs, "mode": "bem_solve_batch of %d" % B,
                      "speedup_mixed_over_fp64": value / fp64_val,
                      "mixed_rel_l2_boundary_err_max": max(errs)},
-        "stage_ms_per_solve": {"assemble": asm_ms / len(infos), "solve": solve_ms / len(infos),
-                               "project": proj_ms / len(infos), "matvec": mv_ms / len(infos),
-                               "iterations": float(np.mean([i["iterations"] for i in infos]))},
-        "roofline": {"bound": "hbm", "kernel": "k_matvec32 (complex64 A x)", "achieved": achieved,
+        "stage_ms_per_solve": {"assemble": asm_ms / n_solves, "solve": solve_ms / n_solves,
+                               "project": proj_ms / n_solves, "matvec": mv_ms / n_solves,
+                               "iterations": float(np.mean(iters))},
+        "roofline": {"bound": "hbm", "kernel": "k_mv<c64> (batched complex64 A x)", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if achieved else None,
-                     "traffic": None, "bytes_per_launch": bytes_mv,
+                     "traffic": None, "bytes_per_product": bytes_one, "products": n_mv,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
@@ -326,17 +356,16 @@ def main():
     }
     if rank == 0:
         threads = cpu_threads()
-        iters = int(round(np.mean([i["iterations"] for i in infos])))
-        t_cpu, det = cpu_port_solve_seconds(v, f, src, pts, 10000.0, iters, threads)
+        it_mean = int(round(np.mean(iters)))
+        t_cpu, det = cpu_port_solve_seconds(v, f, src, pts, 10000.0, it_mean, threads)
         line["cpu_baseline"] = {
             "value": 1.0 / t_cpu, "unit": "solves/s", "cores": threads, "kind": "port",
             "sample": "FP64 C restatement of NumCalc's TBEM path (oracle/bem_oracle.c) at 10 kHz: 2048 "
                       "assembly rows, the dense complex128 matvec of those rows and 256 of the 1730 "
                       "evaluation points, scaled to one 20480-unknown solve with the GPU run's mean "
-                      "iteration count (%d)" % iters,
+                      "iteration count (%d)" % it_mean,
             "breakdown": det}
         print(json.dumps(line))
-    solver.close()
     mesh.close()
     if dist:
         dist.barrier()

@@ -88,7 +88,8 @@ typedef struct {
 
 typedef struct {
     int32_t precision;         /* bem_precision                                */
-    int32_t restart;           /* GMRES restart length (0 = default 60)        */
+    int32_t restart;           /* GMRES restart length (0 = default 60,
+                                  at most 63)                                  */
     int32_t max_iter;          /* total inner iterations (0 = default 1000)    */
     double tol;                /* relative residual target (0 = 1e-9)          */
     double hbm_budget_bytes;   /* admission budget for this solver (0 = all
@@ -210,6 +211,27 @@ bem_status bem_solve_frequency(bem_solver_t solver, const bem_frequency_desc *fr
                                int32_t n_pts, const double *pts, double *x_out,
                                double *pot_out, double *grad_out,
                                bem_solve_info *info);
+
+/* Several frequency steps solved together: count (solver, frequency)
+ * instances, each solver with its own mesh (meshes of different sizes mix
+ * freely; a solver may appear once).  The assembly of all instances runs as
+ * one persistent launch, their GMRES iterations run in lockstep inside one
+ * captured iteration body, and their projections run as one launch.  Each
+ * instance's result is the one bem_solve_frequency gives for it alone.
+ * NumCalc runs such steps as separate processes (manage_numcalc.py:376-378);
+ * no counterpart inside the reference.
+ *
+ * Arrays are indexed by instance; n_pts, pts, x_out, pot_out, grad_out,
+ * infos and statuses may be NULL, and entries of the pointer arrays may be
+ * NULL where nothing is wanted.  infos[i] holds instance i's iterations and
+ * residual; its times are those of the whole batch.  statuses[i] is the
+ * instance's own status; the return value is BEM_OK or the first failing
+ * instance's status.  Runs on a stream owned by the calling thread. */
+bem_status bem_solve_batch(int32_t count, const bem_solver_t *solvers,
+                           const bem_frequency_desc *freqs, const int32_t *n_pts,
+                           const double *const *pts, double *const *x_out,
+                           double *const *pot_out, double *const *grad_out,
+                           bem_solve_info *infos, bem_status *statuses);
 
 #ifdef __cplusplus
 }

@@ -30,7 +30,7 @@ EXPORTED = [
     "bem_last_error", "bem_version", "bem_kernel_launches", "bem_set_device", "bem_footprint_bytes",
     "bem_mesh_create", "bem_mesh_destroy", "bem_solver_create", "bem_solver_destroy", "bem_solver_set_params",
     "bem_assemble", "bem_solve", "bem_get_solution", "bem_get_system", "bem_project",
-    "bem_solve_frequency", "bem_project_static",
+    "bem_solve_frequency", "bem_project_static", "bem_solve_batch",
 ]
 STATIC_MAX_ELEMENTS = 32768
 
@@ -100,6 +100,7 @@ def load(build_if_missing: bool = True):
     lib.bem_project.argtypes = [vp, i32, vp, vp, vp]
     lib.bem_solve_frequency.argtypes = [vp, C.POINTER(FreqDesc), i32, vp, vp, vp, vp, C.POINTER(SolveInfo)]
     lib.bem_project_static.argtypes = [vp, i32, vp, vp, vp, vp]
+    lib.bem_solve_batch.argtypes = [i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     for name in EXPORTED:
         if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes", "bem_kernel_launches"):
             getattr(lib, name).restype = C.c_int
@@ -243,6 +244,39 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+def solve_batch(solvers, freqs, pts_list=None, with_grad=True, allow_not_converged=False):
+    """bem_solve_batch: solve (solver, frequency) instances together.
+
+    Returns a list of (x, pot, grad, info dict, status) per instance."""
+    cnt = len(solvers)
+    if len(freqs) != cnt:
+        raise ValueError("one frequency per solver")
+    SolverArr = C.c_void_p * cnt
+    FreqArr = FreqDesc * cnt
+    PtrArr = C.c_void_p * cnt
+    hs = SolverArr(*[s.handle.value for s in solvers])
+    fs = FreqArr(*[f.desc for f in freqs])
+    xs, pots, grads, ptss = [], [], [], []
+    for i, s in enumerate(solvers):
+        xs.append(np.zeros(s.n, np.complex128))
+        p = np.zeros((0, 3)) if pts_list is None else np.ascontiguousarray(pts_list[i], np.float64).reshape(-1, 3)
+        ptss.append(p)
+        pots.append(np.zeros(len(p), np.complex128))
+        grads.append(np.zeros((len(p), 3), np.complex128) if with_grad else None)
+    npts = (C.c_int32 * cnt)(*[len(p) for p in ptss])
+    pts_a = PtrArr(*[p.ctypes.data if len(p) else None for p in ptss])
+    x_a = PtrArr(*[x.ctypes.data for x in xs])
+    pot_a = PtrArr(*[q.ctypes.data if len(q) else None for q in pots])
+    grad_a = PtrArr(*[(g.ctypes.data if (g is not None and len(g)) else None) for g in grads])
+    infos = (SolveInfo * cnt)()
+    sts = (C.c_int32 * cnt)()
+    allow = (BEM_ERR_NOT_CONVERGED,) if allow_not_converged else ()
+    rc = load().bem_solve_batch(cnt, hs, fs, npts, pts_a, x_a, pot_a, grad_a, infos, sts)
+    if rc != BEM_OK and not all(int(v) in (BEM_OK,) + allow for v in sts):
+        _check(rc, allow)
+    return [(xs[i], pots[i], grads[i], infos[i].as_dict(), int(sts[i])) for i in range(cnt)]
 
 
 def footprint_bytes(n_elem, precision=PREC_MIXED, restart=0):

@@ -1,5 +1,6 @@
 // bem_api.cu - the C ABI of include/bem_gb300.h: handles, device memory,
-// HBM admission, the restarted GMRES driver and the per-frequency sequence.
+// HBM admission and the per-frequency sequence (assembly, solve, projection)
+// for one solver or a batch of solvers.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -8,11 +9,13 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/bem_gb300.h"
+#include "bem_engine.h"
 #include "bem_internal.h"
 
 using cd = std::complex<double>;
@@ -142,6 +145,83 @@ uint64_t spread3(uint64_t v) {
 }  // namespace
 
 // ---------------------------------------------------------------- solver
+namespace bem {
+
+// Sources kept in the solver's block; more are allocated separately.
+constexpr int kInlineSources = 64;
+
+// Every per-solver device buffer, carved from one allocation.
+struct SolverBufs {
+    void *A = nullptr;
+    double2 *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *z = nullptr, *V = nullptr;
+    double2 *mvp = nullptr, *dpa = nullptr, *dpb = nullptr;
+    float2 *xh = nullptr;
+    float4 *xf = nullptr;
+    double *nrmp = nullptr;
+    double2 *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr, *hsum = nullptr;
+    void *Minv = nullptr, *Mwork = nullptr;
+    int *status = nullptr;
+    unsigned *ctr = nullptr;   // 4 words: work queues of the persistent assembly kernels
+    double *phi = nullptr, *vel = nullptr;
+    int *ivi = nullptr;
+    int *bct = nullptr, *cols = nullptr;
+    double *bcv = nullptr, *adm = nullptr, *src = nullptr;
+};
+
+// Byte layout of the block (256-byte aligned pieces).  base == nullptr only
+// sizes it.  The footprint reported by bem_footprint_bytes is this size.
+size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, SolverBufs *o) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> void * {
+        void *p = base ? (void *)(base + off) : nullptr;
+        off += round_up(bytes, 256);
+        return p;
+    };
+    const size_t N = (size_t)n, lda = round_up(N, 32);
+    const size_t esz = prec == 0 ? 16 : 8;
+    SolverBufs d;
+    d.A = take(N * lda * esz);
+    d.b = (double2 *)take(N * 16);
+    d.x = (double2 *)take(N * 16);
+    d.r = (double2 *)take(N * 16);
+    d.w = (double2 *)take(N * 16);
+    d.z = (double2 *)take(N * 16);
+    d.V = (double2 *)take((size_t)(m + 1) * N * 16);
+    d.mvp = (double2 *)take(mvp_elems(n) * 16);
+    if (prec != 0) {   // complex64: float copies of the product's input
+        d.xh = (float2 *)take(xsplit_elems(n) * 8);
+        d.xf = (float4 *)take(xsplit_elems(n) * 16);
+    }
+    d.dpa = (double2 *)take(dp_elems(n) * 16);
+    d.dpb = (double2 *)take(dp_elems(n) * 16);
+    d.nrmp = (double *)take((size_t)vec_blocks(n) * 8);
+    d.H = (double2 *)take((size_t)(m + 1) * m * 16);
+    d.cs = (double2 *)take((size_t)m * 16);
+    d.sn = (double2 *)take((size_t)m * 16);
+    d.g = (double2 *)take((size_t)(m + 1) * 16);
+    d.y = (double2 *)take((size_t)m * 16);
+    d.hsum = (double2 *)take((size_t)(m + 1) * 16);
+    if (pc) {
+        const size_t pb = precond_bytes(n, prec);
+        d.Minv = take(prec == 0 ? pb / 2 : pb);
+        if (prec == 0) d.Mwork = take(pb / 2);
+    }
+    d.status = (int *)take(16);
+    d.ctr = (unsigned *)take(16);
+    d.phi = (double *)take(N * 16);
+    d.vel = (double *)take(4 * N * 16);
+    d.ivi = (int *)take(N * 4);
+    d.bct = (int *)take(N * 4);
+    d.cols = (int *)take(N * 4);
+    d.bcv = (double *)take(8 * N * 8);
+    d.adm = (double *)take(2 * N * 8);
+    d.src = (double *)take(5 * (size_t)kInlineSources * 8);
+    if (o) *o = d;
+    return off;
+}
+
+}  // namespace bem
+
 struct bem_solver_s {
     bem_mesh_t mesh = nullptr;
     int n = 0;
@@ -150,56 +230,453 @@ struct bem_solver_s {
     int max_iter = 1000;
     double tol = 1e-9;
     size_t lda = 0;
+    bool precond = true, have_precond = false;
     cudaStream_t st = nullptr;
     cudaEvent_t ev[8] = {};
-    void *A = nullptr;
-    double *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *V = nullptr;
-    double *hd = nullptr, *hsum = nullptr, *nrm = nullptr, *ydev = nullptr;
-    double *Hd = nullptr, *csd = nullptr, *snd = nullptr, *gd = nullptr, *partial = nullptr;
-    bem::GmresCtrl *ctrl = nullptr;
-    std::vector<cudaEvent_t> mv_ev;   // per Arnoldi step: before/after the matvec
-    void *xf = nullptr;
-    void *Minv = nullptr, *Mwork = nullptr;
-    bool precond = true, have_precond = false;
-    double *z = nullptr;
-    int *status = nullptr;
-    unsigned long long *n_near = nullptr;
-    // per-frequency device data
-    int *f_bct = nullptr, *f_cols = nullptr;
-    double *f_bcv = nullptr, *f_adm = nullptr, *f_src = nullptr;
+    unsigned char *block = nullptr;
+    size_t block_bytes = 0;
+    bem::SolverBufs d;
+    double *src_extra = nullptr;
     bem::DevFreq freq{};
     bool have_freq = false;
     bool solved = false;
-    // fields and projection
-    double *phi = nullptr, *vel = nullptr;
-    int *ivi = nullptr;
     double *pts = nullptr, *pot = nullptr, *grad = nullptr;
     int pts_cap = 0;
-    // pinned staging
-    double *h_pin = nullptr;
+    std::unique_ptr<bem::Engine> eng;
     bem_solve_info info{};
     ~bem_solver_s() {
         if (st) cudaStreamSynchronize(st);
-        cudaFree(A); cudaFree(b); cudaFree(x); cudaFree(r); cudaFree(w); cudaFree(V); cudaFree(hd);
-        cudaFree(hsum); cudaFree(nrm); cudaFree(ydev); cudaFree(xf); cudaFree(status); cudaFree(n_near);
-        cudaFree(Minv); cudaFree(Mwork); cudaFree(z);
-        cudaFree(Hd); cudaFree(csd); cudaFree(snd); cudaFree(gd); cudaFree(partial); cudaFree(ctrl);
-        for (auto &e : mv_ev)
+        eng.reset();
+        cudaFree(block);
+        cudaFree(src_extra);
+        cudaFree(pts); cudaFree(pot); cudaFree(grad);
+        for (auto &e : ev)
             if (e) cudaEventDestroy(e);
-        cudaFree(f_bct); cudaFree(f_cols); cudaFree(f_bcv); cudaFree(f_adm); cudaFree(f_src);
-        cudaFree(phi); cudaFree(vel); cudaFree(ivi); cudaFree(pts); cudaFree(pot); cudaFree(grad);
-        if (h_pin) cudaFreeHost(h_pin);
+        if (st) cudaStreamDestroy(st);
+    }
+    bem::KSys ksys() const {
+        bem::KSys k{};
+        k.A = d.A;
+        k.lda = (long long)lda;
+        k.n = n;
+        k.pc = have_precond ? 1 : 0;
+        k.nchunk = bem::mv_chunks(n);
+        k.nvb = bem::vec_blocks(n);
+        k.Minv = d.Minv;
+        k.x = d.x; k.b = d.b; k.r = d.r; k.w = d.w; k.z = d.z; k.V = d.V;
+        k.xh = d.xh; k.xf = d.xf;
+        k.ldv = n;
+        k.mvp = d.mvp; k.dpa = d.dpa; k.dpb = d.dpb; k.nrmp = d.nrmp;
+        k.H = d.H; k.cs = d.cs; k.sn = d.sn; k.g = d.g; k.y = d.y; k.hsum = d.hsum;
+        return k;
+    }
+    bem::KState kinit() const {
+        bem::KState q{};
+        q.phase = bem::kPhaseUpdate;
+        q.m = restart;
+        q.max_iter = max_iter;
+        q.tol = tol;
+        q.floor_rel = prec == BEM_PREC_MIXED ? 1e-5 : 0.0;
+        return q;
+    }
+    bem::AsmSys asys() const {
+        bem::AsmSys a{};
+        a.m = mesh->view();
+        a.f = freq;
+        a.A = d.A;
+        a.lda = lda;
+        a.near = mesh->d_near;
+        a.n_near = mesh->n_near;
+        a.b = (double *)d.b;
+        a.status = d.status;
+        return a;
+    }
+    bem::PcSys psys() const {
+        bem::PcSys p{};
+        p.A = d.A;
+        p.lda = lda;
+        p.n = n;
+        p.Minv = d.Minv;
+        p.work = d.Mwork;
+        p.status = d.status;
+        return p;
+    }
+    bem::ProjSys prsys(int npts, const double *pts_dev, double *pot_dev, double *grad_dev) const {
+        bem::ProjSys q{};
+        q.m = mesh->view();
+        q.f = freq;
+        q.x = (const double *)d.x;
+        q.phi = d.phi;
+        q.vel = d.vel;
+        q.ivi = d.ivi;
+        q.npts = npts;
+        q.pts = pts_dev;
+        q.pot = pot_dev;
+        q.grad = grad_dev;
+        q.status = d.status;
+        return q;
+    }
+};
+
+namespace {
+
+// host copy of a device buffer
+bem_status fetch(cudaStream_t st, const void *dsrc, void *hdst, size_t bytes) {
+    CU(cudaMemcpyAsync(hdst, dsrc, bytes, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return BEM_OK;
+}
+
+const char *subdivision_message(int code) {
+    return code == 1 ? "number of subelements which are subdivided in a loop must <= 15"
+                     : "number of subelements must be < 220";
+}
+
+// Frequency data into the solver's block (internal element order).  NumCalc
+// does the same per frequency in NC_UpdateFreqCurves before assembly.
+bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f, cudaStream_t st) {
+    const int n = s->n;
+    if (!(f->wave_number > 0.0)) return fail(BEM_ERR_INVALID, "wave number must be > 0");
+    if (f->n_point < 0 || f->n_plane < 0) return fail(BEM_ERR_INVALID, "negative source count");
+    if ((f->n_point && (!f->point_xyz || !f->point_amp)) || (f->n_plane && (!f->plane_dir || !f->plane_amp)))
+        return fail(BEM_ERR_INVALID, "source arrays missing");
+    bem::DevFreq &F = s->freq;
+    F = bem::DevFreq{};
+    const double htf = f->time_factor == -1.0 ? -1.0 : 1.0;
+    const double tao = f->tao == -1.0 ? -1.0 : 1.0;
+    F.k = f->wave_number;
+    F.wr = htf * f->wave_number;
+    F.tao = tao;
+    F.beta_im = tao < 0 ? 0.0 : htf / f->wave_number;   // NC_EquationSystem.cpp:85-86
+    F.kf = (float)F.k;
+    F.wrf = (float)F.wr;
+    F.taof = (float)F.tao;
+    F.beta_imf = (float)F.beta_im;
+    const std::vector<int> &ext = s->mesh->ext_of_int;
+    std::vector<int> cols, bct;
+    std::vector<double> bcv, adm, src;
+    if (f->bc_type) {
+        for (int j = 0; j < n; ++j)
+            if (f->bc_type[j] < 0 || f->bc_type[j] > 2)
+                return fail(BEM_ERR_INVALID, "element %d: boundary condition type %d unsupported", j, f->bc_type[j]);
+        bct.resize(n);
+        for (int i = 0; i < n; ++i) bct[i] = f->bc_type[ext[i]];
+        CU(cudaMemcpyAsync(s->d.bct, bct.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+        F.bc_type = s->d.bct;
+    }
+    if (f->bc_value) {
+        bcv.assign(8 * (size_t)n, 0.0);
+        for (int i = 0; i < n; ++i) {
+            const int j = ext[i];
+            bool nz = false;
+            for (int a = 0; a < 4; ++a) {
+                const double re = f->bc_value[8 * (size_t)j + 2 * a], im = f->bc_value[8 * (size_t)j + 2 * a + 1];
+                bcv[2 * ((size_t)a * n + i)] = re;
+                bcv[2 * ((size_t)a * n + i) + 1] = im;
+                // NumCalc's test: |value| > EPSY on the element's nodes (NC_EquationSystem.cpp:264-275)
+                if (a < s->mesh->nvert[i] && std::sqrt(re * re + im * im) > 1.0e-14) nz = true;
+            }
+            if (nz) cols.push_back(i);
+        }
+        CU(cudaMemcpyAsync(s->d.bcv, bcv.data(), sizeof(double) * bcv.size(), cudaMemcpyHostToDevice, st));
+        F.bc_val = s->d.bcv;
+    }
+    if (f->admittance) {
+        adm.resize(2 * (size_t)n);
+        for (int i = 0; i < n; ++i) {
+            adm[2 * (size_t)i] = f->admittance[2 * (size_t)ext[i]];
+            adm[2 * (size_t)i + 1] = f->admittance[2 * (size_t)ext[i] + 1];
+        }
+        CU(cudaMemcpyAsync(s->d.adm, adm.data(), sizeof(double) * adm.size(), cudaMemcpyHostToDevice, st));
+        F.adm = s->d.adm;
+    }
+    if (!cols.empty()) {
+        CU(cudaMemcpyAsync(s->d.cols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, st));
+        F.bc_cols = s->d.cols;
+        F.n_bc_cols = (int)cols.size();
+    }
+    const size_t nsrc = 5 * (size_t)f->n_point + 5 * (size_t)f->n_plane;
+    if (nsrc) {
+        // complex amplitudes first so that they start on 16-byte boundaries
+        // (the kernels read them as double2), coordinates after them
+        src.reserve(nsrc);
+        for (int i = 0; i < 2 * f->n_point; ++i) src.push_back(f->point_amp[i]);
+        for (int i = 0; i < 2 * f->n_plane; ++i) src.push_back(f->plane_amp[i]);
+        for (int i = 0; i < 3 * f->n_point; ++i) src.push_back(f->point_xyz[i]);
+        for (int i = 0; i < 3 * f->n_plane; ++i) src.push_back(f->plane_dir[i]);
+        double *dst = s->d.src;
+        if (f->n_point + f->n_plane > bem::kInlineSources) {
+            CU(cudaStreamSynchronize(st));
+            cudaFree(s->src_extra);
+            s->src_extra = nullptr;
+            CU(dalloc(&s->src_extra, src.size()));
+            dst = s->src_extra;
+        }
+        CU(cudaMemcpyAsync(dst, src.data(), sizeof(double) * src.size(), cudaMemcpyHostToDevice, st));
+        F.n_point = f->n_point;
+        F.n_plane = f->n_plane;
+        F.ps_amp = dst;
+        F.pw_amp = dst + 2 * (size_t)f->n_point;
+        F.ps_xyz = dst + 2 * (size_t)f->n_point + 2 * (size_t)f->n_plane;
+        F.pw_dir = F.ps_xyz + 3 * (size_t)f->n_point;
+    }
+    // the host vectors above go out of scope: finish the copies
+    CU(cudaStreamSynchronize(st));
+    return BEM_OK;
+}
+
+bem_status map_result(const bem::KState &q, int iters_limit_rc = 1) {
+    (void)iters_limit_rc;
+    switch (q.result) {
+    case bem::kResConverged: return BEM_OK;
+    case bem::kResBreakdown:
+        if (q.cycles == 0) return fail(BEM_ERR_INVALID, "right-hand side is not finite");
+        return fail(BEM_ERR_NOT_CONVERGED, "GMRES breakdown (non-finite residual)");
+    case bem::kResStagnated:
+        return fail(BEM_ERR_NOT_CONVERGED, "iterative refinement stagnated at relative residual %.3e after %d iterations",
+                    q.rel, q.iters);
+    default:
+        return fail(BEM_ERR_NOT_CONVERGED, "GMRES reached %d iterations, relative residual %.3e", q.iters, q.rel);
+    }
+}
+
+// One stream and one Krylov engine per thread and precision for the batched
+// entry points.
+struct BatchCtx {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[6] = {};
+    std::unique_ptr<bem::Engine> eng[2];
+    unsigned *ctr = nullptr;
+    ~BatchCtx() {
+        for (auto &e : eng) e.reset();
+        cudaFree(ctr);
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
         if (st) cudaStreamDestroy(st);
     }
 };
+thread_local std::unique_ptr<BatchCtx> t_batch;
+
+bem_status batch_ctx(BatchCtx **out) {
+    if (!t_batch) {
+        auto c = std::make_unique<BatchCtx>();
+        CU(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+        for (auto &e : c->ev) CU(cudaEventCreate(&e));
+        CU(cudaMalloc(&c->ctr, 4 * sizeof(unsigned)));
+        CU(cudaMemset(c->ctr, 0, 4 * sizeof(unsigned)));
+        t_batch = std::move(c);
+    }
+    *out = t_batch.get();
+    return BEM_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// ---- group operations shared by the single-solver and batched entry points
+
+bem_status assemble_group(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned *ctr, cudaEvent_t e0,
+                          cudaEvent_t e1, bem_status *rcs) {
+    const int prec = ss[0]->prec;
+    for (int i = 0; i < cnt; ++i) CU(cudaMemsetAsync(ss[i]->d.status, 0, sizeof(int), st));
+    CU(cudaEventRecord(e0, st));
+    std::unique_ptr<bem::AsmBatch> t(new bem::AsmBatch());
+    for (int c0 = 0; c0 < cnt; c0 += bem::kMaxAsm) {
+        const int k = std::min(bem::kMaxAsm, cnt - c0);
+        t->B = k;
+        for (int i = 0; i < k; ++i) t->sys[i] = ss[c0 + i]->asys();
+        bem::asm_batch_finish(*t);
+        CU(bem::launch_assemble(*t, prec, ctr, st));
+        CU(bem::launch_rhs(*t, st));
+    }
+    CU(cudaEventRecord(e1, st));
+    std::vector<int> code(cnt, 0);
+    for (int i = 0; i < cnt; ++i)
+        CU(cudaMemcpyAsync(&code[i], ss[i]->d.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, e0, e1));
+    bem_status first = BEM_OK;
+    for (int i = 0; i < cnt; ++i) {
+        bem_solver_t s = ss[i];
+        s->info.assemble_ms = ms;
+        s->info.n_near_pairs = (int64_t)(s->mesh->n_near - s->n);   // subdivided pairs (self pairs excluded)
+        s->have_freq = true;
+        s->solved = false;
+        rcs[i] = BEM_OK;
+        if (code[i] != 0) {
+            rcs[i] = fail(BEM_ERR_SUBDIVISION, "%s", subdivision_message(code[i]));
+            if (first == BEM_OK) first = rcs[i];
+        }
+    }
+    return first;
+}
+
+// Restarted GMRES of every solver in ss on the engine: preconditioner set-up,
+// then iteration bodies until every system has finished.
+bem_status solve_group(bem_solver_t *ss, int cnt, bem::Engine *eng, cudaStream_t st, cudaEvent_t e0,
+                       cudaEvent_t e1, bem_status *rcs) {
+    const int prec = ss[0]->prec;
+    CU(cudaEventRecord(e0, st));
+    std::unique_ptr<bem::PcBatch> pt(new bem::PcBatch());
+    std::vector<bem_solver_t> pcs;
+    for (int i = 0; i < cnt; ++i) {
+        ss[i]->have_precond = false;
+        if (ss[i]->precond) pcs.push_back(ss[i]);
+        CU(cudaMemsetAsync(ss[i]->d.x, 0, sizeof(double2) * ss[i]->n, st));
+    }
+    for (size_t c0 = 0; c0 < pcs.size(); c0 += bem::kMaxAsm) {
+        const int k = (int)std::min<size_t>(bem::kMaxAsm, pcs.size() - c0);
+        pt->B = k;
+        for (int i = 0; i < k; ++i) {
+            CU(cudaMemsetAsync(pcs[c0 + i]->d.status, 0, sizeof(int), st));
+            pt->sys[i] = pcs[c0 + i]->psys();
+        }
+        bem::pc_batch_finish(*pt);
+        CU(bem::launch_block_inverse(*pt, prec, st));
+    }
+    if (!pcs.empty()) {
+        std::vector<int> sing(pcs.size(), 0);
+        for (size_t i = 0; i < pcs.size(); ++i)
+            CU(cudaMemcpyAsync(&sing[i], pcs[i]->d.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < pcs.size(); ++i) pcs[i]->have_precond = sing[i] == 0;   // singular block: no M
+    }
+    bem_status first = BEM_OK;
+    for (int c0 = 0; c0 < cnt; c0 += bem::kMaxSys) {
+        const int k = std::min(bem::kMaxSys, cnt - c0);
+        std::vector<bem::KSys> sys(k);
+        std::vector<bem::KState> init(k);
+        long long guard = 0;
+        for (int i = 0; i < k; ++i) {
+            sys[i] = ss[c0 + i]->ksys();
+            init[i] = ss[c0 + i]->kinit();
+            guard = std::max<long long>(guard, 2LL * ss[c0 + i]->max_iter + 64);
+        }
+        CU(eng->set_batch(sys, init));
+        bool all_done = false;
+        for (long long body = 0; body < guard && !all_done; ++body) {
+            const cudaError_t be = eng->run_body();
+            if (be == cudaErrorLaunchTimeout)
+                return fail(BEM_ERR_DEVICE_TIMEOUT, "matrix-vector product: a bounded device wait gave up");
+            CU(be);
+            all_done = true;
+            for (int i = 0; i < k; ++i)
+                if (eng->states()[i].phase != bem::kPhaseFinished) all_done = false;
+        }
+        CU(cudaEventRecord(e1, st));
+        CU(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, e0, e1));
+        for (int i = 0; i < k; ++i) {
+            bem_solver_t s = ss[c0 + i];
+            const bem::KState &q = eng->states()[i];
+            s->info.solve_ms = ms;
+            s->info.iterations = q.iters;
+            s->info.restarts = q.cycles;
+            s->info.rel_residual = q.rel;
+            s->info.matvec_ms = eng->timing_ok() ? eng->matvec_ms() : 0.0;
+            s->info.n_matvec = q.n_mv;
+            s->solved = true;
+            if (q.phase != bem::kPhaseFinished) rcs[c0 + i] = fail(BEM_ERR_DEVICE_TIMEOUT, "GMRES did not finish");
+            else rcs[c0 + i] = map_result(q);
+            if (rcs[c0 + i] != BEM_OK && first == BEM_OK) first = rcs[c0 + i];
+        }
+        CU(cudaEventRecord(e0, st));
+    }
+    return first;
+}
+
+bem_status ensure_points(bem_solver_t s, int n_pts) {
+    if (n_pts <= s->pts_cap) return BEM_OK;
+    CU(cudaStreamSynchronize(s->st));
+    cudaFree(s->pts); cudaFree(s->pot); cudaFree(s->grad);
+    s->pts = s->pot = s->grad = nullptr;
+    s->pts_cap = 0;
+    CU(dalloc(&s->pts, 3 * (size_t)n_pts));
+    CU(dalloc(&s->pot, 2 * (size_t)n_pts));
+    CU(dalloc(&s->grad, 6 * (size_t)n_pts));
+    s->pts_cap = n_pts;
+    return BEM_OK;
+}
+
+// Fields and projection of every solver in ss; pts[i] (host) may be null
+// when npts[i] == 0.
+bem_status project_group(bem_solver_t *ss, int cnt, const int32_t *npts, const double *const *pts,
+                         double *const *pot_out, double *const *grad_out, cudaStream_t st, cudaEvent_t e0,
+                         cudaEvent_t e1, bem_status *rcs) {
+    const int prec = ss[0]->prec;
+    for (int i = 0; i < cnt; ++i) {
+        const int np = npts ? npts[i] : 0;
+        bem_status rc = ensure_points(ss[i], np);
+        if (rc != BEM_OK) return rc;
+        if (np > 0) CU(cudaMemcpyAsync(ss[i]->pts, pts[i], sizeof(double) * 3 * np, cudaMemcpyHostToDevice, st));
+        CU(cudaMemsetAsync(ss[i]->d.status, 0, sizeof(int), st));
+    }
+    CU(cudaEventRecord(e0, st));
+    std::unique_ptr<bem::ProjBatch> t(new bem::ProjBatch());
+    for (int c0 = 0; c0 < cnt; c0 += bem::kMaxAsm) {
+        const int k = std::min(bem::kMaxAsm, cnt - c0);
+        t->B = k;
+        for (int i = 0; i < k; ++i) {
+            bem_solver_t s = ss[c0 + i];
+            const int np = npts ? npts[c0 + i] : 0;
+            t->sys[i] = s->prsys(np, s->pts, (double *)s->pot, (double *)s->grad);
+        }
+        bem::proj_batch_finish(*t);
+        CU(bem::launch_fields(*t, st));
+        CU(bem::launch_project(*t, prec, st));
+    }
+    CU(cudaEventRecord(e1, st));
+    std::vector<int> code(cnt, 0);
+    for (int i = 0; i < cnt; ++i) {
+        const int np = npts ? npts[i] : 0;
+        if (np > 0 && pot_out && pot_out[i])
+            CU(cudaMemcpyAsync(pot_out[i], ss[i]->pot, sizeof(double) * 2 * np, cudaMemcpyDeviceToHost, st));
+        if (np > 0 && grad_out && grad_out[i])
+            CU(cudaMemcpyAsync(grad_out[i], ss[i]->grad, sizeof(double) * 6 * np, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(&code[i], ss[i]->d.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    }
+    CU(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, e0, e1));
+    bem_status first = BEM_OK;
+    for (int i = 0; i < cnt; ++i) {
+        ss[i]->info.project_ms = ms;
+        rcs[i] = BEM_OK;
+        if (code[i] != 0) {
+            rcs[i] = fail(BEM_ERR_SUBDIVISION, "evaluation point too close to the boundary: subdivision limit");
+            if (first == BEM_OK) first = rcs[i];
+        }
+    }
+    return first;
+}
+
+bem_status solution_to_host(bem_solver_t s, cudaStream_t st, double *x_host) {
+    std::vector<double> t(2 * (size_t)s->n);
+    bem_status rc = fetch(st, s->d.x, t.data(), t.size() * sizeof(double));
+    if (rc != BEM_OK) return rc;
+    const std::vector<int> &ext = s->mesh->ext_of_int;
+    for (int i = 0; i < s->n; ++i) {
+        x_host[2 * (size_t)ext[i]] = t[2 * (size_t)i];
+        x_host[2 * (size_t)ext[i] + 1] = t[2 * (size_t)i + 1];
+    }
+    return BEM_OK;
+}
+
+bem::Engine *solver_engine(bem_solver_t s) {
+    if (!s->eng) s->eng.reset(new bem::Engine(s->prec == BEM_PREC_FP64 ? 0 : 1, s->st));
+    return s->eng.get();
+}
+
+}  // namespace
 
 extern "C" {
 
 const char *bem_last_error(void) { return g_err.c_str(); }
 
-const char *bem_version(void) { return "mesh2hrtf_gb300 1.0 (sm_103a)"; }
+const char *bem_version(void) { return "mesh2hrtf_gb300 1.1 (sm_103a)"; }
 
 int64_t bem_kernel_launches(void) { return (int64_t)bem::launches(); }
 
@@ -209,14 +686,9 @@ bem_status bem_set_device(int32_t device) {
 }
 
 double bem_footprint_bytes(int32_t n_elem, int32_t precision, int32_t restart) {
-    const double n = (double)n_elem;
-    const double lda = (double)round_up((size_t)std::max(n_elem, 1), 32);
-    const double esz = precision == BEM_PREC_FP64 ? 16.0 : 8.0;
     const int m = restart > 0 ? restart : 60;
-    // matrix + Krylov basis + 5 work vectors + split x + fields (phi, 4 vel)
-    // + block-Jacobi inverses
-    return n * lda * esz + (m + 1) * n * 16.0 + 5 * n * 16.0 + n * 16.0 + 5 * n * 16.0 + n * 64.0 +
-           (double)bem::precond_bytes(n_elem, precision);
+    const int prec = precision == BEM_PREC_FP64 ? 0 : 1;
+    return (double)bem::solver_layout(std::max(n_elem, 1), prec, m, true, nullptr, nullptr);
 }
 
 bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
@@ -372,16 +844,19 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     if (p) prm = *p;
     if (prm.precision != BEM_PREC_FP64 && prm.precision != BEM_PREC_MIXED)
         return fail(BEM_ERR_INVALID, "unknown precision %d", prm.precision);
-    const int n = mesh->n;
     const int m = prm.restart > 0 ? prm.restart : 60;
-    const double need = bem_footprint_bytes(n, prm.precision, m);
+    if (m > bem::kMaxRestart) return fail(BEM_ERR_INVALID, "restart length %d above the limit %d", m, bem::kMaxRestart);
+    const int n = mesh->n;
+    const bool pc = prm.no_precond == 0;
+    const int prec = prm.precision == BEM_PREC_FP64 ? 0 : 1;
+    const size_t need = bem::solver_layout(n, prec, m, pc, nullptr, nullptr);
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
     double budget = prm.hbm_budget_bytes > 0 ? prm.hbm_budget_bytes : (double)free_b - 1.0e9;
-    if (need > budget)
+    if ((double)need > budget)
         return fail(BEM_ERR_OUT_OF_HBM, "solver for %d unknowns needs %.3f GB, budget %.3f GB", n, need / 1e9,
                     budget / 1e9);
-    bem_solver_s *s = new bem_solver_s();
+    std::unique_ptr<bem_solver_s> s(new bem_solver_s());
     s->mesh = mesh;
     s->n = n;
     s->prec = prm.precision;
@@ -389,52 +864,20 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     s->max_iter = prm.max_iter > 0 ? prm.max_iter : 1000;
     s->tol = prm.tol > 0 ? prm.tol : 1e-9;
     s->lda = round_up((size_t)n, 32);
-    const size_t esz = s->prec == BEM_PREC_FP64 ? 16 : 8;
-    auto cleanup = [&](cudaError_t e) {
-        delete s;
-        return fail(e == cudaErrorMemoryAllocation ? BEM_ERR_OUT_OF_HBM : BEM_ERR_CUDA, "solver allocation: %s",
-                    cudaGetErrorString(e));
-    };
+    s->precond = pc;
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     for (auto &ev : s->ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);
-    if (e == cudaSuccess) e = cudaMalloc(&s->A, (size_t)n * s->lda * esz);
-    if (e == cudaSuccess) e = dalloc(&s->b, 2 * (size_t)n);
-    if (e == cudaSuccess) e = dalloc(&s->x, 2 * (size_t)n);
-    if (e == cudaSuccess) e = dalloc(&s->r, 2 * (size_t)n);
-    if (e == cudaSuccess) e = dalloc(&s->w, 2 * (size_t)n);
-    if (e == cudaSuccess) e = dalloc(&s->V, 2 * (size_t)n * (m + 1));
-    if (e == cudaSuccess) e = dalloc(&s->hd, 2 * (size_t)(m + 2));
-    if (e == cudaSuccess) e = dalloc(&s->hsum, 2 * (size_t)(m + 2));
-    if (e == cudaSuccess) e = dalloc(&s->nrm, 4);
-    if (e == cudaSuccess) e = dalloc(&s->ydev, 2 * (size_t)(m + 2));
-    if (e == cudaSuccess) e = cudaMalloc(&s->xf, 16 * (size_t)n);
-    s->precond = prm.no_precond == 0;
-    if (s->precond) {
-        const size_t pb = bem::precond_bytes(n, s->prec);
-        const size_t half = s->prec == BEM_PREC_FP64 ? pb / 2 : pb;
-        if (e == cudaSuccess) e = cudaMalloc(&s->Minv, half);
-        if (e == cudaSuccess && s->prec == BEM_PREC_FP64) e = cudaMalloc(&s->Mwork, half);
-        if (e == cudaSuccess) e = dalloc(&s->z, 2 * (size_t)n);
+    if (e == cudaSuccess) e = cudaMalloc(&s->block, need);
+    if (e == cudaSuccess) {
+        s->block_bytes = need;
+        bem::solver_layout(n, prec, m, pc, s->block, &s->d);
+        e = cudaMemset(s->d.ctr, 0, 4 * sizeof(unsigned));
     }
-    if (e == cudaSuccess) e = dalloc(&s->status, 1);
-    if (e == cudaSuccess) e = dalloc(&s->n_near, 1);
-    if (e == cudaSuccess) e = dalloc(&s->phi, 2 * (size_t)n);
-    if (e == cudaSuccess) e = dalloc(&s->vel, 8 * (size_t)n);
-    if (e == cudaSuccess) e = dalloc(&s->ivi, (size_t)n);
-    if (e == cudaSuccess) e = dalloc(&s->Hd, 2 * (size_t)(m + 1) * m);
-    if (e == cudaSuccess) e = dalloc(&s->csd, 2 * (size_t)m);
-    if (e == cudaSuccess) e = dalloc(&s->snd, 2 * (size_t)m);
-    if (e == cudaSuccess) e = dalloc(&s->gd, 2 * (size_t)(m + 1));
-    if (e == cudaSuccess) e = dalloc(&s->partial, 2 * (size_t)(m + 2) * bem::dot_blocks(n));
-    if (e == cudaSuccess) e = cudaMalloc(&s->ctrl, sizeof(bem::GmresCtrl));
-    s->mv_ev.assign(2 * (size_t)m, nullptr);
-    for (auto &ev : s->mv_ev)
-        if (e == cudaSuccess) e = cudaEventCreate(&ev);
-    if (e == cudaSuccess)
-        e = cudaMallocHost(&s->h_pin, sizeof(double) * (2 * (size_t)(m + 1) * m + 2 * (size_t)(m + 4) + 8));
-    if (e != cudaSuccess) return cleanup(e);
-    *out = s;
+    if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? BEM_ERR_OUT_OF_HBM : BEM_ERR_CUDA, "solver allocation: %s",
+                    cudaGetErrorString(e));
+    *out = s.release();
     return BEM_OK;
 }
 
@@ -450,310 +893,32 @@ bem_status bem_solver_set_params(bem_solver_t s, const bem_solver_params *p) {
     return BEM_OK;
 }
 
-static bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f) {
-    const int n = s->n;
-    if (!(f->wave_number > 0.0)) return fail(BEM_ERR_INVALID, "wave number must be > 0");
-    if (f->n_point < 0 || f->n_plane < 0) return fail(BEM_ERR_INVALID, "negative source count");
-    if ((f->n_point && (!f->point_xyz || !f->point_amp)) || (f->n_plane && (!f->plane_dir || !f->plane_amp)))
-        return fail(BEM_ERR_INVALID, "source arrays missing");
-    bem::DevFreq &F = s->freq;
-    F = bem::DevFreq{};
-    const double htf = f->time_factor == -1.0 ? -1.0 : 1.0;
-    const double tao = f->tao == -1.0 ? -1.0 : 1.0;
-    F.k = f->wave_number;
-    F.wr = htf * f->wave_number;
-    F.tao = tao;
-    F.beta_im = tao < 0 ? 0.0 : htf / f->wave_number;   // NC_EquationSystem.cpp:85-86
-    F.kf = (float)F.k;
-    F.wrf = (float)F.wr;
-    F.taof = (float)F.tao;
-    F.beta_imf = (float)F.beta_im;
-    cudaFree(s->f_bct); cudaFree(s->f_cols); cudaFree(s->f_bcv); cudaFree(s->f_adm); cudaFree(s->f_src);
-    s->f_bct = s->f_cols = nullptr;
-    s->f_bcv = s->f_adm = s->f_src = nullptr;
-    std::vector<int> cols;
-    const std::vector<int> &ext = s->mesh->ext_of_int;
-    std::vector<int> bct_int;
-    if (f->bc_type) {
-        for (int j = 0; j < n; ++j)
-            if (f->bc_type[j] < 0 || f->bc_type[j] > 2)
-                return fail(BEM_ERR_INVALID, "element %d: boundary condition type %d unsupported", j, f->bc_type[j]);
-        bct_int.resize(n);
-        for (int i = 0; i < n; ++i) bct_int[i] = f->bc_type[ext[i]];
-        CU(dalloc(&s->f_bct, (size_t)n));
-        CU(cudaMemcpyAsync(s->f_bct, bct_int.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->st));
-        CU(cudaStreamSynchronize(s->st));
-        F.bc_type = s->f_bct;
-    }
-    if (f->bc_value) {
-        std::vector<double> t(8 * (size_t)n);
-        for (int i = 0; i < n; ++i) {
-            const int j = ext[i];
-            bool nz = false;
-            for (int a = 0; a < 4; ++a) {
-                const double re = f->bc_value[8 * (size_t)j + 2 * a], im = f->bc_value[8 * (size_t)j + 2 * a + 1];
-                t[2 * ((size_t)a * n + i)] = re;
-                t[2 * ((size_t)a * n + i) + 1] = im;
-                // NumCalc's test: |value| > EPSY on the element's nodes (NC_EquationSystem.cpp:264-275)
-                if (a < s->mesh->nvert[i] && std::sqrt(re * re + im * im) > 1.0e-14) nz = true;
-            }
-            if (nz) cols.push_back(i);
-        }
-        CU(dalloc(&s->f_bcv, t.size()));
-        CU(cudaMemcpyAsync(s->f_bcv, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, s->st));
-        CU(cudaStreamSynchronize(s->st));
-        F.bc_val = s->f_bcv;
-    }
-    if (f->admittance) {
-        std::vector<double> t(2 * (size_t)n);
-        for (int i = 0; i < n; ++i) {
-            t[2 * (size_t)i] = f->admittance[2 * (size_t)ext[i]];
-            t[2 * (size_t)i + 1] = f->admittance[2 * (size_t)ext[i] + 1];
-        }
-        CU(dalloc(&s->f_adm, 2 * (size_t)n));
-        CU(cudaMemcpyAsync(s->f_adm, t.data(), sizeof(double) * 2 * n, cudaMemcpyHostToDevice, s->st));
-        CU(cudaStreamSynchronize(s->st));
-        F.adm = s->f_adm;
-    }
-    if (!cols.empty()) {
-        CU(dalloc(&s->f_cols, cols.size()));
-        CU(cudaMemcpyAsync(s->f_cols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, s->st));
-        CU(cudaStreamSynchronize(s->st));
-        F.bc_cols = s->f_cols;
-        F.n_bc_cols = (int)cols.size();
-    }
-    const size_t nsrc = 5 * (size_t)f->n_point + 5 * (size_t)f->n_plane;
-    if (nsrc) {
-        // complex amplitudes first so that they start on 16-byte boundaries
-        // (the kernels read them as double2), coordinates after them
-        std::vector<double> src;
-        src.reserve(nsrc);
-        for (int i = 0; i < 2 * f->n_point; ++i) src.push_back(f->point_amp[i]);
-        for (int i = 0; i < 2 * f->n_plane; ++i) src.push_back(f->plane_amp[i]);
-        for (int i = 0; i < 3 * f->n_point; ++i) src.push_back(f->point_xyz[i]);
-        for (int i = 0; i < 3 * f->n_plane; ++i) src.push_back(f->plane_dir[i]);
-        CU(dalloc(&s->f_src, src.size()));
-        CU(cudaMemcpyAsync(s->f_src, src.data(), sizeof(double) * src.size(), cudaMemcpyHostToDevice, s->st));
-        CU(cudaStreamSynchronize(s->st));
-        F.n_point = f->n_point;
-        F.n_plane = f->n_plane;
-        F.ps_amp = s->f_src;
-        F.pw_amp = s->f_src + 2 * (size_t)f->n_point;
-        F.ps_xyz = s->f_src + 2 * (size_t)f->n_point + 2 * (size_t)f->n_plane;
-        F.pw_dir = F.ps_xyz + 3 * (size_t)f->n_point;
-    }
-    return BEM_OK;
-}
-
 bem_status bem_assemble(bem_solver_t s, const bem_frequency_desc *f) {
     if (!s || !f) return fail(BEM_ERR_INVALID, "null argument");
-    bem_status rc = upload_freq(s, f);
+    bem_status rc = upload_freq(s, f, s->st);
     if (rc != BEM_OK) return rc;
-    CU(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
-    CU(cudaEventRecord(s->ev[0], s->st));
-    CU(bem::launch_assemble(s->mesh->view(), s->freq, s->prec, s->A, s->lda, s->mesh->d_near, s->mesh->n_near,
-                            s->status, s->st));
-    CU(bem::launch_rhs(s->mesh->view(), s->freq, s->b, s->status, s->st));
-    CU(cudaEventRecord(s->ev[1], s->st));
-    int st_h = 0;
-    CU(cudaMemcpyAsync(&st_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->st));
-    CU(cudaStreamSynchronize(s->st));
-    const long long nn = s->mesh->n_near - s->n;   // subdivided pairs (self pairs excluded)
-    float ms = 0.f;
-    CU(cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]));
-    s->info.assemble_ms = ms;
-    s->info.n_near_pairs = (int64_t)nn;
-    s->have_freq = true;
-    s->solved = false;
-    if (st_h != 0)
-        return fail(BEM_ERR_SUBDIVISION,
-                    st_h == 1 ? "number of subelements which are subdivided in a loop must <= 15"
-                              : "number of subelements must be < 220");
-    return BEM_OK;
+    bem_status one = BEM_OK;
+    return assemble_group(&s, 1, s->st, s->d.ctr, s->ev[0], s->ev[1], &one);
 }
 
-namespace {
-
-// host copy of a device complex vector
-bem_status fetch(bem_solver_t s, const double *dsrc, double *hdst, size_t ndoubles) {
-    CU(cudaMemcpyAsync(hdst, dsrc, ndoubles * sizeof(double), cudaMemcpyDeviceToHost, s->st));
-    CU(cudaStreamSynchronize(s->st));
-    return BEM_OK;
-}
-
-}  // namespace
-
-// Restarted GMRES.  Each cycle starts from the explicitly computed residual
-// r = b - A x, so with BEM_PREC_MIXED every cycle is one step of iterative
-// refinement: the inner Arnoldi process (FP64 vectors, CGS with one
-// re-orthogonalisation, FP64 inner products) works with the fast FP32
-// matrix-vector product and stops once it has gained five digits, and the
-// outer residual is evaluated with the error-free-transformation product.
+// Restarted GMRES (bem_gmres.cu).  Each cycle starts from the explicitly
+// computed residual r = b - A x, so with BEM_PREC_MIXED every cycle is one
+// step of iterative refinement: the inner Arnoldi process (FP64 vectors,
+// classical Gram-Schmidt with one re-orthogonalisation, FP64 inner products)
+// uses the FP32 matrix-vector product and stops once it has gained five
+// digits, and the outer residual is evaluated with error-free products.
 bem_status bem_solve(bem_solver_t s, bem_solve_info *info) {
     if (!s) return fail(BEM_ERR_INVALID, "null solver");
     if (!s->have_freq) return fail(BEM_ERR_INVALID, "bem_solve before bem_assemble");
-    const int n = s->n, m = s->restart;
-    const size_t ldv = 2 * (size_t)n;      // doubles between basis vectors
-    const size_t ldc = (size_t)n;          // complex entries between basis vectors
-    CU(cudaEventRecord(s->ev[2], s->st));
-    // block-Jacobi inverses of this frequency's matrix
-    s->have_precond = false;
-    if (s->precond) {
-        CU(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
-        CU(bem::launch_block_inverse(s->prec, s->A, s->lda, n, s->Minv, s->Mwork, s->status, s->st));
-        int sing = 0;
-        CU(cudaMemcpyAsync(&sing, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->st));
-        CU(cudaStreamSynchronize(s->st));
-        s->have_precond = sing == 0;   // a singular block: solve unpreconditioned
-    }
-    const bool pc = s->have_precond;
-    CU(cudaMemsetAsync(s->x, 0, sizeof(double) * 2 * n, s->st));
-    CU(bem::launch_norm2(s->b, n, s->nrm, s->st));
-    double *hp = s->h_pin;
-    bem_status rc = fetch(s, s->nrm, hp, 1);
-    if (rc) return rc;
-    const double bnorm = std::sqrt(hp[0]);
-    int iters = 0, cycles = 0, n_mv = 0;
-    double rel = 0.0, mv_ms = 0.0;
-    bool converged = false;
-    if (bnorm == 0.0 || !std::isfinite(bnorm)) {
-        converged = bnorm == 0.0;
-        if (!converged) return fail(BEM_ERR_INVALID, "right-hand side is not finite");
-    } else {
-        CU(cudaMemcpyAsync(s->r, s->b, sizeof(double) * 2 * n, cudaMemcpyDeviceToDevice, s->st));
-        CU(cudaMemcpyAsync(s->nrm + 2, s->nrm, sizeof(double), cudaMemcpyDeviceToDevice, s->st));
-        double beta = bnorm, prev_beta = 0.0;
-        std::vector<cd> H((size_t)(m + 1) * m), g(m + 1), y(m);
-        const int batch = 8;   // Arnoldi steps queued between convergence checks
-        while (true) {
-            ++cycles;
-            // cycle set-up: V0 = r / beta, g = (beta, 0, ...), hsum = 0, ctrl
-            CU(bem::launch_scale_inv(s->r, s->nrm + 2, s->V, n, s->st));
-            CU(cudaMemsetAsync(s->gd, 0, sizeof(double) * 2 * (m + 1), s->st));
-            CU(cudaMemsetAsync(s->hsum, 0, sizeof(double) * 2 * (m + 1), s->st));
-            const double inner_floor = s->prec == BEM_PREC_MIXED ? 1e-5 * beta : 0.0;
-            bem::GmresCtrl c0{0, 0, 0.0, std::max(s->tol * bnorm, inner_floor)};
-            double *hc = hp + 2 * (size_t)(m + 1) * m + 2 * (size_t)(m + 4);
-            std::memcpy(hc, &c0, sizeof(c0));
-            hc[4] = beta;
-            hc[5] = 0.0;
-            CU(cudaMemcpyAsync(s->ctrl, hc, sizeof(c0), cudaMemcpyHostToDevice, s->st));
-            CU(cudaMemcpyAsync(s->gd, hc + 4, sizeof(double) * 2, cudaMemcpyHostToDevice, s->st));
-            const int *done = &s->ctrl->done;
-            const int kmax = std::min(m, s->max_iter - iters);
-            int k = 0, kdone = 0;
-            bool cyc_done = false;
-            while (k < kmax && !cyc_done) {
-                const int k_end = std::min(kmax, k + batch);
-                for (; k < k_end; ++k) {
-                    double *vk = s->V + (size_t)k * ldv;
-                    if (pc) {
-                        CU(bem::launch_block_apply(s->prec, s->Minv, n, vk, s->z, s->st, done));
-                        vk = s->z;
-                    }
-                    CU(cudaEventRecord(s->mv_ev[2 * k], s->st));
-                    CU(bem::launch_matvec(s->prec, false, s->A, n, s->lda, vk, nullptr, s->w, s->xf, s->st, done));
-                    CU(cudaEventRecord(s->mv_ev[2 * k + 1], s->st));
-                    for (int pass = 0; pass < 2; ++pass) {   // classical Gram-Schmidt, twice
-                        CU(bem::launch_multi_dot(s->V, ldc, k + 1, s->w, n, s->partial, s->hd, s->hsum, s->st, done));
-                        CU(bem::launch_multi_axpy(s->V, ldc, k + 1, s->hd, s->w, n, s->st, done));
-                    }
-                    CU(bem::launch_multi_dot(s->w, ldc, 1, s->w, n, s->partial, s->nrm, nullptr, s->st, done));
-                    CU(bem::launch_scale_inv(s->w, s->nrm, s->V + (size_t)(k + 1) * ldv, n, s->st, done));
-                    CU(bem::launch_givens(k, m, s->hsum, s->nrm, s->Hd, s->csd, s->snd, s->gd, s->ctrl, s->st));
-                }
-                bem::GmresCtrl cs_h;
-                CU(cudaMemcpyAsync(hc, s->ctrl, sizeof(cs_h), cudaMemcpyDeviceToHost, s->st));
-                CU(cudaStreamSynchronize(s->st));
-                std::memcpy(&cs_h, hc, sizeof(cs_h));
-                kdone = cs_h.kdone;
-                cyc_done = cs_h.done != 0;
-                if (!std::isfinite(cs_h.res)) return fail(BEM_ERR_NOT_CONVERGED, "GMRES breakdown (non-finite residual)");
-            }
-            for (int q = 0; q < kdone; ++q) {
-                float mv = 0.f;
-                CU(cudaEventElapsedTime(&mv, s->mv_ev[2 * q], s->mv_ev[2 * q + 1]));
-                mv_ms += mv;
-                ++n_mv;
-            }
-            iters += kdone;
-            const int kk = kdone;
-            if (kk > 0) {
-                // y = H^{-1} g on the host (kk x kk upper triangular)
-                CU(cudaMemcpyAsync(hp, s->Hd, sizeof(double) * 2 * (size_t)(m + 1) * m, cudaMemcpyDeviceToHost, s->st));
-                CU(cudaMemcpyAsync(hp + 2 * (size_t)(m + 1) * m, s->gd, sizeof(double) * 2 * (m + 1),
-                                   cudaMemcpyDeviceToHost, s->st));
-                CU(cudaStreamSynchronize(s->st));
-                for (size_t q = 0; q < (size_t)(m + 1) * m; ++q) H[q] = cd(hp[2 * q], hp[2 * q + 1]);
-                const double *gp = hp + 2 * (size_t)(m + 1) * m;
-                for (int q = 0; q <= m; ++q) g[q] = cd(gp[2 * q], gp[2 * q + 1]);
-                for (int i2 = kk - 1; i2 >= 0; --i2) {
-                    cd acc = g[i2];
-                    for (int l = i2 + 1; l < kk; ++l) acc -= H[(size_t)i2 * m + l] * y[l];
-                    y[i2] = acc / H[(size_t)i2 * m + i2];
-                }
-                for (int l = 0; l < kk; ++l) { hp[2 * l] = y[l].real(); hp[2 * l + 1] = y[l].imag(); }
-                CU(cudaMemcpyAsync(s->ydev, hp, sizeof(double) * 2 * kk, cudaMemcpyHostToDevice, s->st));
-                if (pc) {
-                    // x += M^{-1} (V y)
-                    CU(cudaMemsetAsync(s->w, 0, sizeof(double) * 2 * n, s->st));
-                    CU(bem::launch_update_x(s->V, (int)ldc, kk, s->ydev, s->w, n, s->st));
-                    CU(bem::launch_block_apply(s->prec, s->Minv, n, s->w, s->z, s->st));
-                    CU(bem::launch_axpy(s->z, s->x, n, s->st));
-                } else {
-                    CU(bem::launch_update_x(s->V, (int)ldc, kk, s->ydev, s->x, n, s->st));
-                }
-            }
-            // explicit residual (the refinement step)
-            CU(cudaEventRecord(s->ev[6], s->st));
-            CU(bem::launch_matvec(s->prec, true, s->A, n, s->lda, s->x, s->b, s->r, s->xf, s->st));
-            CU(cudaEventRecord(s->ev[7], s->st));
-            CU(bem::launch_norm2(s->r, n, s->nrm + 2, s->st));
-            rc = fetch(s, s->nrm + 2, hp, 1);
-            if (rc) return rc;
-            {
-                float mv = 0.f;
-                CU(cudaEventElapsedTime(&mv, s->ev[6], s->ev[7]));
-                mv_ms += mv;
-                ++n_mv;
-            }
-            prev_beta = beta;
-            beta = std::sqrt(hp[0]);
-            rel = beta / bnorm;
-            if (!std::isfinite(rel)) return fail(BEM_ERR_NOT_CONVERGED, "GMRES breakdown (non-finite residual)");
-            if (rel <= s->tol) { converged = true; break; }
-            if (iters >= s->max_iter) break;
-            if (cycles > 2 && beta > 0.9 * prev_beta && s->prec == BEM_PREC_MIXED) break;  // refinement stagnates
-        }
-    }
-    CU(cudaEventRecord(s->ev[3], s->st));
-    CU(cudaEventSynchronize(s->ev[3]));
-    float ms = 0.f;
-    CU(cudaEventElapsedTime(&ms, s->ev[2], s->ev[3]));
-    s->info.solve_ms = ms;
-    s->info.iterations = iters;
-    s->info.restarts = cycles;
-    s->info.rel_residual = rel;
-    s->info.matvec_ms = mv_ms;
-    s->info.n_matvec = n_mv;
-    s->solved = true;
+    bem_status one = BEM_OK;
+    bem_status rc = solve_group(&s, 1, solver_engine(s), s->st, s->ev[2], s->ev[3], &one);
     if (info) *info = s->info;
-    if (!converged)
-        return fail(BEM_ERR_NOT_CONVERGED, "GMRES reached %d iterations, relative residual %.3e", iters, rel);
-    return BEM_OK;
+    return rc;
 }
 
 bem_status bem_get_solution(bem_solver_t s, double *x_host) {
     if (!s || !x_host) return fail(BEM_ERR_INVALID, "null argument");
-    std::vector<double> t(2 * (size_t)s->n);
-    bem_status rc = fetch(s, s->x, t.data(), t.size());
-    if (rc != BEM_OK) return rc;
-    const std::vector<int> &ext = s->mesh->ext_of_int;
-    for (int i = 0; i < s->n; ++i) {
-        x_host[2 * (size_t)ext[i]] = t[2 * (size_t)i];
-        x_host[2 * (size_t)ext[i] + 1] = t[2 * (size_t)i + 1];
-    }
-    return BEM_OK;
+    return solution_to_host(s, s->st, x_host);
 }
 
 bem_status bem_get_system(bem_solver_t s, int32_t row0, int32_t row1, double *a_host, double *b_host) {
@@ -767,7 +932,7 @@ bem_status bem_get_system(bem_solver_t s, int32_t row0, int32_t row1, double *a_
         std::vector<unsigned char> row(esz * (size_t)n);
         for (int r = row0; r < row1; ++r) {
             const int ir = ie[r];
-            CU(cudaMemcpyAsync(row.data(), (const char *)s->A + (size_t)ir * s->lda * esz, esz * n,
+            CU(cudaMemcpyAsync(row.data(), (const char *)s->d.A + (size_t)ir * s->lda * esz, esz * n,
                                cudaMemcpyDeviceToHost, s->st));
             CU(cudaStreamSynchronize(s->st));
             double *out = a_host + 2 * (size_t)(r - row0) * n;
@@ -787,7 +952,7 @@ bem_status bem_get_system(bem_solver_t s, int32_t row0, int32_t row1, double *a_
     }
     if (b_host) {
         std::vector<double> t(2 * (size_t)n);
-        bem_status rc = fetch(s, s->b, t.data(), t.size());
+        bem_status rc = fetch(s->st, s->d.b, t.data(), t.size() * sizeof(double));
         if (rc != BEM_OK) return rc;
         for (int i = 0; i < n; ++i) {
             b_host[2 * (size_t)ext[i]] = t[2 * (size_t)i];
@@ -801,36 +966,8 @@ bem_status bem_project(bem_solver_t s, int32_t n_pts, const double *pts, double 
     if (!s) return fail(BEM_ERR_INVALID, "null solver");
     if (!s->solved) return fail(BEM_ERR_INVALID, "bem_project before bem_solve");
     if (n_pts < 0 || (n_pts > 0 && (!pts || !pot_out))) return fail(BEM_ERR_INVALID, "bad point arrays");
-    if (n_pts > s->pts_cap) {
-        cudaFree(s->pts); cudaFree(s->pot); cudaFree(s->grad);
-        s->pts = s->pot = s->grad = nullptr;
-        s->pts_cap = 0;
-        CU(dalloc(&s->pts, 3 * (size_t)n_pts));
-        CU(dalloc(&s->pot, 2 * (size_t)n_pts));
-        CU(dalloc(&s->grad, 6 * (size_t)n_pts));
-        s->pts_cap = n_pts;
-    }
-    CU(cudaEventRecord(s->ev[4], s->st));
-    CU(bem::launch_fields(s->mesh->view(), s->freq, s->x, s->phi, s->vel, s->ivi, s->st));
-    if (n_pts > 0) {
-        CU(cudaMemcpyAsync(s->pts, pts, sizeof(double) * 3 * n_pts, cudaMemcpyHostToDevice, s->st));
-        CU(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
-        CU(bem::launch_project(s->mesh->view(), s->freq, s->prec, s->phi, s->vel, s->ivi, n_pts, s->pts, s->pot,
-                               s->grad, s->status, s->st));
-        CU(cudaMemcpyAsync(pot_out, s->pot, sizeof(double) * 2 * n_pts, cudaMemcpyDeviceToHost, s->st));
-        if (grad_out)
-            CU(cudaMemcpyAsync(grad_out, s->grad, sizeof(double) * 6 * n_pts, cudaMemcpyDeviceToHost, s->st));
-    }
-    CU(cudaEventRecord(s->ev[5], s->st));
-    int st_h = 0;
-    CU(cudaMemcpyAsync(&st_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->st));
-    CU(cudaStreamSynchronize(s->st));
-    float ms = 0.f;
-    CU(cudaEventElapsedTime(&ms, s->ev[4], s->ev[5]));
-    s->info.project_ms = ms;
-    if (st_h != 0)
-        return fail(BEM_ERR_SUBDIVISION, "evaluation point too close to the boundary: subdivision limit");
-    return BEM_OK;
+    bem_status one = BEM_OK;
+    return project_group(&s, 1, &n_pts, &pts, &pot_out, &grad_out, s->st, s->ev[4], s->ev[5], &one);
 }
 
 bem_status bem_solve_frequency(bem_solver_t s, const bem_frequency_desc *f, int32_t n_pts, const double *pts,
@@ -850,14 +987,95 @@ bem_status bem_solve_frequency(bem_solver_t s, const bem_frequency_desc *f, int3
     return solve_rc;
 }
 
+bem_status bem_solve_batch(int32_t count, const bem_solver_t *solvers, const bem_frequency_desc *freqs,
+                           const int32_t *n_pts, const double *const *pts, double *const *x_out,
+                           double *const *pot_out, double *const *grad_out, bem_solve_info *infos,
+                           bem_status *statuses) {
+    if (count < 0 || (count > 0 && (!solvers || !freqs))) return fail(BEM_ERR_INVALID, "bad batch arrays");
+    if (count == 0) return BEM_OK;
+    for (int i = 0; i < count; ++i) {
+        if (!solvers[i]) return fail(BEM_ERR_INVALID, "solver %d is null", i);
+        for (int j = 0; j < i; ++j)
+            if (solvers[j] == solvers[i]) return fail(BEM_ERR_INVALID, "solver %d appears twice in the batch", i);
+        const int np = n_pts ? n_pts[i] : 0;
+        if (np < 0 || (np > 0 && (!pts || !pts[i] || !pot_out || !pot_out[i])))
+            return fail(BEM_ERR_INVALID, "bad point arrays of instance %d", i);
+    }
+    BatchCtx *ctx = nullptr;
+    bem_status rc = batch_ctx(&ctx);
+    if (rc != BEM_OK) return rc;
+    for (int i = 0; i < count; ++i) CU(cudaStreamSynchronize(solvers[i]->st));
+    std::vector<bem_status> rcs(count, BEM_OK), tmp(count, BEM_OK);
+    bem_status first = BEM_OK;
+    auto note = [&](int i, bem_status r) {
+        if (r != BEM_OK && rcs[i] == BEM_OK) rcs[i] = r;
+        if (r != BEM_OK && first == BEM_OK) first = r;
+    };
+    // per precision: one group for the assembly, the solve and the projection
+    for (int prec = 0; prec < 2; ++prec) {
+        std::vector<int> idx;
+        for (int i = 0; i < count; ++i)
+            if ((solvers[i]->prec == BEM_PREC_FP64 ? 0 : 1) == prec) idx.push_back(i);
+        if (idx.empty()) continue;
+        std::vector<bem_solver_t> g;
+        for (int i : idx) {
+            bem_status r = upload_freq(solvers[i], &freqs[i], ctx->st);
+            if (r != BEM_OK) note(i, r);
+            else g.push_back(solvers[i]);
+        }
+        if (g.empty()) continue;
+        std::vector<int> gi;
+        for (int i : idx)
+            if (rcs[i] == BEM_OK) gi.push_back(i);
+        const int cnt = (int)g.size();
+        rc = assemble_group(g.data(), cnt, ctx->st, ctx->ctr, ctx->ev[0], ctx->ev[1], tmp.data());
+        if (rc == BEM_ERR_CUDA) return rc;
+        for (int q = 0; q < cnt; ++q) note(gi[q], tmp[q]);
+        if (!ctx->eng[prec]) ctx->eng[prec].reset(new bem::Engine(prec, ctx->st));
+        rc = solve_group(g.data(), cnt, ctx->eng[prec].get(), ctx->st, ctx->ev[2], ctx->ev[3], tmp.data());
+        if (rc == BEM_ERR_CUDA || rc == BEM_ERR_DEVICE_TIMEOUT) return rc;
+        for (int q = 0; q < cnt; ++q) note(gi[q], tmp[q]);
+        std::vector<int32_t> np(cnt, 0);
+        std::vector<const double *> pp(cnt, nullptr);
+        std::vector<double *> po(cnt, nullptr), pg(cnt, nullptr);
+        for (int q = 0; q < cnt; ++q) {
+            const int i = gi[q];
+            np[q] = n_pts ? n_pts[i] : 0;
+            pp[q] = np[q] ? pts[i] : nullptr;
+            po[q] = pot_out ? pot_out[i] : nullptr;
+            pg[q] = grad_out ? grad_out[i] : nullptr;
+        }
+        rc = project_group(g.data(), cnt, np.data(), pp.data(), po.data(), pg.data(), ctx->st, ctx->ev[4],
+                           ctx->ev[5], tmp.data());
+        if (rc == BEM_ERR_CUDA) return rc;
+        for (int q = 0; q < cnt; ++q) note(gi[q], tmp[q]);
+        for (int q = 0; q < cnt; ++q) {
+            const int i = gi[q];
+            if (x_out && x_out[i]) {
+                bem_status r = solution_to_host(g[q], ctx->st, x_out[i]);
+                if (r != BEM_OK) return r;
+            }
+        }
+    }
+    for (int i = 0; i < count; ++i) {
+        if (infos) infos[i] = solvers[i]->info;
+        if (statuses) statuses[i] = rcs[i];
+    }
+    if (first != BEM_OK) {
+        // keep the message of the first failing instance
+        for (int i = 0; i < count; ++i)
+            if (rcs[i] != BEM_OK) return rcs[i];
+    }
+    return BEM_OK;
+}
+
 }  // extern "C"
 
 namespace bem {
 
 // Inputs of the projection kernels held by a solved solver (for
 // bem_project_static in bem_static.cu).
-bool solver_projection_inputs(bem_solver_t s, int max_elem, DevMeshView *m, DevFreq *f, int *prec,
-                              const double **x, int *n) {
+bool solver_projection_inputs(bem_solver_t s, int max_elem, ProjSys *out, int *prec) {
     if (!s) { g_err = "null solver"; return false; }
     if (s->n > max_elem) {
         char buf[160];
@@ -867,11 +1085,8 @@ bool solver_projection_inputs(bem_solver_t s, int max_elem, DevMeshView *m, DevF
         return false;
     }
     if (!s->solved) { g_err = "bem_project_static before bem_solve"; return false; }
-    *m = s->mesh->view();
-    *f = s->freq;
+    *out = s->prsys(0, nullptr, nullptr, nullptr);
     *prec = s->prec;
-    *x = s->x;
-    *n = s->n;
     return true;
 }
 

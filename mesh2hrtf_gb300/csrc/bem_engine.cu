@@ -1,0 +1,131 @@
+// bem_engine.cu - host side of the batched Krylov engine: launch table,
+// work-item lists, graph capture and replay.
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "bem_engine.h"
+
+namespace bem {
+
+Engine::~Engine() {
+    if (st_) cudaStreamSynchronize(st_);
+    if (exec_) cudaGraphExecDestroy(exec_);
+    for (auto &e : ev_)
+        if (e) cudaEventDestroy(e);
+    cudaFree(d_tab_);
+    cudaFree(d_st_);
+    cudaFree(d_items_);
+    if (h_tab_) cudaFreeHost(h_tab_);
+    if (h_st_) cudaFreeHost(h_st_);
+}
+
+cudaError_t Engine::ensure_init() {
+    if (d_tab_) return cudaSuccess;
+    cudaError_t e = krylov_prepare();
+    if (e == cudaSuccess) e = cudaMalloc(&d_tab_, sizeof(KTable));
+    if (e == cudaSuccess) e = cudaMalloc(&d_st_, sizeof(KState) * kMaxSys);
+    if (e == cudaSuccess) e = cudaMallocHost(&h_tab_, sizeof(KTable));
+    if (e == cudaSuccess) e = cudaMallocHost(&h_st_, sizeof(KState) * kMaxSys);
+    for (auto &ev : ev_)
+        if (e == cudaSuccess) e = cudaEventCreate(&ev);
+    if (e == cudaSuccess) {
+        std::memset(h_tab_, 0, sizeof(KTable));
+        std::memset(h_st_, 0, sizeof(KState) * kMaxSys);
+        e = cudaMemcpyAsync(d_tab_, h_tab_, sizeof(KTable), cudaMemcpyHostToDevice, st_);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    return e;
+}
+
+cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KState> &init) {
+    if (sys.size() != init.size() || sys.size() > (size_t)kMaxSys) return cudaErrorInvalidValue;
+    cudaError_t e = ensure_init();
+    if (e != cudaSuccess) return e;
+    // the previous replay (if any) has completed: run_body synchronizes
+    const int B = (int)sys.size();
+    items_.clear();
+    int mv_total = 0, vb_total = 0;
+    for (int b = 0; b < B; ++b) mv_total += mv_items_of(sys[b].n, prec_);
+    for (int b = 0; b < B; ++b) vb_total += sys[b].nvb;
+    items_.reserve((size_t)mv_total + vb_total);
+    for (int b = 0; b < B; ++b) {
+        const int cnt = mv_items_of(sys[b].n, prec_);
+        for (int q = 0; q < cnt; ++q) items_.push_back(make_int2(b, q));
+    }
+    for (int b = 0; b < B; ++b)
+        for (int q = 0; q < sys[b].nvb; ++q) items_.push_back(make_int2(b, q));
+    if (items_.size() > items_cap_) {
+        cudaFree(d_items_);
+        d_items_ = nullptr;
+        items_cap_ = 0;
+        const size_t cap = items_.size() + items_.size() / 4 + 1024;
+        e = cudaMalloc(&d_items_, cap * sizeof(int2));
+        if (e != cudaSuccess) return e;
+        items_cap_ = cap;
+    }
+    if (!items_.empty())
+        e = cudaMemcpyAsync(d_items_, items_.data(), items_.size() * sizeof(int2), cudaMemcpyHostToDevice, st_);
+    if (e != cudaSuccess) return e;
+    std::memset(h_tab_, 0, sizeof(KTable));
+    h_tab_->B = B;
+    h_tab_->mv_total = mv_total;
+    h_tab_->vb_total = vb_total;
+    h_tab_->mv_items = d_items_;
+    h_tab_->vb_items = d_items_ + mv_total;
+    for (int b = 0; b < B; ++b) {
+        h_tab_->sys[b] = sys[b];
+        h_tab_->sys[b].st = d_st_ + b;
+        h_st_[b] = init[b];
+    }
+    e = cudaMemcpyAsync(d_tab_, h_tab_, sizeof(KTable), cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess && B > 0)
+        e = cudaMemcpyAsync(d_st_, h_st_, sizeof(KState) * B, cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    B_ = B;
+    mv_ms_ = 0.0;
+    bodies_ = 0;
+    return e;
+}
+
+cudaError_t Engine::run_body() {
+    cudaError_t e = ensure_init();
+    if (e != cudaSuccess) return e;
+    if (!exec_) {
+        cudaGraph_t g = nullptr;
+        e = cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        cudaError_t le = launch_krylov_body(prec_, d_tab_, ev_, st_, &body_launches_);
+        e = cudaStreamEndCapture(st_, &g);
+        if (le != cudaSuccess) e = le;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec_, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            exec_ = nullptr;
+            return e;
+        }
+    }
+    e = cudaGraphLaunch(exec_, st_);
+    if (e == cudaSuccess && B_ > 0)
+        e = cudaMemcpyAsync(h_st_, d_st_, sizeof(KState) * B_, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h_tab_->err, &d_tab_->err, sizeof(int), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return e;
+    if (h_tab_->err) return cudaErrorLaunchTimeout;   // a bounded wait in the product gave up
+    count_launches(body_launches_);
+    ++bodies_;
+    if (timing_ok_) {
+        for (int q = 0; q <= kSteps; ++q) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ev_[2 * q], ev_[2 * q + 1]) != cudaSuccess) {
+                cudaGetLastError();
+                timing_ok_ = false;
+                break;
+            }
+            mv_ms_ += ms;
+        }
+    }
+    return cudaSuccess;
+}
+
+}  // namespace bem

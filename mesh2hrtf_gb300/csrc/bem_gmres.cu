@@ -1,0 +1,853 @@
+// bem_gmres.cu - restarted GMRES with iterative refinement for a batch of
+// dense BEM systems, driven entirely on the device.
+//
+// Counterpart of NumCalc's NC_IterativeSolverCGS with its preconditioners
+// and matrix-vector product (NC_CommonFunctions.cpp:1066-1245, 1322-1721).
+// The method is different (GMRES with a block-Jacobi preconditioner and
+// refinement instead of CGS with a threshold ILU); the system solved and the
+// stopping rule (relative residual below 1e-9 by default) are NumCalc's.
+//
+// Every system of the batch carries a small state machine (KState) in device
+// memory.  An iteration body runs kSteps Arnoldi steps for each system in
+// phase ARNOLDI and then the end of cycle for each system in phase UPDATE;
+// kernels skip the systems that are in another phase.  The body never needs
+// the host, so it is captured once as a CUDA graph and replayed; the host
+// reads the states after each replay and admits or retires systems between
+// replays.  The per-system arithmetic does not depend on the other systems of
+// the batch, so a system's result is the same alone and in any mix.
+//
+// Arnoldi step k (6 launches):
+//   k_mv_tma      w_parts = A z_k               complex64: bulk-copy pipeline
+//   (k_mv64)                                    complex128: persistent tiles
+//   k_dot1        w = sum parts; h1 = V^H w     per 256-row block
+//   k_axpy<1>     w -= V h1; h2 = V^H w         (classical Gram-Schmidt, twice)
+//   k_axpy<2>     w -= V h2; |w|^2 partials
+//   k_scale       v_{k+1} = w / |w|; z_{k+1} = M^{-1} v_{k+1}
+//   k_givens      column k of H, rotations, residual estimate, phase
+// End of cycle (6 launches):
+//   k_trisolve    y = H^{-1} g                   warp per system
+//   k_xupdate     x += M^{-1} (V y)
+//   k_mv_tma      b - A x with error-free products (the refinement residual)
+//   k_resid       r, |r|^2 partials
+//   k_decide      convergence / stagnation / limit, restart set-up
+//   k_scale       v_0 = r / |r|; z_0 = M^{-1} v_0 (restarted systems)
+//
+// Inner products are summed in a fixed order (per block, then over blocks in
+// block order, every block computing the same sums), so results are
+// deterministic run to run.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <mutex>
+
+#include "bem_engine.h"
+#include "bem_internal.h"
+
+namespace bem {
+namespace {
+
+constexpr int kThreads = kVecBlock;        // vector kernels: one row per thread
+constexpr int kMaxV = kMaxRestart + 1;     // basis vectors
+static_assert(kThreads == 2 * kBlock, "a vector block holds two preconditioner blocks");
+static_assert(kMaxV <= 64, "inner products are computed in groups of 8 up to 64 vectors");
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// error-free transformations (Knuth two-sum, FMA two-product)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void acc_exact(float &s, float &e, float a, float b) {
+    const float p = a * b;
+    const float q = fmaf(a, b, -p);
+    float t, u;
+    two_sum(s, p, t, u);
+    s = t;
+    e += u + q;
+}
+
+__device__ __forceinline__ bool mv_active(const KState *st, bool exact) {
+    return exact ? (st->phase == kPhaseUpdate && st->cycles > 0) : st->phase == kPhaseArnoldi;
+}
+
+// ------------------------------------------------------------ matvec (complex128)
+// Persistent grid; blocks take tiles (system, 32 rows x 1024 columns) from a
+// queue.  The x chunk is staged in shared memory; 8 warps x 4 rows; each lane
+// streams 16-byte loads (one complex128 entry) of its 4 rows.  The FP64 path
+// is bound by the FP64 pipe (4 DFMA per entry), not by HBM.  The tile writes
+// one partial per row; the consumer sums the chunks in order.
+template <bool EXACT>
+__global__ void __launch_bounds__(256, 4) k_mv64(KTable *tb) {
+    __shared__ __align__(16) double2 xd[kMvChunk];
+    __shared__ int item_s;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int total = tb->mv_total;
+    while (true) {
+        if (threadIdx.x == 0) item_s = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+        __syncthreads();
+        const int item = item_s;
+        __syncthreads();
+        if (item >= total) break;
+        const int2 it = tb->mv_items[item];
+        const KSys &S = tb->sys[it.x];
+        const KState *st = S.st;
+        if (!mv_active(st, EXACT)) continue;
+        const int n = S.n;
+        const int chunk = it.y % S.nchunk, tile = it.y / S.nchunk;
+        const int c0 = chunk * kMvChunk, len = min(kMvChunk, n - c0);
+        const double2 *xs = EXACT ? S.x : (S.pc ? S.z : S.V + (size_t)st->k * S.ldv);
+        for (int t = threadIdx.x; t < len; t += blockDim.x) xd[t] = xs[c0 + t];
+        __syncthreads();
+        const int row0 = tile * kMvRows + warp * 4;
+        double re[4] = {0.0, 0.0, 0.0, 0.0}, im[4] = {0.0, 0.0, 0.0, 0.0};
+        const double2 *A = (const double2 *)S.A;
+#pragma unroll 2
+        for (int c = lane; c < len; c += 32) {
+            const double2 xv = xd[c];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                if (row0 + r < n) {
+                    const double2 a = __ldcs(A + (size_t)(row0 + r) * S.lda + c0 + c);
+                    re[r] = fma(a.x, xv.x, re[r]);
+                    re[r] = fma(-a.y, xv.y, re[r]);
+                    im[r] = fma(a.x, xv.y, im[r]);
+                    im[r] = fma(a.y, xv.x, im[r]);
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            re[r] = warp_sum_d(re[r]);
+            im[r] = warp_sum_d(im[r]);
+        }
+        if (lane == 0)
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (row0 + r < n) S.mvp[(size_t)chunk * n + row0 + r] = make_double2(re[r], im[r]);
+    }
+    // the last block to leave resets the queue for the next launch
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
+            tb->mv_ctr[0] = 0u;
+            tb->mv_ctr[1] = 0u;
+            __threadfence();
+        }
+    }
+}
+
+// ------------------------------------------------------------ bulk-copy matvec
+// complex64 product with a bulk-copy (TMA) pipeline.  A persistent block per
+// SM: one producer warp and 8 consumer warps.  The producer takes items
+// (system, 1024-column chunk, strip of 64 rows) from the queue and streams
+// them through a ring of kTmaStages stages of kTmaRows row segments (8 KB
+// each, one cp.async.bulk per segment) into shared memory; the chunk of x
+// (float hi parts, or hi/lo pairs for the refinement residual) goes into one
+// of two x buffers.  mbarriers carry the byte counts (full) and the
+// consumers' releases (empty).  Consumer warp w takes row w of a stage.
+// Every wait is bounded (kWaitCycles); on expiry the kernel sets tb->err,
+// lets its own copies land and returns.
+constexpr int kTmaStages = 3;
+constexpr int kTmaConsumers = 8;
+static_assert(kTmaConsumers == kTmaRows, "one consumer warp per row of a stage");
+constexpr long long kWaitCycles = 4000000000LL;   // about 2 s at 2 GHz
+constexpr int kStageBytes = kTmaRows * kMvChunk * 8;   // 64 KB
+
+struct TmaMeta {
+    int b, chunk, row0, nrows, len, first, last, xslot;
+};
+
+__host__ __device__ constexpr int tma_x_bytes(bool exact) { return kMvChunk * (exact ? 16 : 8); }
+__host__ __device__ constexpr int tma_smem_bytes(bool exact) {
+    return kTmaStages * kStageBytes + 2 * tma_x_bytes(exact) + 256;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for the completion of the phase with the given parity
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, int *err) {
+    if (mbar_try(a, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try(a, parity)) {
+        if (clock64() - t0 > kWaitCycles) {
+            atomicExch(err, 1);
+            return false;
+        }
+    }
+    return true;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *tb) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    unsigned char *ring = smem;                                       // kTmaStages x 64 KB
+    unsigned char *xbuf = smem + kTmaStages * kStageBytes;           // 2 x chunk of x
+    uint64_t *bars = reinterpret_cast<uint64_t *>(xbuf + 2 * tma_x_bytes(EXACT));
+    // bars: full[3], empty[3], xfull[2], xempty[2]; then the stage metadata
+    TmaMeta *meta = reinterpret_cast<TmaMeta *>(bars + 2 * kTmaStages + 4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kTmaStages);
+    const uint32_t xfull0 = smem_u32(bars + 2 * kTmaStages), xempty0 = smem_u32(bars + 2 * kTmaStages + 2);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kTmaStages; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, kTmaConsumers);
+        }
+        for (int q = 0; q < 2; ++q) {
+            mbar_init(xfull0 + 8 * q, 1);
+            mbar_init(xempty0 + 8 * q, kTmaConsumers);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int *err = &tb->err;
+    if (warp == kTmaConsumers) {
+        // ---------------- producer (one lane)
+        if (lane != 0) return;
+        const int total = tb->mv_total;
+        int stage = 0, xs = 0;
+        uint32_t eph = 1, xeph[2] = {1, 1};   // a fresh barrier's previous phase counts as complete
+        int issued[kTmaStages] = {0, 0, 0};   // stage holds copies not yet seen complete by us
+        uint32_t fph[kTmaStages] = {0, 0, 0};
+        bool ok = true;
+        while (ok) {
+            const int item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+            if (item >= total) break;
+            const int2 it = tb->mv_items[item];
+            const KSys &S = tb->sys[it.x];
+            if (!mv_active(S.st, EXACT)) continue;
+            const int n = S.n;
+            const int chunk = it.y % S.nchunk, strip = it.y / S.nchunk;
+            const int c0 = chunk * kMvChunk, len = min(kMvChunk, n - c0), lenp = (len + 1) & ~1;
+            const int rbase = strip * kTmaStrip;
+            const int nst = min(kTmaStrip / kTmaRows, (n - rbase + kTmaRows - 1) / kTmaRows);
+            // x chunk
+            if (!mbar_wait(xempty0 + 8 * xs, xeph[xs], err)) { ok = false; break; }
+            xeph[xs] ^= 1;
+            const uint32_t xdst = smem_u32(xbuf + xs * tma_x_bytes(EXACT));
+            if (EXACT) {
+                mbar_expect_tx(xfull0 + 8 * xs, kMvChunk * 16);
+                bulk_g2s(xdst, S.xf + c0, kMvChunk * 16, xfull0 + 8 * xs);
+            } else {
+                mbar_expect_tx(xfull0 + 8 * xs, lenp * 8);
+                bulk_g2s(xdst, S.xh + c0, lenp * 8, xfull0 + 8 * xs);
+            }
+            const float2 *A = (const float2 *)S.A;
+            for (int g = 0; g < nst && ok; ++g) {
+                if (!mbar_wait(empty0 + 8 * stage, eph, err)) { ok = false; break; }
+                const int row0 = rbase + g * kTmaRows, nrows = min(kTmaRows, n - row0);
+                TmaMeta mt;
+                mt.b = it.x; mt.chunk = chunk; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
+                mt.first = g == 0; mt.last = g == nst - 1; mt.xslot = xs;
+                meta[stage] = mt;
+                mbar_expect_tx(full0 + 8 * stage, (uint32_t)(nrows * lenp * 8));
+                const uint32_t dst = smem_u32(ring + stage * kStageBytes);
+                for (int r = 0; r < nrows; ++r)
+                    bulk_g2s(dst + r * kMvChunk * 8, A + (size_t)(row0 + r) * S.lda + c0, lenp * 8,
+                             full0 + 8 * stage);
+                issued[stage] = 1;
+                fph[stage] ^= 1;
+                if (++stage == kTmaStages) { stage = 0; eph ^= 1; }
+            }
+            xs ^= 1;
+        }
+        if (ok) {
+            // sentinel: consumers stop at the next stage
+            if (mbar_wait(empty0 + 8 * stage, eph, err)) {
+                meta[stage].b = -1;
+                mbar_arrive(full0 + 8 * stage);
+            } else {
+                ok = false;
+            }
+        }
+        if (!ok) {
+            // a wait gave up: let this block's copies land before leaving
+            for (int s = 0; s < kTmaStages; ++s)
+                if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
+        }
+        __threadfence();
+        if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
+            tb->mv_ctr[0] = 0u;
+            tb->mv_ctr[1] = 0u;
+            __threadfence();
+        }
+        return;
+    }
+    // ---------------- consumers: warp w takes row w of each stage
+    int stage = 0;
+    uint32_t fph = 0, xph[2] = {0, 0};
+    while (true) {
+        if (!mbar_wait(full0 + 8 * stage, fph, err)) return;
+        const TmaMeta mt = meta[stage];
+        if (mt.b < 0) return;
+        const KSys &S = tb->sys[mt.b];
+        if (mt.first) {
+            if (!mbar_wait(xfull0 + 8 * mt.xslot, xph[mt.xslot], err)) return;
+        }
+        const unsigned char *xb = xbuf + mt.xslot * tma_x_bytes(EXACT);
+        if (warp < mt.nrows) {
+            const float4 *A4 = reinterpret_cast<const float4 *>(ring + stage * kStageBytes) + warp * (kMvChunk / 2);
+            const int len = mt.len, len2 = len >> 1;
+            float sr = 0.f, si = 0.f, er = 0.f, ei = 0.f;
+            if (!EXACT) {
+                const float4 *x4 = reinterpret_cast<const float4 *>(xb);   // hi parts of entries 2c, 2c + 1
+#pragma unroll 4
+                for (int c = lane; c < len2; c += 32) {
+                    const float4 a = A4[c], xv = x4[c];
+                    sr = fmaf(a.x, xv.x, sr); sr = fmaf(-a.y, xv.y, sr);
+                    si = fmaf(a.x, xv.y, si); si = fmaf(a.y, xv.x, si);
+                    sr = fmaf(a.z, xv.z, sr); sr = fmaf(-a.w, xv.w, sr);
+                    si = fmaf(a.z, xv.w, si); si = fmaf(a.w, xv.z, si);
+                }
+                if ((len & 1) && lane == 0) {
+                    const float2 a = reinterpret_cast<const float2 *>(A4)[len - 1];
+                    const float2 xv = reinterpret_cast<const float2 *>(xb)[len - 1];
+                    sr = fmaf(a.x, xv.x, sr); sr = fmaf(-a.y, xv.y, sr);
+                    si = fmaf(a.x, xv.y, si); si = fmaf(a.y, xv.x, si);
+                }
+            } else {
+                // x chunk permuted: entry 2c at xa[c], entry 2c + 1 at xb2[c]
+                const float4 *xa = reinterpret_cast<const float4 *>(xb), *xb2 = xa + kMvChunk / 2;
+#pragma unroll 2
+                for (int c = lane; c < len2; c += 32) {
+                    const float4 a = A4[c], x0 = xa[c], x1 = xb2[c];
+                    acc_exact(sr, er, a.x, x0.x); acc_exact(sr, er, -a.y, x0.y);
+                    acc_exact(si, ei, a.x, x0.y); acc_exact(si, ei, a.y, x0.x);
+                    er = fmaf(a.x, x0.z, er); er = fmaf(-a.y, x0.w, er);
+                    ei = fmaf(a.x, x0.w, ei); ei = fmaf(a.y, x0.z, ei);
+                    acc_exact(sr, er, a.z, x1.x); acc_exact(sr, er, -a.w, x1.y);
+                    acc_exact(si, ei, a.z, x1.y); acc_exact(si, ei, a.w, x1.x);
+                    er = fmaf(a.z, x1.z, er); er = fmaf(-a.w, x1.w, er);
+                    ei = fmaf(a.z, x1.w, ei); ei = fmaf(a.w, x1.z, ei);
+                }
+                if ((len & 1) && lane == 0) {
+                    const float2 a = reinterpret_cast<const float2 *>(A4)[len - 1];
+                    const float4 x0 = xa[(len - 1) >> 1];
+                    acc_exact(sr, er, a.x, x0.x); acc_exact(sr, er, -a.y, x0.y);
+                    acc_exact(si, ei, a.x, x0.y); acc_exact(si, ei, a.y, x0.x);
+                    er = fmaf(a.x, x0.z, er); er = fmaf(-a.y, x0.w, er);
+                    ei = fmaf(a.x, x0.w, ei); ei = fmaf(a.y, x0.z, ei);
+                }
+            }
+            const double tr = warp_sum_d((double)sr + (double)er);
+            const double ti = warp_sum_d((double)si + (double)ei);
+            if (lane == 0) S.mvp[(size_t)mt.chunk * S.n + mt.row0 + warp] = make_double2(tr, ti);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            mbar_arrive(empty0 + 8 * stage);
+            if (mt.last) mbar_arrive(xempty0 + 8 * mt.xslot);
+        }
+        if (mt.first) xph[mt.xslot] ^= 1;
+        if (++stage == kTmaStages) { stage = 0; fph ^= 1; }
+    }
+}
+
+// ------------------------------------------------------------ block helpers
+// dp[l * nvb + blk] = sum over the block's rows of conj(V_l[row]) w[row], l < nv.
+__device__ void block_dots(const double2 *__restrict__ V, long long ldv, int nv, double2 wv, bool ok, int row,
+                           double2 *__restrict__ dp, int nvb, int blk, double (*red)[16]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int l0 = 0; l0 < nv; l0 += 8) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            double re = 0.0, im = 0.0;
+            if (ok && l0 + q < nv) {
+                const double2 a = V[(size_t)(l0 + q) * ldv + row];
+                re = fma(a.x, wv.x, a.y * wv.y);
+                im = fma(a.x, wv.y, -a.y * wv.x);
+            }
+            re = warp_sum_d(re);
+            im = warp_sum_d(im);
+            if (lane == 0) {
+                red[warp][2 * q] = re;
+                red[warp][2 * q + 1] = im;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 16) {
+            double t = 0.0;
+#pragma unroll
+            for (int w8 = 0; w8 < 8; ++w8) t += red[w8][threadIdx.x];
+            const int q = threadIdx.x >> 1;
+            if (l0 + q < nv) reinterpret_cast<double *>(dp + (size_t)(l0 + q) * nvb + blk)[threadIdx.x & 1] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// nrmp[blk] = sum over the block's rows of |w|^2
+__device__ void block_norm(double2 wv, bool ok, double *__restrict__ nrmp, int blk, double (*red)[16]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double t = ok ? fma(wv.x, wv.x, wv.y * wv.y) : 0.0;
+    t = warp_sum_d(t);
+    if (lane == 0) red[warp][0] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+#pragma unroll
+        for (int w8 = 0; w8 < 8; ++w8) s += red[w8][0];
+        nrmp[blk] = s;
+    }
+    __syncthreads();
+}
+
+// sum of the squared-norm partials, in block order
+__device__ __forceinline__ double norm_total(const double *__restrict__ nrmp, int nvb) {
+    double t = 0.0;
+    for (int c = 0; c < nvb; ++c) t += nrmp[c];
+    return t;
+}
+
+// (M^{-1} v)[row] for the thread's own row: vs holds the block's 256 values
+// of v; the thread's 128-row preconditioner block is rows (tid & 128) .. +127.
+// Inverse blocks are stored transposed ([col][row]), so the loads coalesce.
+template <bool C128>
+__device__ __forceinline__ double2 apply_minv(const void *Minv, int n, int blk, const double2 *vs) {
+    const int tid = threadIdx.x;
+    const int pb = blk * 2 + (tid >> 7), rr = tid & 127, r0 = pb * kBlock;
+    const int nb = min(kBlock, n - r0);
+    if (nb <= 0 || rr >= nb) return make_double2(0.0, 0.0);
+    const double2 *x = vs + (tid & 128);
+    double sr = 0.0, si = 0.0;
+    if (C128) {
+        const double2 *M = (const double2 *)Minv + (size_t)pb * kBlock * kBlock;
+        for (int c = 0; c < nb; ++c) {
+            const double2 m = M[(size_t)c * kBlock + rr];
+            const double2 xv = x[c];
+            sr = fma(m.x, xv.x, sr); sr = fma(-m.y, xv.y, sr);
+            si = fma(m.x, xv.y, si); si = fma(m.y, xv.x, si);
+        }
+    } else {
+        // FP32 products, FP64 accumulation in chunks of 16
+        const float2 *M = (const float2 *)Minv + (size_t)pb * kBlock * kBlock;
+        for (int c0 = 0; c0 < nb; c0 += 16) {
+            float ar = 0.f, ai = 0.f;
+            const int ce = min(c0 + 16, nb);
+            for (int c = c0; c < ce; ++c) {
+                const float2 m = M[(size_t)c * kBlock + rr];
+                const float xr = (float)x[c].x, xi = (float)x[c].y;
+                ar += m.x * xr - m.y * xi;
+                ai += m.x * xi + m.y * xr;
+            }
+            sr += (double)ar;
+            si += (double)ai;
+        }
+    }
+    return make_double2(sr, si);
+}
+
+// ------------------------------------------------------------ Arnoldi step
+// w = sum of the matvec partials; dpa = V^H w
+__global__ void __launch_bounds__(kThreads) k_dot1(const KTable *tb) {
+    __shared__ double red[8][16];
+    for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
+        const int2 bi = tb->vb_items[it];
+        const KSys &S = tb->sys[bi.x];
+        const KState *st = S.st;
+        if (st->phase != kPhaseArnoldi) continue;
+        const int n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x;
+        const bool ok = row < n;
+        double2 wv = make_double2(0.0, 0.0);
+        if (ok) {
+            for (int c = 0; c < S.nchunk; ++c) {
+                const double2 p = S.mvp[(size_t)c * n + row];
+                wv.x += p.x;
+                wv.y += p.y;
+            }
+            S.w[row] = wv;
+        }
+        block_dots(S.V, S.ldv, st->k + 1, wv, ok, row, S.dpa, S.nvb, blk, red);
+    }
+}
+
+// PASS 1: h = sum(dpa); w -= V h; hsum += h; dpb = V^H w.
+// PASS 2: h = sum(dpb); w -= V h; hsum += h; nrmp = |w|^2 partials.
+template <int PASS>
+__global__ void __launch_bounds__(kThreads) k_axpy(const KTable *tb) {
+    __shared__ double2 hs[kMaxV];
+    __shared__ double red[8][16];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
+        const int2 bi = tb->vb_items[it];
+        const KSys &S = tb->sys[bi.x];
+        const KState *st = S.st;
+        if (st->phase != kPhaseArnoldi) continue;
+        const int n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x, nvb = S.nvb;
+        const bool ok = row < n;
+        const int nv = st->k + 1;
+        const double2 *dp = PASS == 1 ? S.dpa : S.dpb;
+        for (int l = warp; l < nv; l += 8) {
+            double re = 0.0, im = 0.0;
+            for (int c = lane; c < nvb; c += 32) {
+                const double2 p = dp[(size_t)l * nvb + c];
+                re += p.x;
+                im += p.y;
+            }
+            re = warp_sum_d(re);
+            im = warp_sum_d(im);
+            if (lane == 0) hs[l] = make_double2(re, im);
+        }
+        __syncthreads();
+        if (blk == 0 && threadIdx.x < nv) {
+            double2 hh = S.hsum[threadIdx.x];
+            hh.x += hs[threadIdx.x].x;
+            hh.y += hs[threadIdx.x].y;
+            S.hsum[threadIdx.x] = hh;
+        }
+        double2 wv = make_double2(0.0, 0.0);
+        if (ok) {
+            wv = S.w[row];
+#pragma unroll 8
+            for (int l = 0; l < nv; ++l) {
+                const double2 v = S.V[(size_t)l * S.ldv + row], c = hs[l];
+                wv.x -= c.x * v.x - c.y * v.y;
+                wv.y -= c.x * v.y + c.y * v.x;
+            }
+            S.w[row] = wv;
+        }
+        if (PASS == 1) block_dots(S.V, S.ldv, nv, wv, ok, row, S.dpb, nvb, blk, red);
+        else block_norm(wv, ok, S.nrmp, blk, red);
+    }
+}
+
+// RESTART = false: v_{k+1} = w / |w| (phase ARNOLDI).
+// RESTART = true:  v_0 = r / beta for systems that have just restarted.
+// Then z = M^{-1} v when the system is preconditioned.
+template <bool C128, bool RESTART>
+__global__ void __launch_bounds__(kThreads) k_scale(const KTable *tb) {
+    __shared__ double2 vs[kThreads];
+    for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
+        const int2 bi = tb->vb_items[it];
+        const KSys &S = tb->sys[bi.x];
+        const KState *st = S.st;
+        if (st->phase != kPhaseArnoldi) continue;
+        if (RESTART && st->k != 0) continue;
+        const int n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x;
+        const double s = RESTART ? 1.0 / st->beta : 1.0 / sqrt(norm_total(S.nrmp, S.nvb));
+        const int dst = RESTART ? 0 : st->k + 1;
+        const double2 *src = RESTART ? S.r : S.w;
+        double2 v = make_double2(0.0, 0.0);
+        if (row < n) {
+            const double2 a = src[row];
+            v = make_double2(a.x * s, a.y * s);
+            S.V[(size_t)dst * S.ldv + row] = v;
+        }
+        double2 u = v;   // input of the next product
+        if (S.pc) {
+            vs[threadIdx.x] = v;
+            __syncthreads();
+            u = apply_minv<C128>(S.Minv, n, blk, vs);
+            if (row < n) S.z[row] = u;
+            __syncthreads();
+        }
+        if (!C128 && row < n) S.xh[row] = make_float2((float)u.x, (float)u.y);
+    }
+}
+
+// One thread per system: column k of H from hsum and |w|, the previous
+// rotations, the new rotation, |g[k+1]|; ends the cycle (phase UPDATE) when
+// the residual estimate reaches the cycle's target, at breakdown, after m
+// steps or at the iteration limit.  Clears hsum for the next step.
+__global__ void k_givens(const KTable *tb) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= tb->B) return;
+    const KSys &S = tb->sys[b];
+    KState *st = S.st;
+    if (st->phase != kPhaseArnoldi) return;
+    const int k = st->k, m = st->m;
+    double2 *H = S.H, *cs = S.cs, *sn = S.sn, *g = S.g, *hsum = S.hsum;
+    for (int l = 0; l <= k; ++l) {
+        H[(size_t)l * m + k] = hsum[l];
+        hsum[l] = make_double2(0.0, 0.0);
+    }
+    const double hn = sqrt(norm_total(S.nrmp, S.nvb));
+    // previous rotations: [a; b] <- [[conj(c), conj(s)], [-s, c]] [a; b]
+    for (int l = 0; l < k; ++l) {
+        const double2 a = H[(size_t)l * m + k], bb = H[(size_t)(l + 1) * m + k];
+        const double2 c = cs[l], s = sn[l];
+        H[(size_t)l * m + k] = make_double2(c.x * a.x + c.y * a.y + s.x * bb.x + s.y * bb.y,
+                                            c.x * a.y - c.y * a.x + s.x * bb.y - s.y * bb.x);
+        H[(size_t)(l + 1) * m + k] = make_double2(-(s.x * a.x - s.y * a.y) + c.x * bb.x - c.y * bb.y,
+                                                  -(s.x * a.y + s.y * a.x) + c.x * bb.y + c.y * bb.x);
+    }
+    const double2 a = H[(size_t)k * m + k];
+    const double den = sqrt(a.x * a.x + a.y * a.y + hn * hn);
+    double2 c, s;
+    if (den == 0.0) { c = make_double2(1.0, 0.0); s = make_double2(0.0, 0.0); }
+    else { c = make_double2(a.x / den, a.y / den); s = make_double2(hn / den, 0.0); }
+    cs[k] = c;
+    sn[k] = s;
+    H[(size_t)k * m + k] = make_double2(c.x * a.x + c.y * a.y + s.x * hn, c.x * a.y - c.y * a.x + s.y * hn);
+    const double2 gk = g[k];
+    g[k + 1] = make_double2(-(s.x * gk.x - s.y * gk.y), -(s.x * gk.y + s.y * gk.x));
+    g[k] = make_double2(c.x * gk.x + c.y * gk.y, c.x * gk.y - c.y * gk.x);
+    const double res = sqrt(g[k + 1].x * g[k + 1].x + g[k + 1].y * g[k + 1].y);
+    st->k = k + 1;
+    st->iters += 1;
+    st->n_mv += 1;
+    st->res = res;
+    if (!(res > st->thr) || hn == 0.0 || !isfinite(res) || k + 1 >= m || st->iters >= st->max_iter)
+        st->phase = kPhaseUpdate;
+}
+
+// ------------------------------------------------------------ end of cycle
+// y = H^{-1} g (k x k upper triangular), one warp per system.
+__global__ void __launch_bounds__(128) k_trisolve(const KTable *tb) {
+    __shared__ double2 ys[4][kMaxV];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.x * 4 + warp;
+    if (b >= tb->B) return;
+    const KSys &S = tb->sys[b];
+    const KState *st = S.st;
+    if (st->phase != kPhaseUpdate || st->k == 0) return;
+    const int kk = st->k, m = st->m;
+    for (int i = kk - 1; i >= 0; --i) {
+        double re = 0.0, im = 0.0;
+        for (int l = i + 1 + lane; l < kk; l += 32) {
+            const double2 h = S.H[(size_t)i * m + l], yl = ys[warp][l];
+            re += h.x * yl.x - h.y * yl.y;
+            im += h.x * yl.y + h.y * yl.x;
+        }
+        re = warp_sum_d(re);
+        im = warp_sum_d(im);
+        if (lane == 0) {
+            const double2 gi = S.g[i], d = S.H[(size_t)i * m + i];
+            const double ar = gi.x - re, ai = gi.y - im;
+            const double dd = d.x * d.x + d.y * d.y;
+            const double2 y = make_double2((ar * d.x + ai * d.y) / dd, (ai * d.x - ar * d.y) / dd);
+            ys[warp][i] = y;
+            S.y[i] = y;
+        }
+        __syncwarp();
+    }
+}
+
+// x += M^{-1} (V y)
+template <bool C128>
+__global__ void __launch_bounds__(kThreads) k_xupdate(const KTable *tb) {
+    __shared__ double2 ys[kMaxV];
+    __shared__ double2 vs[kThreads];
+    for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
+        const int2 bi = tb->vb_items[it];
+        const KSys &S = tb->sys[bi.x];
+        const KState *st = S.st;
+        if (st->phase != kPhaseUpdate || st->k == 0) continue;
+        const int kk = st->k, n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x;
+        if (threadIdx.x < kk) ys[threadIdx.x] = S.y[threadIdx.x];
+        __syncthreads();
+        double2 t = make_double2(0.0, 0.0);
+        if (row < n) {
+#pragma unroll 8
+            for (int l = 0; l < kk; ++l) {
+                const double2 v = S.V[(size_t)l * S.ldv + row], c = ys[l];
+                t.x += c.x * v.x - c.y * v.y;
+                t.y += c.x * v.y + c.y * v.x;
+            }
+        }
+        if (S.pc) {
+            vs[threadIdx.x] = t;
+            __syncthreads();
+            t = apply_minv<C128>(S.Minv, n, blk, vs);
+        }
+        if (row < n) {
+            double2 xv = S.x[row];
+            xv.x += t.x;
+            xv.y += t.y;
+            S.x[row] = xv;
+            if (!C128) {
+                // (hi, lo) float split for the refinement residual, stored so
+                // that chunk entries 2c and 2c + 1 land in the chunk's first and
+                // second half (conflict-free reads in the product)
+                const float hr = (float)xv.x, hi = (float)xv.y;
+                const int c = row & (kMvChunk - 1);
+                S.xf[(size_t)(row - c) + (c & 1) * (kMvChunk / 2) + (c >> 1)] =
+                    make_float4(hr, hi, (float)(xv.x - (double)hr), (float)(xv.y - (double)hi));
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// r = b - A x (or r = b before the first cycle); |r|^2 partials
+__global__ void __launch_bounds__(kThreads) k_resid(const KTable *tb) {
+    __shared__ double red[8][16];
+    for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
+        const int2 bi = tb->vb_items[it];
+        const KSys &S = tb->sys[bi.x];
+        const KState *st = S.st;
+        if (st->phase != kPhaseUpdate) continue;
+        const int n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x;
+        const bool ok = row < n;
+        double2 r = make_double2(0.0, 0.0);
+        if (ok) {
+            r = S.b[row];
+            if (st->cycles > 0) {
+                double ax = 0.0, ay = 0.0;
+                for (int c = 0; c < S.nchunk; ++c) {
+                    const double2 p = S.mvp[(size_t)c * n + row];
+                    ax += p.x;
+                    ay += p.y;
+                }
+                r.x -= ax;
+                r.y -= ay;
+            }
+            S.r[row] = r;
+        }
+        block_norm(r, ok, S.nrmp, blk, red);
+    }
+}
+
+// One thread per system: convergence decision after a cycle (or the initial
+// residual), then the restart: g = beta e_1, hsum = 0, the cycle's target.
+__global__ void k_decide(const KTable *tb) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= tb->B) return;
+    const KSys &S = tb->sys[b];
+    KState *st = S.st;
+    if (st->phase != kPhaseUpdate) return;
+    const double beta = sqrt(norm_total(S.nrmp, S.nvb));
+    if (st->cycles == 0) {
+        st->bnorm = beta;
+        st->beta = beta;
+        if (beta == 0.0) {   // zero right-hand side: x = 0
+            st->rel = 0.0;
+            st->result = kResConverged;
+            st->phase = kPhaseFinished;
+            return;
+        }
+        st->rel = 1.0;
+        if (!isfinite(beta)) {
+            st->result = kResBreakdown;
+            st->phase = kPhaseFinished;
+            return;
+        }
+    } else {
+        st->n_mv += 1;   // the refinement residual
+        st->prev_beta = st->beta;
+        st->beta = beta;
+        const double rel = beta / st->bnorm;
+        st->rel = rel;
+        int res = kResRunning;
+        if (!isfinite(rel)) res = kResBreakdown;
+        else if (rel <= st->tol) res = kResConverged;
+        else if (st->iters >= st->max_iter) res = kResMaxIter;
+        else if (st->floor_rel > 0.0 && st->cycles > 2 && beta > 0.9 * st->prev_beta) res = kResStagnated;
+        if (res != kResRunning) {
+            st->result = res;
+            st->phase = kPhaseFinished;
+            return;
+        }
+    }
+    const int m = st->m;
+    st->cycles += 1;
+    st->k = 0;
+    st->thr = fmax(st->tol * st->bnorm, st->floor_rel * beta);
+    S.g[0] = make_double2(beta, 0.0);
+    for (int l = 1; l <= m; ++l) S.g[l] = make_double2(0.0, 0.0);
+    for (int l = 0; l <= m; ++l) S.hsum[l] = make_double2(0.0, 0.0);
+    st->phase = kPhaseArnoldi;
+}
+
+int g_mv_grid[2] = {0, 0};
+int g_vec_grid = 0;
+std::atomic<long long> g_launches{0};
+
+}  // namespace
+
+void count_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+long long launches() { return g_launches.load(std::memory_order_relaxed); }
+
+cudaError_t krylov_prepare() {
+    static std::once_flag once;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [] {
+        int dev = 0, sms = 0, per = 0;
+        err = cudaGetDevice(&dev);
+        if (err == cudaSuccess) err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k_mv_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       tma_smem_bytes(false));
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k_mv_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       tma_smem_bytes(true));
+        g_mv_grid[1] = sms;   // one bulk-copy block per SM
+        if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mv64<false>, 256, 0);
+        g_mv_grid[0] = sms * (per > 0 ? per : 1);
+        g_vec_grid = 2 * sms;
+    });
+    return err;
+}
+
+cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev, cudaStream_t st,
+                               int *launches_out) {
+    KTable *tb = const_cast<KTable *>(d_tab);
+    const bool c128 = prec == 0;
+    if (!g_vec_grid) return cudaErrorNotReady;   // krylov_prepare() first
+    const int gmv = g_mv_grid[c128 ? 0 : 1], gv = g_vec_grid;
+    const int gsys = (kMaxSys + 127) / 128;
+    int nl = 0;
+    cudaError_t e = cudaSuccess;
+    for (int q = 0; q < kSteps; ++q) {
+        if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q], st, cudaEventRecordExternal);
+        if (c128) k_mv64<false><<<gmv, 256, 0, st>>>(tb);
+        else k_mv_tma<false><<<gmv, 32 * (kTmaConsumers + 1), tma_smem_bytes(false), st>>>(tb);
+        if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q + 1], st, cudaEventRecordExternal);
+        k_dot1<<<gv, kThreads, 0, st>>>(d_tab);
+        k_axpy<1><<<gv, kThreads, 0, st>>>(d_tab);
+        k_axpy<2><<<gv, kThreads, 0, st>>>(d_tab);
+        if (c128) k_scale<true, false><<<gv, kThreads, 0, st>>>(d_tab);
+        else k_scale<false, false><<<gv, kThreads, 0, st>>>(d_tab);
+        k_givens<<<gsys, 128, 0, st>>>(d_tab);
+        nl += 6;
+    }
+    k_trisolve<<<(kMaxSys + 3) / 4, 128, 0, st>>>(d_tab);
+    if (c128) k_xupdate<true><<<gv, kThreads, 0, st>>>(d_tab);
+    else k_xupdate<false><<<gv, kThreads, 0, st>>>(d_tab);
+    if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * kSteps], st, cudaEventRecordExternal);
+    if (c128) k_mv64<true><<<gmv, 256, 0, st>>>(tb);
+    else k_mv_tma<true><<<gmv, 32 * (kTmaConsumers + 1), tma_smem_bytes(true), st>>>(tb);
+    if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * kSteps + 1], st, cudaEventRecordExternal);
+    k_resid<<<gv, kThreads, 0, st>>>(d_tab);
+    k_decide<<<gsys, 128, 0, st>>>(d_tab);
+    if (c128) k_scale<true, true><<<gv, kThreads, 0, st>>>(d_tab);
+    else k_scale<false, true><<<gv, kThreads, 0, st>>>(d_tab);
+    nl += 6;
+    e = cudaGetLastError();
+    if (launches_out) *launches_out = nl;
+    return e;
+}
+
+}  // namespace bem

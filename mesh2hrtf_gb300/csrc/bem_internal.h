@@ -1,5 +1,13 @@
-// bem_internal.h - host-side interface between the C ABI (bem_api.cu) and the
-// kernel translation units (bem_kernels.cu, bem_krylov.cu).
+// bem_internal.h - host-side interface between the C ABI (bem_api.cu, the
+// engine) and the kernel translation units (bem_kernels.cu, bem_gmres.cu,
+// bem_precond.cu).
+//
+// Every launch is batched: it works on a table of systems ((mesh, frequency)
+// instances), and a single solve is a batch of one.  Assembly, right-hand
+// side, preconditioner set-up and projection take their table by value (kernel
+// parameter space, __grid_constant__); the Krylov kernels read theirs from
+// device memory so that one captured CUDA graph serves any composition of the
+// batch.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -33,86 +41,166 @@ struct DevFreq {
 
 // Unknowns per diagonal block of the block-Jacobi preconditioner.
 constexpr int kBlock = 128;
+// Rows per block of the vector kernels (two preconditioner blocks).
+constexpr int kVecBlock = 256;
+// Matrix-vector product tile: kMvRows rows x kMvChunk columns.
+constexpr int kMvRows = 32;
+constexpr int kMvChunk = 1024;
+// Largest GMRES restart length (basis of kMaxRestart + 1 vectors).
+constexpr int kMaxRestart = 63;
+// Systems per launch table.
+constexpr int kMaxAsm = 64;    // assembly / projection / preconditioner set-up
+constexpr int kMaxSys = 128;   // Krylov engine slots
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+inline int mv_chunks(int n) { return ceil_div(n, kMvChunk); }
+inline int vec_blocks(int n) { return ceil_div(n, kVecBlock); }
+inline int pc_blocks(int n) { return ceil_div(n, kBlock); }
 
 // Process-wide count of kernel launches issued by the launch_* functions.
-void count_launches(int k);
+void count_launches(long long k);
 long long launches();
 
 // Copies the quadrature tables into constant memory of the current device.
 cudaError_t init_device_tables();
 
+// ---------------------------------------------------------------- assembly
+struct AsmSys {
+    DevMeshView m;
+    DevFreq f;
+    void *A;                // row-major n x n, leading dimension lda
+    size_t lda;
+    const int2 *near;       // near list of the mesh: (row, column)
+    long long n_near;
+    double *b;              // right-hand side (complex)
+    int *status;            // subdivision errors (atomicMax)
+};
+struct AsmBatch {
+    int B;
+    int far_off[kMaxAsm + 1];    // tiles of 32 x 32 entries
+    int near_off[kMaxAsm + 1];   // near pairs
+    int rhs_off[kMaxAsm + 1];    // blocks of 8 rows
+    AsmSys sys[kMaxAsm];
+};
+// Fills the offset tables from sys[0..B).
+void asm_batch_finish(AsmBatch &t);
+
 // Pairs integrated with subdivision plus self pairs, (row, column);
 // list == nullptr only counts.
 cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long *count, cudaStream_t st);
-// A = assembled TBEM matrix, row-major n x n with leading dimension lda,
-// complex128 (prec 0) or complex64 (prec 1): regular pairs, then the near
-// list.  status: device int receiving subdivision errors.
-cudaError_t launch_assemble(const DevMeshView &m, const DevFreq &f, int prec, void *A, size_t lda,
-                            const int2 *near_list, long long n_near, int *status, cudaStream_t st);
+// A = assembled TBEM matrices of the batch, complex128 (prec 0) or complex64
+// (prec 1): regular pairs (persistent k_far), then the near lists (persistent
+// k_near).  ctr: 4 device words, zero before the first use; the kernels leave
+// them zero.
+cudaError_t launch_assemble(const AsmBatch &t, int prec, unsigned *ctr, cudaStream_t st);
 // b = free terms + incident waves + columns with prescribed values (FP64).
-cudaError_t launch_rhs(const DevMeshView &m, const DevFreq &f, double *b, int *status, cudaStream_t st);
-// Element potentials and nodal normal velocities from the unknowns x.
-cudaError_t launch_fields(const DevMeshView &m, const DevFreq &f, const double *x, double *phi,
-                          double *vel, int *ivi, cudaStream_t st);
-// Potential and gradient at npts points (pts: [npts][3] FP64 on the device).
-cudaError_t launch_project(const DevMeshView &m, const DevFreq &f, int prec, const double *phi,
-                           const double *vel, const int *ivi, int npts, const double *pts,
-                           double *pot, double *grad, int *status, cudaStream_t st);
+cudaError_t launch_rhs(const AsmBatch &t, cudaStream_t st);
 
-// ---- Krylov building blocks (bem_krylov.cu); vectors are complex128 ----
-// Device-side control word of one GMRES cycle.  Kernels given `done` return
-// at once when it is set, so the host can queue several Arnoldi steps ahead
-// and check convergence once per batch.
-struct GmresCtrl {
-    int done;     // residual estimate reached thr (or breakdown)
-    int kdone;    // Arnoldi steps completed in this cycle
-    double res;   // |g[k+1]| after the last step
-    double thr;   // absolute residual target of the cycle
+// ---------------------------------------------------------------- projection
+struct ProjSys {
+    DevMeshView m;
+    DevFreq f;
+    const double *x;        // solution (complex)
+    double *phi, *vel;      // scratch: element potentials [n], nodal velocities [4][n]
+    int *ivi;               // [n] nonzero-velocity flags
+    int npts;
+    const double *pts;      // [npts][3]
+    double *pot, *grad;     // [npts], [npts][3] complex; grad may be nullptr
+    int *status;
+};
+struct ProjBatch {
+    int B;
+    int fld_off[kMaxAsm + 1];    // blocks of 256 elements
+    int pt_off[kMaxAsm + 1];     // blocks of 8 points
+    ProjSys sys[kMaxAsm];
+};
+void proj_batch_finish(ProjBatch &t);
+// Element potentials and nodal normal velocities from the unknowns, then
+// potential and gradient at the points.
+cudaError_t launch_fields(const ProjBatch &t, cudaStream_t st);
+cudaError_t launch_project(const ProjBatch &t, int prec, cudaStream_t st);
+
+// ---------------------------------------------------------------- preconditioner
+struct PcSys {
+    const void *A;
+    size_t lda;
+    int n;
+    void *Minv;             // pc_blocks(n) blocks of kBlock x kBlock, transposed
+    void *work;             // FP64 only: inversion workspace of the same size
+    int *status;            // 1: a singular block
+};
+struct PcBatch {
+    int B;
+    int off[kMaxAsm + 1];
+    PcSys sys[kMaxAsm];
+};
+void pc_batch_finish(PcBatch &t);
+size_t precond_bytes(int n, int prec);
+cudaError_t launch_block_inverse(const PcBatch &t, int prec, cudaStream_t st);
+
+// ---------------------------------------------------------------- Krylov engine
+// Restarted GMRES of one system as a state machine on the device.  An
+// iteration body (one captured graph) runs kSteps Arnoldi steps for every
+// system in phase ARNOLDI, then the cycle end for every system in phase
+// UPDATE: y = H^{-1} g, x += M^{-1} V y, the refinement residual r = b - A x
+// (compensated product), the convergence decision and the restart.
+enum KPhase : int { kPhaseIdle = 0, kPhaseArnoldi = 1, kPhaseUpdate = 2, kPhaseFinished = 3 };
+enum KResult : int { kResRunning = 0, kResConverged = 1, kResMaxIter = 2, kResStagnated = 3, kResBreakdown = 4 };
+
+struct KState {
+    int phase, k, iters, cycles;
+    int result, m, max_iter, n_mv;
+    double tol;          // relative residual target
+    double floor_rel;    // inner cycle stops at floor_rel * beta (mixed: 1e-5)
+    double bnorm, beta, prev_beta, thr, res, rel;
 };
 
-// y = A x for a row-major n x n matrix with leading dimension lda
-// (r_in != nullptr: y = r_in - A x).
-// prec 0: complex128 A, FP64 arithmetic.
-// prec 1, exact = false: complex64 A, x rounded to complex64, FP32 products
-//   and per-lane sums, FP64 reduction across lanes (Krylov inner products).
-// prec 1, exact = true: complex64 A times x = x_hi + x_lo with error-free
-//   products (FMA two-product) and two-sum accumulation, i.e. twice-FP32
-//   accuracy (the refinement residual).
-// xf: scratch of 2 * n float2 for the split of x.
-cudaError_t launch_matvec(int prec, bool exact, const void *A, int n, size_t lda, const double *x,
-                          const double *r_in, double *y, void *xf, cudaStream_t st, const int *done = nullptr);
-// Blocks of partial sums used by launch_multi_dot.
-int dot_blocks(int n);
-// h[l] = <V[l], w> (conjugated in V) for l < nv, V with leading dimension
-// ldv (complex entries); hsum[l] += h[l] if hsum != nullptr.  partial: nv *
-// dot_blocks(n) complex scratch.
-cudaError_t launch_multi_dot(const double *V, size_t ldv, int nv, const double *w, int n, double *partial,
-                             double *h, double *hsum, cudaStream_t st, const int *done = nullptr);
-// w -= sum_l h[l] V[l]
-cudaError_t launch_multi_axpy(const double *V, size_t ldv, int nv, const double *h, double *w, int n,
-                              cudaStream_t st, const int *done = nullptr);
-// out[0] = ||w||^2
-cudaError_t launch_norm2(const double *w, int n, double *out, cudaStream_t st);
-// v = w * (1 / sqrt(nrm2[0]))
-cudaError_t launch_scale_inv(const double *w, const double *nrm2, double *v, int n, cudaStream_t st,
-                             const int *done = nullptr);
-// Givens step k of the cycle on the device (see GmresCtrl).
-cudaError_t launch_givens(int k, int m, double *hsum, const double *wnorm2, double *H, double *cs, double *sn,
-                          double *g, GmresCtrl *ctrl, cudaStream_t st);
-// x += sum_l y[l] V[l]  (y complex on the device)
-cudaError_t launch_update_x(const double *V, int ldv, int nv, const double *y, double *x, int n,
-                            cudaStream_t st);
+struct KSys {
+    const void *A;          // complex64 or complex128, row-major
+    long long lda;
+    int n, pc;              // pc: apply Minv
+    int nchunk, nvb;        // mv_chunks(n), vec_blocks(n)
+    const void *Minv;
+    double2 *x, *b, *r, *w, *z, *V;   // V: kMaxRestart + 1 vectors, stride ldv
+    float2 *xh;             // complex64 systems: float copy of the next product's input
+    float4 *xf;             // complex64 systems: x as (hi, lo) floats, chunk-permuted
+    long long ldv;
+    double2 *mvp;           // matvec partials [nchunk][n]
+    double2 *dpa, *dpb;     // inner-product partials [kMaxRestart + 1][nvb]
+    double *nrmp;           // squared-norm partials [nvb]
+    double2 *H, *cs, *sn, *g, *y, *hsum;   // H: (m + 1) x m row-major
+    KState *st;
+};
 
-// ---- block-Jacobi preconditioner (bem_precond.cu) ----
-size_t precond_bytes(int n, int prec);
-// Inverts the kBlock x kBlock diagonal blocks of A into Minv (transposed
-// blocks); FP64 uses `work` (same size as Minv) as inversion workspace.
-cudaError_t launch_block_inverse(int prec, const void *A, size_t lda, int n, void *Minv, void *work, int *status,
-                                 cudaStream_t st);
-// z = M^{-1} v
-cudaError_t launch_block_apply(int prec, const void *Minv, int n, const double *v, double *z, cudaStream_t st,
-                               const int *done = nullptr);
-// x += z
-cudaError_t launch_axpy(const double *z, double *x, int n, cudaStream_t st);
+struct KTable {
+    int B;
+    int mv_total;           // matvec tiles of all systems
+    int vb_total;           // vector blocks of all systems
+    int err;                // set when a bounded device wait gave up
+    unsigned mv_ctr[2];     // work queue of the persistent matvec
+    const int2 *mv_items;   // (system, tile)
+    const int2 *vb_items;   // (system, block)
+    KSys sys[kMaxSys];
+};
+
+// Arnoldi steps per iteration body.
+constexpr int kSteps = 8;
+// Enqueues one iteration body for the systems of *d_tab (device memory) on
+// st.  mv_ev: 2 * (kSteps + 1) events recorded around the matrix-vector
+// products (may be nullptr).  prec: 0 complex128, 1 complex64 matrices.
+// Returns the number of kernel launches enqueued through *launches_out.
+cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev, cudaStream_t st,
+                               int *launches_out);
+// complex64 matrices: the product streams row segments with bulk copies
+// (TMA) in strips of kTmaStrip rows; complex128: tiles of kMvRows rows.
+constexpr int kTmaRows = 8;
+constexpr int kTmaStrip = 64;
+inline int mv_items_of(int n, int prec) {
+    return ceil_div(n, prec == 0 ? kMvRows : kTmaStrip) * mv_chunks(n);
+}
+// Scratch sizes of one system (complex entries).
+inline size_t mvp_elems(int n) { return (size_t)mv_chunks(n) * (size_t)n; }
+inline size_t xsplit_elems(int n) { return (size_t)mv_chunks(n) * kMvChunk; }
+inline size_t dp_elems(int n) { return (size_t)(kMaxRestart + 1) * (size_t)vec_blocks(n); }
 
 }  // namespace bem

@@ -1,13 +1,18 @@
 // bem_kernels.cu - assembly, right-hand side and field-projection kernels.
 //
-// Assembly tile: a block of 8 warps covers 8 rows x 32 columns of A; each
-// warp owns one row i (collocation point = centre of element i) and 32
-// consecutive columns j (one per lane).  A lane classifies its pair with
-// NumCalc's level-0 subdivision test; regular pairs are integrated in the
-// lane with the Gauss order NumCalc would pick, pairs that NumCalc
-// subdivides and the self pair are integrated afterwards by the whole warp,
-// one after the other (warp_subdivide / warp_singular).  Each entry is
-// written once, by its lane, as a coalesced row segment.
+// Every launch covers a batch of systems ((mesh, frequency) instances) whose
+// table travels in kernel parameter space (__grid_constant__); a single solve
+// is a batch of one.
+//
+// Regular pairs (k_far): a persistent grid pulls tiles of 32 rows x 32
+// columns from a work queue that spans all systems of the batch; in a tile,
+// each of 8 warps owns 4 rows and each lane one column, so the column
+// element's tables are loaded once per lane and reused for 4 rows, and the
+// entries go out as coalesced row segments.  Pairs that NumCalc subdivides
+// and the self pairs are skipped there and integrated by k_near: warps pull
+// entries of the per-mesh near lists from a second queue and integrate them
+// cooperatively (warp_subdivide / warp_singular).
+#include <algorithm>
 #include <type_traits>
 
 #include "bem_internal.h"
@@ -27,6 +32,30 @@ __device__ __forceinline__ DevMesh to_dev(const DevMeshView &v) {
     m.area64 = v.area64; m.sqa64 = v.sqa64; m.chi = v.chi; m.clo = v.clo; m.t32 = v.t32;
     m.q32 = v.q32; m.isqa32 = v.isqa32; m.n32 = v.n32;
     return m;
+}
+
+// Largest b with off[b] <= item (off ascending, off[0] = 0, item < off[B]).
+__device__ __forceinline__ int find_sys(const int *off, int B, int item) {
+    int lo = 0, hi = B - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Persistent-grid exit: the last block to leave resets the queue counters
+// (ctr[0] = items handed out, ctr[1] = blocks finished) for the next launch.
+__device__ __forceinline__ void queue_exit(unsigned *ctr) {
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();
+        if (atomicAdd(ctr + 1, 1u) == gridDim.x - 1) {
+            ctr[0] = 0u;
+            ctr[1] = 0u;
+            __threadfence();
+        }
+    }
 }
 
 __device__ __forceinline__ cplx<double> ld_c(const double *p, int idx) {
@@ -153,12 +182,12 @@ __global__ void __launch_bounds__(256) k_near_list(DevMeshView mv, int2 *list, u
 constexpr int kRowsPerThread = 4;
 
 template <typename T>
-__global__ void __launch_bounds__(256, 3) k_far(DevMeshView mv, DevFreq f, typename Vec2<T>::type *__restrict__ A,
-                                             size_t lda) {
+__device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f,
+                                         typename Vec2<T>::type *__restrict__ A, size_t lda, int tx, int ty) {
     const DevMesh m = to_dev(mv);
     const int lane = threadIdx.x, n = m.n;
-    const int i0 = (blockIdx.y * 8 + threadIdx.y) * kRowsPerThread;
-    const int j = blockIdx.x * 32 + lane;
+    const int i0 = (ty * 8 + threadIdx.y) * kRowsPerThread;
+    const int j = tx * 32 + lane;
     if (i0 >= n || j >= n) return;
     Phys<T> PT;
     if constexpr (std::is_same<T, double>::value) PT = {f.k, f.wr, f.tao, f.beta_im};
@@ -210,20 +239,37 @@ __global__ void __launch_bounds__(256, 3) k_far(DevMeshView mv, DevFreq f, typen
     }
 }
 
+// ONE: the batch holds a single system, whose table then stays in constant
+// operands instead of registers.
+template <typename T, bool ONE>
+__global__ void __launch_bounds__(256, 3) k_far(const __grid_constant__ AsmBatch tb, unsigned *ctr) {
+    __shared__ int item_s;
+    const int total = tb.far_off[tb.B];
+    while (true) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) item_s = (int)atomicAdd(ctr, 1u);
+        __syncthreads();
+        const int item = item_s;
+        __syncthreads();
+        if (item >= total) break;
+        const int b = ONE ? 0 : find_sys(tb.far_off, tb.B, item);
+        const AsmSys &S = tb.sys[ONE ? 0 : b];
+        const int local = item - tb.far_off[b];
+        const int ntx = (S.m.n + 31) / 32;
+        far_tile<T>(S.m, S.f, (typename Vec2<T>::type *)S.A, S.lda, local % ntx, local / ntx);
+    }
+    queue_exit(ctr);
+}
+
 // ------------------------------------------------------------ near pairs
 // One warp per entry of the near list: the self pair by warp_singular (FP64,
 // plus NumCalc's free term), subdivided pairs by warp_subdivide with the
 // kernel arithmetic in T.
 template <typename T>
-__global__ void __launch_bounds__(256) k_near(DevMeshView mv, DevFreq f, const int2 *__restrict__ list, long long count,
-                                              typename Vec2<T>::type *__restrict__ A, size_t lda, int *status) {
-    __shared__ WarpScratch ws_all[8];
+__device__ __forceinline__ void near_pair(const DevMeshView &mv, const DevFreq &f, int2 ij,
+                                          typename Vec2<T>::type *__restrict__ A, size_t lda, int *status,
+                                          WarpScratch &ws) {
     const DevMesh m = to_dev(mv);
     const int lane = threadIdx.x, n = m.n;
-    const long long idx = (long long)blockIdx.x * 8 + threadIdx.y;
-    if (idx >= count) return;
-    WarpScratch &ws = ws_all[threadIdx.y];
-    const int2 ij = list[idx];
     const int i = ij.x, j = ij.y;
     const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
     const double nx64[3] = {m.n64[i], m.n64[n + i], m.n64[2 * n + i]};
@@ -271,6 +317,25 @@ __global__ void __launch_bounds__(256) k_near(DevMeshView mv, DevFreq f, const i
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) k_near(const __grid_constant__ AsmBatch tb, unsigned *ctr) {
+    __shared__ WarpScratch ws_all[8];
+    WarpScratch &ws = ws_all[threadIdx.y];
+    const int total = tb.near_off[tb.B];
+    while (true) {
+        int item = 0;
+        if (threadIdx.x == 0) item = (int)atomicAdd(ctr, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        const int b = find_sys(tb.near_off, tb.B, item);
+        const AsmSys &S = tb.sys[b];
+        const int2 ij = S.near[item - tb.near_off[b]];
+        near_pair<T>(S.m, S.f, ij, (typename Vec2<T>::type *)S.A, S.lda, S.status, ws);
+        __syncwarp();
+    }
+    queue_exit(ctr);
+}
+
 // Incident waves at a collocation point (NC_IncidentWaveRHS,
 // NC_EquationSystem.cpp:1731-1812), without symmetry planes.
 __device__ cplx<double> incident_rhs(const DevFreq &f, const double x[3], const double nx[3]) {
@@ -307,12 +372,17 @@ __device__ cplx<double> incident_rhs(const DevFreq &f, const double x[3], const 
 // Right-hand side, one warp per row (FP64): free term of the prescribed value
 // (NC_EquationSystem.cpp:233-244), incident waves, and the columns whose
 // prescribed values are nonzero (Zrsintel[4], NC_EquationSystem.cpp:188-198).
-__global__ void __launch_bounds__(256) k_rhs(DevMeshView mv, DevFreq f, double2 *b, int *status) {
+__global__ void __launch_bounds__(256) k_rhs(const __grid_constant__ AsmBatch tb) {
     __shared__ WarpScratch ws_all[8];
-    const DevMesh m = to_dev(mv);
+    const int sb = find_sys(tb.rhs_off, tb.B, blockIdx.x);
+    const AsmSys &S = tb.sys[sb];
+    const DevMesh m = to_dev(S.m);
+    const DevFreq &f = S.f;
+    double2 *b = (double2 *)S.b;
+    int *status = S.status;
     const int lane = threadIdx.x, w = threadIdx.y;
     const int n = m.n;
-    const int i = blockIdx.x * 8 + w;
+    const int i = (blockIdx.x - tb.rhs_off[sb]) * 8 + w;
     if (i >= n) return;
     WarpScratch &ws = ws_all[w];
     const double x[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
@@ -361,8 +431,15 @@ __global__ void __launch_bounds__(256) k_rhs(DevMeshView mv, DevFreq f, double2 
 
 // Element potentials and nodal normal velocities after the solve
 // (NC_WriteResultsObjectMesh, NC_PostProcessing.cpp:389-410).
-__global__ void k_fields(DevMeshView mv, DevFreq f, const double2 *x, double2 *phi, double2 *vel, int *ivi) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_fields(const __grid_constant__ ProjBatch tb) {
+    const int sb = find_sys(tb.fld_off, tb.B, blockIdx.x);
+    const ProjSys &S = tb.sys[sb];
+    const DevMeshView &mv = S.m;
+    const DevFreq &f = S.f;
+    const double2 *x = (const double2 *)S.x;
+    double2 *phi = (double2 *)S.phi, *vel = (double2 *)S.vel;
+    int *ivi = S.ivi;
+    const int j = (blockIdx.x - tb.fld_off[sb]) * blockDim.x + threadIdx.x;
     const int n = mv.n;
     if (j >= n) return;
     const int bc = f.bc_type ? f.bc_type[j] : 0;
@@ -392,14 +469,21 @@ __global__ void k_fields(DevMeshView mv, DevFreq f, const double2 *x, double2 *p
 // Field projection, one warp per point: lanes sweep the elements 32 at a time;
 // regular pairs in the lane, subdivided pairs by the whole warp.
 template <typename T>
-__global__ void __launch_bounds__(256) k_project(DevMeshView mv, DevFreq f, const double2 *phi, const double2 *vel,
-                                                 const int *ivi, int npts, const double *pts, double2 *pot,
-                                                 double2 *grad, int *status) {
+__global__ void __launch_bounds__(256) k_project(const __grid_constant__ ProjBatch tb) {
     __shared__ WarpScratch ws_all[8];
-    const DevMesh m = to_dev(mv);
+    const int sb = find_sys(tb.pt_off, tb.B, blockIdx.x);
+    const ProjSys &S = tb.sys[sb];
+    const DevMesh m = to_dev(S.m);
+    const DevFreq &f = S.f;
+    const double2 *phi = (const double2 *)S.phi, *vel = (const double2 *)S.vel;
+    const int *ivi = S.ivi;
+    const int npts = S.npts;
+    const double *pts = S.pts;
+    double2 *pot = (double2 *)S.pot, *grad = (double2 *)S.grad;
+    int *status = S.status;
     const int lane = threadIdx.x, w = threadIdx.y;
     const int n = m.n;
-    const int p = blockIdx.x * 8 + w;
+    const int p = (blockIdx.x - tb.pt_off[sb]) * 8 + w;
     if (p >= npts) return;
     WarpScratch &ws = ws_all[w];
     const double x64[3] = {pts[3 * p], pts[3 * p + 1], pts[3 * p + 2]};
@@ -658,47 +742,82 @@ cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long lon
     return cudaGetLastError();
 }
 
-cudaError_t launch_assemble(const DevMeshView &m, const DevFreq &f, int prec, void *A, size_t lda,
-                            const int2 *near_list, long long n_near, int *status, cudaStream_t st) {
-    dim3 block(32, 8), grid((m.n + 31) / 32, (m.n + 8 * kRowsPerThread - 1) / (8 * kRowsPerThread));
-    const int nblk = (int)((n_near + 7) / 8);
-    count_launches(2);
+void asm_batch_finish(AsmBatch &t) {
+    t.far_off[0] = t.near_off[0] = t.rhs_off[0] = 0;
+    for (int b = 0; b < t.B; ++b) {
+        const int n = t.sys[b].m.n;
+        const int nt = (n + 31) / 32;
+        t.far_off[b + 1] = t.far_off[b] + nt * ((n + 8 * kRowsPerThread - 1) / (8 * kRowsPerThread));
+        t.near_off[b + 1] = t.near_off[b] + (int)t.sys[b].n_near;
+        t.rhs_off[b + 1] = t.rhs_off[b] + (n + 7) / 8;
+    }
+}
+
+void proj_batch_finish(ProjBatch &t) {
+    t.fld_off[0] = t.pt_off[0] = 0;
+    for (int b = 0; b < t.B; ++b) {
+        t.fld_off[b + 1] = t.fld_off[b] + (t.sys[b].m.n + 255) / 256;
+        t.pt_off[b + 1] = t.pt_off[b] + (t.sys[b].npts + 7) / 8;
+    }
+}
+
+namespace {
+int g_sms = 0;
+int sm_count() {
+    if (g_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+    }
+    return g_sms;
+}
+}  // namespace
+
+cudaError_t launch_assemble(const AsmBatch &t, int prec, unsigned *ctr, cudaStream_t st) {
+    if (t.B <= 0) return cudaSuccess;
+    dim3 block(32, 8);
+    const int far_items = t.far_off[t.B], near_items = t.near_off[t.B];
+    // persistent grids: 3 resident blocks of k_far per SM (launch bounds), 4 of k_near
+    const int gfar = std::max(1, std::min(far_items, 3 * sm_count()));
+    const int gnear = std::max(1, std::min((near_items + 7) / 8, 4 * sm_count()));
+    count_launches(near_items ? 2 : 1);
+    const bool one = t.B == 1;
     if (prec == 0) {
-        k_far<double><<<grid, block, 0, st>>>(m, f, (double2 *)A, lda);
-        if (nblk) k_near<double><<<nblk, block, 0, st>>>(m, f, near_list, n_near, (double2 *)A, lda, status);
+        if (one) k_far<double, true><<<gfar, block, 0, st>>>(t, ctr);
+        else k_far<double, false><<<gfar, block, 0, st>>>(t, ctr);
+        if (near_items) k_near<double><<<gnear, block, 0, st>>>(t, ctr + 2);
     } else {
-        k_far<float><<<grid, block, 0, st>>>(m, f, (float2 *)A, lda);
-        if (nblk) k_near<float><<<nblk, block, 0, st>>>(m, f, near_list, n_near, (float2 *)A, lda, status);
+        if (one) k_far<float, true><<<gfar, block, 0, st>>>(t, ctr);
+        else k_far<float, false><<<gfar, block, 0, st>>>(t, ctr);
+        if (near_items) k_near<float><<<gnear, block, 0, st>>>(t, ctr + 2);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_rhs(const DevMeshView &m, const DevFreq &f, double *b, int *status, cudaStream_t st) {
-    dim3 block(32, 8), grid((m.n + 7) / 8);
+cudaError_t launch_rhs(const AsmBatch &t, cudaStream_t st) {
+    if (t.B <= 0) return cudaSuccess;
+    dim3 block(32, 8);
     count_launches(1);
-    k_rhs<<<grid, block, 0, st>>>(m, f, (double2 *)b, status);
+    k_rhs<<<t.rhs_off[t.B], block, 0, st>>>(t);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fields(const DevMeshView &m, const DevFreq &f, const double *x, double *phi, double *vel,
-                          int *ivi, cudaStream_t st) {
+cudaError_t launch_fields(const ProjBatch &t, cudaStream_t st) {
+    if (t.B <= 0 || t.fld_off[t.B] == 0) return cudaSuccess;
     count_launches(1);
-    k_fields<<<(m.n + 255) / 256, 256, 0, st>>>(m, f, (const double2 *)x, (double2 *)phi, (double2 *)vel, ivi);
+    k_fields<<<t.fld_off[t.B], 256, 0, st>>>(t);
     return cudaGetLastError();
 }
 
-cudaError_t launch_project(const DevMeshView &m, const DevFreq &f, int prec, const double *phi, const double *vel,
-                           const int *ivi, int npts, const double *pts, double *pot, double *grad, int *status,
-                           cudaStream_t st) {
-    if (npts <= 0) return cudaSuccess;
-    dim3 block(32, 8), grid((npts + 7) / 8);
+cudaError_t launch_project(const ProjBatch &t, int prec, cudaStream_t st) {
+    if (t.B <= 0 || t.pt_off[t.B] == 0) return cudaSuccess;
+    dim3 block(32, 8);
     count_launches(1);
     if (prec == 0)
-        k_project<double><<<grid, block, 0, st>>>(m, f, (const double2 *)phi, (const double2 *)vel, ivi, npts, pts,
-                                                  (double2 *)pot, (double2 *)grad, status);
+        k_project<double><<<t.pt_off[t.B], block, 0, st>>>(t);
     else
-        k_project<float><<<grid, block, 0, st>>>(m, f, (const double2 *)phi, (const double2 *)vel, ivi, npts, pts,
-                                                 (double2 *)pot, (double2 *)grad, status);
+        k_project<float><<<t.pt_off[t.B], block, 0, st>>>(t);
     return cudaGetLastError();
 }
 

@@ -7,10 +7,11 @@
 // inverted once per frequency; NumCalc's own preconditioner is a threshold
 // ILU on the same near-field entries (NC_CommonFunctions.cpp:1357-1721).
 //
-// Inversion: one CTA per block, in-place Gauss-Jordan with partial pivoting.
-// complex64 blocks live in shared memory (128 KB); complex128 blocks are
-// inverted in a global workspace (L2 resident).  Inverses are stored
-// transposed so that the application reads them coalesced.
+// Inversion: one CTA per block of any system in the batch, in-place
+// Gauss-Jordan with partial pivoting.  complex64 blocks live in shared memory
+// (128 KB); complex128 blocks are inverted in a global workspace (L2
+// resident).  Inverses are stored transposed so that the application (inside
+// the Krylov kernels, bem_gmres.cu) reads them coalesced.
 #include <cuda_runtime.h>
 
 #include "bem_internal.h"
@@ -108,15 +109,27 @@ __device__ void gauss_jordan(typename C2<T>::t *W, int ld, int nb, typename C2<T
     }
 }
 
+__device__ __forceinline__ int find_blk(const int *off, int B, int item) {
+    int lo = 0, hi = B - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
 // complex64: block in shared memory
-__global__ void __launch_bounds__(512) k_binv32(const float2 *__restrict__ A, size_t lda, int n, float2 *__restrict__ Minv,
-                                                int *status) {
+__global__ void __launch_bounds__(512) k_binv32(const __grid_constant__ PcBatch tb) {
     extern __shared__ float2 smem[];
     __shared__ float2 colk[kBlock];
     __shared__ int piv[kBlock];
     __shared__ int pivrow, singular;
-    const int b = blockIdx.x, r0 = b * kBlock;
-    const int nb = min(kBlock, n - r0);
+    const int sb = find_blk(tb.off, tb.B, blockIdx.x);
+    const PcSys &S = tb.sys[sb];
+    const float2 *A = (const float2 *)S.A;
+    const size_t lda = S.lda;
+    const int b = blockIdx.x - tb.off[sb], r0 = b * kBlock;
+    const int nb = min(kBlock, S.n - r0);
     if (threadIdx.x == 0) singular = 0;
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
         const int i = e / nb, j = e - i * nb;
@@ -125,23 +138,26 @@ __global__ void __launch_bounds__(512) k_binv32(const float2 *__restrict__ A, si
     __syncthreads();
     gauss_jordan<float>(smem, kBlock, nb, colk, piv, &pivrow, &singular);
     // store transposed: Minv[b][c][r] = inv[r][c]
-    float2 *out = Minv + (size_t)b * kBlock * kBlock;
+    float2 *out = (float2 *)S.Minv + (size_t)b * kBlock * kBlock;
     for (int e = threadIdx.x; e < kBlock * kBlock; e += blockDim.x) {
         const int c = e / kBlock, r = e - c * kBlock;
         out[e] = (r < nb && c < nb) ? smem[r * kBlock + c] : make_float2(0.f, 0.f);
     }
-    if (threadIdx.x == 0 && singular) atomicMax(status, 1);
+    if (threadIdx.x == 0 && singular) atomicMax(S.status, 1);
 }
 
 // complex128: block in a global workspace
-__global__ void __launch_bounds__(512) k_binv64(const double2 *__restrict__ A, size_t lda, int n, double2 *__restrict__ W,
-                                                double2 *__restrict__ Minv, int *status) {
+__global__ void __launch_bounds__(512) k_binv64(const __grid_constant__ PcBatch tb) {
     __shared__ double2 colk[kBlock];
     __shared__ int piv[kBlock];
     __shared__ int pivrow, singular;
-    const int b = blockIdx.x, r0 = b * kBlock;
-    const int nb = min(kBlock, n - r0);
-    double2 *w = W + (size_t)b * kBlock * kBlock;
+    const int sb = find_blk(tb.off, tb.B, blockIdx.x);
+    const PcSys &S = tb.sys[sb];
+    const double2 *A = (const double2 *)S.A;
+    const size_t lda = S.lda;
+    const int b = blockIdx.x - tb.off[sb], r0 = b * kBlock;
+    const int nb = min(kBlock, S.n - r0);
+    double2 *w = (double2 *)S.work + (size_t)b * kBlock * kBlock;
     if (threadIdx.x == 0) singular = 0;
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
         const int i = e / nb, j = e - i * nb;
@@ -149,74 +165,38 @@ __global__ void __launch_bounds__(512) k_binv64(const double2 *__restrict__ A, s
     }
     __syncthreads();
     gauss_jordan<double>(w, kBlock, nb, colk, piv, &pivrow, &singular);
-    double2 *out = Minv + (size_t)b * kBlock * kBlock;
+    double2 *out = (double2 *)S.Minv + (size_t)b * kBlock * kBlock;
     for (int e = threadIdx.x; e < kBlock * kBlock; e += blockDim.x) {
         const int c = e / kBlock, r = e - c * kBlock;
         out[e] = (r < nb && c < nb) ? w[r * kBlock + c] : make_double2(0.0, 0.0);
     }
-    if (threadIdx.x == 0 && singular) atomicMax(status, 1);
-}
-
-// z = M^{-1} v, one CTA of kBlock threads per block; thread r owns row r.
-template <typename V>
-__global__ void __launch_bounds__(kBlock) k_bapply(const V *__restrict__ Minv, int n, const double2 *__restrict__ v,
-                                                   double2 *__restrict__ z, const int *done) {
-    __shared__ double2 xs[kBlock];
-    if (done && *done) return;
-    const int b = blockIdx.x, r0 = b * kBlock, r = threadIdx.x;
-    const int nb = min(kBlock, n - r0);
-    xs[r] = r < nb ? v[r0 + r] : make_double2(0.0, 0.0);
-    __syncthreads();
-    if (r >= nb) return;
-    const V *M = Minv + (size_t)b * kBlock * kBlock;
-    double sr = 0.0, si = 0.0;
-    // float blocks: FP32 products, FP64 accumulation in chunks of 16
-    for (int c0 = 0; c0 < nb; c0 += 16) {
-        decltype(M[0].x) ar = 0, ai = 0;
-        const int ce = min(c0 + 16, nb);
-        for (int c = c0; c < ce; ++c) {
-            const V m = M[(size_t)c * kBlock + r];
-            const decltype(m.x) xr = (decltype(m.x))xs[c].x, xi = (decltype(m.x))xs[c].y;
-            ar += m.x * xr - m.y * xi;
-            ai += m.x * xi + m.y * xr;
-        }
-        sr += (double)ar;
-        si += (double)ai;
-    }
-    z[r0 + r] = make_double2(sr, si);
+    if (threadIdx.x == 0 && singular) atomicMax(S.status, 1);
 }
 
 }  // namespace
 
 size_t precond_bytes(int n, int prec) {
-    const size_t nb = (size_t)(n + kBlock - 1) / kBlock;
+    const size_t nb = (size_t)pc_blocks(n);
     const size_t per = (size_t)kBlock * kBlock * (prec == 0 ? 16 : 8);
     return nb * per * (prec == 0 ? 2 : 1);   // FP64 needs the inversion workspace too
 }
 
-cudaError_t launch_block_inverse(int prec, const void *A, size_t lda, int n, void *Minv, void *work, int *status,
-                                 cudaStream_t st) {
-    const int nb = (n + kBlock - 1) / kBlock;
+void pc_batch_finish(PcBatch &t) {
+    t.off[0] = 0;
+    for (int b = 0; b < t.B; ++b) t.off[b + 1] = t.off[b] + pc_blocks(t.sys[b].n);
+}
+
+cudaError_t launch_block_inverse(const PcBatch &t, int prec, cudaStream_t st) {
+    if (t.B <= 0 || t.off[t.B] == 0) return cudaSuccess;
     count_launches(1);
     if (prec == 0) {
-        k_binv64<<<nb, 512, 0, st>>>((const double2 *)A, lda, n, (double2 *)work, (double2 *)Minv, status);
+        k_binv64<<<t.off[t.B], 512, 0, st>>>(t);
     } else {
         const int smem = kBlock * kBlock * sizeof(float2);
         cudaError_t e = cudaFuncSetAttribute(k_binv32, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_binv32<<<nb, 512, smem, st>>>((const float2 *)A, lda, n, (float2 *)Minv, status);
+        k_binv32<<<t.off[t.B], 512, smem, st>>>(t);
     }
-    return cudaGetLastError();
-}
-
-cudaError_t launch_block_apply(int prec, const void *Minv, int n, const double *v, double *z, cudaStream_t st,
-                               const int *done) {
-    const int nb = (n + kBlock - 1) / kBlock;
-    count_launches(1);
-    if (prec == 0)
-        k_bapply<double2><<<nb, kBlock, 0, st>>>((const double2 *)Minv, n, (const double2 *)v, (double2 *)z, done);
-    else
-        k_bapply<float2><<<nb, kBlock, 0, st>>>((const float2 *)Minv, n, (const double2 *)v, (double2 *)z, done);
     return cudaGetLastError();
 }
 

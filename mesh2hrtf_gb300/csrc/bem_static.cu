@@ -31,18 +31,15 @@ void *g_addr[64];   // device address of g_project_scratch, per device
 
 namespace bem {
 // accessors of the solver state, defined in bem_api.cu
-bool solver_projection_inputs(bem_solver_t s, int max_elem, DevMeshView *m, DevFreq *f, int *prec,
-                              const double **x, int *n);
+bool solver_projection_inputs(bem_solver_t s, int max_elem, ProjSys *out, int *prec);
 void set_error(const char *msg);
 }  // namespace bem
 
 extern "C" bem_status bem_project_static(bem_solver_t solver, int32_t n_pts, const double *pts_dev,
                                          double *pot_dev, double *grad_dev, void *stream) {
-    bem::DevMeshView m;
-    bem::DevFreq f;
-    int prec = 0, n = 0;
-    const double *x = nullptr;
-    if (!bem::solver_projection_inputs(solver, kStaticMaxElem, &m, &f, &prec, &x, &n)) return BEM_ERR_INVALID;
+    bem::ProjBatch t;
+    int prec = 0;
+    if (!bem::solver_projection_inputs(solver, kStaticMaxElem, &t.sys[0], &prec)) return BEM_ERR_INVALID;
     if (n_pts < 0 || (n_pts > 0 && (!pts_dev || !pot_dev))) {
         bem::set_error("bem_project_static: bad point or output pointers");
         return BEM_ERR_INVALID;
@@ -68,16 +65,23 @@ extern "C" bem_status bem_project_static(bem_solver_t solver, int32_t n_pts, con
     }
     cudaStream_t st = (cudaStream_t)stream;
     unsigned char *b = (unsigned char *)base;
-    double *phi = (double *)b;
-    double *vel = (double *)(b + (size_t)kStaticMaxElem * 16);
-    int *ivi = (int *)(b + (size_t)kStaticMaxElem * 80);
     int *status = (int *)(b + (size_t)kStaticMaxElem * 84);
-    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), st);
     // the fields kernel indexes vel as [4][n] with row stride n, so the
     // scratch layout holds for any n up to the maximum
-    if (e == cudaSuccess) e = bem::launch_fields(m, f, x, phi, vel, ivi, st);
-    if (e == cudaSuccess && n_pts > 0)
-        e = bem::launch_project(m, f, prec, phi, vel, ivi, n_pts, pts_dev, pot_dev, grad_dev, status, st);
+    bem::ProjSys &S = t.sys[0];
+    S.phi = (double *)b;
+    S.vel = (double *)(b + (size_t)kStaticMaxElem * 16);
+    S.ivi = (int *)(b + (size_t)kStaticMaxElem * 80);
+    S.status = status;
+    S.npts = n_pts;
+    S.pts = pts_dev;
+    S.pot = pot_dev;
+    S.grad = grad_dev;
+    t.B = 1;
+    bem::proj_batch_finish(t);
+    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = bem::launch_fields(t, st);
+    if (e == cudaSuccess && n_pts > 0) e = bem::launch_project(t, prec, st);
     int st_h = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&st_h, status, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
