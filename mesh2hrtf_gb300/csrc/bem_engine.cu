@@ -45,14 +45,9 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
     // the previous replay (if any) has completed: run_body synchronizes
     const int B = (int)sys.size();
     items_.clear();
-    int mv_total = 0, vb_total = 0;
-    for (int b = 0; b < B; ++b) mv_total += mv_items_of(sys[b].n, prec_);
+    int vb_total = 0;
     for (int b = 0; b < B; ++b) vb_total += sys[b].nvb;
-    items_.reserve((size_t)mv_total + vb_total);
-    for (int b = 0; b < B; ++b) {
-        const int cnt = mv_items_of(sys[b].n, prec_);
-        for (int q = 0; q < cnt; ++q) items_.push_back(make_int2(b, q));
-    }
+    items_.reserve((size_t)vb_total);
     for (int b = 0; b < B; ++b)
         for (int q = 0; q < sys[b].nvb; ++q) items_.push_back(make_int2(b, q));
     if (items_.size() > items_cap_) {
@@ -67,12 +62,11 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
     if (!items_.empty())
         e = cudaMemcpyAsync(d_items_, items_.data(), items_.size() * sizeof(int2), cudaMemcpyHostToDevice, st_);
     if (e != cudaSuccess) return e;
-    std::memset(h_tab_, 0, sizeof(KTable));
+    std::memset(h_tab_, 0, sizeof(KTable));   // empty plans: the first body starts at the cycle end
     h_tab_->B = B;
-    h_tab_->mv_total = mv_total;
+    h_tab_->prec = prec_;
     h_tab_->vb_total = vb_total;
-    h_tab_->mv_items = d_items_;
-    h_tab_->vb_items = d_items_ + mv_total;
+    h_tab_->vb_items = d_items_;
     for (int b = 0; b < B; ++b) {
         h_tab_->sys[b] = sys[b];
         h_tab_->sys[b].st = d_st_ + b;

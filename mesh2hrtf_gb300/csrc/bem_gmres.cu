@@ -76,6 +76,59 @@ __device__ __forceinline__ bool mv_active(const KState *st, bool exact) {
     return exact ? (st->phase == kPhaseUpdate && st->cycles > 0) : st->phase == kPhaseArnoldi;
 }
 
+// ------------------------------------------------------------ launch plans
+// Slot j of a plan with plan.off[j] <= item < plan.off[j + 1].
+__device__ __forceinline__ int plan_find(const int *off, int n, int item) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Copy of a plan in shared memory, loaded by the whole block.
+struct PlanSmem {
+    int n;
+    int off[kMaxSys + 1];
+    int sys[kMaxSys];
+};
+__device__ __forceinline__ void plan_load(const KPlan &p, PlanSmem &s) {
+    if (threadIdx.x == 0) s.n = p.n;
+    for (int i = threadIdx.x; i <= kMaxSys; i += blockDim.x) s.off[i] = p.off[i];
+    for (int i = threadIdx.x; i < kMaxSys; i += blockDim.x) s.sys[i] = p.sys[i];
+    __syncthreads();
+}
+
+// Rebuild plan `which` (0: Krylov product, 1: refinement residual) from the
+// current phases; one block of kMaxSys threads, thread t = slot t.
+__device__ void plan_build(KTable *tb, int which) {
+    __shared__ int cnt[kMaxSys], act[kMaxSys];
+    const int t = threadIdx.x;
+    int c = 0;
+    if (t < tb->B) {
+        const KSys &S = tb->sys[t];
+        if (mv_active(S.st, which == 1)) c = mv_items_of(S.n, tb->prec);
+    }
+    cnt[t] = c;
+    act[t] = c > 0;
+    __syncthreads();
+    if (t == 0) {   // serial scan over at most kMaxSys slots
+        KPlan &p = tb->plan[which];
+        int n = 0, off = 0;
+        for (int j = 0; j < kMaxSys; ++j)
+            if (act[j]) {
+                p.sys[n] = j;
+                p.off[n] = off;
+                off += cnt[j];
+                ++n;
+            }
+        p.off[n] = off;
+        p.n = n;
+    }
+    __syncthreads();
+}
+
 // ------------------------------------------------------------ matvec (complex128)
 // Persistent grid; blocks take tiles (system, 32 rows x 1024 columns) from a
 // queue.  The x chunk is staged in shared memory; 8 warps x 4 rows; each lane
@@ -86,20 +139,22 @@ template <bool EXACT>
 __global__ void __launch_bounds__(256, 4) k_mv64(KTable *tb) {
     __shared__ __align__(16) double2 xd[kMvChunk];
     __shared__ int item_s;
+    __shared__ PlanSmem pl;
+    plan_load(tb->plan[EXACT ? 1 : 0], pl);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int total = tb->mv_total;
-    while (true) {
+    const int total = pl.off[pl.n];
+    while (total > 0) {
         if (threadIdx.x == 0) item_s = (int)atomicAdd(&tb->mv_ctr[0], 1u);
         __syncthreads();
         const int item = item_s;
         __syncthreads();
         if (item >= total) break;
-        const int2 it = tb->mv_items[item];
-        const KSys &S = tb->sys[it.x];
+        const int j = plan_find(pl.off, pl.n, item);
+        const KSys &S = tb->sys[pl.sys[j]];
         const KState *st = S.st;
-        if (!mv_active(st, EXACT)) continue;
+        const int local = item - pl.off[j];
         const int n = S.n;
-        const int chunk = it.y % S.nchunk, tile = it.y / S.nchunk;
+        const int chunk = local % S.nchunk, tile = local / S.nchunk;
         const int c0 = chunk * kMvChunk, len = min(kMvChunk, n - c0);
         const double2 *xs = EXACT ? S.x : (S.pc ? S.z : S.V + (size_t)st->k * S.ldv);
         for (int t = threadIdx.x; t < len; t += blockDim.x) xd[t] = xs[c0 + t];
@@ -230,25 +285,27 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    __syncthreads();
+    __shared__ PlanSmem pl;
+    plan_load(tb->plan[EXACT ? 1 : 0], pl);   // includes a block barrier
     int *err = &tb->err;
     if (warp == kTmaConsumers) {
         // ---------------- producer (one lane)
         if (lane != 0) return;
-        const int total = tb->mv_total;
+        const int total = pl.off[pl.n];
         int stage = 0, xs = 0;
         uint32_t eph = 1, xeph[2] = {1, 1};   // a fresh barrier's previous phase counts as complete
         int issued[kTmaStages] = {0, 0, 0};   // stage holds copies not yet seen complete by us
         uint32_t fph[kTmaStages] = {0, 0, 0};
         bool ok = true;
         while (ok) {
+            if (total == 0) break;
             const int item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
             if (item >= total) break;
-            const int2 it = tb->mv_items[item];
-            const KSys &S = tb->sys[it.x];
-            if (!mv_active(S.st, EXACT)) continue;
+            const int j = plan_find(pl.off, pl.n, item);
+            const int sb = pl.sys[j], local = item - pl.off[j];
+            const KSys &S = tb->sys[sb];
             const int n = S.n;
-            const int chunk = it.y % S.nchunk, strip = it.y / S.nchunk;
+            const int chunk = local % S.nchunk, strip = local / S.nchunk;
             const int c0 = chunk * kMvChunk, len = min(kMvChunk, n - c0), lenp = (len + 1) & ~1;
             const int rbase = strip * kTmaStrip;
             const int nst = min(kTmaStrip / kTmaRows, (n - rbase + kTmaRows - 1) / kTmaRows);
@@ -268,7 +325,7 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
                 if (!mbar_wait(empty0 + 8 * stage, eph, err)) { ok = false; break; }
                 const int row0 = rbase + g * kTmaRows, nrows = min(kTmaRows, n - row0);
                 TmaMeta mt;
-                mt.b = it.x; mt.chunk = chunk; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
+                mt.b = sb; mt.chunk = chunk; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
                 mt.first = g == 0; mt.last = g == nst - 1; mt.xslot = xs;
                 meta[stage] = mt;
                 mbar_expect_tx(full0 + 8 * stage, (uint32_t)(nrows * lenp * 8));
@@ -580,12 +637,8 @@ __global__ void __launch_bounds__(kThreads) k_scale(const KTable *tb) {
 // rotations, the new rotation, |g[k+1]|; ends the cycle (phase UPDATE) when
 // the residual estimate reaches the cycle's target, at breakdown, after m
 // steps or at the iteration limit.  Clears hsum for the next step.
-__global__ void k_givens(const KTable *tb) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= tb->B) return;
-    const KSys &S = tb->sys[b];
+__device__ void givens_step(const KSys &S) {
     KState *st = S.st;
-    if (st->phase != kPhaseArnoldi) return;
     const int k = st->k, m = st->m;
     double2 *H = S.H, *cs = S.cs, *sn = S.sn, *g = S.g, *hsum = S.hsum;
     for (int l = 0; l <= k; ++l) {
@@ -593,16 +646,17 @@ __global__ void k_givens(const KTable *tb) {
         hsum[l] = make_double2(0.0, 0.0);
     }
     const double hn = sqrt(norm_total(S.nrmp, S.nvb));
-    // previous rotations: [a; b] <- [[conj(c), conj(s)], [-s, c]] [a; b]
+    // previous rotations: [a; b] <- [[conj(c), conj(s)], [-s, c]] [a; b];
+    // the running entry stays in registers
+    double2 a = H[k];
     for (int l = 0; l < k; ++l) {
-        const double2 a = H[(size_t)l * m + k], bb = H[(size_t)(l + 1) * m + k];
+        const double2 bb = H[(size_t)(l + 1) * m + k];
         const double2 c = cs[l], s = sn[l];
         H[(size_t)l * m + k] = make_double2(c.x * a.x + c.y * a.y + s.x * bb.x + s.y * bb.y,
                                             c.x * a.y - c.y * a.x + s.x * bb.y - s.y * bb.x);
-        H[(size_t)(l + 1) * m + k] = make_double2(-(s.x * a.x - s.y * a.y) + c.x * bb.x - c.y * bb.y,
-                                                  -(s.x * a.y + s.y * a.x) + c.x * bb.y + c.y * bb.x);
+        a = make_double2(-(s.x * a.x - s.y * a.y) + c.x * bb.x - c.y * bb.y,
+                         -(s.x * a.y + s.y * a.x) + c.x * bb.y + c.y * bb.x);
     }
-    const double2 a = H[(size_t)k * m + k];
     const double den = sqrt(a.x * a.x + a.y * a.y + hn * hn);
     double2 c, s;
     if (den == 0.0) { c = make_double2(1.0, 0.0); s = make_double2(0.0, 0.0); }
@@ -611,15 +665,27 @@ __global__ void k_givens(const KTable *tb) {
     sn[k] = s;
     H[(size_t)k * m + k] = make_double2(c.x * a.x + c.y * a.y + s.x * hn, c.x * a.y - c.y * a.x + s.y * hn);
     const double2 gk = g[k];
-    g[k + 1] = make_double2(-(s.x * gk.x - s.y * gk.y), -(s.x * gk.y + s.y * gk.x));
+    const double2 g1 = make_double2(-(s.x * gk.x - s.y * gk.y), -(s.x * gk.y + s.y * gk.x));
+    g[k + 1] = g1;
     g[k] = make_double2(c.x * gk.x + c.y * gk.y, c.x * gk.y - c.y * gk.x);
-    const double res = sqrt(g[k + 1].x * g[k + 1].x + g[k + 1].y * g[k + 1].y);
+    const double res = sqrt(g1.x * g1.x + g1.y * g1.y);
     st->k = k + 1;
     st->iters += 1;
     st->n_mv += 1;
     st->res = res;
     if (!(res > st->thr) || hn == 0.0 || !isfinite(res) || k + 1 >= m || st->iters >= st->max_iter)
         st->phase = kPhaseUpdate;
+}
+
+// One block of kMaxSys threads, thread t = system t: the Givens step of every
+// system in phase ARNOLDI, then the plans of the next Krylov product and of
+// the refinement residual.
+__global__ void __launch_bounds__(kMaxSys) k_givens(KTable *tb) {
+    const int b = threadIdx.x;
+    if (b < tb->B && tb->sys[b].st->phase == kPhaseArnoldi) givens_step(tb->sys[b]);
+    __syncthreads();
+    plan_build(tb, 0);
+    plan_build(tb, 1);
 }
 
 // ------------------------------------------------------------ end of cycle
@@ -731,12 +797,8 @@ __global__ void __launch_bounds__(kThreads) k_resid(const KTable *tb) {
 
 // One thread per system: convergence decision after a cycle (or the initial
 // residual), then the restart: g = beta e_1, hsum = 0, the cycle's target.
-__global__ void k_decide(const KTable *tb) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= tb->B) return;
-    const KSys &S = tb->sys[b];
+__device__ void decide_step(const KSys &S) {
     KState *st = S.st;
-    if (st->phase != kPhaseUpdate) return;
     const double beta = sqrt(norm_total(S.nrmp, S.nvb));
     if (st->cycles == 0) {
         st->bnorm = beta;
@@ -780,6 +842,16 @@ __global__ void k_decide(const KTable *tb) {
     st->phase = kPhaseArnoldi;
 }
 
+// One block of kMaxSys threads: convergence decision after a cycle (or the
+// initial residual) and the restart of every system in phase UPDATE, then the
+// plan of the next body's first Krylov product.
+__global__ void __launch_bounds__(kMaxSys) k_decide(KTable *tb) {
+    const int b = threadIdx.x;
+    if (b < tb->B && tb->sys[b].st->phase == kPhaseUpdate) decide_step(tb->sys[b]);
+    __syncthreads();
+    plan_build(tb, 0);
+}
+
 int g_mv_grid[2] = {0, 0};
 int g_vec_grid = 0;
 std::atomic<long long> g_launches{0};
@@ -817,7 +889,6 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
     const bool c128 = prec == 0;
     if (!g_vec_grid) return cudaErrorNotReady;   // krylov_prepare() first
     const int gmv = g_mv_grid[c128 ? 0 : 1], gv = g_vec_grid;
-    const int gsys = (kMaxSys + 127) / 128;
     int nl = 0;
     cudaError_t e = cudaSuccess;
     for (int q = 0; q < kSteps; ++q) {
@@ -830,7 +901,7 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
         k_axpy<2><<<gv, kThreads, 0, st>>>(d_tab);
         if (c128) k_scale<true, false><<<gv, kThreads, 0, st>>>(d_tab);
         else k_scale<false, false><<<gv, kThreads, 0, st>>>(d_tab);
-        k_givens<<<gsys, 128, 0, st>>>(d_tab);
+        k_givens<<<1, kMaxSys, 0, st>>>(tb);
         nl += 6;
     }
     k_trisolve<<<(kMaxSys + 3) / 4, 128, 0, st>>>(d_tab);
@@ -841,7 +912,7 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
     else k_mv_tma<true><<<gmv, 32 * (kTmaConsumers + 1), tma_smem_bytes(true), st>>>(tb);
     if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * kSteps + 1], st, cudaEventRecordExternal);
     k_resid<<<gv, kThreads, 0, st>>>(d_tab);
-    k_decide<<<gsys, 128, 0, st>>>(d_tab);
+    k_decide<<<1, kMaxSys, 0, st>>>(tb);
     if (c128) k_scale<true, true><<<gv, kThreads, 0, st>>>(d_tab);
     else k_scale<false, true><<<gv, kThreads, 0, st>>>(d_tab);
     nl += 6;

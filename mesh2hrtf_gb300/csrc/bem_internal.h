@@ -52,8 +52,8 @@ constexpr int kMaxRestart = 63;
 constexpr int kMaxAsm = 64;    // assembly / projection / preconditioner set-up
 constexpr int kMaxSys = 128;   // Krylov engine slots
 
-inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
-inline int mv_chunks(int n) { return ceil_div(n, kMvChunk); }
+__host__ __device__ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+__host__ __device__ inline int mv_chunks(int n) { return ceil_div(n, kMvChunk); }
 inline int vec_blocks(int n) { return ceil_div(n, kVecBlock); }
 inline int pc_blocks(int n) { return ceil_div(n, kBlock); }
 
@@ -172,13 +172,22 @@ struct KSys {
     KState *st;
 };
 
+// Systems taking part in one matrix-vector launch and their item offsets;
+// rebuilt on the device (k_givens, k_decide) before each launch, so that a
+// launch touches only active systems and an empty launch ends at once.
+struct KPlan {
+    int n;                   // systems in the plan
+    int off[kMaxSys + 1];    // prefix sums of their items; off[n] = total
+    int sys[kMaxSys];        // their slots in the table
+};
+
 struct KTable {
     int B;
-    int mv_total;           // matvec tiles of all systems
+    int prec;               // 0: complex128 tiles, 1: complex64 strips
     int vb_total;           // vector blocks of all systems
     int err;                // set when a bounded device wait gave up
     unsigned mv_ctr[2];     // work queue of the persistent matvec
-    const int2 *mv_items;   // (system, tile)
+    KPlan plan[2];          // [0] Krylov product, [1] refinement residual
     const int2 *vb_items;   // (system, block)
     KSys sys[kMaxSys];
 };
@@ -195,7 +204,7 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
 // (TMA) in strips of kTmaStrip rows; complex128: tiles of kMvRows rows.
 constexpr int kTmaRows = 8;
 constexpr int kTmaStrip = 64;
-inline int mv_items_of(int n, int prec) {
+__host__ __device__ inline int mv_items_of(int n, int prec) {
     return ceil_div(n, prec == 0 ? kMvRows : kTmaStrip) * mv_chunks(n);
 }
 // Scratch sizes of one system (complex entries).
