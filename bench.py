@@ -50,6 +50,9 @@ RHO, C0 = 1.21, 343.0
 N_TRI = 20480
 SEED = 20261204
 METRIC = "freq solves/s at <=1e-4 rel err, mixed vs plain FP64 GPU BEM; p50/p99 latency"
+# DRAM bytes (read + write) of one complex64 product at N = 20480, measured by
+# ncu on this workload: 3.3566 GB read + 13.2 MB of row partials written
+MV_TRAFFIC = 3.3698e9
 
 
 def workload():
@@ -347,7 +350,10 @@ def main():
                                "iterations": float(np.mean(iters))},
         "roofline": {"bound": "hbm", "kernel": "k_mv<c64> (batched complex64 A x)", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if achieved else None,
-                     "traffic": None, "bytes_per_product": bytes_one, "products": n_mv,
+                     "traffic": MV_TRAFFIC if n == N_TRI else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per k_mv_tma<0> launch, "
+                                       "same N (profiles/k_mv_tma_head20480.md)",
+                     "bytes_per_product": bytes_one, "products": n_mv,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),

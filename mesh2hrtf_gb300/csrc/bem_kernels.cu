@@ -109,30 +109,101 @@ template <> struct FarPair<double> {
     }
 };
 
-template <> struct FarPair<float> {
-    static __device__ __forceinline__ KVals<float> run(const Elem32 &e, const float nx[3], int order, float k,
-                                                       float wr) {
-        KVals<float> acc;
-        acc.G = acc.H = acc.HT = acc.E = cmk(0.f, 0.f);
-        const int np = e.nv == 3 ? tri_count(order) : quad_count(order);
-        for (int g = 0; g < np; ++g) {
-            float s, t, w;
-            if (e.nv == 3) {
-                const int o = tri_offset(order) + g;
-                s = c_trif[o][0]; t = c_trif[o][1]; w = c_trif[o][2];
-            } else {
-                const int a = g / order, b = g - a * order;
-                s = c_glxf[order][a]; t = c_glxf[order][b];
-                w = c_glwf[order][a] * c_glwf[order][b];
-            }
-            QPoint<float> q;
-            map_point(e, s, t, w, q);
-            KVals<float> v = kernel_values(q, nx, k, wr);
-            acc.G += v.G; acc.H += v.H; acc.HT += v.HT; acc.E += v.E;
-        }
-        return acc;
-    }
+// Fused float evaluation of a regular pair's matrix entry.  The entry is
+// linear in the kernel values, so each quadrature point contributes
+// G * F with F built from the point's geometry and the column's boundary
+// condition (NC_AssembleTBEM, NC_EquationSystem.cpp:165-207):
+//   velocity:        H tau + E beta            -> F = tau z1 re1 + i b ze1
+//   + admittance:    ... + (G + HT beta tau) Y -> F += Y (1 + i b tau z1 re2)
+//   pressure:        -G tau - HT beta          -> F = -tau - i b z1 re2
+// with z1 = -1/r + i wr, re1 = r^.n_y, re2 = -r^.n_x,
+// ze1 = (3/r^2 - k^2) rq + n_x.n_y/r^2 - i wr/r (3 rq + n_x.n_y), rq = re1 re2,
+// beta = i b.  One complex accumulator per entry instead of four.
+struct FusedCol {
+    int bc;
+    float yr, yi;          // admittance (bc 2)
+    float tau, b, k2, wr;  // tau, beta / i, k^2, time factor * k
 };
+
+__device__ __forceinline__ void fused_point(const FusedCol &c, float dny, float dnx, float nn, float r2, float w,
+                                            float &acc_re, float &acc_im) {
+    const float ir = rsqrtf(r2);
+    const float r = r2 * ir;
+    float sn, cs;
+    phase_sincos(c.wr * r, &sn, &cs);
+    const float amp = w * (float)(1.0 / kPI4) * ir;
+    const float gr = cs * amp, gi = sn * amp;   // G
+    const float re1 = dny * ir, re2 = -dnx * ir;
+    float fr, fi;
+    if (c.bc == 1) {
+        // -tau - i b (-ir re2 + i wr re2) = (-tau + b wr re2, b ir re2)
+        fr = fmaf(c.b * c.wr, re2, -c.tau);
+        fi = c.b * ir * re2;
+    } else {
+        const float rq = re1 * re2, ir2 = ir * ir;
+        const float e_re = fmaf(3.f * ir2 - c.k2, rq, nn * ir2);
+        const float e_im = -c.wr * ir * fmaf(3.f, rq, nn);
+        // tau z1 re1 + i b ze1
+        fr = fmaf(-c.tau * ir, re1, -c.b * e_im);
+        fi = fmaf(c.tau * c.wr, re1, c.b * e_re);
+        if (c.bc == 2) {
+            // Y (1 + i b tau z1 re2) = Y (1 - b tau wr re2, -b tau ir re2)
+            const float pr = fmaf(-c.b * c.tau * c.wr, re2, 1.f), pi = -c.b * c.tau * ir * re2;
+            fr += c.yr * pr - c.yi * pi;
+            fi += c.yr * pi + c.yi * pr;
+        }
+    }
+    acc_re = fmaf(gr, fr, fmaf(-gi, fi, acc_re));
+    acc_im = fmaf(gr, fi, fmaf(gi, fr, acc_im));
+}
+
+// Points O0 .. O0+NP-1 of the triangle rules, unrolled so that the rule's
+// constants are constant-bank operands (the order is uniform across most
+// warps: neighbouring columns are neighbouring elements).
+template <int NP, int O0>
+__device__ __forceinline__ void tri_points(const Elem32 &e, float dny, float dnx0, float anx, float bnx, float nn,
+                                           const FusedCol &c, float &ar, float &ai) {
+#pragma unroll
+    for (int g = 0; g < NP; ++g) {
+        const float ss = c_trif[O0 + g][0] - (1.0f / 3.0f), tt = c_trif[O0 + g][1] - (1.0f / 3.0f);
+        const float w = c_trif[O0 + g][2] * e.J;
+        float d[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) d[k] = fmaf(tt, e.b[k], fmaf(ss, e.a[k], e.D[k]));
+        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        fused_point(c, dny, fmaf(tt, bnx, fmaf(ss, anx, dnx0)), nn, r2, w, ar, ai);
+    }
+}
+
+// Matrix entry of a regular pair in float with a fixed Gauss order.  Flat
+// triangles: n_y is constant and d.n_y = D.n_y at every point; d.n_x is
+// affine in (s, t).
+__device__ __forceinline__ float2 far_entry_f(const Elem32 &e, const float nx[3], int order, const FusedCol &c) {
+    float ar = 0.f, ai = 0.f;
+    if (e.nv == 3) {
+        const float dny = e.D[0] * e.n[0] + e.D[1] * e.n[1] + e.D[2] * e.n[2];
+        const float dnx0 = e.D[0] * nx[0] + e.D[1] * nx[1] + e.D[2] * nx[2];
+        const float anx = e.a[0] * nx[0] + e.a[1] * nx[1] + e.a[2] * nx[2];
+        const float bnx = e.b[0] * nx[0] + e.b[1] * nx[1] + e.b[2] * nx[2];
+        const float nn = e.n[0] * nx[0] + e.n[1] * nx[1] + e.n[2] * nx[2];
+        if (order <= 2) tri_points<4, 0>(e, dny, dnx0, anx, bnx, nn, c, ar, ai);
+        else if (order == 3) tri_points<7, 4>(e, dny, dnx0, anx, bnx, nn, c, ar, ai);
+        else tri_points<13, 11>(e, dny, dnx0, anx, bnx, nn, c, ar, ai);
+    } else {
+        const int np = quad_count(order);
+        for (int g = 0; g < np; ++g) {
+            const int a = g / order, b = g - a * order;
+            QPoint<float> q;
+            map_point(e, c_glxf[order][a], c_glxf[order][b], c_glwf[order][a] * c_glwf[order][b], q);
+            const float dny = q.d[0] * q.ny[0] + q.d[1] * q.ny[1] + q.d[2] * q.ny[2];
+            const float dnx = q.d[0] * nx[0] + q.d[1] * nx[1] + q.d[2] * nx[2];
+            const float nn = q.ny[0] * nx[0] + q.ny[1] * nx[1] + q.ny[2] * nx[2];
+            const float r2 = q.d[0] * q.d[0] + q.d[1] * q.d[1] + q.d[2] * q.d[2];
+            fused_point(c, dny, dnx, nn, r2, q.wj, ar, ai);
+        }
+    }
+    return make_float2(ar, ai);
+}
 
 template <typename T>
 __device__ __forceinline__ cplx<T> col_adm(const DevFreq &f, int j, int bc) {
@@ -216,6 +287,14 @@ __device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f
         const float cjh[3] = {m.chi[j], m.chi[n + j], m.chi[2 * n + j]};
         const float cjl[3] = {m.clo[j], m.clo[n + j], m.clo[2 * n + j]};
         const float isq = m.isqa32[j];
+        FusedCol fc;
+        fc.bc = bcj;
+        fc.yr = admj.re;
+        fc.yi = admj.im;
+        fc.tau = PT.tao;
+        fc.b = PT.beta_im;
+        fc.k2 = PT.k * PT.k;
+        fc.wr = PT.wr;
         for (int r = 0; r < kRowsPerThread; ++r) {
             const int i = i0 + r;
             if (i >= n) break;
@@ -232,9 +311,7 @@ __device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f
             }
             if (near) continue;
             const float nx[3] = {m.n32[i], m.n32[n + i], m.n32[2 * n + i]};
-            KVals<float> v = FarPair<float>::run(e, nx, order, PT.k, PT.wr);
-            const cplx<float> val = combine_entry(v, bcj, admj, PT);
-            A[(size_t)i * lda + j] = make_float2(val.re, val.im);
+            A[(size_t)i * lda + j] = far_entry_f(e, nx, order, fc);
         }
     }
 }
