@@ -35,8 +35,9 @@ typedef enum {
     BEM_ERR_NOT_CONVERGED = 3,  /* Krylov solver hit its iteration limit       */
     BEM_ERR_DEVICE_TIMEOUT = 4, /* a bounded device wait gave up               */
     BEM_ERR_CUDA = 5,           /* CUDA runtime error                          */
-    BEM_ERR_SUBDIVISION = 6     /* element subdivision limit exceeded (NumCalc
+    BEM_ERR_SUBDIVISION = 6,    /* element subdivision limit exceeded (NumCalc
                                    stops with the same condition)              */
+    BEM_ERR_PENDING = 7         /* a served request is not finished yet        */
 } bem_status;
 
 typedef enum {
@@ -232,6 +233,56 @@ bem_status bem_solve_batch(int32_t count, const bem_solver_t *solvers,
                            const double *const *pts, double *const *x_out,
                            double *const *pot_out, double *const *grad_out,
                            bem_solve_info *infos, bem_status *statuses);
+
+/* Serving ----------------------------------------------------------------
+ * A server takes solve requests ((mesh, frequency, evaluation points)) as
+ * they arrive and runs them with continuous batching: a request is admitted
+ * when its footprint (bem_footprint_bytes plus its points) fits the free part
+ * of the server's device-memory budget and an iteration slot is free; its
+ * assembly runs on a second stream while the admitted requests iterate; it
+ * joins the batched GMRES at the next iteration body and leaves it when it
+ * has converged, after which it is projected and its memory is returned.
+ * Requests are admitted in arrival order.  A request's result is the one
+ * bem_solve_frequency gives for it alone.  NumCalc has no counterpart: its
+ * steps run as processes that manage_numcalc starts while host RAM allows
+ * (manage_numcalc.py:284-385). */
+typedef struct bem_server_s *bem_server_t;
+
+typedef struct {
+    int32_t precision;         /* bem_precision of every request               */
+    double hbm_budget_bytes;   /* device memory reserved for the requests
+                                  (0 = free memory minus 1 GB)                 */
+    int32_t max_active;        /* requests iterating together (0 = 128, the
+                                  most)                                        */
+    int32_t restart;           /* as in bem_solver_params; 0 = defaults        */
+    int32_t max_iter;
+    double tol;
+    int32_t device;            /* CUDA device of the server                    */
+} bem_server_params;
+
+typedef struct {
+    double queued_ms;          /* submit -> admitted                            */
+    double latency_ms;         /* submit -> results ready                       */
+    bem_solve_info solve;      /* iterations and residual of the request; the
+                                  stage times are those of the launches it took
+                                  part in                                       */
+} bem_request_info;
+
+/* Reserves the budget on the device and starts the server's worker thread. */
+bem_status bem_server_create(const bem_server_params *params, bem_server_t *out);
+/* Queue one request; freq, its arrays and pts [n_pts][3] are copied.  The
+ * mesh must stay alive until the request has been waited for.  A request
+ * whose footprint exceeds the whole budget gets BEM_ERR_OUT_OF_HBM here. */
+bem_status bem_server_submit(bem_server_t server, bem_mesh_t mesh, const bem_frequency_desc *freq,
+                             int32_t n_pts, const double *pts, uint64_t *ticket);
+/* Wait up to timeout_s seconds (< 0: no limit) for a request; copy its
+ * unknowns (n_elem complex, may be NULL), potentials [n_pts] and gradients
+ * [n_pts][3] (may be NULL) and release the ticket.  Returns the request's own
+ * status, or BEM_ERR_PENDING (ticket kept) if it has not finished in time. */
+bem_status bem_server_wait(bem_server_t server, uint64_t ticket, double timeout_s, double *x_out,
+                           double *pot_out, double *grad_out, bem_request_info *info);
+/* Finish the requests already admitted, drop the queued ones, stop. */
+bem_status bem_server_destroy(bem_server_t server);
 
 #ifdef __cplusplus
 }

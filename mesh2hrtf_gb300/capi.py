@@ -23,6 +23,7 @@ BEM_ERR_NOT_CONVERGED = 3
 BEM_ERR_DEVICE_TIMEOUT = 4
 BEM_ERR_CUDA = 5
 BEM_ERR_SUBDIVISION = 6
+BEM_ERR_PENDING = 7
 PREC_FP64 = 0
 PREC_MIXED = 1
 
@@ -31,6 +32,7 @@ EXPORTED = [
     "bem_mesh_create", "bem_mesh_destroy", "bem_solver_create", "bem_solver_destroy", "bem_solver_set_params",
     "bem_assemble", "bem_solve", "bem_get_solution", "bem_get_system", "bem_project",
     "bem_solve_frequency", "bem_project_static", "bem_solve_batch",
+    "bem_server_create", "bem_server_submit", "bem_server_wait", "bem_server_destroy",
 ]
 STATIC_MAX_ELEMENTS = 32768
 
@@ -68,6 +70,20 @@ class SolveInfo(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ServerParams(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("hbm_budget_bytes", C.c_double), ("max_active", C.c_int32),
+                ("restart", C.c_int32), ("max_iter", C.c_int32), ("tol", C.c_double), ("device", C.c_int32)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("queued_ms", C.c_double), ("latency_ms", C.c_double), ("solve", SolveInfo)]
+
+    def as_dict(self):
+        d = {"queued_ms": self.queued_ms, "latency_ms": self.latency_ms}
+        d.update(self.solve.as_dict())
+        return d
+
+
 _lib = None
 
 
@@ -101,6 +117,10 @@ def load(build_if_missing: bool = True):
     lib.bem_solve_frequency.argtypes = [vp, C.POINTER(FreqDesc), i32, vp, vp, vp, vp, C.POINTER(SolveInfo)]
     lib.bem_project_static.argtypes = [vp, i32, vp, vp, vp, vp]
     lib.bem_solve_batch.argtypes = [i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.bem_server_create.argtypes = [C.POINTER(ServerParams), C.POINTER(vp)]
+    lib.bem_server_submit.argtypes = [vp, vp, C.POINTER(FreqDesc), i32, vp, C.POINTER(C.c_uint64)]
+    lib.bem_server_wait.argtypes = [vp, C.c_uint64, C.c_double, vp, vp, vp, C.POINTER(RequestInfo)]
+    lib.bem_server_destroy.argtypes = [vp]
     for name in EXPORTED:
         if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes", "bem_kernel_launches"):
             getattr(lib, name).restype = C.c_int
@@ -277,6 +297,54 @@ def solve_batch(solvers, freqs, pts_list=None, with_grad=True, allow_not_converg
     if rc != BEM_OK and not all(int(v) in (BEM_OK,) + allow for v in sts):
         _check(rc, allow)
     return [(xs[i], pots[i], grads[i], infos[i].as_dict(), int(sts[i])) for i in range(cnt)]
+
+
+class Server:
+    """bem_server_t: solve requests served with continuous batching."""
+
+    def __init__(self, precision=PREC_MIXED, hbm_budget=0.0, max_active=0, restart=0, max_iter=0, tol=0.0,
+                 device=0):
+        p = ServerParams(precision, hbm_budget, max_active, restart, max_iter, tol, device)
+        h = C.c_void_p()
+        _check(load().bem_server_create(C.byref(p), C.byref(h)))
+        self.handle = h
+        self._req = {}
+
+    def submit(self, mesh: Mesh, freq: Frequency, pts):
+        """Queue one request; returns its ticket.  Inputs are copied."""
+        pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+        t = C.c_uint64()
+        _check(load().bem_server_submit(self.handle, mesh.handle, C.byref(freq.desc), len(pts),
+                                        _ptr(pts) if len(pts) else None, C.byref(t)))
+        self._req[t.value] = (mesh.n, len(pts))
+        return t.value
+
+    def wait(self, ticket, timeout=-1.0, allow_not_converged=False):
+        """Result of a request: (x, pot, grad, info dict, status); None while pending."""
+        n, m = self._req[ticket]
+        x = np.zeros(n, np.complex128)
+        pot = np.zeros(m, np.complex128)
+        grad = np.zeros((m, 3), np.complex128)
+        info = RequestInfo()
+        rc = load().bem_server_wait(self.handle, ticket, timeout, _ptr(x), _ptr(pot) if m else None,
+                                    _ptr(grad) if m else None, C.byref(info))
+        if rc == BEM_ERR_PENDING:
+            return None
+        del self._req[ticket]
+        allow = (BEM_ERR_NOT_CONVERGED,) if allow_not_converged else ()
+        _check(rc, allow)
+        return x, pot, grad, info.as_dict(), rc
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().bem_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def footprint_bytes(n_elem, precision=PREC_MIXED, restart=0):

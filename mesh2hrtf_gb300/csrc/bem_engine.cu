@@ -62,7 +62,7 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
     if (!items_.empty())
         e = cudaMemcpyAsync(d_items_, items_.data(), items_.size() * sizeof(int2), cudaMemcpyHostToDevice, st_);
     if (e != cudaSuccess) return e;
-    std::memset(h_tab_, 0, sizeof(KTable));   // empty plans: the first body starts at the cycle end
+    std::memset(h_tab_, 0, sizeof(KTable));   // plans are rebuilt on the device below
     h_tab_->B = B;
     h_tab_->prec = prec_;
     h_tab_->vb_total = vb_total;
@@ -75,6 +75,8 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
     e = cudaMemcpyAsync(d_tab_, h_tab_, sizeof(KTable), cudaMemcpyHostToDevice, st_);
     if (e == cudaSuccess && B > 0)
         e = cudaMemcpyAsync(d_st_, h_st_, sizeof(KState) * B, cudaMemcpyHostToDevice, st_);
+    // systems may be in the middle of a cycle: their next products need plans
+    if (e == cudaSuccess) e = launch_plans(d_tab_, st_);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
     B_ = B;
     mv_ms_ = 0.0;

@@ -852,6 +852,12 @@ __global__ void __launch_bounds__(kMaxSys) k_decide(KTable *tb) {
     plan_build(tb, 0);
 }
 
+// Both plans from the current phases (after the host rewrote the table).
+__global__ void __launch_bounds__(kMaxSys) k_plans(KTable *tb) {
+    plan_build(tb, 0);
+    plan_build(tb, 1);
+}
+
 int g_mv_grid[2] = {0, 0};
 int g_vec_grid = 0;
 std::atomic<long long> g_launches{0};
@@ -881,6 +887,12 @@ cudaError_t krylov_prepare() {
         g_vec_grid = 2 * sms;
     });
     return err;
+}
+
+cudaError_t launch_plans(KTable *d_tab, cudaStream_t st) {
+    count_launches(1);
+    k_plans<<<1, kMaxSys, 0, st>>>(d_tab);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev, cudaStream_t st,

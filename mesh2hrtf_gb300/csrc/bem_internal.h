@@ -207,6 +207,8 @@ constexpr int kTmaStrip = 64;
 __host__ __device__ inline int mv_items_of(int n, int prec) {
     return ceil_div(n, prec == 0 ? kMvRows : kTmaStrip) * mv_chunks(n);
 }
+// Rebuilds both launch plans of *d_tab from the systems' current phases.
+cudaError_t launch_plans(KTable *d_tab, cudaStream_t st);
 // Scratch sizes of one system (complex entries).
 inline size_t mvp_elems(int n) { return (size_t)mv_chunks(n) * (size_t)n; }
 inline size_t xsplit_elems(int n) { return (size_t)mv_chunks(n) * kMvChunk; }
