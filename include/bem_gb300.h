@@ -97,6 +97,8 @@ typedef struct {
                                   free device memory minus a reserve)          */
     int32_t no_precond;        /* 0: block-Jacobi preconditioner (default),
                                   1: none                                      */
+    int32_t n_rhs;             /* right-hand sides the solver can hold for
+                                  bem_solve_multi (0 or 1: one; at most 16)    */
 } bem_solver_params;
 
 typedef struct {
@@ -126,6 +128,8 @@ bem_status bem_set_device(int32_t device);
  * admission footprint (NumCalc's host RAM estimate, NC_Main.cpp:524-541,
  * counts (N + N^2) * 16 bytes for the same data). */
 double bem_footprint_bytes(int32_t n_elem, int32_t precision, int32_t restart);
+/* The same for a solver holding n_rhs right-hand sides (bem_solve_multi). */
+double bem_footprint_multi(int32_t n_elem, int32_t precision, int32_t restart, int32_t n_rhs);
 
 /* Mesh: upload and precompute element tables.
  * Replaces NC_ReadMesh's geometry part (NC_Input.cpp:522-602) and the per-pair
@@ -212,6 +216,23 @@ bem_status bem_solve_frequency(bem_solver_t solver, const bem_frequency_desc *fr
                                int32_t n_pts, const double *pts, double *x_out,
                                double *pot_out, double *grad_out,
                                bem_solve_info *info);
+
+/* Several right-hand sides on one matrix: one assembly of A, one
+ * preconditioner, then n_rhs GMRES iterations in lockstep whose products
+ * share each read of A, and one projection pass.  Right-hand side r takes the
+ * sources and prescribed boundary values of freqs[r]; the wave number,
+ * time factor, tao, boundary-condition types and admittances (which define
+ * the matrix) are those of freqs[0].  NumCalc sums all sources of a project
+ * into one right-hand side (NC_IncidentWaveRHS, NC_EquationSystem.cpp:
+ * 1731-1812); Mesh2HRTF runs one project per source (the ears), i.e. one
+ * NumCalc per right-hand side.  Needs a solver created with n_rhs >= the
+ * count.  x_out[r] (n_elem complex), pot_out[r] ([n_pts] complex) and
+ * grad_out[r] ([n_pts][3] complex) may be NULL arrays or hold NULLs;
+ * infos[r] (may be NULL) gets right-hand side r's iterations and residual. */
+bem_status bem_solve_multi(bem_solver_t solver, int32_t n_rhs, const bem_frequency_desc *freqs,
+                           int32_t n_pts, const double *pts, double *const *x_out,
+                           double *const *pot_out, double *const *grad_out,
+                           bem_solve_info *infos);
 
 /* Several frequency steps solved together: count (solver, frequency)
  * instances, each solver with its own mesh (meshes of different sizes mix

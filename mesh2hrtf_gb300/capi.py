@@ -31,7 +31,7 @@ EXPORTED = [
     "bem_last_error", "bem_version", "bem_kernel_launches", "bem_set_device", "bem_footprint_bytes",
     "bem_mesh_create", "bem_mesh_destroy", "bem_solver_create", "bem_solver_destroy", "bem_solver_set_params",
     "bem_assemble", "bem_solve", "bem_get_solution", "bem_get_system", "bem_project",
-    "bem_solve_frequency", "bem_project_static", "bem_solve_batch",
+    "bem_solve_frequency", "bem_project_static", "bem_solve_batch", "bem_solve_multi", "bem_footprint_multi",
     "bem_server_create", "bem_server_submit", "bem_server_wait", "bem_server_destroy",
 ]
 STATIC_MAX_ELEMENTS = 32768
@@ -58,7 +58,8 @@ class FreqDesc(C.Structure):
 
 class SolverParams(C.Structure):
     _fields_ = [("precision", C.c_int32), ("restart", C.c_int32), ("max_iter", C.c_int32),
-                ("tol", C.c_double), ("hbm_budget_bytes", C.c_double), ("no_precond", C.c_int32)]
+                ("tol", C.c_double), ("hbm_budget_bytes", C.c_double), ("no_precond", C.c_int32),
+                ("n_rhs", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -104,6 +105,9 @@ def load(build_if_missing: bool = True):
     lib.bem_set_device.argtypes = [i32]
     lib.bem_footprint_bytes.argtypes = [i32, i32, i32]
     lib.bem_footprint_bytes.restype = C.c_double
+    lib.bem_footprint_multi.argtypes = [i32, i32, i32, i32]
+    lib.bem_footprint_multi.restype = C.c_double
+    lib.bem_solve_multi.argtypes = [vp, i32, vp, i32, vp, vp, vp, vp, vp]
     lib.bem_mesh_create.argtypes = [C.POINTER(MeshDesc), C.POINTER(vp)]
     lib.bem_mesh_destroy.argtypes = [vp]
     lib.bem_solver_create.argtypes = [vp, C.POINTER(SolverParams), C.POINTER(vp)]
@@ -122,7 +126,8 @@ def load(build_if_missing: bool = True):
     lib.bem_server_wait.argtypes = [vp, C.c_uint64, C.c_double, vp, vp, vp, C.POINTER(RequestInfo)]
     lib.bem_server_destroy.argtypes = [vp]
     for name in EXPORTED:
-        if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes", "bem_kernel_launches"):
+        if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes", "bem_footprint_multi",
+                        "bem_kernel_launches"):
             getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -199,18 +204,18 @@ class Solver:
     """bem_solver_t: matrix + Krylov workspace for one mesh on the device."""
 
     def __init__(self, mesh: Mesh, precision=PREC_FP64, restart=0, max_iter=0, tol=0.0, hbm_budget=0.0,
-                 precond=True):
+                 precond=True, n_rhs=1):
         lib = load()
         self.mesh = mesh
         self.n = mesh.n
-        p = SolverParams(precision, restart, max_iter, tol, hbm_budget, 0 if precond else 1)
+        p = SolverParams(precision, restart, max_iter, tol, hbm_budget, 0 if precond else 1, n_rhs)
         h = C.c_void_p()
         _check(lib.bem_solver_create(mesh.handle, C.byref(p), C.byref(h)))
         self.handle = h
         self.info = SolveInfo()
 
     def set_params(self, max_iter=0, tol=0.0):
-        p = SolverParams(0, 0, max_iter, tol, 0.0, 0)
+        p = SolverParams(0, 0, max_iter, tol, 0.0, 0, 0)
         _check(load().bem_solver_set_params(self.handle, C.byref(p)))
 
     def assemble(self, freq: Frequency):
@@ -253,6 +258,27 @@ class Solver:
         _check(load().bem_solve_frequency(self.handle, C.byref(freq.desc), len(pts), _ptr(pts), _ptr(x),
                                           _ptr(pot), _ptr(grad), C.byref(self.info)), allow)
         return x, pot, grad
+
+    def solve_multi(self, freqs, pts, with_grad=True, allow_not_converged=False):
+        """bem_solve_multi: one matrix, len(freqs) right-hand sides.
+
+        Returns lists x[r], pot[r], grad[r] and the infos (dicts)."""
+        R = len(freqs)
+        pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+        m = len(pts)
+        xs = [np.zeros(self.n, np.complex128) for _ in range(R)]
+        pots = [np.zeros(m, np.complex128) for _ in range(R)]
+        grads = [np.zeros((m, 3), np.complex128) for _ in range(R)] if with_grad else None
+        PtrArr = C.c_void_p * R
+        fs = (FreqDesc * R)(*[f.desc for f in freqs])
+        infos = (SolveInfo * R)()
+        allow = (BEM_ERR_NOT_CONVERGED,) if allow_not_converged else ()
+        _check(load().bem_solve_multi(self.handle, R, fs, m, _ptr(pts) if m else None,
+                                      PtrArr(*[x.ctypes.data for x in xs]),
+                                      PtrArr(*[p.ctypes.data if m else None for p in pots]),
+                                      PtrArr(*[g.ctypes.data if m else None for g in grads]) if with_grad else None,
+                                      infos), allow)
+        return xs, pots, grads, [i.as_dict() for i in infos]
 
     def close(self):
         if getattr(self, "handle", None):

@@ -126,9 +126,14 @@ uint64_t spread3(uint64_t v) {
 
 namespace bem {
 
-// Byte layout of the block (256-byte aligned pieces).  base == nullptr only
-// sizes it.  The footprint reported by bem_footprint_bytes is this size.
-size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, SolverBufs *o) {
+// Byte layout of the block (256-byte aligned pieces): the matrix and what
+// the right-hand sides share, then the per-right-hand-side buffers (Krylov
+// workspace, projection scratch, boundary values and sources) of n_rhs
+// right-hand sides.  base == nullptr only sizes it.  extra (n_rhs - 1
+// entries) receives right-hand sides 1..n_rhs-1, whose shared fields repeat
+// those of *o.
+size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, SolverBufs *o, int n_rhs,
+                     SolverBufs *extra) {
     size_t off = 0;
     auto take = [&](size_t bytes) -> void * {
         void *p = base ? (void *)(base + off) : nullptr;
@@ -139,26 +144,6 @@ size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, Solve
     const size_t esz = prec == 0 ? 16 : 8;
     SolverBufs d;
     d.A = take(N * lda * esz);
-    d.b = (double2 *)take(N * 16);
-    d.x = (double2 *)take(N * 16);
-    d.r = (double2 *)take(N * 16);
-    d.w = (double2 *)take(N * 16);
-    d.z = (double2 *)take(N * 16);
-    d.V = (double2 *)take((size_t)(m + 1) * N * 16);
-    d.mvp = (double2 *)take(mvp_elems(n) * 16);
-    if (prec != 0) {   // complex64: float copies of the product's input
-        d.xh = (float2 *)take(xsplit_elems(n) * 8);
-        d.xf = (float4 *)take(xsplit_elems(n) * 16);
-    }
-    d.dpa = (double2 *)take(dp_elems(n) * 16);
-    d.dpb = (double2 *)take(dp_elems(n) * 16);
-    d.nrmp = (double *)take((size_t)vec_blocks(n) * 8);
-    d.H = (double2 *)take((size_t)(m + 1) * m * 16);
-    d.cs = (double2 *)take((size_t)m * 16);
-    d.sn = (double2 *)take((size_t)m * 16);
-    d.g = (double2 *)take((size_t)(m + 1) * 16);
-    d.y = (double2 *)take((size_t)m * 16);
-    d.hsum = (double2 *)take((size_t)(m + 1) * 16);
     if (pc) {
         const size_t pb = precond_bytes(n, prec);
         d.Minv = take(prec == 0 ? pb / 2 : pb);
@@ -166,14 +151,42 @@ size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, Solve
     }
     d.status = (int *)take(16);
     d.ctr = (unsigned *)take(16);
-    d.phi = (double *)take(N * 16);
-    d.vel = (double *)take(4 * N * 16);
-    d.ivi = (int *)take(N * 4);
     d.bct = (int *)take(N * 4);
-    d.cols = (int *)take(N * 4);
-    d.bcv = (double *)take(8 * N * 8);
     d.adm = (double *)take(2 * N * 8);
-    d.src = (double *)take(5 * (size_t)kInlineSources * 8);
+    auto per_rhs = [&](SolverBufs &q) {
+        q.b = (double2 *)take(N * 16);
+        q.x = (double2 *)take(N * 16);
+        q.r = (double2 *)take(N * 16);
+        q.w = (double2 *)take(N * 16);
+        q.z = (double2 *)take(N * 16);
+        q.V = (double2 *)take((size_t)(m + 1) * N * 16);
+        q.mvp = (double2 *)take(mvp_elems(n) * 16);
+        if (prec != 0) {   // complex64: float copies of the product's input
+            q.xh = (float2 *)take(xsplit_elems(n) * 8);
+            q.xf = (float4 *)take(xsplit_elems(n) * 16);
+        }
+        q.dpa = (double2 *)take(dp_elems(n) * 16);
+        q.dpb = (double2 *)take(dp_elems(n) * 16);
+        q.nrmp = (double *)take((size_t)vec_blocks(n) * 8);
+        q.H = (double2 *)take((size_t)(m + 1) * m * 16);
+        q.cs = (double2 *)take((size_t)m * 16);
+        q.sn = (double2 *)take((size_t)m * 16);
+        q.g = (double2 *)take((size_t)(m + 1) * 16);
+        q.y = (double2 *)take((size_t)m * 16);
+        q.hsum = (double2 *)take((size_t)(m + 1) * 16);
+        q.phi = (double *)take(N * 16);
+        q.vel = (double *)take(4 * N * 16);
+        q.ivi = (int *)take(N * 4);
+        q.cols = (int *)take(N * 4);
+        q.bcv = (double *)take(8 * N * 8);
+        q.src = (double *)take(5 * (size_t)kInlineSources * 8);
+    };
+    per_rhs(d);
+    for (int r = 1; r < n_rhs; ++r) {
+        SolverBufs q = d;   // shared fields
+        per_rhs(q);
+        if (extra) extra[r - 1] = q;
+    }
     if (o) *o = d;
     return off;
 }
@@ -201,13 +214,15 @@ namespace bem {
 
 // Frequency data into the solver's block (internal element order).  NumCalc
 // does the same per frequency in NC_UpdateFreqCurves before assembly.
-bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f, cudaStream_t st) {
+bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f, cudaStream_t st, int rhs) {
     const int n = s->n;
+    if (rhs < 0 || rhs >= s->n_rhs) return fail(BEM_ERR_INVALID, "right-hand side %d of %d", rhs, s->n_rhs);
+    const SolverBufs &B = s->buf(rhs);
     if (!(f->wave_number > 0.0)) return fail(BEM_ERR_INVALID, "wave number must be > 0");
     if (f->n_point < 0 || f->n_plane < 0) return fail(BEM_ERR_INVALID, "negative source count");
     if ((f->n_point && (!f->point_xyz || !f->point_amp)) || (f->n_plane && (!f->plane_dir || !f->plane_amp)))
         return fail(BEM_ERR_INVALID, "source arrays missing");
-    bem::DevFreq &F = s->freq;
+    bem::DevFreq &F = rhs == 0 ? s->freq : s->xfreq[rhs - 1];
     F = bem::DevFreq{};
     const double htf = f->time_factor == -1.0 ? -1.0 : 1.0;
     const double tao = f->tao == -1.0 ? -1.0 : 1.0;
@@ -222,14 +237,18 @@ bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f, cudaStream_t
     const std::vector<int> &ext = s->mesh->ext_of_int;
     std::vector<int> cols, bct;
     std::vector<double> bcv, adm, src;
-    if (f->bc_type) {
+    if (rhs > 0) {   // the matrix data of right-hand side 0
+        F.bc_type = s->freq.bc_type;
+        F.adm = s->freq.adm;
+    }
+    if (f->bc_type && rhs == 0) {
         for (int j = 0; j < n; ++j)
             if (f->bc_type[j] < 0 || f->bc_type[j] > 2)
                 return fail(BEM_ERR_INVALID, "element %d: boundary condition type %d unsupported", j, f->bc_type[j]);
         bct.resize(n);
         for (int i = 0; i < n; ++i) bct[i] = f->bc_type[ext[i]];
-        CU(cudaMemcpyAsync(s->d.bct, bct.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
-        F.bc_type = s->d.bct;
+        CU(cudaMemcpyAsync(B.bct, bct.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+        F.bc_type = B.bct;
     }
     if (f->bc_value) {
         bcv.assign(8 * (size_t)n, 0.0);
@@ -245,21 +264,21 @@ bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f, cudaStream_t
             }
             if (nz) cols.push_back(i);
         }
-        CU(cudaMemcpyAsync(s->d.bcv, bcv.data(), sizeof(double) * bcv.size(), cudaMemcpyHostToDevice, st));
-        F.bc_val = s->d.bcv;
+        CU(cudaMemcpyAsync(B.bcv, bcv.data(), sizeof(double) * bcv.size(), cudaMemcpyHostToDevice, st));
+        F.bc_val = B.bcv;
     }
-    if (f->admittance) {
+    if (f->admittance && rhs == 0) {
         adm.resize(2 * (size_t)n);
         for (int i = 0; i < n; ++i) {
             adm[2 * (size_t)i] = f->admittance[2 * (size_t)ext[i]];
             adm[2 * (size_t)i + 1] = f->admittance[2 * (size_t)ext[i] + 1];
         }
-        CU(cudaMemcpyAsync(s->d.adm, adm.data(), sizeof(double) * adm.size(), cudaMemcpyHostToDevice, st));
-        F.adm = s->d.adm;
+        CU(cudaMemcpyAsync(B.adm, adm.data(), sizeof(double) * adm.size(), cudaMemcpyHostToDevice, st));
+        F.adm = B.adm;
     }
     if (!cols.empty()) {
-        CU(cudaMemcpyAsync(s->d.cols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, st));
-        F.bc_cols = s->d.cols;
+        CU(cudaMemcpyAsync(B.cols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, st));
+        F.bc_cols = B.cols;
         F.n_bc_cols = (int)cols.size();
     }
     const size_t nsrc = 5 * (size_t)f->n_point + 5 * (size_t)f->n_plane;
@@ -271,8 +290,9 @@ bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f, cudaStream_t
         for (int i = 0; i < 2 * f->n_plane; ++i) src.push_back(f->plane_amp[i]);
         for (int i = 0; i < 3 * f->n_point; ++i) src.push_back(f->point_xyz[i]);
         for (int i = 0; i < 3 * f->n_plane; ++i) src.push_back(f->plane_dir[i]);
-        double *dst = s->d.src;
+        double *dst = B.src;
         if (f->n_point + f->n_plane > bem::kInlineSources) {
+            if (rhs > 0) return fail(BEM_ERR_INVALID, "more than %d sources on right-hand side %d", bem::kInlineSources, rhs);
             CU(cudaStreamSynchronize(st));
             cudaFree(s->src_extra);
             s->src_extra = nullptr;
@@ -464,6 +484,8 @@ bem_status solve_group(bem_solver_t *ss, int cnt, bem::Engine *eng, cudaStream_t
     return first;
 }
 
+// Point buffers for n_pts points: the points, and potentials and gradients
+// for each of the solver's right-hand sides.
 bem_status ensure_points(bem_solver_t s, int n_pts) {
     if (n_pts <= s->pts_cap) return BEM_OK;
     CU(cudaStreamSynchronize(s->st));
@@ -471,8 +493,8 @@ bem_status ensure_points(bem_solver_t s, int n_pts) {
     s->pts = s->pot = s->grad = nullptr;
     s->pts_cap = 0;
     CU(dalloc(&s->pts, 3 * (size_t)n_pts));
-    CU(dalloc(&s->pot, 2 * (size_t)n_pts));
-    CU(dalloc(&s->grad, 6 * (size_t)n_pts));
+    CU(dalloc(&s->pot, 2 * (size_t)n_pts * s->n_rhs));
+    CU(dalloc(&s->grad, 6 * (size_t)n_pts * s->n_rhs));
     s->pts_cap = n_pts;
     return BEM_OK;
 }
@@ -529,9 +551,9 @@ bem_status project_group(bem_solver_t *ss, int cnt, const int32_t *npts, const d
     return first;
 }
 
-bem_status solution_to_host(bem_solver_t s, cudaStream_t st, double *x_host) {
+bem_status solution_to_host(bem_solver_t s, cudaStream_t st, double *x_host, int rhs) {
     std::vector<double> t(2 * (size_t)s->n);
-    bem_status rc = fetch(st, s->d.x, t.data(), t.size() * sizeof(double));
+    bem_status rc = fetch(st, s->buf(rhs).x, t.data(), t.size() * sizeof(double));
     if (rc != BEM_OK) return rc;
     const std::vector<int> &ext = s->mesh->ext_of_int;
     for (int i = 0; i < s->n; ++i) {
@@ -549,6 +571,7 @@ bem::Engine *solver_engine(bem_solver_t s) {
 }  // namespace bem
 
 using bem::assemble_group;
+using bem::ensure_points;
 using bem::map_result;
 using bem::precond_group;
 using bem::project_group;
@@ -571,9 +594,13 @@ bem_status bem_set_device(int32_t device) {
 }
 
 double bem_footprint_bytes(int32_t n_elem, int32_t precision, int32_t restart) {
+    return bem_footprint_multi(n_elem, precision, restart, 1);
+}
+
+double bem_footprint_multi(int32_t n_elem, int32_t precision, int32_t restart, int32_t n_rhs) {
     const int m = restart > 0 ? restart : 60;
     const int prec = precision == BEM_PREC_FP64 ? 0 : 1;
-    return (double)bem::solver_layout(std::max(n_elem, 1), prec, m, true, nullptr, nullptr);
+    return (double)bem::solver_layout(std::max(n_elem, 1), prec, m, true, nullptr, nullptr, std::max(n_rhs, 1));
 }
 
 bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
@@ -734,7 +761,9 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     const int n = mesh->n;
     const bool pc = prm.no_precond == 0;
     const int prec = prm.precision == BEM_PREC_FP64 ? 0 : 1;
-    const size_t need = bem::solver_layout(n, prec, m, pc, nullptr, nullptr);
+    const int n_rhs = prm.n_rhs > 0 ? prm.n_rhs : 1;
+    if (n_rhs > bem::kMaxRhs) return fail(BEM_ERR_INVALID, "n_rhs %d above the limit %d", n_rhs, bem::kMaxRhs);
+    const size_t need = bem::solver_layout(n, prec, m, pc, nullptr, nullptr, n_rhs);
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
     double budget = prm.hbm_budget_bytes > 0 ? prm.hbm_budget_bytes : (double)free_b - 1.0e9;
@@ -756,7 +785,10 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     if (e == cudaSuccess) e = cudaMalloc(&s->block, need);
     if (e == cudaSuccess) {
         s->block_bytes = need;
-        bem::solver_layout(n, prec, m, pc, s->block, &s->d);
+        s->n_rhs = n_rhs;
+        s->xr.resize(n_rhs - 1);
+        s->xfreq.resize(n_rhs - 1);
+        bem::solver_layout(n, prec, m, pc, s->block, &s->d, n_rhs, s->xr.data());
         e = cudaMemset(s->d.ctr, 0, 4 * sizeof(unsigned));
     }
     if (e != cudaSuccess)
@@ -870,6 +902,130 @@ bem_status bem_solve_frequency(bem_solver_t s, const bem_frequency_desc *f, int3
     if (rc != BEM_OK) return rc;
     if (info) *info = s->info;
     return solve_rc;
+}
+
+bem_status bem_solve_multi(bem_solver_t s, int32_t R, const bem_frequency_desc *freqs, int32_t n_pts,
+                           const double *pts, double *const *x_out, double *const *pot_out, double *const *grad_out,
+                           bem_solve_info *infos) {
+    if (!s || !freqs) return fail(BEM_ERR_INVALID, "null argument");
+    if (R < 1 || R > s->n_rhs)
+        return fail(BEM_ERR_INVALID, "%d right-hand sides, the solver holds %d (bem_solver_params.n_rhs)", R, s->n_rhs);
+    if (n_pts < 0 || (n_pts > 0 && !pts)) return fail(BEM_ERR_INVALID, "bad point arrays");
+    cudaStream_t st = s->st;
+    for (int r = 0; r < R; ++r) {
+        bem_status rc = upload_freq(s, &freqs[r], st, r);
+        if (rc != BEM_OK) return rc;
+    }
+    // the matrix once, the R right-hand sides in one launch
+    CU(cudaMemsetAsync(s->d.status, 0, sizeof(int), st));
+    CU(cudaEventRecord(s->ev[0], st));
+    {
+        std::unique_ptr<bem::AsmBatch> t(new bem::AsmBatch());
+        t->B = 1;
+        t->sys[0] = s->asys(0);
+        bem::asm_batch_finish(*t);
+        CU(bem::launch_assemble(*t, s->prec == BEM_PREC_FP64 ? 0 : 1, s->d.ctr, st));
+        t->B = R;
+        for (int r = 0; r < R; ++r) t->sys[r] = s->asys(r);
+        bem::asm_batch_finish(*t);
+        CU(bem::launch_rhs(*t, st));
+    }
+    CU(cudaEventRecord(s->ev[1], st));
+    int code = 0;
+    CU(cudaMemcpyAsync(&code, s->d.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    float ams = 0.f;
+    CU(cudaEventElapsedTime(&ams, s->ev[0], s->ev[1]));
+    s->info.assemble_ms = ams;
+    s->info.n_near_pairs = (int64_t)(s->mesh->n_near - s->n);
+    if (code != 0) return fail(BEM_ERR_SUBDIVISION, "%s", subdivision_message(code));
+    s->have_freq = true;
+    s->solved = false;
+    // preconditioner of the shared matrix, x = 0, then the R systems in lockstep
+    CU(cudaEventRecord(s->ev[2], st));
+    bem_status rc = precond_group(&s, 1, st);
+    if (rc != BEM_OK) return rc;
+    std::vector<bem::KSys> sys(R);
+    std::vector<bem::KState> init(R);
+    for (int r = 0; r < R; ++r) {
+        if (r > 0) CU(cudaMemsetAsync(s->buf(r).x, 0, sizeof(double2) * s->n, st));
+        sys[r] = s->ksys(r);
+        init[r] = s->kinit();
+    }
+    bem::Engine *eng = solver_engine(s);
+    CU(eng->set_batch(sys, init));
+    bool all_done = false;
+    for (long long body = 0; body < 2LL * s->max_iter + 64 && !all_done; ++body) {
+        const cudaError_t be = eng->run_body();
+        if (be == cudaErrorLaunchTimeout)
+            return fail(BEM_ERR_DEVICE_TIMEOUT, "matrix-vector product: a bounded device wait gave up");
+        CU(be);
+        all_done = true;
+        for (int r = 0; r < R; ++r)
+            if (eng->states()[r].phase != bem::kPhaseFinished) all_done = false;
+    }
+    CU(cudaEventRecord(s->ev[3], st));
+    CU(cudaEventSynchronize(s->ev[3]));
+    float sms = 0.f;
+    CU(cudaEventElapsedTime(&sms, s->ev[2], s->ev[3]));
+    s->info.solve_ms = sms;
+    s->info.matvec_ms = eng->timing_ok() ? eng->matvec_ms() : 0.0;
+    s->solved = true;
+    bem_status first = BEM_OK;
+    std::vector<bem::KState> fin(eng->states(), eng->states() + R);
+    for (int r = 0; r < R; ++r) {
+        bem_status q = fin[r].phase == bem::kPhaseFinished ? map_result(fin[r])
+                                                           : fail(BEM_ERR_DEVICE_TIMEOUT, "GMRES did not finish");
+        if (q != BEM_OK && first == BEM_OK) first = q;
+    }
+    // projection of all right-hand sides
+    rc = ensure_points(s, n_pts);
+    if (rc != BEM_OK) return rc;
+    CU(cudaMemsetAsync(s->d.status, 0, sizeof(int), st));
+    CU(cudaEventRecord(s->ev[4], st));
+    if (n_pts > 0) CU(cudaMemcpyAsync(s->pts, pts, sizeof(double) * 3 * n_pts, cudaMemcpyHostToDevice, st));
+    {
+        std::unique_ptr<bem::ProjBatch> t(new bem::ProjBatch());
+        t->B = R;
+        for (int r = 0; r < R; ++r)
+            t->sys[r] = s->prsys(n_pts, s->pts, s->pot + 2 * (size_t)n_pts * r, s->grad + 6 * (size_t)n_pts * r, r);
+        bem::proj_batch_finish(*t);
+        CU(bem::launch_fields(*t, st));
+        CU(bem::launch_project(*t, s->prec == BEM_PREC_FP64 ? 0 : 1, st));
+    }
+    CU(cudaEventRecord(s->ev[5], st));
+    for (int r = 0; r < R && n_pts > 0; ++r) {
+        if (pot_out && pot_out[r])
+            CU(cudaMemcpyAsync(pot_out[r], s->pot + 2 * (size_t)n_pts * r, sizeof(double) * 2 * n_pts,
+                               cudaMemcpyDeviceToHost, st));
+        if (grad_out && grad_out[r])
+            CU(cudaMemcpyAsync(grad_out[r], s->grad + 6 * (size_t)n_pts * r, sizeof(double) * 6 * n_pts,
+                               cudaMemcpyDeviceToHost, st));
+    }
+    CU(cudaMemcpyAsync(&code, s->d.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    float pms = 0.f;
+    CU(cudaEventElapsedTime(&pms, s->ev[4], s->ev[5]));
+    s->info.project_ms = pms;
+    if (code != 0) return fail(BEM_ERR_SUBDIVISION, "evaluation point too close to the boundary: subdivision limit");
+    for (int r = 0; r < R; ++r) {
+        if (x_out && x_out[r]) {
+            rc = solution_to_host(s, st, x_out[r], r);
+            if (rc != BEM_OK) return rc;
+        }
+        if (infos) {
+            infos[r] = s->info;
+            infos[r].iterations = fin[r].iters;
+            infos[r].restarts = fin[r].cycles;
+            infos[r].rel_residual = fin[r].rel;
+            infos[r].n_matvec = fin[r].n_mv;
+        }
+    }
+    if (first != BEM_OK) {
+        for (int r = 0; r < R; ++r)
+            if (fin[r].result != bem::kResConverged) return map_result(fin[r]);
+    }
+    return BEM_OK;
 }
 
 bem_status bem_solve_batch(int32_t count, const bem_solver_t *solvers, const bem_frequency_desc *freqs,

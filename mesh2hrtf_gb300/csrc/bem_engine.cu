@@ -70,8 +70,27 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
     for (int b = 0; b < B; ++b) {
         h_tab_->sys[b] = sys[b];
         h_tab_->sys[b].st = d_st_ + b;
+        h_tab_->sys[b].shared = 0;
         h_st_[b] = init[b];
     }
+    // complex64 systems next to each other on the same matrix (the right-hand
+    // sides of one solver) form groups whose products share each read of A
+    int ng = 0;
+    for (int b = 0; b < B && prec_ == 1;) {
+        int e = b + 1;
+        while (e < B && e - b < kMaxGroup && sys[e].A == sys[b].A) ++e;
+        if (e - b >= 2) {
+            h_tab_->grp[ng].first = b;
+            h_tab_->grp[ng].count = e - b;
+            ++ng;
+            for (int q = b; q < e; ++q) {
+                h_tab_->sys[q].shared = 1;
+                h_tab_->sys[q].nchunk = 1;   // the group product writes full rows
+            }
+        }
+        b = e;
+    }
+    h_tab_->n_groups = ng;
     e = cudaMemcpyAsync(d_tab_, h_tab_, sizeof(KTable), cudaMemcpyHostToDevice, st_);
     if (e == cudaSuccess && B > 0)
         e = cudaMemcpyAsync(d_st_, h_st_, sizeof(KState) * B, cudaMemcpyHostToDevice, st_);

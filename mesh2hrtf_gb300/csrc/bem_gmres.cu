@@ -104,16 +104,25 @@ __device__ __forceinline__ void plan_load(const KPlan &p, PlanSmem &s) {
 // current phases; one block of kMaxSys threads, thread t = slot t.
 __device__ void plan_build(KTable *tb, int which) {
     __shared__ int cnt[kMaxSys], act[kMaxSys];
+    __shared__ unsigned gm[kMaxSys];
     const int t = threadIdx.x;
     int c = 0;
     if (t < tb->B) {
         const KSys &S = tb->sys[t];
-        if (mv_active(S.st, which == 1)) c = mv_items_of(S.n, tb->prec);
+        if (!S.shared && mv_active(S.st, which == 1)) c = mv_items_of(S.n, tb->prec);
     }
     cnt[t] = c;
     act[t] = c > 0;
+    // shared-matrix groups: members taking part, strips of the group
+    unsigned mask = 0;
+    if (t < tb->n_groups) {
+        const KGroup g = tb->grp[t];
+        for (int q = 0; q < g.count; ++q)
+            if (mv_active(tb->sys[g.first + q].st, which == 1)) mask |= 1u << q;
+    }
+    gm[t] = mask;
     __syncthreads();
-    if (t == 0) {   // serial scan over at most kMaxSys slots
+    if (t == 0) {   // serial scans over at most kMaxSys slots
         KPlan &p = tb->plan[which];
         int n = 0, off = 0;
         for (int j = 0; j < kMaxSys; ++j)
@@ -125,6 +134,19 @@ __device__ void plan_build(KTable *tb, int which) {
             }
         p.off[n] = off;
         p.n = n;
+        KPlan &gp = tb->gplan[which];
+        n = 0;
+        off = 0;
+        for (int j = 0; j < tb->n_groups; ++j)
+            if (gm[j]) {
+                gp.sys[n] = j;
+                gp.off[n] = off;
+                tb->gmask[which][n] = gm[j];
+                off += ceil_div(tb->sys[tb->grp[j].first].n, kGrpRows);
+                ++n;
+            }
+        gp.off[n] = off;
+        gp.n = n;
     }
     __syncthreads();
 }
@@ -428,6 +450,220 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
         }
         if (mt.first) xph[mt.xslot] ^= 1;
         if (++stage == kTmaStages) { stage = 0; fph ^= 1; }
+    }
+}
+
+// ------------------------------------------------------------ shared-matrix product
+// Right-hand sides of one solver share A (complex64).  One launch streams
+// every tile of A once: an item is a strip of kGrpRows rows of one group over
+// all columns; a stage holds kGrpRows x kGrpCols of A (32 KB, one bulk copy
+// per row segment) and the x chunks of the group's members that take part
+// (2 KB each for the Krylov product, 4 KB of hi/lo pairs for the residual).
+// Consumer warp w owns rows 2w, 2w + 1 of the strip and keeps, in registers,
+// one accumulator per (row, member) across all column chunks; at the strip's
+// last chunk it writes the members' full-row products (nchunk = 1).
+constexpr int kGrpStages = 3;
+constexpr int kGrpAStage = kGrpRows * kGrpCols * 8;
+static_assert(kGrpRows == 2 * kTmaConsumers, "two rows per consumer warp");
+__host__ __device__ constexpr int grp_x_bytes(bool exact) { return exact ? kGrpCols * 16 : kGrpCols * 8; }
+__host__ __device__ constexpr int grp_stage_bytes(bool exact) { return kGrpAStage + kMaxGroup * grp_x_bytes(exact); }
+__host__ __device__ constexpr int grp_smem_bytes(bool exact) { return kGrpStages * grp_stage_bytes(exact) + 512; }
+
+struct GrpMeta {
+    int first, chunk, row0, nrows, len, last, mask, pad;
+};
+
+template <bool EXACT>
+__global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_grp(KTable *tb) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr int SB = grp_stage_bytes(EXACT), XB = grp_x_bytes(EXACT);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kGrpStages * SB);
+    GrpMeta *meta = reinterpret_cast<GrpMeta *>(bars + 2 * kGrpStages);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kGrpStages);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kGrpStages; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, kTmaConsumers);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __shared__ PlanSmem pl;
+    plan_load(tb->gplan[EXACT ? 1 : 0], pl);   // includes a block barrier
+    int *err = &tb->err;
+    if (warp == kTmaConsumers) {
+        // ---------------- producer (one lane)
+        if (lane != 0) return;
+        const int total = pl.off[pl.n];
+        int stage = 0;
+        uint32_t eph = 1;
+        int issued[kGrpStages] = {0, 0, 0};
+        uint32_t fph[kGrpStages] = {0, 0, 0};
+        bool ok = true;
+        while (ok && total > 0) {
+            const int item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+            if (item >= total) break;
+            const int j = plan_find(pl.off, pl.n, item);
+            const KGroup g = tb->grp[pl.sys[j]];
+            const unsigned mask = tb->gmask[EXACT ? 1 : 0][j];
+            const KSys &S0 = tb->sys[g.first];
+            const int n = S0.n;
+            const int row0 = (item - pl.off[j]) * kGrpRows, nrows = min(kGrpRows, n - row0);
+            const int nck = (n + kGrpCols - 1) / kGrpCols;
+            const float2 *A = (const float2 *)S0.A;
+            for (int ck = 0; ck < nck && ok; ++ck) {
+                if (!mbar_wait(empty0 + 8 * stage, eph, err)) { ok = false; break; }
+                const int c0 = ck * kGrpCols, len = min(kGrpCols, n - c0), lenp = (len + 1) & ~1;
+                GrpMeta mt;
+                mt.first = g.first; mt.chunk = ck; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
+                mt.last = ck == nck - 1; mt.mask = (int)mask; mt.pad = 0;
+                meta[stage] = mt;
+                int nmem = 0;
+                for (int q = 0; q < g.count; ++q) nmem += (mask >> q) & 1;
+                const uint32_t xbytes = EXACT ? (uint32_t)XB : (uint32_t)(lenp * 8);
+                mbar_expect_tx(full0 + 8 * stage, (uint32_t)(nrows * lenp * 8) + nmem * xbytes);
+                const uint32_t dst = smem_u32(smem + stage * SB);
+                for (int r = 0; r < nrows; ++r)
+                    bulk_g2s(dst + r * kGrpCols * 8, A + (size_t)(row0 + r) * S0.lda + c0, lenp * 8, full0 + 8 * stage);
+                for (int q = 0; q < g.count; ++q) {
+                    if (!((mask >> q) & 1)) continue;
+                    const KSys &S = tb->sys[g.first + q];
+                    const uint32_t xd = dst + kGrpAStage + q * XB;
+                    if (EXACT) {
+                        // chunk-permuted (hi, lo) pairs: the stage's even entries, then its odd ones
+                        const float4 *base = S.xf + (size_t)(c0 & ~(kMvChunk - 1));
+                        const int o = (c0 & (kMvChunk - 1)) >> 1;
+                        bulk_g2s(xd, base + o, kGrpCols * 8, full0 + 8 * stage);
+                        bulk_g2s(xd + kGrpCols * 8, base + kMvChunk / 2 + o, kGrpCols * 8, full0 + 8 * stage);
+                    } else {
+                        bulk_g2s(xd, S.xh + c0, lenp * 8, full0 + 8 * stage);
+                    }
+                }
+                issued[stage] = 1;
+                fph[stage] ^= 1;
+                if (++stage == kGrpStages) { stage = 0; eph ^= 1; }
+            }
+        }
+        if (ok) {
+            if (mbar_wait(empty0 + 8 * stage, eph, err)) {
+                meta[stage].first = -1;
+                mbar_arrive(full0 + 8 * stage);
+            } else {
+                ok = false;
+            }
+        }
+        if (!ok)
+            for (int s = 0; s < kGrpStages; ++s)
+                if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
+        __threadfence();
+        if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
+            tb->mv_ctr[0] = 0u;
+            tb->mv_ctr[1] = 0u;
+            __threadfence();
+        }
+        return;
+    }
+    // ---------------- consumers: warp w takes rows 2w, 2w + 1 of each strip
+    float ar[2][kMaxGroup], ai[2][kMaxGroup], er[2][kMaxGroup], ei[2][kMaxGroup];
+    int stage = 0;
+    uint32_t fph = 0;
+    while (true) {
+        if (!mbar_wait(full0 + 8 * stage, fph, err)) return;
+        const GrpMeta mt = meta[stage];
+        if (mt.first < 0) return;
+        if (mt.chunk == 0) {
+#pragma unroll
+            for (int q = 0; q < kMaxGroup; ++q)
+#pragma unroll
+                for (int r = 0; r < 2; ++r) ar[r][q] = ai[r][q] = er[r][q] = ei[r][q] = 0.f;
+        }
+        const unsigned char *sb = smem + stage * SB;
+        const int r0 = 2 * warp;
+        const bool v0 = r0 < mt.nrows, v1 = r0 + 1 < mt.nrows;
+        const float4 *A0 = reinterpret_cast<const float4 *>(sb) + r0 * (kGrpCols / 2);
+        const float4 *A1 = A0 + kGrpCols / 2;
+        const int len = mt.len, len2 = len >> 1;
+        for (int c = lane; c < len2; c += 32) {
+            const float4 a0 = v0 ? A0[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 a1 = v1 ? A1[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < kMaxGroup; ++q) {
+                if (!((mt.mask >> q) & 1)) continue;
+                const unsigned char *xq = sb + kGrpAStage + q * XB;
+                if (!EXACT) {
+                    const float4 xv = reinterpret_cast<const float4 *>(xq)[c];   // hi of entries 2c, 2c + 1
+                    ar[0][q] = fmaf(a0.x, xv.x, ar[0][q]); ar[0][q] = fmaf(-a0.y, xv.y, ar[0][q]);
+                    ai[0][q] = fmaf(a0.x, xv.y, ai[0][q]); ai[0][q] = fmaf(a0.y, xv.x, ai[0][q]);
+                    ar[0][q] = fmaf(a0.z, xv.z, ar[0][q]); ar[0][q] = fmaf(-a0.w, xv.w, ar[0][q]);
+                    ai[0][q] = fmaf(a0.z, xv.w, ai[0][q]); ai[0][q] = fmaf(a0.w, xv.z, ai[0][q]);
+                    ar[1][q] = fmaf(a1.x, xv.x, ar[1][q]); ar[1][q] = fmaf(-a1.y, xv.y, ar[1][q]);
+                    ai[1][q] = fmaf(a1.x, xv.y, ai[1][q]); ai[1][q] = fmaf(a1.y, xv.x, ai[1][q]);
+                    ar[1][q] = fmaf(a1.z, xv.z, ar[1][q]); ar[1][q] = fmaf(-a1.w, xv.w, ar[1][q]);
+                    ai[1][q] = fmaf(a1.z, xv.w, ai[1][q]); ai[1][q] = fmaf(a1.w, xv.z, ai[1][q]);
+                } else {
+                    const float4 x0 = reinterpret_cast<const float4 *>(xq)[c];
+                    const float4 x1 = reinterpret_cast<const float4 *>(xq + kGrpCols * 8)[c];
+#pragma unroll
+                    for (int r = 0; r < 2; ++r) {
+                        const float4 a = r == 0 ? a0 : a1;
+                        acc_exact(ar[r][q], er[r][q], a.x, x0.x); acc_exact(ar[r][q], er[r][q], -a.y, x0.y);
+                        acc_exact(ai[r][q], ei[r][q], a.x, x0.y); acc_exact(ai[r][q], ei[r][q], a.y, x0.x);
+                        er[r][q] = fmaf(a.x, x0.z, er[r][q]); er[r][q] = fmaf(-a.y, x0.w, er[r][q]);
+                        ei[r][q] = fmaf(a.x, x0.w, ei[r][q]); ei[r][q] = fmaf(a.y, x0.z, ei[r][q]);
+                        acc_exact(ar[r][q], er[r][q], a.z, x1.x); acc_exact(ar[r][q], er[r][q], -a.w, x1.y);
+                        acc_exact(ai[r][q], ei[r][q], a.z, x1.y); acc_exact(ai[r][q], ei[r][q], a.w, x1.x);
+                        er[r][q] = fmaf(a.z, x1.z, er[r][q]); er[r][q] = fmaf(-a.w, x1.w, er[r][q]);
+                        ei[r][q] = fmaf(a.z, x1.w, ei[r][q]); ei[r][q] = fmaf(a.w, x1.z, ei[r][q]);
+                    }
+                }
+            }
+        }
+        if ((len & 1) && lane == 0) {   // odd tail: entry len - 1
+            const float2 b0 = v0 ? reinterpret_cast<const float2 *>(A0)[len - 1] : make_float2(0.f, 0.f);
+            const float2 b1 = v1 ? reinterpret_cast<const float2 *>(A1)[len - 1] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < kMaxGroup; ++q) {
+                if (!((mt.mask >> q) & 1)) continue;
+                const unsigned char *xq = sb + kGrpAStage + q * XB;
+                float xr, xi, lr = 0.f, li = 0.f;
+                if (!EXACT) {
+                    const float2 xv = reinterpret_cast<const float2 *>(xq)[len - 1];
+                    xr = xv.x; xi = xv.y;
+                } else {
+                    const float4 x0 = reinterpret_cast<const float4 *>(xq)[(len - 1) >> 1];
+                    xr = x0.x; xi = x0.y; lr = x0.z; li = x0.w;
+                }
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    const float2 b = r == 0 ? b0 : b1;
+                    if (!EXACT) {
+                        ar[r][q] = fmaf(b.x, xr, ar[r][q]); ar[r][q] = fmaf(-b.y, xi, ar[r][q]);
+                        ai[r][q] = fmaf(b.x, xi, ai[r][q]); ai[r][q] = fmaf(b.y, xr, ai[r][q]);
+                    } else {
+                        acc_exact(ar[r][q], er[r][q], b.x, xr); acc_exact(ar[r][q], er[r][q], -b.y, xi);
+                        acc_exact(ai[r][q], ei[r][q], b.x, xi); acc_exact(ai[r][q], ei[r][q], b.y, xr);
+                        er[r][q] = fmaf(b.x, lr, er[r][q]); er[r][q] = fmaf(-b.y, li, er[r][q]);
+                        ei[r][q] = fmaf(b.x, li, ei[r][q]); ei[r][q] = fmaf(b.y, lr, ei[r][q]);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty0 + 8 * stage);
+        if (mt.last) {
+#pragma unroll
+            for (int q = 0; q < kMaxGroup; ++q) {
+                if (!((mt.mask >> q) & 1)) continue;
+                const KSys &S = tb->sys[mt.first + q];
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    const double tr = warp_sum_d((double)ar[r][q] + (double)er[r][q]);
+                    const double ti = warp_sum_d((double)ai[r][q] + (double)ei[r][q]);
+                    if (lane == 0 && r0 + r < mt.nrows) S.mvp[mt.row0 + r0 + r] = make_double2(tr, ti);
+                }
+            }
+        }
+        if (++stage == kGrpStages) { stage = 0; fph ^= 1; }
     }
 }
 
@@ -881,6 +1117,12 @@ cudaError_t krylov_prepare() {
         if (err == cudaSuccess)
             err = cudaFuncSetAttribute(k_mv_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        tma_smem_bytes(true));
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k_mv_grp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       grp_smem_bytes(false));
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k_mv_grp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       grp_smem_bytes(true));
         g_mv_grid[1] = sms;   // one bulk-copy block per SM
         if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mv64<false>, 256, 0);
         g_mv_grid[0] = sms * (per > 0 ? per : 1);
@@ -906,7 +1148,11 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
     for (int q = 0; q < kSteps; ++q) {
         if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q], st, cudaEventRecordExternal);
         if (c128) k_mv64<false><<<gmv, 256, 0, st>>>(tb);
-        else k_mv_tma<false><<<gmv, 32 * (kTmaConsumers + 1), tma_smem_bytes(false), st>>>(tb);
+        else {
+            k_mv_tma<false><<<gmv, 32 * (kTmaConsumers + 1), tma_smem_bytes(false), st>>>(tb);
+            k_mv_grp<false><<<gmv, 32 * (kTmaConsumers + 1), grp_smem_bytes(false), st>>>(tb);
+            ++nl;
+        }
         if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q + 1], st, cudaEventRecordExternal);
         k_dot1<<<gv, kThreads, 0, st>>>(d_tab);
         k_axpy<1><<<gv, kThreads, 0, st>>>(d_tab);
@@ -921,7 +1167,11 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
     else k_xupdate<false><<<gv, kThreads, 0, st>>>(d_tab);
     if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * kSteps], st, cudaEventRecordExternal);
     if (c128) k_mv64<true><<<gmv, 256, 0, st>>>(tb);
-    else k_mv_tma<true><<<gmv, 32 * (kTmaConsumers + 1), tma_smem_bytes(true), st>>>(tb);
+    else {
+        k_mv_tma<true><<<gmv, 32 * (kTmaConsumers + 1), tma_smem_bytes(true), st>>>(tb);
+        k_mv_grp<true><<<gmv, 32 * (kTmaConsumers + 1), grp_smem_bytes(true), st>>>(tb);
+        ++nl;
+    }
     if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * kSteps + 1], st, cudaEventRecordExternal);
     k_resid<<<gv, kThreads, 0, st>>>(d_tab);
     k_decide<<<1, kMaxSys, 0, st>>>(tb);

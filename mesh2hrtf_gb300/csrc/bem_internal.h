@@ -51,6 +51,7 @@ constexpr int kMaxRestart = 63;
 // Systems per launch table.
 constexpr int kMaxAsm = 64;    // assembly / projection / preconditioner set-up
 constexpr int kMaxSys = 128;   // Krylov engine slots
+constexpr int kMaxRhs = 16;    // right-hand sides of one solver
 
 __host__ __device__ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 __host__ __device__ inline int mv_chunks(int n) { return ceil_div(n, kMvChunk); }
@@ -169,7 +170,16 @@ struct KSys {
     double2 *dpa, *dpb;     // inner-product partials [kMaxRestart + 1][nvb]
     double *nrmp;           // squared-norm partials [nvb]
     double2 *H, *cs, *sn, *g, *y, *hsum;   // H: (m + 1) x m row-major
+    int shared;             // 1: shares A with its neighbours in the table (one
+                            // solver's right-hand sides; complex64 only); its
+                            // product is one full-row partial (nchunk = 1)
     KState *st;
+};
+
+// Systems first .. first + count - 1 of a table share one complex64 matrix.
+constexpr int kMaxGroup = 8;   // right-hand sides per shared-matrix product
+struct KGroup {
+    int first, count;
 };
 
 // Systems taking part in one matrix-vector launch and their item offsets;
@@ -188,9 +198,17 @@ struct KTable {
     int err;                // set when a bounded device wait gave up
     unsigned mv_ctr[2];     // work queue of the persistent matvec
     KPlan plan[2];          // [0] Krylov product, [1] refinement residual
+    int n_groups;           // shared-matrix groups
+    KGroup grp[kMaxSys];
+    KPlan gplan[2];         // plans of the shared-matrix products (entries = groups)
+    unsigned gmask[2][kMaxSys];   // per plan entry: members taking part
     const int2 *vb_items;   // (system, block)
     KSys sys[kMaxSys];
 };
+
+// Shared-matrix product: items are strips of kGrpRows rows over all columns.
+constexpr int kGrpRows = 16;
+constexpr int kGrpCols = 256;
 
 // Arnoldi steps per iteration body.
 constexpr int kSteps = 8;

@@ -76,9 +76,10 @@ struct SolverBufs {
     double *bcv = nullptr, *adm = nullptr, *src = nullptr;
 };
 
-// Byte layout of the block (256-byte aligned pieces).  base == nullptr only
-// sizes it.  The footprint reported by bem_footprint_bytes is this size.
-size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, SolverBufs *o);
+// Byte layout of a solver's block for n_rhs right-hand sides; base ==
+// nullptr only sizes it (bem_footprint_bytes is this size for one).
+size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, SolverBufs *o, int n_rhs = 1,
+                     SolverBufs *extra = nullptr);
 
 }  // namespace bem
 
@@ -95,7 +96,10 @@ struct bem_solver_s {
     cudaEvent_t ev[8] = {};
     unsigned char *block = nullptr;
     size_t block_bytes = 0;
-    bem::SolverBufs d;
+    bem::SolverBufs d;                     // right-hand side 0 and the shared buffers
+    int n_rhs = 1;
+    std::vector<bem::SolverBufs> xr;       // right-hand sides 1 .. n_rhs-1
+    std::vector<bem::DevFreq> xfreq;       // their frequency data (sources, boundary values)
     double *src_extra = nullptr;
     bem::DevFreq freq{};
     bool have_freq = false;
@@ -117,7 +121,10 @@ struct bem_solver_s {
             if (e) cudaEventDestroy(e);
         if (st) cudaStreamDestroy(st);
     }
-    bem::KSys ksys() const {
+    const bem::SolverBufs &buf(int r) const { return r == 0 ? d : xr[r - 1]; }
+    const bem::DevFreq &fq(int r) const { return r == 0 ? freq : xfreq[r - 1]; }
+    bem::KSys ksys(int r = 0) const {
+        const bem::SolverBufs &d = buf(r);
         bem::KSys k{};
         k.A = d.A;
         k.lda = (long long)lda;
@@ -142,10 +149,11 @@ struct bem_solver_s {
         q.floor_rel = prec == BEM_PREC_MIXED ? 1e-5 : 0.0;
         return q;
     }
-    bem::AsmSys asys() const {
+    bem::AsmSys asys(int r = 0) const {
+        const bem::SolverBufs &d = buf(r);
         bem::AsmSys a{};
         a.m = mesh->view();
-        a.f = freq;
+        a.f = fq(r);
         a.A = d.A;
         a.lda = lda;
         a.near = mesh->d_near;
@@ -164,10 +172,11 @@ struct bem_solver_s {
         p.status = d.status;
         return p;
     }
-    bem::ProjSys prsys(int npts, const double *pts_dev, double *pot_dev, double *grad_dev) const {
+    bem::ProjSys prsys(int npts, const double *pts_dev, double *pot_dev, double *grad_dev, int r = 0) const {
+        const bem::SolverBufs &d = buf(r);
         bem::ProjSys q{};
         q.m = mesh->view();
-        q.f = freq;
+        q.f = fq(r);
         q.x = (const double *)d.x;
         q.phi = d.phi;
         q.vel = d.vel;
@@ -183,8 +192,10 @@ struct bem_solver_s {
 
 namespace bem {
 
-// Frequency data into the solver's block (internal element order).
-bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f, cudaStream_t st);
+// Frequency data into the solver's block (internal element order); rhs > 0
+// takes only the boundary values and sources of right-hand side rhs (the
+// matrix data comes from right-hand side 0).
+bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f, cudaStream_t st, int rhs = 0);
 // Map a finished GMRES state to a status (and message).
 bem_status map_result(const KState &q);
 // Assembly + right-hand side of every solver in ss (frequencies uploaded).
@@ -200,6 +211,6 @@ bem_status project_group(bem_solver_t *ss, int cnt, const int32_t *npts, const d
                          double *const *pot_out, double *const *grad_out, cudaStream_t st, cudaEvent_t e0,
                          cudaEvent_t e1, bem_status *rcs);
 // Unknowns to host memory in the caller's element order.
-bem_status solution_to_host(bem_solver_t s, cudaStream_t st, double *x_host);
+bem_status solution_to_host(bem_solver_t s, cudaStream_t st, double *x_host, int rhs = 0);
 
 }  // namespace bem

@@ -1,0 +1,54 @@
+"""Several right-hand sides on one matrix (bem_solve_multi).
+
+Right-hand side r must give what bem_solve_frequency gives for its sources
+alone.  FP64: bit for bit (each right-hand side iterates as its own system
+with the same products).  Mixed: the right-hand sides share each read of A
+in one product (full-row accumulation instead of 1024-column partials), so
+the rounding differs; both solutions meet the 1e-9 residual on the same
+complex64 matrix and agree to 1e-7.
+"""
+import numpy as np
+import pytest
+
+from mesh2hrtf_gb300 import capi, meshes, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_MIXED, capi.PREC_FP64])
+def test_multi_rhs_equals_single(prec):
+    v, f = meshes.perturbed_ellipsoid(9, 77)   # 1620 triangles
+    m = capi.Mesh(v, f)
+    pts = meshes.random_sphere_points(80, 1.2, 4)
+    srcs = [meshes.surface_point_with_normal(v, f, 100 + r) for r in range(5)]
+    fh = 7000.0
+    freqs = [workloads.frequency(capi, len(f), fh, s) for s in srcs]
+    s = capi.Solver(m, precision=prec, tol=1e-9, n_rhs=8)
+    xs, pots, grads, infos = s.solve_multi(freqs, pts)
+    one = capi.Solver(m, precision=prec, tol=1e-9)
+    for r in range(len(srcs)):
+        x0, p0, g0 = one.solve_frequency(freqs[r], pts)
+        assert infos[r]["rel_residual"] <= 1e-9
+        if prec == capi.PREC_FP64:
+            assert infos[r]["iterations"] == one.info.iterations
+            assert np.array_equal(xs[r], x0)
+            assert np.array_equal(pots[r], p0)
+            assert np.array_equal(grads[r], g0)
+        else:
+            assert abs(infos[r]["iterations"] - one.info.iterations) <= 2
+            assert np.linalg.norm(xs[r] - x0) <= 1e-7 * np.linalg.norm(x0)
+            assert np.linalg.norm(pots[r] - p0) <= 1e-7 * np.linalg.norm(p0)
+    # the right-hand sides really differ
+    assert np.linalg.norm(xs[0] - xs[1]) > 1e-3 * np.linalg.norm(xs[0])
+
+
+def test_multi_rhs_footprint_and_limit():
+    fp1 = capi.load().bem_footprint_multi(4000, capi.PREC_MIXED, 0, 1)
+    fp8 = capi.load().bem_footprint_multi(4000, capi.PREC_MIXED, 0, 8)
+    assert fp8 > fp1 and fp8 < 2 * fp1   # the matrix is shared
+    v, f = meshes.icosphere(320, 0.1)
+    m = capi.Mesh(v, f)
+    s = capi.Solver(m, precision=capi.PREC_MIXED, n_rhs=2)
+    fr = [workloads.frequency(capi, len(f), 1000.0, [1.0, 0, 0])] * 3
+    with pytest.raises(capi.BemError):
+        s.solve_multi(fr, np.zeros((0, 3)))
