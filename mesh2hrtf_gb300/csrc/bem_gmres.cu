@@ -72,8 +72,14 @@ __device__ __forceinline__ void acc_exact(float &s, float &e, float a, float b) 
     e += u + q;
 }
 
-__device__ __forceinline__ bool mv_active(const KState *st, bool exact) {
-    return exact ? (st->phase == kPhaseUpdate && st->cycles > 0) : st->phase == kPhaseArnoldi;
+// Does a system take part in a product of this kind?  0: Krylov product;
+// 1: residual with error-free products (the first cycle's, and every one for
+// complex128); 2: recursive residual update (complex64, later cycles).
+__device__ __forceinline__ bool mv_active(const KState *st, int kind, int prec) {
+    if (kind == 0) return st->phase == kPhaseArnoldi;
+    if (st->phase != kPhaseUpdate || st->cycles == 0) return false;
+    if (kind == 1) return prec == 0 || st->cycles == 1;
+    return prec == 1 && st->cycles >= 2;
 }
 
 // ------------------------------------------------------------ launch plans
@@ -100,8 +106,8 @@ __device__ __forceinline__ void plan_load(const KPlan &p, PlanSmem &s) {
     __syncthreads();
 }
 
-// Rebuild plan `which` (0: Krylov product, 1: refinement residual) from the
-// current phases; one block of kMaxSys threads, thread t = slot t.
+// Rebuild plan `which` (a product kind, see mv_active) from the current
+// phases; one block of kMaxSys threads, thread t = slot t.
 __device__ void plan_build(KTable *tb, int which) {
     __shared__ int cnt[kMaxSys], act[kMaxSys];
     __shared__ unsigned gm[kMaxSys];
@@ -109,7 +115,7 @@ __device__ void plan_build(KTable *tb, int which) {
     int c = 0;
     if (t < tb->B) {
         const KSys &S = tb->sys[t];
-        if (!S.shared && mv_active(S.st, which == 1)) c = mv_items_of(S.n, tb->prec);
+        if (!S.shared && mv_active(S.st, which, tb->prec)) c = mv_items_of(S.n, tb->prec);
     }
     cnt[t] = c;
     act[t] = c > 0;
@@ -118,7 +124,7 @@ __device__ void plan_build(KTable *tb, int which) {
     if (t < tb->n_groups) {
         const KGroup g = tb->grp[t];
         for (int q = 0; q < g.count; ++q)
-            if (mv_active(tb->sys[g.first + q].st, which == 1)) mask |= 1u << q;
+            if (mv_active(tb->sys[g.first + q].st, which, tb->prec)) mask |= 1u << q;
     }
     gm[t] = mask;
     __syncthreads();
@@ -142,7 +148,7 @@ __device__ void plan_build(KTable *tb, int which) {
                 gp.sys[n] = j;
                 gp.off[n] = off;
                 tb->gmask[which][n] = gm[j];
-                off += ceil_div(tb->sys[tb->grp[j].first].n, kGrpRows);
+                off += ceil_div(tb->sys[tb->grp[j].first].n, which == 1 ? kGrpRowsExact : kGrpRowsInner);
                 ++n;
             }
         gp.off[n] = off;
@@ -158,11 +164,11 @@ __device__ void plan_build(KTable *tb, int which) {
 // is bound by the FP64 pipe (4 DFMA per entry), not by HBM.  The tile writes
 // one partial per row; the consumer sums the chunks in order.
 template <bool EXACT>
-__global__ void __launch_bounds__(256, 4) k_mv64(KTable *tb) {
+__global__ void __launch_bounds__(256, 4) k_mv64(KTable *tb, int kind) {
     __shared__ __align__(16) double2 xd[kMvChunk];
     __shared__ int item_s;
     __shared__ PlanSmem pl;
-    plan_load(tb->plan[EXACT ? 1 : 0], pl);
+    plan_load(tb->plan[kind], pl);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int total = pl.off[pl.n];
     while (total > 0) {
@@ -286,7 +292,7 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
 }
 
 template <bool EXACT>
-__global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *tb) {
+__global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *tb, int kind) {
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char *ring = smem;                                       // kTmaStages x 64 KB
     unsigned char *xbuf = smem + kTmaStages * kStageBytes;           // 2 x chunk of x
@@ -308,7 +314,7 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __shared__ PlanSmem pl;
-    plan_load(tb->plan[EXACT ? 1 : 0], pl);   // includes a block barrier
+    plan_load(tb->plan[kind], pl);   // includes a block barrier
     int *err = &tb->err;
     if (warp == kTmaConsumers) {
         // ---------------- producer (one lane)
@@ -455,62 +461,88 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
 
 // ------------------------------------------------------------ shared-matrix product
 // Right-hand sides of one solver share A (complex64).  One launch streams
-// every tile of A once: an item is a strip of kGrpRows rows of one group over
-// all columns; a stage holds kGrpRows x kGrpCols of A (32 KB, one bulk copy
-// per row segment) and the x chunks of the group's members that take part
-// (2 KB each for the Krylov product, 4 KB of hi/lo pairs for the residual).
-// Consumer warp w owns rows 2w, 2w + 1 of the strip and keeps, in registers,
-// one accumulator per (row, member) across all column chunks; at the strip's
-// last chunk it writes the members' full-row products (nchunk = 1).
-constexpr int kGrpStages = 3;
-constexpr int kGrpAStage = kGrpRows * kGrpCols * 8;
-static_assert(kGrpRows == 2 * kTmaConsumers, "two rows per consumer warp");
-__host__ __device__ constexpr int grp_x_bytes(bool exact) { return exact ? kGrpCols * 16 : kGrpCols * 8; }
-__host__ __device__ constexpr int grp_stage_bytes(bool exact) { return kGrpAStage + kMaxGroup * grp_x_bytes(exact); }
-__host__ __device__ constexpr int grp_smem_bytes(bool exact) { return kGrpStages * grp_stage_bytes(exact) + 512; }
+// every tile of A once: an item is a strip of rows of one group over all
+// columns; a stage holds the strip's rows x kGrpCols columns of A (one bulk
+// copy per 2 KB row segment) and the x chunks of the group's members that
+// take part (2 KB each for the Krylov product, 4 KB of hi/lo pairs for the
+// residual).
+// Consumer warps own 4 rows x 4 members each and keep, in registers, one
+// accumulator per (row, member) across all column chunks; at the strip's
+// last chunk they write the members' full-row products (nchunk = 1).
+// Krylov product: 16 consumer warps, 32-row strips, 2 stages of 80 KB.
+// Refinement residual (twice the registers): 8 warps, 16 rows, 3 x 64 KB.
+template <bool EXACT> struct GrpCfg {
+    static constexpr int kWarps = EXACT ? 8 : 16;
+    static constexpr int kRows = 2 * kWarps;          // 4 rows per warp pair
+    static constexpr int kStages = EXACT ? 3 : 2;
+    static constexpr int kXBytes = EXACT ? kGrpCols * 16 : kGrpCols * 8;
+    static constexpr int kABytes = kRows * kGrpCols * 8;
+    static constexpr int kStageBytes = kABytes + kMaxGroup * kXBytes;
+    static constexpr int kSmem = kStages * kStageBytes + 512;
+};
+static_assert(GrpCfg<false>::kSmem <= 227 * 1024 && GrpCfg<true>::kSmem <= 227 * 1024, "shared memory");
+static_assert(GrpCfg<false>::kRows == kGrpRowsInner && GrpCfg<true>::kRows == kGrpRowsExact, "plan strip heights");
+__host__ __device__ constexpr int grp_smem_bytes(bool exact) {
+    return exact ? GrpCfg<true>::kSmem : GrpCfg<false>::kSmem;
+}
 
 struct GrpMeta {
     int first, chunk, row0, nrows, len, last, mask, pad;
 };
 
 template <bool EXACT>
-__global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_grp(KTable *tb) {
+__global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(KTable *tb, int kind) {
     extern __shared__ __align__(128) unsigned char smem[];
-    constexpr int SB = grp_stage_bytes(EXACT), XB = grp_x_bytes(EXACT);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kGrpStages * SB);
-    GrpMeta *meta = reinterpret_cast<GrpMeta *>(bars + 2 * kGrpStages);
+    using Cfg = GrpCfg<EXACT>;
+    constexpr int SB = Cfg::kStageBytes, XB = Cfg::kXBytes, NW = Cfg::kWarps, ROWS = Cfg::kRows;
+    constexpr int NS = Cfg::kStages, ASTAGE = Cfg::kABytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NS * SB);
+    GrpMeta *meta = reinterpret_cast<GrpMeta *>(bars + 2 * NS);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kGrpStages);
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + NS);
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kGrpStages; ++s) {
+        for (int s = 0; s < NS; ++s) {
             mbar_init(full0 + 8 * s, 1);
-            mbar_init(empty0 + 8 * s, kTmaConsumers);
+            mbar_init(empty0 + 8 * s, NW);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __shared__ PlanSmem pl;
-    plan_load(tb->gplan[EXACT ? 1 : 0], pl);   // includes a block barrier
+    plan_load(tb->gplan[kind], pl);   // includes a block barrier
     int *err = &tb->err;
-    if (warp == kTmaConsumers) {
+    if (warp == NW) {
         // ---------------- producer (one lane)
         if (lane != 0) return;
         const int total = pl.off[pl.n];
         int stage = 0;
         uint32_t eph = 1;
-        int issued[kGrpStages] = {0, 0, 0};
-        uint32_t fph[kGrpStages] = {0, 0, 0};
+        int issued[NS];
+        uint32_t fph[NS];
+        for (int q = 0; q < NS; ++q) { issued[q] = 0; fph[q] = 0; }
         bool ok = true;
         while (ok && total > 0) {
             const int item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
             if (item >= total) break;
             const int j = plan_find(pl.off, pl.n, item);
             const KGroup g = tb->grp[pl.sys[j]];
-            const unsigned mask = tb->gmask[EXACT ? 1 : 0][j];
+            const unsigned mask = tb->gmask[kind][j];
             const KSys &S0 = tb->sys[g.first];
             const int n = S0.n;
-            const int row0 = (item - pl.off[j]) * kGrpRows, nrows = min(kGrpRows, n - row0);
+            const int row0 = (item - pl.off[j]) * ROWS, nrows = min(ROWS, n - row0);
             const int nck = (n + kGrpCols - 1) / kGrpCols;
             const float2 *A = (const float2 *)S0.A;
+            const size_t lda = (size_t)S0.lda;
+            // the members' x arrays, read once per strip
+            const void *xsrc[kMaxGroup];
+            int nmem = 0;
+#pragma unroll
+            for (int q = 0; q < kMaxGroup; ++q) {
+                xsrc[q] = nullptr;
+                if (q < g.count && ((mask >> q) & 1)) {
+                    xsrc[q] = EXACT ? (const void *)tb->sys[g.first + q].xf : (const void *)tb->sys[g.first + q].xh;
+                    ++nmem;
+                }
+            }
             for (int ck = 0; ck < nck && ok; ++ck) {
                 if (!mbar_wait(empty0 + 8 * stage, eph, err)) { ok = false; break; }
                 const int c0 = ck * kGrpCols, len = min(kGrpCols, n - c0), lenp = (len + 1) & ~1;
@@ -518,30 +550,29 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_grp(KTable *
                 mt.first = g.first; mt.chunk = ck; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
                 mt.last = ck == nck - 1; mt.mask = (int)mask; mt.pad = 0;
                 meta[stage] = mt;
-                int nmem = 0;
-                for (int q = 0; q < g.count; ++q) nmem += (mask >> q) & 1;
                 const uint32_t xbytes = EXACT ? (uint32_t)XB : (uint32_t)(lenp * 8);
-                mbar_expect_tx(full0 + 8 * stage, (uint32_t)(nrows * lenp * 8) + nmem * xbytes);
+                const uint32_t fb = full0 + 8 * stage;
+                mbar_expect_tx(fb, (uint32_t)(nrows * lenp * 8) + nmem * xbytes);
                 const uint32_t dst = smem_u32(smem + stage * SB);
-                for (int r = 0; r < nrows; ++r)
-                    bulk_g2s(dst + r * kGrpCols * 8, A + (size_t)(row0 + r) * S0.lda + c0, lenp * 8, full0 + 8 * stage);
-                for (int q = 0; q < g.count; ++q) {
-                    if (!((mask >> q) & 1)) continue;
-                    const KSys &S = tb->sys[g.first + q];
-                    const uint32_t xd = dst + kGrpAStage + q * XB;
+                const float2 *Arow = A + (size_t)row0 * lda + c0;
+                for (int r = 0; r < nrows; ++r) bulk_g2s(dst + r * kGrpCols * 8, Arow + r * lda, lenp * 8, fb);
+#pragma unroll
+                for (int q = 0; q < kMaxGroup; ++q) {
+                    if (!xsrc[q]) continue;
+                    const uint32_t xd = dst + ASTAGE + q * XB;
                     if (EXACT) {
                         // chunk-permuted (hi, lo) pairs: the stage's even entries, then its odd ones
-                        const float4 *base = S.xf + (size_t)(c0 & ~(kMvChunk - 1));
+                        const float4 *base = (const float4 *)xsrc[q] + (size_t)(c0 & ~(kMvChunk - 1));
                         const int o = (c0 & (kMvChunk - 1)) >> 1;
-                        bulk_g2s(xd, base + o, kGrpCols * 8, full0 + 8 * stage);
-                        bulk_g2s(xd + kGrpCols * 8, base + kMvChunk / 2 + o, kGrpCols * 8, full0 + 8 * stage);
+                        bulk_g2s(xd, base + o, kGrpCols * 8, fb);
+                        bulk_g2s(xd + kGrpCols * 8, base + kMvChunk / 2 + o, kGrpCols * 8, fb);
                     } else {
-                        bulk_g2s(xd, S.xh + c0, lenp * 8, full0 + 8 * stage);
+                        bulk_g2s(xd, (const float2 *)xsrc[q] + c0, lenp * 8, fb);
                     }
                 }
                 issued[stage] = 1;
                 fph[stage] ^= 1;
-                if (++stage == kGrpStages) { stage = 0; eph ^= 1; }
+                if (++stage == NS) { stage = 0; eph ^= 1; }
             }
         }
         if (ok) {
@@ -553,7 +584,7 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_grp(KTable *
             }
         }
         if (!ok)
-            for (int s = 0; s < kGrpStages; ++s)
+            for (int s = 0; s < NS; ++s)
                 if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
         __threadfence();
         if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
@@ -563,8 +594,12 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_grp(KTable *
         }
         return;
     }
-    // ---------------- consumers: warp w takes rows 2w, 2w + 1 of each strip
-    float ar[2][kMaxGroup], ai[2][kMaxGroup], er[2][kMaxGroup], ei[2][kMaxGroup];
+    // ---------------- consumers: warp w takes rows 4(w/2) .. 4(w/2)+3 of each
+    // strip and members 4(w%2) .. 4(w%2)+3: every A value loaded from shared
+    // memory serves 4 members, every x value 4 rows
+    constexpr int RW = 4, MW = kMaxGroup / 2;
+    float ar[RW][MW], ai[RW][MW], er[RW][MW], ei[RW][MW];
+    const int rbase = RW * (warp >> 1), mbase = MW * (warp & 1);
     int stage = 0;
     uint32_t fph = 0;
     while (true) {
@@ -573,97 +608,100 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_grp(KTable *
         if (mt.first < 0) return;
         if (mt.chunk == 0) {
 #pragma unroll
-            for (int q = 0; q < kMaxGroup; ++q)
+            for (int r = 0; r < RW; ++r)
 #pragma unroll
-                for (int r = 0; r < 2; ++r) ar[r][q] = ai[r][q] = er[r][q] = ei[r][q] = 0.f;
+                for (int q = 0; q < MW; ++q) ar[r][q] = ai[r][q] = er[r][q] = ei[r][q] = 0.f;
         }
         const unsigned char *sb = smem + stage * SB;
-        const int r0 = 2 * warp;
-        const bool v0 = r0 < mt.nrows, v1 = r0 + 1 < mt.nrows;
-        const float4 *A0 = reinterpret_cast<const float4 *>(sb) + r0 * (kGrpCols / 2);
-        const float4 *A1 = A0 + kGrpCols / 2;
+        const unsigned mymask = ((unsigned)mt.mask >> mbase) & ((1u << MW) - 1u);
         const int len = mt.len, len2 = len >> 1;
-        for (int c = lane; c < len2; c += 32) {
-            const float4 a0 = v0 ? A0[c] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 a1 = v1 ? A1[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 *Ab = reinterpret_cast<const float4 *>(sb) + rbase * (kGrpCols / 2);
+        if (mymask) {
+#pragma unroll 2
+            for (int c = lane; c < len2; c += 32) {
+                float4 a[RW];
 #pragma unroll
-            for (int q = 0; q < kMaxGroup; ++q) {
-                if (!((mt.mask >> q) & 1)) continue;
-                const unsigned char *xq = sb + kGrpAStage + q * XB;
-                if (!EXACT) {
-                    const float4 xv = reinterpret_cast<const float4 *>(xq)[c];   // hi of entries 2c, 2c + 1
-                    ar[0][q] = fmaf(a0.x, xv.x, ar[0][q]); ar[0][q] = fmaf(-a0.y, xv.y, ar[0][q]);
-                    ai[0][q] = fmaf(a0.x, xv.y, ai[0][q]); ai[0][q] = fmaf(a0.y, xv.x, ai[0][q]);
-                    ar[0][q] = fmaf(a0.z, xv.z, ar[0][q]); ar[0][q] = fmaf(-a0.w, xv.w, ar[0][q]);
-                    ai[0][q] = fmaf(a0.z, xv.w, ai[0][q]); ai[0][q] = fmaf(a0.w, xv.z, ai[0][q]);
-                    ar[1][q] = fmaf(a1.x, xv.x, ar[1][q]); ar[1][q] = fmaf(-a1.y, xv.y, ar[1][q]);
-                    ai[1][q] = fmaf(a1.x, xv.y, ai[1][q]); ai[1][q] = fmaf(a1.y, xv.x, ai[1][q]);
-                    ar[1][q] = fmaf(a1.z, xv.z, ar[1][q]); ar[1][q] = fmaf(-a1.w, xv.w, ar[1][q]);
-                    ai[1][q] = fmaf(a1.z, xv.w, ai[1][q]); ai[1][q] = fmaf(a1.w, xv.z, ai[1][q]);
-                } else {
-                    const float4 x0 = reinterpret_cast<const float4 *>(xq)[c];
-                    const float4 x1 = reinterpret_cast<const float4 *>(xq + kGrpCols * 8)[c];
+                for (int r = 0; r < RW; ++r)
+                    a[r] = rbase + r < mt.nrows ? Ab[r * (kGrpCols / 2) + c] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-                    for (int r = 0; r < 2; ++r) {
-                        const float4 a = r == 0 ? a0 : a1;
-                        acc_exact(ar[r][q], er[r][q], a.x, x0.x); acc_exact(ar[r][q], er[r][q], -a.y, x0.y);
-                        acc_exact(ai[r][q], ei[r][q], a.x, x0.y); acc_exact(ai[r][q], ei[r][q], a.y, x0.x);
-                        er[r][q] = fmaf(a.x, x0.z, er[r][q]); er[r][q] = fmaf(-a.y, x0.w, er[r][q]);
-                        ei[r][q] = fmaf(a.x, x0.w, ei[r][q]); ei[r][q] = fmaf(a.y, x0.z, ei[r][q]);
-                        acc_exact(ar[r][q], er[r][q], a.z, x1.x); acc_exact(ar[r][q], er[r][q], -a.w, x1.y);
-                        acc_exact(ai[r][q], ei[r][q], a.z, x1.y); acc_exact(ai[r][q], ei[r][q], a.w, x1.x);
-                        er[r][q] = fmaf(a.z, x1.z, er[r][q]); er[r][q] = fmaf(-a.w, x1.w, er[r][q]);
-                        ei[r][q] = fmaf(a.z, x1.w, ei[r][q]); ei[r][q] = fmaf(a.w, x1.z, ei[r][q]);
+                for (int q = 0; q < MW; ++q) {
+                    if (!((mymask >> q) & 1)) continue;
+                    const unsigned char *xq = sb + ASTAGE + (mbase + q) * XB;
+                    if (!EXACT) {
+                        const float4 xv = reinterpret_cast<const float4 *>(xq)[c];   // hi of entries 2c, 2c + 1
+#pragma unroll
+                        for (int r = 0; r < RW; ++r) {
+                            ar[r][q] = fmaf(a[r].x, xv.x, ar[r][q]); ar[r][q] = fmaf(-a[r].y, xv.y, ar[r][q]);
+                            ai[r][q] = fmaf(a[r].x, xv.y, ai[r][q]); ai[r][q] = fmaf(a[r].y, xv.x, ai[r][q]);
+                            ar[r][q] = fmaf(a[r].z, xv.z, ar[r][q]); ar[r][q] = fmaf(-a[r].w, xv.w, ar[r][q]);
+                            ai[r][q] = fmaf(a[r].z, xv.w, ai[r][q]); ai[r][q] = fmaf(a[r].w, xv.z, ai[r][q]);
+                        }
+                    } else {
+                        const float4 x0 = reinterpret_cast<const float4 *>(xq)[c];
+                        const float4 x1 = reinterpret_cast<const float4 *>(xq + kGrpCols * 8)[c];
+#pragma unroll
+                        for (int r = 0; r < RW; ++r) {
+                            acc_exact(ar[r][q], er[r][q], a[r].x, x0.x); acc_exact(ar[r][q], er[r][q], -a[r].y, x0.y);
+                            acc_exact(ai[r][q], ei[r][q], a[r].x, x0.y); acc_exact(ai[r][q], ei[r][q], a[r].y, x0.x);
+                            er[r][q] = fmaf(a[r].x, x0.z, er[r][q]); er[r][q] = fmaf(-a[r].y, x0.w, er[r][q]);
+                            ei[r][q] = fmaf(a[r].x, x0.w, ei[r][q]); ei[r][q] = fmaf(a[r].y, x0.z, ei[r][q]);
+                            acc_exact(ar[r][q], er[r][q], a[r].z, x1.x); acc_exact(ar[r][q], er[r][q], -a[r].w, x1.y);
+                            acc_exact(ai[r][q], ei[r][q], a[r].z, x1.y); acc_exact(ai[r][q], ei[r][q], a[r].w, x1.x);
+                            er[r][q] = fmaf(a[r].z, x1.z, er[r][q]); er[r][q] = fmaf(-a[r].w, x1.w, er[r][q]);
+                            ei[r][q] = fmaf(a[r].z, x1.w, ei[r][q]); ei[r][q] = fmaf(a[r].w, x1.z, ei[r][q]);
+                        }
                     }
                 }
             }
-        }
-        if ((len & 1) && lane == 0) {   // odd tail: entry len - 1
-            const float2 b0 = v0 ? reinterpret_cast<const float2 *>(A0)[len - 1] : make_float2(0.f, 0.f);
-            const float2 b1 = v1 ? reinterpret_cast<const float2 *>(A1)[len - 1] : make_float2(0.f, 0.f);
+            if ((len & 1) && lane == 0) {   // odd tail: entry len - 1
+                float2 b[RW];
 #pragma unroll
-            for (int q = 0; q < kMaxGroup; ++q) {
-                if (!((mt.mask >> q) & 1)) continue;
-                const unsigned char *xq = sb + kGrpAStage + q * XB;
-                float xr, xi, lr = 0.f, li = 0.f;
-                if (!EXACT) {
-                    const float2 xv = reinterpret_cast<const float2 *>(xq)[len - 1];
-                    xr = xv.x; xi = xv.y;
-                } else {
-                    const float4 x0 = reinterpret_cast<const float4 *>(xq)[(len - 1) >> 1];
-                    xr = x0.x; xi = x0.y; lr = x0.z; li = x0.w;
-                }
+                for (int r = 0; r < RW; ++r)
+                    b[r] = rbase + r < mt.nrows ? reinterpret_cast<const float2 *>(Ab + r * (kGrpCols / 2))[len - 1]
+                                                : make_float2(0.f, 0.f);
 #pragma unroll
-                for (int r = 0; r < 2; ++r) {
-                    const float2 b = r == 0 ? b0 : b1;
+                for (int q = 0; q < MW; ++q) {
+                    if (!((mymask >> q) & 1)) continue;
+                    const unsigned char *xq = sb + ASTAGE + (mbase + q) * XB;
+                    float xr, xi, lr = 0.f, li = 0.f;
                     if (!EXACT) {
-                        ar[r][q] = fmaf(b.x, xr, ar[r][q]); ar[r][q] = fmaf(-b.y, xi, ar[r][q]);
-                        ai[r][q] = fmaf(b.x, xi, ai[r][q]); ai[r][q] = fmaf(b.y, xr, ai[r][q]);
+                        const float2 xv = reinterpret_cast<const float2 *>(xq)[len - 1];
+                        xr = xv.x; xi = xv.y;
                     } else {
-                        acc_exact(ar[r][q], er[r][q], b.x, xr); acc_exact(ar[r][q], er[r][q], -b.y, xi);
-                        acc_exact(ai[r][q], ei[r][q], b.x, xi); acc_exact(ai[r][q], ei[r][q], b.y, xr);
-                        er[r][q] = fmaf(b.x, lr, er[r][q]); er[r][q] = fmaf(-b.y, li, er[r][q]);
-                        ei[r][q] = fmaf(b.x, li, ei[r][q]); ei[r][q] = fmaf(b.y, lr, ei[r][q]);
+                        const float4 x0 = reinterpret_cast<const float4 *>(xq)[(len - 1) >> 1];
+                        xr = x0.x; xi = x0.y; lr = x0.z; li = x0.w;
+                    }
+#pragma unroll
+                    for (int r = 0; r < RW; ++r) {
+                        if (!EXACT) {
+                            ar[r][q] = fmaf(b[r].x, xr, ar[r][q]); ar[r][q] = fmaf(-b[r].y, xi, ar[r][q]);
+                            ai[r][q] = fmaf(b[r].x, xi, ai[r][q]); ai[r][q] = fmaf(b[r].y, xr, ai[r][q]);
+                        } else {
+                            acc_exact(ar[r][q], er[r][q], b[r].x, xr); acc_exact(ar[r][q], er[r][q], -b[r].y, xi);
+                            acc_exact(ai[r][q], ei[r][q], b[r].x, xi); acc_exact(ai[r][q], ei[r][q], b[r].y, xr);
+                            er[r][q] = fmaf(b[r].x, lr, er[r][q]); er[r][q] = fmaf(-b[r].y, li, er[r][q]);
+                            ei[r][q] = fmaf(b[r].x, li, ei[r][q]); ei[r][q] = fmaf(b[r].y, lr, ei[r][q]);
+                        }
                     }
                 }
             }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(empty0 + 8 * stage);
-        if (mt.last) {
+        if (mt.last && mymask) {
 #pragma unroll
-            for (int q = 0; q < kMaxGroup; ++q) {
-                if (!((mt.mask >> q) & 1)) continue;
-                const KSys &S = tb->sys[mt.first + q];
+            for (int q = 0; q < MW; ++q) {
+                if (!((mymask >> q) & 1)) continue;
+                const KSys &S = tb->sys[mt.first + mbase + q];
 #pragma unroll
-                for (int r = 0; r < 2; ++r) {
+                for (int r = 0; r < RW; ++r) {
                     const double tr = warp_sum_d((double)ar[r][q] + (double)er[r][q]);
                     const double ti = warp_sum_d((double)ai[r][q] + (double)ei[r][q]);
-                    if (lane == 0 && r0 + r < mt.nrows) S.mvp[mt.row0 + r0 + r] = make_double2(tr, ti);
+                    if (lane == 0 && rbase + r < mt.nrows) S.mvp[mt.row0 + rbase + r] = make_double2(tr, ti);
                 }
             }
         }
-        if (++stage == kGrpStages) { stage = 0; fph ^= 1; }
+        if (++stage == NS) { stage = 0; fph ^= 1; }
     }
 }
 
@@ -922,6 +960,7 @@ __global__ void __launch_bounds__(kMaxSys) k_givens(KTable *tb) {
     __syncthreads();
     plan_build(tb, 0);
     plan_build(tb, 1);
+    plan_build(tb, 2);
 }
 
 // ------------------------------------------------------------ end of cycle
@@ -988,21 +1027,25 @@ __global__ void __launch_bounds__(kThreads) k_xupdate(const KTable *tb) {
             xv.x += t.x;
             xv.y += t.y;
             S.x[row] = xv;
-            if (!C128) {
-                // (hi, lo) float split for the refinement residual, stored so
-                // that chunk entries 2c and 2c + 1 land in the chunk's first and
+            if (!C128 && st->cycles == 1) {
+                // first residual: (hi, lo) float split of x, stored so that
+                // chunk entries 2c and 2c + 1 land in the chunk's first and
                 // second half (conflict-free reads in the product)
                 const float hr = (float)xv.x, hi = (float)xv.y;
                 const int c = row & (kMvChunk - 1);
                 S.xf[(size_t)(row - c) + (c & 1) * (kMvChunk / 2) + (c >> 1)] =
                     make_float4(hr, hi, (float)(xv.x - (double)hr), (float)(xv.y - (double)hi));
+            } else if (!C128) {
+                // later residuals: r -= A d, with the float copy of d
+                S.xh[row] = make_float2((float)t.x, (float)t.y);
             }
         }
         __syncthreads();
     }
 }
 
-// r = b - A x (or r = b before the first cycle); |r|^2 partials
+// r = b - A x, or r - A d (complex64 after the first cycle), or r = b before
+// the first cycle; |r|^2 partials
 __global__ void __launch_bounds__(kThreads) k_resid(const KTable *tb) {
     __shared__ double red[8][16];
     for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
@@ -1014,7 +1057,8 @@ __global__ void __launch_bounds__(kThreads) k_resid(const KTable *tb) {
         const bool ok = row < n;
         double2 r = make_double2(0.0, 0.0);
         if (ok) {
-            r = S.b[row];
+            // complex64 after the first cycle: recursive update r -= A d
+            r = (tb->prec == 1 && st->cycles >= 2) ? S.r[row] : S.b[row];
             if (st->cycles > 0) {
                 double ax = 0.0, ay = 0.0;
                 for (int c = 0; c < S.nchunk; ++c) {
@@ -1092,6 +1136,7 @@ __global__ void __launch_bounds__(kMaxSys) k_decide(KTable *tb) {
 __global__ void __launch_bounds__(kMaxSys) k_plans(KTable *tb) {
     plan_build(tb, 0);
     plan_build(tb, 1);
+    plan_build(tb, 2);
 }
 
 int g_mv_grid[2] = {0, 0};
@@ -1145,12 +1190,13 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
     const int gmv = g_mv_grid[c128 ? 0 : 1], gv = g_vec_grid;
     int nl = 0;
     cudaError_t e = cudaSuccess;
+    constexpr int kTmaThreads = 32 * (kTmaConsumers + 1);
     for (int q = 0; q < kSteps; ++q) {
         if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q], st, cudaEventRecordExternal);
-        if (c128) k_mv64<false><<<gmv, 256, 0, st>>>(tb);
+        if (c128) k_mv64<false><<<gmv, 256, 0, st>>>(tb, 0);
         else {
-            k_mv_tma<false><<<gmv, 32 * (kTmaConsumers + 1), tma_smem_bytes(false), st>>>(tb);
-            k_mv_grp<false><<<gmv, 32 * (kTmaConsumers + 1), grp_smem_bytes(false), st>>>(tb);
+            k_mv_tma<false><<<gmv, kTmaThreads, tma_smem_bytes(false), st>>>(tb, 0);
+            k_mv_grp<false><<<gmv, 32 * (GrpCfg<false>::kWarps + 1), grp_smem_bytes(false), st>>>(tb, 0);
             ++nl;
         }
         if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q + 1], st, cudaEventRecordExternal);
@@ -1166,11 +1212,14 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
     if (c128) k_xupdate<true><<<gv, kThreads, 0, st>>>(d_tab);
     else k_xupdate<false><<<gv, kThreads, 0, st>>>(d_tab);
     if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * kSteps], st, cudaEventRecordExternal);
-    if (c128) k_mv64<true><<<gmv, 256, 0, st>>>(tb);
+    if (c128) k_mv64<true><<<gmv, 256, 0, st>>>(tb, 1);
     else {
-        k_mv_tma<true><<<gmv, 32 * (kTmaConsumers + 1), tma_smem_bytes(true), st>>>(tb);
-        k_mv_grp<true><<<gmv, 32 * (kTmaConsumers + 1), grp_smem_bytes(true), st>>>(tb);
-        ++nl;
+        // first-cycle residuals with error-free products, then the recursive updates
+        k_mv_tma<true><<<gmv, kTmaThreads, tma_smem_bytes(true), st>>>(tb, 1);
+        k_mv_grp<true><<<gmv, 32 * (GrpCfg<true>::kWarps + 1), grp_smem_bytes(true), st>>>(tb, 1);
+        k_mv_tma<false><<<gmv, kTmaThreads, tma_smem_bytes(false), st>>>(tb, 2);
+        k_mv_grp<false><<<gmv, 32 * (GrpCfg<false>::kWarps + 1), grp_smem_bytes(false), st>>>(tb, 2);
+        nl += 3;
     }
     if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * kSteps + 1], st, cudaEventRecordExternal);
     k_resid<<<gv, kThreads, 0, st>>>(d_tab);

@@ -143,8 +143,12 @@ cudaError_t launch_block_inverse(const PcBatch &t, int prec, cudaStream_t st);
 // Restarted GMRES of one system as a state machine on the device.  An
 // iteration body (one captured graph) runs kSteps Arnoldi steps for every
 // system in phase ARNOLDI, then the cycle end for every system in phase
-// UPDATE: y = H^{-1} g, x += M^{-1} V y, the refinement residual r = b - A x
-// (compensated product), the convergence decision and the restart.
+// UPDATE: y = H^{-1} g, x += d = M^{-1} V y, the refinement residual, the
+// convergence decision and the restart.  The residual is r = b - A x with
+// error-free products after the first cycle (and always for complex128);
+// complex64 systems then update it as r -= A d with the plain product: the
+// later corrections d are about 1e-5 |x|, so the product's rounding stays
+// near 1e-10 |b|.
 enum KPhase : int { kPhaseIdle = 0, kPhaseArnoldi = 1, kPhaseUpdate = 2, kPhaseFinished = 3 };
 enum KResult : int { kResRunning = 0, kResConverged = 1, kResMaxIter = 2, kResStagnated = 3, kResBreakdown = 4 };
 
@@ -197,17 +201,21 @@ struct KTable {
     int vb_total;           // vector blocks of all systems
     int err;                // set when a bounded device wait gave up
     unsigned mv_ctr[2];     // work queue of the persistent matvec
-    KPlan plan[2];          // [0] Krylov product, [1] refinement residual
+    KPlan plan[3];          // [0] Krylov product, [1] refinement residual with
+                            // error-free products, [2] recursive residual update
     int n_groups;           // shared-matrix groups
     KGroup grp[kMaxSys];
-    KPlan gplan[2];         // plans of the shared-matrix products (entries = groups)
-    unsigned gmask[2][kMaxSys];   // per plan entry: members taking part
+    KPlan gplan[3];         // plans of the shared-matrix products (entries = groups)
+    unsigned gmask[3][kMaxSys];   // per plan entry: members taking part
     const int2 *vb_items;   // (system, block)
     KSys sys[kMaxSys];
 };
 
-// Shared-matrix product: items are strips of kGrpRows rows over all columns.
-constexpr int kGrpRows = 16;
+// Shared-matrix product: items are strips of rows over all columns (32 rows
+// for the Krylov product, 16 for the refinement residual), stages of 256
+// columns.
+constexpr int kGrpRowsInner = 32;
+constexpr int kGrpRowsExact = 16;
 constexpr int kGrpCols = 256;
 
 // Arnoldi steps per iteration body.
