@@ -47,35 +47,19 @@ template <typename T> __device__ __forceinline__ cplx<T> warp_sum(cplx<T> v) {
     return {warp_sum(v.re), warp_sum(v.im)};
 }
 
-// sin and cos of a float phase k*r: Cody & Waite argument reduction by pi/2
-// (FMA variant, pi/2 split into three floats), then the Taylor polynomials of
-// sin (through r^9) and cos (through r^10) on |r| <= pi/4, whose truncation
-// error (< 3e-9) is below float rounding.  Phases in this library stay below
-// ~10^3, where the reduction is accurate to a few float ulps.
-//
-// The quadrant is rounded with the 1.5*2^23 shifter instead of rintf/F2I: on
-// GB300 conversion instructions share the narrow FP64 pipe, while the shifter
-// needs only FP32 adds and integer bit operations.
+// sin and cos of a float phase k*r: Cody & Waite reduction by 2 pi (2 pi
+// split into two floats, x / 2 pi rounded with the 1.5 * 2^23 shifter, which
+// needs no float-to-integer conversion: on GB300 those issue on the narrow
+// FP64 pipe), then the hardware approximations __sinf / __cosf, accurate to
+// about 2^-21 absolute on [-pi, pi].  The mixed-precision path's error budget
+// is 1e-4 against FP64; this keeps it near 3e-6.
 __device__ __forceinline__ void phase_sincos(float x, float *s, float *c) {
-    const float sh = fmaf(x, 0.636619772f, 12582912.0f);   // 1.5 * 2^23
-    const int qi = __float_as_int(sh);                      // low bits: round(x 2/pi)
+    const float sh = fmaf(x, 0.159154943f, 12582912.0f);   // 1 / (2 pi), 1.5 * 2^23
     const float q = sh - 12582912.0f;
-    float r = fmaf(q, -1.57079637050628662f, x);
-    r = fmaf(q, 4.37113882867379e-08f, r);
-    r = fmaf(q, 1.71512451000588e-15f, r);
-    const float r2 = r * r;
-    float ps = fmaf(r2, 2.755731922e-6f, -1.984126984e-4f);
-    ps = fmaf(ps, r2, 8.333333333e-3f);
-    ps = fmaf(ps, r2, -0.1666666667f);
-    const float sn = fmaf(ps * r2, r, r);
-    float pc = fmaf(r2, -2.755731922e-7f, 2.480158730e-5f);
-    pc = fmaf(pc, r2, -1.388888889e-3f);
-    pc = fmaf(pc, r2, 4.166666667e-2f);
-    pc = fmaf(pc, r2, -0.5f);
-    const float cs = fmaf(pc, r2, 1.0f);
-    float so = (qi & 1) ? cs : sn, co = (qi & 1) ? sn : cs;
-    *s = (qi & 2) ? -so : so;
-    *c = ((qi + 1) & 2) ? -co : co;
+    float r = fmaf(q, -6.28318548202514648f, x);
+    r = fmaf(q, 1.74845553146951e-07f, r);
+    *s = __sinf(r);
+    *c = __cosf(r);
 }
 
 __device__ __forceinline__ void sincos_t(double x, double *s, double *c) { sincos(x, s, c); }
