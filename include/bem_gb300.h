@@ -195,7 +195,7 @@ bem_status bem_project(bem_solver_t solver, int32_t n_pts, const double *pts,
  *
  * Limits and rules:
  *  - at most BEM_STATIC_MAX_ELEMENTS boundary elements (larger solvers get
- *    BEM_ERR_INVALID); the scratch array (about 2.8 MB) is held on every
+ *    BEM_ERR_INVALID); the scratch array (about 4.1 MB) is held on every
  *    device that loads the library until the process exits;
  *  - the first call on a device looks up the array's device address; make
  *    that first call before any stream capture;

@@ -176,6 +176,8 @@ size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, Solve
         q.hsum = (double2 *)take((size_t)(m + 1) * 16);
         q.phi = (double *)take(N * 16);
         q.vel = (double *)take(4 * N * 16);
+        q.phi32 = (float *)take(N * 8);
+        q.vel32 = (float *)take(4 * N * 8);
         q.ivi = (int *)take(N * 4);
         q.cols = (int *)take(N * 4);
         q.bcv = (double *)take(8 * N * 8);

@@ -705,6 +705,256 @@ __global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(
     }
 }
 
+// ------------------------------------------------------------ shared-matrix product on tensor cores
+// The Krylov product of a shared-matrix group as a real GEMM on the tensor
+// cores (mma.sync m16n8k8, TF32 inputs, FP32 accumulation, three products
+// per step so that the result has FP32 accuracy: A_hi X_hi + A_hi X_lo +
+// A_lo X_hi with hi = A rounded to TF32, lo = A - hi).  The complex product
+// is real-ified on A's own memory layout: a complex64 row (re, im, re, im,
+// ...) is a real row A^ of twice the length, and with
+//   X^[2j][r] = re x_j(r), X^[2j+1][r] = -im x_j(r)      (output column r: Re y_r)
+//   X^[2j][8+r] = im x_j(r), X^[2j+1][8+r] = re x_j(r)   (output column 8+r: Im y_r)
+// Y^ = A^ X^ holds the real and imaginary parts of the 8 members' products.
+// The producer is the one of k_mv_grp (32-row strips, stages of 256 columns);
+// rows and member x chunks sit at padded strides in shared memory so that the
+// fragment loads are free of bank conflicts.  Consumer warp w takes row block
+// w & 1 (16 rows) and the slice w >> 1 of each stage's columns.  The MMA
+// accumulators hold one stage's partial; each stage's partial is added into
+// a float-float (two-sum) accumulator, so the strip's long sum keeps about
+// twice-FP32 accuracy; the slice sums of a row block are added in FP64 at
+// the end of the strip.
+constexpr int kTcRows = kGrpRowsInner;                 // 32
+constexpr int kTcRowStride = kGrpCols * 8 + 16;        // bytes, padded row
+constexpr int kTcXStride = kGrpCols * 8 + 16;          // bytes, padded member chunk
+constexpr int kTcABytes = kTcRows * kTcRowStride;
+constexpr int kTcStageBytes = kTcABytes + kMaxGroup * kTcXStride;
+constexpr int kTcStages = 2;
+constexpr int kTcWarps = 8;                             // consumer warps: 2 row blocks x 4 column slices
+constexpr int kTcSlice = kGrpCols / (kTcWarps / 2);      // complex columns of a warp's slice
+constexpr int kTcRedBytes = kTcWarps * 16 * 16 * 8;     // per warp a 16 x 16 FP64 tile
+constexpr int kTcSmem = kTcStages * kTcStageBytes + kTcRedBytes + 512;
+static_assert(kTcSmem <= 227 * 1024, "shared memory");
+static_assert(kTcRows == 32 && kTcSlice % 4 == 0 && kTcWarps * 32 >= 256, "row blocks x column slices");
+
+// round to TF32 (nearest, ties away from zero) and the remainder
+__device__ __forceinline__ void tf32_split(float v, uint32_t &hi, uint32_t &lo) {
+    const uint32_t b = __float_as_uint(v);
+    hi = (b + 0x1000u) & 0xffffe000u;
+    lo = __float_as_uint(v - __uint_as_float(hi));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+                 "{%8, %9}, {%0, %1, %2, %3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb, int kind) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    double *red = reinterpret_cast<double *>(smem + kTcStages * kTcStageBytes);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcStages * kTcStageBytes + kTcRedBytes);
+    // bars: full[2], empty[2], then the two barriers of the end-of-strip reduction
+    GrpMeta *meta = reinterpret_cast<GrpMeta *>(bars + 2 * kTcStages + 2);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kTcStages);
+    const uint32_t redw = smem_u32(bars + 2 * kTcStages), redr = redw + 8;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kTcStages; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, kTcWarps);
+        }
+        mbar_init(redw, kTcWarps);
+        mbar_init(redr, kTcWarps);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __shared__ PlanSmem pl;
+    plan_load(tb->gplan[kind], pl);   // includes a block barrier
+    int *err = &tb->err;
+    if (warp == kTcWarps) {
+        // ---------------- producer (one lane)
+        if (lane != 0) return;
+        const int total = pl.off[pl.n];
+        int stage = 0;
+        uint32_t eph = 1;
+        int issued[kTcStages] = {0, 0};
+        uint32_t fph[kTcStages] = {0, 0};
+        bool ok = true;
+        while (ok && total > 0) {
+            const int item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+            if (item >= total) break;
+            const int j = plan_find(pl.off, pl.n, item);
+            const KGroup g = tb->grp[pl.sys[j]];
+            const unsigned mask = tb->gmask[kind][j];
+            const KSys &S0 = tb->sys[g.first];
+            const int n = S0.n;
+            const int row0 = (item - pl.off[j]) * kTcRows, nrows = min(kTcRows, n - row0);
+            const int nck = (n + kGrpCols - 1) / kGrpCols;
+            const float2 *A = (const float2 *)S0.A;
+            const size_t lda = (size_t)S0.lda;
+            const float2 *xsrc[kMaxGroup];
+            int nmem = 0;
+#pragma unroll
+            for (int q = 0; q < kMaxGroup; ++q) {
+                xsrc[q] = nullptr;
+                if (q < g.count && ((mask >> q) & 1)) {
+                    xsrc[q] = tb->sys[g.first + q].xh;
+                    ++nmem;
+                }
+            }
+            for (int ck = 0; ck < nck && ok; ++ck) {
+                if (!mbar_wait(empty0 + 8 * stage, eph, err)) { ok = false; break; }
+                const int c0 = ck * kGrpCols, len = min(kGrpCols, n - c0), lenp = (len + 1) & ~1;
+                GrpMeta mt;
+                mt.first = g.first; mt.chunk = ck; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
+                mt.last = ck == nck - 1; mt.mask = (int)mask; mt.pad = 0;
+                meta[stage] = mt;
+                const uint32_t fb = full0 + 8 * stage;
+                mbar_expect_tx(fb, (uint32_t)((nrows + nmem) * lenp * 8));
+                const uint32_t dst = smem_u32(smem + stage * kTcStageBytes);
+                const float2 *Arow = A + (size_t)row0 * lda + c0;
+                for (int r = 0; r < nrows; ++r) bulk_g2s(dst + r * kTcRowStride, Arow + r * lda, lenp * 8, fb);
+#pragma unroll
+                for (int q = 0; q < kMaxGroup; ++q)
+                    if (xsrc[q]) bulk_g2s(dst + kTcABytes + q * kTcXStride, xsrc[q] + c0, lenp * 8, fb);
+                issued[stage] = 1;
+                fph[stage] ^= 1;
+                if (++stage == kTcStages) { stage = 0; eph ^= 1; }
+            }
+        }
+        if (ok) {
+            if (mbar_wait(empty0 + 8 * stage, eph, err)) {
+                meta[stage].first = -1;
+                mbar_arrive(full0 + 8 * stage);
+            } else {
+                ok = false;
+            }
+        }
+        if (!ok)
+            for (int s = 0; s < kTcStages; ++s)
+                if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
+        __threadfence();
+        if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
+            tb->mv_ctr[0] = 0u;
+            tb->mv_ctr[1] = 0u;
+            __threadfence();
+        }
+        return;
+    }
+    // ---------------- consumers
+    const int gid = lane >> 2, tig = lane & 3;
+    const int rb = warp & 1, kq = warp >> 1;   // kq: column slice
+    // three independent MMA accumulators per tile (hi*hi, hi*lo, lo*hi), so
+    // that consecutive MMAs do not wait on each other
+    float dre[3][4], dim[3][4];
+    float sh[8], sl[8];   // float-float strip sums of the Re (0-3) and Im (4-7) tiles
+    int stage = 0;
+    uint32_t fph = 0, rph = 0;
+    while (true) {
+        if (!mbar_wait(full0 + 8 * stage, fph, err)) return;
+        const GrpMeta mt = meta[stage];
+        if (mt.first < 0) return;
+        if (mt.chunk == 0) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) sh[i] = sl[i] = 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 3; ++u)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) dre[u][i] = dim[u][i] = 0.f;
+        const unsigned char *sb = smem + stage * kTcStageBytes;
+        const float *Ar0 = reinterpret_cast<const float *>(sb + (rb * 16 + gid) * kTcRowStride);
+        const float *Ar8 = reinterpret_cast<const float *>(sb + (rb * 16 + gid + 8) * kTcRowStride);
+        const bool mem_ok = (mt.mask >> gid) & 1;
+        const float2 *xm = reinterpret_cast<const float2 *>(sb + kTcABytes + gid * kTcXStride);
+        // this warp's slice of the stage, 4 complex columns per step
+#pragma unroll 4
+        for (int st4 = 0; st4 < kTcSlice / 4; ++st4) {
+            const int j0 = kq * kTcSlice + st4 * 4;
+            if (j0 >= mt.len) break;
+            // A fragment: real columns 2 j0 + tig and 2 j0 + tig + 4
+            const int ka = 2 * j0 + tig, kb = ka + 4;
+            const bool va = (ka >> 1) < mt.len, vb = (kb >> 1) < mt.len;
+            const float fa0 = va ? Ar0[ka] : 0.f, fa1 = va ? Ar8[ka] : 0.f;
+            const float fa2 = vb ? Ar0[kb] : 0.f, fa3 = vb ? Ar8[kb] : 0.f;
+            uint32_t ah[4], al[4];
+            tf32_split(fa0, ah[0], al[0]);
+            tf32_split(fa1, ah[1], al[1]);
+            tf32_split(fa2, ah[2], al[2]);
+            tf32_split(fa3, ah[3], al[3]);
+            // B fragments: member gid, complex entries j0 + (tig >> 1) and j0 + 2 + (tig >> 1)
+            const int ja = j0 + (tig >> 1), jb = ja + 2;
+            const float2 xa = (mem_ok && ja < mt.len) ? xm[ja] : make_float2(0.f, 0.f);
+            const float2 xb = (mem_ok && jb < mt.len) ? xm[jb] : make_float2(0.f, 0.f);
+            const bool odd = tig & 1;
+            // Re tile: (re, -im) pattern; Im tile: (im, re) pattern
+            const float br0 = odd ? -xa.y : xa.x, br1 = odd ? -xb.y : xb.x;
+            const float bi0 = odd ? xa.x : xa.y, bi1 = odd ? xb.x : xb.y;
+            uint32_t brh0, brl0, brh1, brl1, bih0, bil0, bih1, bil1;
+            tf32_split(br0, brh0, brl0);
+            tf32_split(br1, brh1, brl1);
+            tf32_split(bi0, bih0, bil0);
+            tf32_split(bi1, bih1, bil1);
+            mma_tf32(dre[0], ah[0], ah[1], ah[2], ah[3], brh0, brh1);
+            mma_tf32(dim[0], ah[0], ah[1], ah[2], ah[3], bih0, bih1);
+            mma_tf32(dre[1], ah[0], ah[1], ah[2], ah[3], brl0, brl1);
+            mma_tf32(dim[1], ah[0], ah[1], ah[2], ah[3], bil0, bil1);
+            mma_tf32(dre[2], al[0], al[1], al[2], al[3], brh0, brh1);
+            mma_tf32(dim[2], al[0], al[1], al[2], al[3], bih0, bih1);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty0 + 8 * stage);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float t, e;
+            two_sum(sh[i], dre[0][i] + (dre[1][i] + dre[2][i]), t, e);
+            sh[i] = t;
+            sl[i] += e;
+            two_sum(sh[4 + i], dim[0][i] + (dim[1][i] + dim[2][i]), t, e);
+            sh[4 + i] = t;
+            sl[4 + i] += e;
+        }
+        if (mt.last) {
+            // this warp's 16 x 16 tile (columns 0-7 Re, 8-15 Im) to shared memory;
+            // C fragment: rows gid, gid + 8; columns 2 tig, 2 tig + 1
+            double *t = red + warp * 256;
+            t[gid * 16 + 2 * tig] = (double)sh[0] + (double)sl[0];
+            t[gid * 16 + 2 * tig + 1] = (double)sh[1] + (double)sl[1];
+            t[(gid + 8) * 16 + 2 * tig] = (double)sh[2] + (double)sl[2];
+            t[(gid + 8) * 16 + 2 * tig + 1] = (double)sh[3] + (double)sl[3];
+            t[gid * 16 + 8 + 2 * tig] = (double)sh[4] + (double)sl[4];
+            t[gid * 16 + 8 + 2 * tig + 1] = (double)sh[5] + (double)sl[5];
+            t[(gid + 8) * 16 + 8 + 2 * tig] = (double)sh[6] + (double)sl[6];
+            t[(gid + 8) * 16 + 8 + 2 * tig + 1] = (double)sh[7] + (double)sl[7];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(redw);
+            if (!mbar_wait(redw, rph, err)) return;
+            // outputs (row block, row, member) = consumer thread index < 256; the
+            // sum of the slices of its row block (warps rb, rb + 2, ...)
+            const int ot = warp * 32 + lane;
+            if (ot < 256) {
+                const int orb = ot >> 7, row = (ot >> 3) & 15, q = ot & 7;
+                double yr = 0.0, yi = 0.0;
+#pragma unroll
+                for (int k8 = 0; k8 < kTcWarps / 2; ++k8) {
+                    const double *u = red + (orb + 2 * k8) * 256 + row * 16;
+                    yr += u[q];
+                    yi += u[8 + q];
+                }
+                const int grow = orb * 16 + row;
+                if (grow < mt.nrows && ((mt.mask >> q) & 1))
+                    tb->sys[mt.first + q].mvp[mt.row0 + grow] = make_double2(yr, yi);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(redr);
+            if (!mbar_wait(redr, rph, err)) return;   // the tile is free for the next strip
+            rph ^= 1;
+        }
+        if (++stage == kTcStages) { stage = 0; fph ^= 1; }
+    }
+}
+
 // ------------------------------------------------------------ block helpers
 // dp[l * nvb + blk] = sum over the block's rows of conj(V_l[row]) w[row], l < nv.
 __device__ void block_dots(const double2 *__restrict__ V, long long ldv, int nv, double2 wv, bool ok, int row,
@@ -1168,6 +1418,8 @@ cudaError_t krylov_prepare() {
         if (err == cudaSuccess)
             err = cudaFuncSetAttribute(k_mv_grp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        grp_smem_bytes(true));
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k_mv_grp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
         g_mv_grid[1] = sms;   // one bulk-copy block per SM
         if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mv64<false>, 256, 0);
         g_mv_grid[0] = sms * (per > 0 ? per : 1);
@@ -1196,7 +1448,7 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
         if (c128) k_mv64<false><<<gmv, 256, 0, st>>>(tb, 0);
         else {
             k_mv_tma<false><<<gmv, kTmaThreads, tma_smem_bytes(false), st>>>(tb, 0);
-            k_mv_grp<false><<<gmv, 32 * (GrpCfg<false>::kWarps + 1), grp_smem_bytes(false), st>>>(tb, 0);
+            k_mv_grp_tc<<<gmv, 32 * (kTcWarps + 1), kTcSmem, st>>>(tb, 0);
             ++nl;
         }
         if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q + 1], st, cudaEventRecordExternal);
@@ -1218,7 +1470,7 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
         k_mv_tma<true><<<gmv, kTmaThreads, tma_smem_bytes(true), st>>>(tb, 1);
         k_mv_grp<true><<<gmv, 32 * (GrpCfg<true>::kWarps + 1), grp_smem_bytes(true), st>>>(tb, 1);
         k_mv_tma<false><<<gmv, kTmaThreads, tma_smem_bytes(false), st>>>(tb, 2);
-        k_mv_grp<false><<<gmv, 32 * (GrpCfg<false>::kWarps + 1), grp_smem_bytes(false), st>>>(tb, 2);
+        k_mv_grp_tc<<<gmv, 32 * (kTcWarps + 1), kTcSmem, st>>>(tb, 2);
         nl += 3;
     }
     if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * kSteps + 1], st, cudaEventRecordExternal);

@@ -103,6 +103,7 @@ struct ProjSys {
     DevFreq f;
     const double *x;        // solution (complex)
     double *phi, *vel;      // scratch: element potentials [n], nodal velocities [4][n]
+    float *phi32, *vel32;   // the same in float (read by the float projection)
     int *ivi;               // [n] nonzero-velocity flags
     int npts;
     const double *pts;      // [npts][3]

@@ -540,6 +540,9 @@ __global__ void __launch_bounds__(256) k_fields(const __grid_constant__ ProjBatc
         if (sqrt(v[a].re * v[a].re + v[a].im * v[a].im) > kEPSY) any = 1;
     phi[j] = make_double2(p.re, p.im);
     for (int a = 0; a < 4; ++a) vel[a * n + j] = make_double2(v[a].re, v[a].im);
+    float2 *phi32 = (float2 *)S.phi32, *vel32 = (float2 *)S.vel32;
+    phi32[j] = make_float2((float)p.re, (float)p.im);
+    for (int a = 0; a < 4; ++a) vel32[a * n + j] = make_float2((float)v[a].re, (float)v[a].im);
     ivi[j] = any;
 }
 
@@ -553,6 +556,7 @@ __global__ void __launch_bounds__(256) k_project(const __grid_constant__ ProjBat
     const DevMesh m = to_dev(S.m);
     const DevFreq &f = S.f;
     const double2 *phi = (const double2 *)S.phi, *vel = (const double2 *)S.vel;
+    const float2 *phi32 = (const float2 *)S.phi32, *vel32 = (const float2 *)S.vel32;
     const int *ivi = S.ivi;
     const int npts = S.npts;
     const double *pts = S.pts;
@@ -579,10 +583,20 @@ __global__ void __launch_bounds__(256) k_project(const __grid_constant__ ProjBat
         bool near = false;
         int order = 2;
         if (valid) {
-            cplx<T> ph = {(T)phi[j].x, (T)phi[j].y};
+            // element data in T (float copies for the float path: no FP64 conversions)
             const bool iv = ivi[j] != 0;
-            cplx<T> vl[4];
-            for (int a = 0; a < 4; ++a) vl[a] = {(T)vel[a * n + j].x, (T)vel[a * n + j].y};
+            cplx<T> ph, vl[4];
+            if constexpr (std::is_same<T, double>::value) {
+                ph = {phi[j].x, phi[j].y};
+                for (int a = 0; a < 4; ++a) vl[a] = iv ? cplx<T>{vel[a * n + j].x, vel[a * n + j].y} : cplx<T>{0, 0};
+            } else {
+                const float2 p2 = phi32[j];
+                ph = {p2.x, p2.y};
+                for (int a = 0; a < 4; ++a) {
+                    const float2 v2 = iv ? vel32[a * n + j] : make_float2(0.f, 0.f);
+                    vl[a] = {v2.x, v2.y};
+                }
+            }
             if constexpr (std::is_same<T, double>::value) {
                 const double rd = ratio0_exact(m, j, x64);
                 near = rd < kTolf;
@@ -634,10 +648,19 @@ __global__ void __launch_bounds__(256) k_project(const __grid_constant__ ProjBat
             const int jl = base + L;
             Elem64 e;
             load_elem64(m, jl, e);
-            cplx<T> ph = {(T)phi[jl].x, (T)phi[jl].y};
-            cplx<T> vl[4];
-            for (int a = 0; a < 4; ++a) vl[a] = {(T)vel[a * n + jl].x, (T)vel[a * n + jl].y};
             const bool iv = ivi[jl] != 0;
+            cplx<T> ph, vl[4];
+            if constexpr (std::is_same<T, double>::value) {
+                ph = {phi[jl].x, phi[jl].y};
+                for (int a = 0; a < 4; ++a) vl[a] = {vel[a * n + jl].x, vel[a * n + jl].y};
+            } else {
+                const float2 p2 = phi32[jl];
+                ph = {p2.x, p2.y};
+                for (int a = 0; a < 4; ++a) {
+                    const float2 v2 = vel32[a * n + jl];
+                    vl[a] = {v2.x, v2.y};
+                }
+            }
             ProjAcc<T> r;
             int rc;
             if constexpr (std::is_same<T, double>::value) {

@@ -71,6 +71,7 @@ struct SolverBufs {
     int *status = nullptr;
     unsigned *ctr = nullptr;   // 4 words: work queues of the persistent assembly kernels
     double *phi = nullptr, *vel = nullptr;
+    float *phi32 = nullptr, *vel32 = nullptr;
     int *ivi = nullptr;
     int *bct = nullptr, *cols = nullptr;
     double *bcv = nullptr, *adm = nullptr, *src = nullptr;
@@ -180,6 +181,8 @@ struct bem_solver_s {
         q.x = (const double *)d.x;
         q.phi = d.phi;
         q.vel = d.vel;
+        q.phi32 = d.phi32;
+        q.vel32 = d.vel32;
         q.ivi = d.ivi;
         q.npts = npts;
         q.pts = pts_dev;

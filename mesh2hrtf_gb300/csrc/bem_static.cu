@@ -18,9 +18,9 @@
 namespace {
 
 constexpr int kStaticMaxElem = BEM_STATIC_MAX_ELEMENTS;
-// per element: phi (16 B) + 4 nodal velocities (64 B) + flag (4 B), then the
-// error word
-constexpr size_t kScratchBytes = (size_t)kStaticMaxElem * (16 + 64 + 4) + 256;
+// per element: phi (16 B) + 4 nodal velocities (64 B) + their float copies
+// (8 + 32 B) + flag (4 B), then the error word
+constexpr size_t kScratchBytes = (size_t)kStaticMaxElem * (16 + 64 + 8 + 32 + 4) + 256;
 
 static __device__ __align__(256) unsigned char g_project_scratch[kScratchBytes];
 
@@ -65,13 +65,15 @@ extern "C" bem_status bem_project_static(bem_solver_t solver, int32_t n_pts, con
     }
     cudaStream_t st = (cudaStream_t)stream;
     unsigned char *b = (unsigned char *)base;
-    int *status = (int *)(b + (size_t)kStaticMaxElem * 84);
+    int *status = (int *)(b + (size_t)kStaticMaxElem * 124);
     // the fields kernel indexes vel as [4][n] with row stride n, so the
     // scratch layout holds for any n up to the maximum
     bem::ProjSys &S = t.sys[0];
     S.phi = (double *)b;
     S.vel = (double *)(b + (size_t)kStaticMaxElem * 16);
-    S.ivi = (int *)(b + (size_t)kStaticMaxElem * 80);
+    S.phi32 = (float *)(b + (size_t)kStaticMaxElem * 80);
+    S.vel32 = (float *)(b + (size_t)kStaticMaxElem * 88);
+    S.ivi = (int *)(b + (size_t)kStaticMaxElem * 120);
     S.status = status;
     S.npts = n_pts;
     S.pts = pts_dev;
