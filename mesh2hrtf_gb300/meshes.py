@@ -13,6 +13,9 @@ workloads are generated here from seeded parameters:
   stereographic dilation on the parameter sphere.
 * ``perturbed_ellipsoid(...)``: the same ellipsoid with smooth, seeded radial
   noise and an arbitrary ``20*n**2`` triangle count.
+* ``sphere_sector(...)``: the part of a cube-projected sphere on the positive
+  side of one to three coordinate planes, the input of a problem with
+  symmetry planes (NumCalc's SYMMETRY block, ``NC_Input.cpp:459-494``).
 
 All triangles are oriented so that (P0-P2) x (P1-P2) points into the fluid,
 the orientation the reference's sphere fixture uses
@@ -250,3 +253,65 @@ def shells_triangles(shells):
         tris.append(grid_triangles(np.asarray(pts)) + off)
         off += len(pts)
     return np.vstack(tris)
+
+
+def cube_sphere(n: int, radius: float):
+    """Quadrilateral sphere: every cube face split into n x n quads and
+    projected; quads ordered so that NumCalc's quad normal dx/ds x dx/dt
+    (``NC_3dFunctions.cpp:132-178``) points outward."""
+    pts, quads, idx = [], [], {}
+
+    def vid(p):
+        key = tuple(np.round(p, 12))
+        if key not in idx:
+            idx[key] = len(pts)
+            pts.append(p)
+        return idx[key]
+
+    g = np.linspace(-1.0, 1.0, n + 1)
+    for ax in range(3):
+        for sgn in (-1.0, 1.0):
+            for a in range(n):
+                for b in range(n):
+                    cs = []
+                    for (u, w) in ((g[a], g[b]), (g[a + 1], g[b]), (g[a + 1], g[b + 1]), (g[a], g[b + 1])):
+                        p = np.zeros(3)
+                        p[ax] = sgn
+                        p[(ax + 1) % 3] = u
+                        p[(ax + 2) % 3] = w
+                        cs.append(vid(p))
+                    quads.append(cs)
+    v = np.array(pts)
+    v = v / np.linalg.norm(v, axis=1)[:, None] * radius
+    q = np.array(quads)
+    for e in range(len(q)):
+        P = v[q[e]]
+        dxs = 0.25 * (P[0] - P[1] - P[2] + P[3])
+        dxt = 0.25 * (P[0] + P[1] - P[2] - P[3])
+        if np.dot(np.cross(dxs, dxt), P.mean(axis=0)) < 0:
+            q[e] = q[e][::-1]
+    return v, q
+
+
+def sphere_sector(n: int, radius: float, axes, center=(0.0, 0.0, 0.0), triangles: bool = False):
+    """The quads of ``cube_sphere(n, radius)`` (n even) whose centres lie on
+    the positive side of the planes normal to ``axes``, moved by ``center``
+    (the planes then pass through ``center``).  ``triangles`` splits every
+    quad (P0, P1, P2, P3) into (P0, P1, P2) and (P0, P2, P3), keeping the
+    normal.  Nodes on a plane lie on it exactly when ``center`` is zero."""
+    if n % 2:
+        raise ValueError("n must be even so that grid lines lie on the planes")
+    v, q = cube_sphere(n, radius)
+    cen = v[q].mean(axis=1)
+    keep = np.ones(len(q), bool)
+    for ax in axes:
+        keep &= cen[:, ax] > 0.0
+    q = q[keep]
+    used = np.unique(q)
+    remap = -np.ones(len(v), np.int64)
+    remap[used] = np.arange(len(used))
+    v = v[used] + np.asarray(center, float)[None, :]
+    q = remap[q]
+    if triangles:
+        q = np.concatenate([q[:, [0, 1, 2]], q[:, [0, 2, 3]]], axis=0)
+    return v, q

@@ -125,6 +125,67 @@ static void load_elem(const or_mesh *m, int j, elem_t *e)
         for (int k = 0; k < 3; ++k) e->c[a][k] = m->nodes[3 * m->conn[4 * j + a] + k];
 }
 
+/* ---------------------------------------------------- symmetry planes */
+/* Images per element: 2^(number of planes), NC_Input.cpp:342-343. */
+static int n_images(const or_mesh *m)
+{
+    int c = 0;
+    for (int k = 0; k < 3; ++k) if (m->sym[k]) ++c;
+    return 1 << c;
+}
+
+/* Axis of reflection number kref = 1 .. nref-1: the images are visited in
+ * a Gray-code order, one reflection per step (NC_ReflectPointVector,
+ * NC_3dFunctions.cpp:190-228). */
+static int reflect_dir(const or_mesh *m, int nref, int kref)
+{
+    static const int nrefdi[8] = {0, 0, 1, 0, 2, 0, 1, 0};
+    int nrdir = 0;
+    if (nref == 8) {
+        nrdir = nrefdi[kref];
+    } else if (nref == 4) {
+        int i0 = 0;
+        for (int i = 0; i < 3; ++i) if (m->sym[i] == 0) { i0 = i + 1; break; }
+        nrdir = i0 + nrefdi[kref];
+        if (nrdir >= 3) nrdir -= 3;
+    } else if (nref == 2) {
+        for (int i = 0; i < 3; ++i) if (m->sym[i] != 0) { nrdir = i; break; }
+    }
+    return nrdir;
+}
+
+/* NC_ReflectElement, NC_3dFunctions.cpp:357-452: mirror the element (already
+ * holding the previous image) in the plane of step kref, flip the reflection
+ * factor and, for velocity data (ibvj0 == 0), the nodal values at an
+ * antisymmetric plane, then swap nodes 0/1 (and 2/3) to keep the normal
+ * outward. */
+static void reflect_elem(const or_mesh *m, int nref, int kref, int ibvj0, int *ireffac, elem_t *e, cx *bc)
+{
+    const int d = reflect_dir(m, nref, kref);
+    if (m->sym[d] < 0) {
+        *ireffac = -*ireffac;
+        if (ibvj0 == 0)
+            for (int a = 0; a < e->nv; ++a) bc[a] = cmk(-bc[a].re, -bc[a].im);
+    }
+    for (int a = 0; a < e->nv; ++a) e->c[a][d] = 2.0 * m->sym_coord[d] - e->c[a][d];
+    for (int p = 0; p < (e->nv == 4 ? 2 : 1); ++p) {
+        const int a = 2 * p, b = 2 * p + 1;
+        for (int k = 0; k < 3; ++k) { double t = e->c[a][k]; e->c[a][k] = e->c[b][k]; e->c[b][k] = t; }
+        cx t = bc[a]; bc[a] = bc[b]; bc[b] = t;
+    }
+}
+
+/* NC_ReflectPointVector, NC_3dFunctions.cpp:181-242: image of a source
+ * point (ifpoi = 1) or of a plane-wave direction (ifpoi = 0). */
+static double reflect_point(const or_mesh *m, int nref, int kref, double *v, double reffac, int ifpoi)
+{
+    const int d = reflect_dir(m, nref, kref);
+    if (ifpoi) v[d] = 2.0 * m->sym_coord[d] - v[d];
+    else v[d] = -v[d];
+    if (m->sym[d] < 0) reffac = -reffac;
+    return reffac;
+}
+
 /* NC_ComputeGlobalCoordinates, NC_3dFunctions.cpp:95-129. */
 static void global_coords(const elem_t *e, double s, double t, double *x, double *sh)
 {
@@ -440,30 +501,53 @@ static void singular(const elem_t *e, const double *x, const double *nx, int ifc
     }
 }
 
-/* NC_IncidentWaveRHS, NC_EquationSystem.cpp:1731-1812 (no symmetry planes). */
-static cx incident_rhs(const or_freq *f, const double *x, const double *nx, const consts_t *K)
+/* The point at which plane waves take their phase: x minus the plane
+ * positions on the axes that carry a plane (NC_EquationSystem.cpp:1743-1748,
+ * NC_PostProcessing.cpp:794-799). */
+static void plane_wave_origin(const or_mesh *m, const double *x, double *xs)
 {
+    int any = 0;
+    for (int k = 0; k < 3; ++k) { xs[k] = x[k]; if (m->sym[k]) any = 1; }
+    if (any)
+        for (int k = 0; k < 3; ++k) if (m->sym[k] != 0) xs[k] -= m->sym_coord[k];
+}
+
+/* NC_IncidentWaveRHS, NC_EquationSystem.cpp:1731-1812, with the images of
+ * the waves and sources in the symmetry planes. */
+static cx incident_rhs(const or_mesh *m, const or_freq *f, const double *x, const double *nx, const consts_t *K)
+{
+    const int nref = n_images(m);
     cx zrc = cmk(0.0, 0.0);
+    double xs[3];
+    plane_wave_origin(m, x, xs);
     for (int i = 0; i < f->n_plane; ++i) {
-        const double *v = f->pw_dir + 3 * i;
+        double v[3] = {f->pw_dir[3 * i], f->pw_dir[3 * i + 1], f->pw_dir[3 * i + 2]};
         cx zini = cmk(f->pw_amp[2 * i], f->pw_amp[2 * i + 1]);
-        double re1 = (v[0] * x[0] + v[1] * x[1] + v[2] * x[2]) * K->wr;
-        cx zg = cmul(cmk(cos(re1), sin(re1)), zini);
-        double re2 = K->wr * (v[0] * nx[0] + v[1] * nx[1] + v[2] * nx[2]);
-        cx zv = cmk(-zg.im * re2, zg.re * re2);
-        zrc = csub(zrc, cadd(cscl(zg, K->gamma), cmul(zv, cscl(K->beta, K->tao))));
+        double reffac = 1.0;
+        for (int kref = 0; kref < nref; ++kref) {
+            if (kref > 0) reffac = reflect_point(m, nref, kref, v, reffac, 0);
+            double re1 = (v[0] * xs[0] + v[1] * xs[1] + v[2] * xs[2]) * K->wr;
+            cx zg = cmul(cmk(cos(re1) * reffac, sin(re1) * reffac), zini);
+            double re2 = K->wr * (v[0] * nx[0] + v[1] * nx[1] + v[2] * nx[2]);
+            cx zv = cmk(-zg.im * re2, zg.re * re2);
+            zrc = csub(zrc, cadd(cscl(zg, K->gamma), cmul(zv, cscl(K->beta, K->tao))));
+        }
     }
     for (int i = 0; i < f->n_point; ++i) {
-        const double *s = f->ps_xyz + 3 * i;
+        double s[3] = {f->ps_xyz[3 * i], f->ps_xyz[3 * i + 1], f->ps_xyz[3 * i + 2]};
         cx zini = cmk(f->ps_amp[2 * i], f->ps_amp[2 * i + 1]);
-        double d[3] = {x[0] - s[0], x[1] - s[1], x[2] - s[2]};
-        double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-        d[0] /= r; d[1] /= r; d[2] /= r;
-        double re1 = K->wr * r, re2 = 1.0 / PI4 / r;
-        cx zg = cmul(cmk(cos(re1) * re2, sin(re1) * re2), zini);
-        re1 = d[0] * nx[0] + d[1] * nx[1] + d[2] * nx[2];
-        cx zv = cmul(cmk(-re1 / r, K->wr * re1), zg);
-        zrc = csub(zrc, cadd(cscl(zg, K->gamma), cmul(zv, cscl(K->beta, K->tao))));
+        double reffac = 1.0;
+        for (int kref = 0; kref < nref; ++kref) {
+            if (kref > 0) reffac = reflect_point(m, nref, kref, s, reffac, 1);
+            double d[3] = {x[0] - s[0], x[1] - s[1], x[2] - s[2]};
+            double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            d[0] /= r; d[1] /= r; d[2] /= r;
+            double re1 = K->wr * r, re2 = reffac / PI4 / r;
+            cx zg = cmul(cmk(cos(re1) * re2, sin(re1) * re2), zini);
+            re1 = d[0] * nx[0] + d[1] * nx[1] + d[2] * nx[2];
+            cx zv = cmul(cmk(-re1 / r, K->wr * re1), zg);
+            zrc = csub(zrc, cadd(cscl(zg, K->gamma), cmul(zv, cscl(K->beta, K->tao))));
+        }
     }
     return zrc;
 }
@@ -511,10 +595,12 @@ int or_assemble(const or_mesh *m, const double *centers, const double *normals, 
         cx z0 = cmk(0.0, 0.0);
         if (ibi == 0) z0 = cadd(z0, cscl(cscl(cmul(zbvi, K.beta), K.tao), 0.5));
         else z0 = cadd(z0, cscl(cscl(zbvi, K.tao), 0.5));
-        if (f->n_plane + f->n_point > 0) z0 = cadd(z0, incident_rhs(f, x, nx, &K));
+        if (f->n_plane + f->n_point > 0) z0 = cadd(z0, incident_rhs(m, f, x, nx, &K));
         cx ri = z0;
-        cx diag_acc = aii;
-        for (int j = 0; j < n; ++j) {
+        Arow[2 * i] = aii.re;
+        Arow[2 * i + 1] = aii.im;
+        const int nref = n_images(m);
+        for (int j = 0; j < n && !err; ++j) {
             elem_t e;
             load_elem(m, j, &e);
             int ibj = m->bc_type[j] == 1 ? 1 : 0, admj = m->bc_type[j] == 2;
@@ -522,27 +608,27 @@ int or_assemble(const or_mesh *m, const double *centers, const double *normals, 
             bc_of(m, j, bcj);
             int ifc = 0;
             for (int a = 0; a < e.nv; ++a) if (cabs_(bcj[a]) > EPSY) { ifc = 1; break; }
-            cx zr[5];
-            if (j == i) singular(&e, x, nx, ifc, ibj, bcj, &K, zr);
-            else if (regular(&e, areas[j], x, nx, ifc, ibj, bcj, &K, zr)) { err = 1; break; }
-            cx zs;
-            if (ibj == 0) {
-                zs = cadd(cscl(zr[1], K.gamma * K.tao), cmul(zr[3], K.beta));
-                if (admj) {
-                    cx Y = cmk(m->adm[2 * j], m->adm[2 * j + 1]);
-                    zs = cadd(zs, cmul(cadd(cscl(zr[0], K.gamma), cmul(zr[2], cscl(K.beta, K.tao))), Y));
+            /* images of element j, NC_EquationSystem.cpp:277-300 */
+            int ireffac = 1;
+            for (int kref = 0; kref < nref; ++kref) {
+                if (kref > 0) reflect_elem(m, nref, kref, ibj, &ireffac, &e, bcj);
+                cx zr[5];
+                if (kref == 0 && j == i) singular(&e, x, nx, ifc, ibj, bcj, &K, zr);
+                else if (regular(&e, areas[j], x, nx, ifc, ibj, bcj, &K, zr)) { err = 1; break; }
+                cx zs;
+                if (ibj == 0) {
+                    zs = cadd(cscl(zr[1], K.gamma * K.tao), cmul(zr[3], K.beta));
+                    if (admj) {
+                        cx Y = cmk(m->adm[2 * j], m->adm[2 * j + 1]);
+                        zs = cadd(zs, cmul(cadd(cscl(zr[0], K.gamma), cmul(zr[2], cscl(K.beta, K.tao))), Y));
+                    }
+                } else {
+                    zs = csub(cscl(zr[0], -K.gamma * K.tao), cmul(zr[2], K.beta));
                 }
-            } else {
-                zs = csub(cscl(zr[0], -K.gamma * K.tao), cmul(zr[2], K.beta));
-            }
-            if (ifc) ri = cadd(ri, zr[4]);
-            if (j == i) {
-                diag_acc = cadd(diag_acc, zs);
-                Arow[2 * j] = diag_acc.re;
-                Arow[2 * j + 1] = diag_acc.im;
-            } else {
-                Arow[2 * j] += zs.re;
-                Arow[2 * j + 1] += zs.im;
+                if (ifc) ri = cadd(ri, zr[4]);
+                const double reffact = ireffac == -1 ? -1.0 : 1.0;   /* NC_AssembleTBEM:181 */
+                Arow[2 * j] += zs.re * reffact;
+                Arow[2 * j + 1] += zs.im * reffact;
             }
         }
         rhs[2 * (i - row0)] = ri.re;
@@ -646,6 +732,7 @@ int or_project(const or_mesh *m, const double *centers, const double *normals, c
     consts_t K;
     make_consts(f, &K);
     int err = 0;
+    const int nref = n_images(m);
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 4) reduction(| : err)
@@ -653,48 +740,66 @@ int or_project(const or_mesh *m, const double *centers, const double *normals, c
     for (int p = 0; p < npts; ++p) {
         const double *xp = pts + 3 * p;
         cx zp_tot = cmk(0.0, 0.0), zv_tot[3] = {{0, 0}, {0, 0}, {0, 0}};
-        for (int j = 0; j < m->n_elem; ++j) {
+        for (int j = 0; j < m->n_elem && !err; ++j) {
             elem_t e;
             load_elem(m, j, &e);
-            cx zpot = cmk(phi[2 * j], phi[2 * j + 1]), v[4];
+            cx zpoto = cmk(phi[2 * j], phi[2 * j + 1]), v[4];
             int ivi = 0;
             for (int a = 0; a < e.nv; ++a) {
                 v[a] = cmk(vel[8 * j + 2 * a], vel[8 * j + 2 * a + 1]);
                 if (cabs_(v[a]) > EPSY) ivi = 1;
             }
-            double xs[MSBE], es[MSBE], fs[MSBE];
-            int ng[MSBE];
-            int nsbe = subelements(&e, xp, areas[j], xs, es, fs, ng);
-            if (nsbe < 0) { err = 1; break; }
-            cx zp = cmk(0.0, 0.0), zv[3] = {{0, 0}, {0, 0}, {0, 0}};
-            for (int s = 0; s < nsbe; ++s)
-                zp = cadd(zp, project_sub(&e, xp, xs[s], es[s], ng[s], fs[s], zpot, ivi, v, &K, zv));
-            if (K.tao != 1.0) { zp = cscl(zp, K.tao); for (int k = 0; k < 3; ++k) zv[k] = cscl(zv[k], K.tao); }
-            zp_tot = cadd(zp_tot, zp);
-            for (int k = 0; k < 3; ++k) zv_tot[k] = cadd(zv_tot[k], zv[k]);
+            /* images of element j: velocity data (ibvj0 = 0) flips at
+             * antisymmetric planes, the potential with the reflection
+             * factor (NC_PostProcessing.cpp:925-972) */
+            int ireffac = 1;
+            for (int kref = 0; kref < nref; ++kref) {
+                if (kref > 0) reflect_elem(m, nref, kref, 0, &ireffac, &e, v);
+                cx zpot = ireffac == -1 ? cscl(zpoto, -1.0) : zpoto;
+                double xs[MSBE], es[MSBE], fs[MSBE];
+                int ng[MSBE];
+                int nsbe = subelements(&e, xp, areas[j], xs, es, fs, ng);
+                if (nsbe < 0) { err = 1; break; }
+                cx zp = cmk(0.0, 0.0), zv[3] = {{0, 0}, {0, 0}, {0, 0}};
+                for (int s = 0; s < nsbe; ++s)
+                    zp = cadd(zp, project_sub(&e, xp, xs[s], es[s], ng[s], fs[s], zpot, ivi, v, &K, zv));
+                if (K.tao != 1.0) { zp = cscl(zp, K.tao); for (int k = 0; k < 3; ++k) zv[k] = cscl(zv[k], K.tao); }
+                zp_tot = cadd(zp_tot, zp);
+                for (int k = 0; k < 3; ++k) zv_tot[k] = cadd(zv_tot[k], zv[k]);
+            }
         }
         /* NC_ContributionIncidentWaves, NC_PostProcessing.cpp:776-866 */
         cx zinc = cmk(0.0, 0.0), vinc[3] = {{0, 0}, {0, 0}, {0, 0}};
+        double xs0[3];
+        plane_wave_origin(m, xp, xs0);
         for (int i = 0; i < f->n_plane; ++i) {
-            const double *d = f->pw_dir + 3 * i;
+            double d[3] = {f->pw_dir[3 * i], f->pw_dir[3 * i + 1], f->pw_dir[3 * i + 2]};
             cx zini = cmk(f->pw_amp[2 * i], f->pw_amp[2 * i + 1]);
-            double re1 = (d[0] * xp[0] + d[1] * xp[1] + d[2] * xp[2]) * K.wr;
-            cx zg = cmul(cmk(cos(re1), sin(re1)), zini);
-            zinc = cadd(zinc, zg);
-            cx zv = cmk(-zg.im * K.wr, zg.re * K.wr);
-            for (int k = 0; k < 3; ++k) vinc[k] = cadd(vinc[k], cscl(zv, d[k]));
+            double reffac = 1.0;
+            for (int kref = 0; kref < nref; ++kref) {
+                if (kref > 0) reffac = reflect_point(m, nref, kref, d, reffac, 0);
+                double re1 = (d[0] * xs0[0] + d[1] * xs0[1] + d[2] * xs0[2]) * K.wr;
+                cx zg = cmul(cmk(cos(re1) * reffac, sin(re1) * reffac), zini);
+                zinc = cadd(zinc, zg);
+                cx zv = cmk(-zg.im * K.wr, zg.re * K.wr);
+                for (int k = 0; k < 3; ++k) vinc[k] = cadd(vinc[k], cscl(zv, d[k]));
+            }
         }
         for (int i = 0; i < f->n_point; ++i) {
-            const double *s = f->ps_xyz + 3 * i;
+            double s[3] = {f->ps_xyz[3 * i], f->ps_xyz[3 * i + 1], f->ps_xyz[3 * i + 2]};
             cx zini = cmk(f->ps_amp[2 * i], f->ps_amp[2 * i + 1]);
-            double d[3] = {xp[0] - s[0], xp[1] - s[1], xp[2] - s[2]};
-            double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-            d[0] /= r; d[1] /= r; d[2] /= r;
-            double re1 = K.wr * r, re2 = 1.0 / PI4 / r;
-            cx zg = cmul(cmk(cos(re1) * re2, sin(re1) * re2), zini);
-            zinc = cadd(zinc, zg);
-            cx zv = cmul(cmk(-1.0 / r, K.wr), zg);
-            for (int k = 0; k < 3; ++k) vinc[k] = cadd(vinc[k], cscl(zv, d[k]));
+            double reffac = 1.0;
+            for (int kref = 0; kref < nref; ++kref) {
+                if (kref > 0) reffac = reflect_point(m, nref, kref, s, reffac, 1);
+                double d[3] = {xp[0] - s[0], xp[1] - s[1], xp[2] - s[2]};
+                double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                d[0] /= r; d[1] /= r; d[2] /= r;
+                double re1 = K.wr * r, re2 = reffac / PI4 / r;
+                cx zg = cmul(cmk(cos(re1) * re2, sin(re1) * re2), zini);
+                zinc = cadd(zinc, zg);
+                cx zv = cmul(cmk(-1.0 / r, K.wr), zg);
+                for (int k = 0; k < 3; ++k) vinc[k] = cadd(vinc[k], cscl(zv, d[k]));
+            }
         }
         if (f->n_plane || f->n_point) {
             zp_tot = cadd(zp_tot, zinc);

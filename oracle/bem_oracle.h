@@ -21,6 +21,10 @@ typedef struct {
     const double *bc_val;   /* [n_elem][4] complex nodal BC value (zbval0), */
                             /* already in potential units                   */
     const double *adm;      /* [n_elem] complex admittance (zbval1), scaled */
+    int sym[3];             /* symmetry plane normal to axis k, coded as the */
+                            /* reference holds it after NC_Input.cpp:470-491: */
+                            /* 0 none, 1 / 2 symmetric, -1 / -2 antisymmetric */
+    double sym_coord[3];    /* plane position on axis k                      */
 } or_mesh;
 
 typedef struct {
@@ -49,7 +53,9 @@ int or_subelements(const or_mesh *m, int j, const double x[3], double area,
  * dimension n_elem) and the matching right-hand side entries:
  * NC_BuildSystemTBEM / NC_ComputeEntriesForTBEM / NC_AssembleTBEM /
  * NC_SingularIntegration / NC_RegularIntegration / NC_IncidentWaveRHS,
- * NC_EquationSystem.cpp:79-302,1408-1812.  Returns 0 or -1 on error. */
+ * NC_EquationSystem.cpp:79-302,1408-1812, with the images of every element
+ * in the symmetry planes (NC_ReflectElement / NC_ReflectPointVector,
+ * NC_3dFunctions.cpp:181-242,357-452).  Returns 0 or -1 on error. */
 int or_assemble(const or_mesh *m, const double *centers, const double *normals,
                 const double *areas, const or_freq *f, int row0, int row1,
                 double *A, double *rhs, int nthreads);
@@ -59,7 +65,8 @@ int or_solve_dense(int n, double *A, const double *b, double *x);
 
 /* Potential and its gradient at points: NC_ContributionTBEM /
  * NC_IntegrationTBEM / NC_ContributionIncidentWaves,
- * NC_PostProcessing.cpp:776-975,1217-1322.  phi: element potentials
+ * NC_PostProcessing.cpp:776-975,1217-1322 (with the element and source
+ * images of the symmetry planes).  phi: element potentials
  * (cVpotele), vel: [n][4] complex nodal normal velocities (cVeloele). */
 int or_project(const or_mesh *m, const double *centers, const double *normals,
                const double *areas, const or_freq *f, const double *phi,

@@ -41,7 +41,11 @@ def lib():
 class _Mesh(C.Structure):
     _fields_ = [("n_elem", C.c_int), ("nodes", C.c_void_p), ("conn", C.c_void_p),
                 ("nvert", C.c_void_p), ("bc_type", C.c_void_p), ("bc_val", C.c_void_p),
-                ("adm", C.c_void_p)]
+                ("adm", C.c_void_p), ("sym", C.c_int * 3), ("sym_coord", C.c_double * 3)]
+
+
+# NC.inp symmetry codes -> the reference's internal codes (NC_Input.cpp:470-491)
+SYM_CODES = {0: 0, 1: 1, 2: -1, 3: 2, 4: -2}
 
 
 class _Freq(C.Structure):
@@ -57,7 +61,10 @@ def _p(a):
 class OracleMesh:
     """Boundary mesh in the oracle's layout (keeps the numpy buffers alive)."""
 
-    def __init__(self, nodes, elems, bc_type=None, bc_val=None, adm=None):
+    def __init__(self, nodes, elems, bc_type=None, bc_val=None, adm=None, sym=(0, 0, 0),
+                 sym_coord=(0.0, 0.0, 0.0)):
+        """sym: per axis the NC.inp SYMMETRY code (0 none, 1 symmetric,
+        2 antisymmetric, 3 / 4 reflecting, treated as 1 / 2 on this path)."""
         elems = np.asarray(elems)
         n = len(elems)
         self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
@@ -70,8 +77,11 @@ class OracleMesh:
         self.bc_val = np.zeros((n, 4), np.complex128) if bc_val is None else np.asarray(bc_val, np.complex128)
         self.adm = np.zeros(n, np.complex128) if adm is None else np.asarray(adm, np.complex128)
         self.n = n
+        self.sym = tuple(SYM_CODES[int(c)] for c in sym)
+        self.sym_coord = tuple(float(c) for c in sym_coord)
         self._s = _Mesh(n, self.nodes.ctypes.data, self.conn.ctypes.data, self.nvert.ctypes.data,
-                        self.bc_type.ctypes.data, self.bc_val.ctypes.data, self.adm.ctypes.data)
+                        self.bc_type.ctypes.data, self.bc_val.ctypes.data, self.adm.ctypes.data,
+                        (C.c_int * 3)(*self.sym), (C.c_double * 3)(*self.sym_coord))
         self.centers = np.zeros((n, 3))
         self.normals = np.zeros((n, 15))
         self.areas = np.zeros(n)

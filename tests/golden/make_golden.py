@@ -29,40 +29,7 @@ REF_FIXTURES = "/root/reference/tests/resources/test_numcalc"
 
 
 def cube_sphere(n, radius):
-    """Quadrilateral sphere: cube faces split n x n, projected (outward)."""
-    pts, quads, idx = [], [], {}
-
-    def vid(p):
-        key = tuple(np.round(p, 12))
-        if key not in idx:
-            idx[key] = len(pts)
-            pts.append(p)
-        return idx[key]
-
-    g = np.linspace(-1, 1, n + 1)
-    for ax in range(3):
-        for sgn in (-1, 1):
-            for a in range(n):
-                for b in range(n):
-                    cs = []
-                    for (u, v) in ((g[a], g[b]), (g[a + 1], g[b]), (g[a + 1], g[b + 1]), (g[a], g[b + 1])):
-                        p = np.zeros(3)
-                        p[ax] = sgn
-                        p[(ax + 1) % 3] = u
-                        p[(ax + 2) % 3] = v
-                        cs.append(vid(p))
-                    quads.append(cs)
-    v = np.array(pts)
-    v = v / np.linalg.norm(v, axis=1)[:, None] * radius
-    q = np.array(quads)
-    # NumCalc quad normal: dx/ds x dx/dt at the centre, outward wanted
-    for e in range(len(q)):
-        P = v[q[e]]
-        dxs = 0.25 * (P[0] - P[1] - P[2] + P[3])
-        dxt = 0.25 * (P[0] + P[1] - P[2] - P[3])
-        if np.dot(np.cross(dxs, dxt), P.mean(axis=0)) < 0:
-            q[e] = q[e][::-1]
-    return v, q
+    return meshes.cube_sphere(n, radius)
 
 
 def run_case(name, proj: project.Project, rows=None, n_entries=0, seed=0, full=False):
@@ -83,6 +50,9 @@ def run_case(name, proj: project.Project, rows=None, n_entries=0, seed=0, full=F
     out["point_sources"] = np.asarray(proj.point_sources, float).reshape(-1, 5)
     out["plane_waves"] = np.asarray(proj.plane_waves, float).reshape(-1, 5)
     out["speed_density"] = np.array([proj.speed_of_sound, proj.density])
+    if proj.nsym:
+        out["sym_planes"] = np.asarray(proj.sym_planes, np.int32)   # NC.inp codes
+        out["sym_coords"] = np.asarray(proj.sym_coords, float)
     out["elem_center"] = tab["elem_center"].reshape(-1, 3)[: len(proj.elems)]
     out["elem_normal"] = tab["elem_normals"].reshape(-1, 15)[: len(proj.elems), :3]
     out["elem_area"] = tab["elem_area"][: len(proj.elems)]
@@ -179,8 +149,57 @@ def case_pspw():
     run_case("pspw2412_4k", p, rows=[0, 1205, 2411], n_entries=1000, seed=2)
 
 
+def case_sym1():
+    """Half sphere (x >= 0) of 216 triangles, one symmetric plane x = 0,
+    rigid, point source off the plane; two frequencies."""
+    v, f = meshes.sphere_sector(6, 0.1, (0,), triangles=True)
+    sh = [meshes.random_sphere_points(24, 0.3, 31), meshes.random_sphere_points(8, 0.104, 32)]
+    pts = np.vstack(sh)
+    p = project.Project(root="", nodes=v, elems=f, eval_points=pts, eval_elems=meshes.shells_triangles(sh),
+                        freqs=[1500.0, 4000.0], point_sources=[(0.25, 0.05, 0.02, 1.0, 0.0)],
+                        boundary=["ELEM 0 TO %d VELO 0.0 -1 0.0 -1" % (len(f) - 1)],
+                        nsym=1, sym_planes=(1, 0, 0))
+    run_case("sym1_half216", p, rows=[0, 5, 60, 107, 108, 150, 215], n_entries=1500, seed=4)
+
+
+def case_sym2():
+    """Quarter sphere (y, z >= 0) of 54 quads: antisymmetric plane y = 0,
+    symmetric plane z = 0; admittance everywhere, a vibrating patch, a
+    sound-soft patch, a plane wave and a point source."""
+    v, q = meshes.sphere_sector(6, 0.1, (1, 2))
+    pts = meshes.random_sphere_points(30, 0.35, 33)
+    d = np.array([0.3, -0.5, 0.81])
+    d /= np.linalg.norm(d)
+    p = project.Project(root="", nodes=v, elems=q, eval_points=pts, eval_elems=meshes.grid_triangles(pts),
+                        freqs=[2500.0], point_sources=[(0.05, 0.2, 0.1, 1.0, 0.5)],
+                        plane_waves=[(d[0], d[1], d[2], 0.7, -0.2)],
+                        boundary=["ELEM 0 TO 53 ADMI 0.3 -1 0.1 -1", "ELEM 4 TO 7 VELO 0.2 -1 -0.1 -1",
+                                  "ELEM 30 TO 32 PRES 0.05 -1 0.02 -1"],
+                        nsym=2, sym_planes=(0, 2, 1))
+    run_case("sym2_quarter54", p, full=True)
+
+
+def case_sym3():
+    """Octant of 54 triangles moved off the origin: three planes through
+    (0.02, -0.01, 0.03) - symmetric x, antisymmetric y, hard reflecting z
+    (NC.inp code 3, the reference treats it as symmetric); rigid with a
+    point source and a plane wave."""
+    c = (0.02, -0.01, 0.03)
+    v, f = meshes.sphere_sector(6, 0.1, (0, 1, 2), center=c, triangles=True)
+    pts = meshes.random_sphere_points(24, 0.3, 34) + np.asarray(c)
+    d = np.array([-0.4, 0.2, -0.9])
+    d /= np.linalg.norm(d)
+    p = project.Project(root="", nodes=v, elems=f, eval_points=pts, eval_elems=meshes.grid_triangles(pts),
+                        freqs=[3000.0], point_sources=[(0.12, 0.09, 0.15, 1.0, 0.0)],
+                        plane_waves=[(d[0], d[1], d[2], 0.5, 0.0)],
+                        boundary=["ELEM 0 TO %d VELO 0.0 -1 0.0 -1" % (len(f) - 1)],
+                        nsym=3, sym_planes=(1, 2, 3), sym_coords=c)
+    run_case("sym3_octant54", p, full=True)
+
+
 CASES = {"sphere80": case_sphere80, "quad": case_quad_soft, "adm": case_admittance,
-         "sphere1280": case_sphere1280, "pspw": case_pspw}
+         "sphere1280": case_sphere1280, "pspw": case_pspw, "sym1": case_sym1, "sym2": case_sym2,
+         "sym3": case_sym3}
 
 if __name__ == "__main__":
     if not refdump.available():

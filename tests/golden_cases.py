@@ -8,6 +8,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 CASES = ["sphere80", "quad96_soft_plane", "sphere320_adm_velo", "sphere1280_1k", "pspw2412_4k"]
+# projects with symmetry planes (NC.inp SYMMETRY block)
+SYM_CASES = ["sym1_half216", "sym2_quarter54", "sym3_octant54"]
 
 
 class Case:
@@ -22,6 +24,10 @@ class Case:
         self.freqs = d["freqs"]
         self.ibval = d["elem_ibval"].astype(np.int32)
         self.rho = float(d["speed_density"][1])
+        # NC.inp symmetry codes per axis (0 none, 1 symmetric, 2 antisymmetric,
+        # 3 / 4 reflecting) and the plane positions
+        self.sym = tuple(int(v) for v in d.get("sym_planes", np.zeros(3, np.int32)))
+        self.sym_coords = tuple(float(v) for v in d.get("sym_coords", np.zeros(3)))
 
     def step(self, s):
         d = self.d

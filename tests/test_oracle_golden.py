@@ -11,14 +11,14 @@ from tests import golden_cases as gc
 def _mesh(case):
     s = case.step(1)
     return op.OracleMesh(case.nodes, case.elems, bc_type=s["bc_type"], bc_val=s["bc_value"],
-                         adm=s["admittance"])
+                         adm=s["admittance"], sym=case.sym, sym_coord=case.sym_coords)
 
 
 def _freq(s):
     return op.OracleFreq(s["k"], s["point_sources"], s["point_amps"], s["plane_dirs"], s["plane_amps"])
 
 
-@pytest.mark.parametrize("name", gc.CASES)
+@pytest.mark.parametrize("name", gc.CASES + gc.SYM_CASES)
 def test_geometry_matches_reference(name):
     c = gc.load(name)
     m = _mesh(c)
@@ -89,3 +89,31 @@ def test_analytic_series_vs_reference_bem():
     st = c.step(1)
     pa = analytic.point_source_sphere(c.pts, [1.0, 0, 0], 0.1, st["k"], Q=1.0)
     assert gc.rel_err(c["s1_pEvalGrid"], pa) < 1e-3
+
+
+@pytest.mark.parametrize("name", gc.SYM_CASES)
+def test_symmetry_planes_match_reference(name):
+    """Images of the elements, sources and waves in one to three symmetry
+    planes (symmetric, antisymmetric, reflecting; planes off the origin):
+    matrix, right-hand side and evaluation-grid fields against the
+    reference run on the same project."""
+    c = gc.load(name)
+    m = _mesh(c)
+    assert any(c.sym)
+    for s in range(1, len(c.freqs) + 1):
+        st = c.step(s)
+        A, b = op.assemble(m, _freq(st), nthreads=4)
+        if c.has("s%d_A" % s):
+            Aref = c["s%d_A" % s]
+            assert np.abs(A - Aref).max() <= 1e-13 * np.abs(Aref).max()
+        else:
+            rr, Ar = c["s%d_rows" % s], c["s%d_A_rows" % s]
+            assert np.abs(A[rr] - Ar).max() <= 1e-13 * np.abs(Ar).max()
+            ij = c["s%d_ent_ij" % s]
+            assert np.abs(A[ij[:, 0], ij[:, 1]] - c["s%d_ent_val" % s]).max() <= 1e-13 * np.abs(Ar).max()
+        assert gc.rel_err(b, c["s%d_b" % s]) < 1e-13
+        assert gc.rel_err(op.solve_dense(A, b), c["s%d_x_dense" % s]) < 1e-12
+        phi, vel = op.boundary_fields(m, c["s%d_x_cgs" % s])
+        pot, grad = op.project(m, _freq(st), phi, vel, c.pts, nthreads=4)
+        assert gc.rel_err(1j * st["rpfact"] * pot, c["s%d_pEvalGrid" % s]) < 1e-12
+        assert gc.rel_err(grad, c["s%d_vEvalGrid" % s]) < 1e-12
