@@ -65,6 +65,15 @@ typedef struct {
     const double *centers;   /* [n_elem][3] or NULL                           */
     const double *normals;   /* [n_elem][3] unit normal at the centre or NULL */
     const double *areas;     /* [n_elem] or NULL                              */
+    /* Symmetry planes (NC.inp SYMMETRY block, NC_Input.cpp:459-494): per axis
+     * the NC.inp code (0 none, 1 symmetric, 2 antisymmetric, 3 / 4 hard /
+     * soft reflecting, which the traditional BEM treats as 1 / 2) and the
+     * plane's position on that axis.  The mesh is the part on one side of
+     * the planes; every element is integrated with its 1, 2, 4 or 8 images
+     * (NC_ReflectElement, NC_3dFunctions.cpp:357-452) and incident waves
+     * with theirs.  All zero: no planes. */
+    int32_t sym_planes[3];
+    double sym_coords[3];
 } bem_mesh_desc;
 
 /* Per-frequency data: NumCalc's state after NC_UpdateFreqCurves

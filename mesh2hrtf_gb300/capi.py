@@ -46,7 +46,8 @@ class BemError(RuntimeError):
 class MeshDesc(C.Structure):
     _fields_ = [("n_elem", C.c_int32), ("n_nodes", C.c_int32), ("nodes", C.c_void_p),
                 ("conn", C.c_void_p), ("nvert", C.c_void_p), ("centers", C.c_void_p),
-                ("normals", C.c_void_p), ("areas", C.c_void_p)]
+                ("normals", C.c_void_p), ("areas", C.c_void_p), ("sym_planes", C.c_int32 * 3),
+                ("sym_coords", C.c_double * 3)]
 
 
 class FreqDesc(C.Structure):
@@ -144,9 +145,14 @@ def _ptr(a):
 
 
 class Mesh:
-    """Device-resident boundary mesh (bem_mesh_create)."""
+    """Device-resident boundary mesh (bem_mesh_create).
 
-    def __init__(self, nodes, elems, centers=None, normals=None, areas=None, device=0):
+    sym_planes / sym_coords: NumCalc's SYMMETRY block, per axis the NC.inp
+    code (0 none, 1 symmetric, 2 antisymmetric, 3 / 4 reflecting) and the
+    plane position; the mesh is the part on one side of the planes."""
+
+    def __init__(self, nodes, elems, centers=None, normals=None, areas=None, device=0,
+                 sym_planes=(0, 0, 0), sym_coords=(0.0, 0.0, 0.0)):
         lib = load()
         _check(lib.bem_set_device(device))
         elems = np.asarray(elems)
@@ -164,7 +170,8 @@ class Mesh:
         ar = None if areas is None else np.ascontiguousarray(areas, np.float64)
         keep += [cen, nor, ar]
         d = MeshDesc(n, len(self.nodes), _ptr(self.nodes), _ptr(self.conn), _ptr(self.nvert),
-                     _ptr(cen), _ptr(nor), _ptr(ar))
+                     _ptr(cen), _ptr(nor), _ptr(ar), (C.c_int32 * 3)(*[int(c) for c in sym_planes]),
+                     (C.c_double * 3)(*[float(c) for c in sym_coords]))
         h = C.c_void_p()
         _check(lib.bem_mesh_create(C.byref(d), C.byref(h)))
         self.handle = h

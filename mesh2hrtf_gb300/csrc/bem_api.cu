@@ -610,6 +610,43 @@ bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
     *out = nullptr;
     if (d->n_elem <= 0 || d->n_nodes <= 0 || !d->nodes || !d->conn || !d->nvert)
         return fail(BEM_ERR_INVALID, "mesh needs elements, nodes, connectivity and vertex counts");
+    if (d->n_elem > bem::kMaxElements)
+        return fail(BEM_ERR_INVALID, "%d elements: at most %d", d->n_elem, bem::kMaxElements);
+    // symmetry planes: NC.inp codes -> images (NC_Input.cpp:342-343,470-491)
+    bem::DevSym sym{};
+    int sign[3] = {0, 0, 0}, nplanes = 0;
+    for (int k = 0; k < 3; ++k) {
+        const int c = d->sym_planes[k];
+        if (c < 0 || c > 4) return fail(BEM_ERR_INVALID, "symmetry code %d on axis %d (0 .. 4 allowed)", c, k);
+        sym.coord[k] = d->sym_coords[k];
+        if (c) {
+            sign[k] = (c == 2 || c == 4) ? -1 : 1;
+            sym.axes |= 1u << k;
+            ++nplanes;
+        }
+    }
+    sym.nref = 1 << nplanes;
+    {
+        // axis of each reflection step, NC_ReflectPointVector (NC_3dFunctions.cpp:190-228)
+        static const int nrefdi[8] = {0, 0, 1, 0, 2, 0, 1, 0};
+        int first_free = 0, first_plane = 0;
+        for (int k = 2; k >= 0; --k) {
+            if (!sign[k]) first_free = k + 1;
+            else first_plane = k;
+        }
+        int rf = 1;
+        for (int kref = 1; kref < sym.nref; ++kref) {
+            int dir = 0;
+            if (sym.nref == 8) dir = nrefdi[kref];
+            else if (sym.nref == 4) {
+                dir = first_free + nrefdi[kref];
+                if (dir >= 3) dir -= 3;
+            } else dir = first_plane;
+            sym.rdir[kref] = (unsigned char)dir;
+            if (sign[dir] < 0) rf = -rf;
+            if (rf < 0) sym.rneg |= 1u << kref;
+        }
+    }
     bem_status s = ensure_device_init();
     if (s != BEM_OK) return s;
     const int n = d->n_elem;
@@ -634,6 +671,27 @@ bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
         if (!(ar > 0.0)) return fail(BEM_ERR_INVALID, "element %d has area %g", j, ar);
         for (int k = 0; k < 3; ++k) { C[3 * (size_t)j + k] = c[k]; NR[3 * (size_t)j + k] = nr[k]; }
         AR[j] = ar;
+    }
+    if (nplanes) {
+        // all boundary nodes on one side of every plane, within a hundredth of
+        // the mean element size (NC_Input.cpp:660-699)
+        double asum = 0.0;
+        for (int j = 0; j < n; ++j) asum += AR[j];
+        const double dtl = std::sqrt(asum / n) / 100.0;
+        for (int k = 0; k < 3; ++k) {
+            if (!sign[k]) continue;
+            double hi = -9.9e20, lo = 9.9e20;
+            for (int j = 0; j < n; ++j)
+                for (int a = 0; a < nvx[j]; ++a) {
+                    const double v = P[12 * (size_t)j + 3 * a + k];
+                    hi = std::max(hi, v);
+                    lo = std::min(lo, v);
+                }
+            const double c = sym.coord[k];
+            if (!((hi >= c - dtl && lo >= c - dtl) || (hi <= c + dtl && lo <= c + dtl)))
+                return fail(BEM_ERR_INVALID, "All BE nodes must be located on the same side of a symmetric plane! "
+                            "(axis %d)", k);
+        }
     }
     // internal numbering along a Morton curve of the centres: consecutive
     // unknowns are neighbours, so the diagonal blocks of A carry the near
@@ -720,6 +778,26 @@ bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
     if (e == cudaSuccess) e = up(&m->d_q32, q32);
     if (e == cudaSuccess) e = up(&m->d_isqa, isqa);
     if (e == cudaSuccess) e = up(&m->d_n32, n32);
+    // symmetry images: one allocation, laid out as DevSym describes
+    if (e == cudaSuccess && sym.nref > 1) {
+        const size_t ni = (size_t)(sym.nref - 1) * (size_t)n;
+        e = cudaMalloc(&m->d_img, bem::image_table_bytes(n, sym.nref));
+        if (e == cudaSuccess) {
+            bem::ImageTables it;
+            it.v64 = (double *)m->d_img;
+            it.c64 = it.v64 + 12 * ni;
+            it.chi = (float *)(it.c64 + 3 * ni);
+            it.clo = it.chi + 3 * ni;
+            it.t32 = it.clo + 3 * ni;
+            it.q32 = it.t32 + 10 * ni;
+            sym.v64 = it.v64; sym.c64 = it.c64; sym.chi = it.chi; sym.clo = it.clo;
+            sym.t32 = it.t32; sym.q32 = it.q32;
+            m->sym = sym;
+            e = bem::launch_image_tables(m->view(), it, 0);
+        }
+    } else {
+        m->sym = sym;
+    }
     // near list: count, allocate, fill (geometry only, reused by every frequency)
     unsigned long long *d_cnt = nullptr, cnt = 0;
     if (e == cudaSuccess) e = dalloc(&d_cnt, 1);

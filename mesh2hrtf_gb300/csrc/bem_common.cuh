@@ -14,6 +14,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "bem_internal.h"
+
 namespace bem {
 
 constexpr double kPI4 = 12.566370614359172944;   // 4 pi, NC_ConstantsVariables.h:66
@@ -145,7 +147,37 @@ struct DevMesh {
     const float *q32;       // 12 rows (quads): vertex offsets from the centre
     const float *isqa32;    // 1 / sqrt(areael) in float (approximate ratios)
     const float *n32;       // 3 rows: centre normal in float
+    DevSym sym;             // symmetry-plane images (sym.nref = 1: none)
 };
+
+// Element tables of image kref of every element (kref = 0: the mesh).  The
+// images share nvert, areas and 1/sqrt(area) with their elements; their
+// v64/c64/chi/clo/t32/q32 rows hold the mirrored vertices in the
+// reference's node order and the centre NumCalc's subdivision computes from
+// them (global coordinates at the local centre, NC_3dFunctions.cpp:625-640).
+// n64/n32 stay the mesh's own: they are read for collocation rows only.
+__device__ __forceinline__ DevMesh image_mesh(const DevMesh &m, int kref) {
+    if (kref == 0) return m;
+    DevMesh r = m;
+    const size_t n = (size_t)m.n, k = (size_t)(kref - 1);
+    r.v64 = m.sym.v64 + k * 12 * n;
+    r.c64 = m.sym.c64 + k * 3 * n;
+    r.chi = m.sym.chi + k * 3 * n;
+    r.clo = m.sym.clo + k * 3 * n;
+    r.t32 = m.sym.t32 + k * 10 * n;
+    r.q32 = m.sym.q32 + k * 12 * n;
+    return r;
+}
+
+// Reflection factor (+1 / -1) of image kref.
+__device__ __forceinline__ bool image_negated(const DevMesh &m, int kref) { return (m.sym.rneg >> kref) & 1u; }
+
+// Node a of image kref holds the data of the element's node image_node(a):
+// every reflection swaps nodes 0/1, and 2/3 of quadrilaterals
+// (NC_3dFunctions.cpp:427-451).
+__device__ __forceinline__ int image_node(int a, int kref, int nv) {
+    return ((kref & 1) && (a < 2 || nv == 4)) ? (a ^ 1) : a;
+}
 
 // One element in registers (FP64), for decisions and the FP64 arithmetic.
 struct Elem64 {

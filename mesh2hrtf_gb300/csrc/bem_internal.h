@@ -15,13 +15,38 @@
 
 namespace bem {
 
+// Images of the elements in up to three symmetry planes (NumCalc's SYMMETRY
+// block).  Image kref = 1 .. nref-1 is image kref-1 reflected once, across
+// the plane normal to axis rdir[kref] (the reference's Gray-code order,
+// NC_3dFunctions.cpp:181-242,357-452); its vertices are stored in the
+// reference's node order after the reflections (nodes 0/1 and 2/3 swapped
+// for odd kref).
+struct DevSym {
+    int nref;                 // images per element: 1, 2, 4 or 8
+    unsigned rneg;            // bit kref: the reflection factor of image kref is -1
+    unsigned axes;            // bit k: a plane is normal to axis k
+    unsigned char rdir[8];    // axis reflected in step kref (1 .. nref-1)
+    double coord[3];          // plane positions on the axes
+    // tables of images 1 .. nref-1, each laid out like the mesh's own
+    // (stride n); image kref starts at (kref - 1) * rows * n
+    const double *v64, *c64;
+    const float *chi, *clo, *t32, *q32;
+};
+
 // Device element tables; layout documented in bem_common.cuh (DevMesh).
 struct DevMeshView {
     int n;
     const int *nvert;
     const double *v64, *c64, *n64, *area64, *sqa64;
     const float *chi, *clo, *t32, *q32, *isqa32, *n32;
+    DevSym sym;
 };
+
+// Near-list entries are (row, column | image mask << 24): bit kref of the
+// mask marks image kref of the column element as integrated with
+// subdivision (or, for kref = 0 on the diagonal, the singular integral).
+constexpr int kNearColBits = 24;
+constexpr int kMaxElements = (1 << kNearColBits) - 1;
 
 // One frequency's data on the device.
 struct DevFreq {
@@ -78,6 +103,7 @@ struct AsmSys {
 };
 struct AsmBatch {
     int B;
+    int img;                     // some system's mesh has symmetry images
     int far_off[kMaxAsm + 1];    // tiles of 32 x 32 entries
     int near_off[kMaxAsm + 1];   // near pairs
     int rhs_off[kMaxAsm + 1];    // blocks of 8 rows
@@ -86,9 +112,20 @@ struct AsmBatch {
 // Fills the offset tables from sys[0..B).
 void asm_batch_finish(AsmBatch &t);
 
-// Pairs integrated with subdivision plus self pairs, (row, column);
-// list == nullptr only counts.
+// Pairs integrated with subdivision plus self pairs (row, column | image
+// mask << kNearColBits); list == nullptr only counts.
 cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long *count, cudaStream_t st);
+// Writable image tables of a mesh (DevSym's layout).
+struct ImageTables {
+    double *v64, *c64;
+    float *chi, *clo, *t32, *q32;
+};
+// Fills the image tables of m (m.sym.nref > 1) from the mesh's own tables.
+cudaError_t launch_image_tables(const DevMeshView &m, const ImageTables &out, cudaStream_t st);
+// Device bytes of the image tables of n elements with nref images.
+inline size_t image_table_bytes(int n, int nref) {
+    return (size_t)(nref - 1) * (size_t)n * (15 * sizeof(double) + 28 * sizeof(float));
+}
 // A = assembled TBEM matrices of the batch, complex128 (prec 0) or complex64
 // (prec 1): regular pairs (persistent k_far), then the near lists (persistent
 // k_near).  ctr: 4 device words, zero before the first use; the kernels leave

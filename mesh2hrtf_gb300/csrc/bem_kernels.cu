@@ -31,6 +31,7 @@ __device__ __forceinline__ DevMesh to_dev(const DevMeshView &v) {
     m.n = v.n; m.nvert = v.nvert; m.v64 = v.v64; m.c64 = v.c64; m.n64 = v.n64;
     m.area64 = v.area64; m.sqa64 = v.sqa64; m.chi = v.chi; m.clo = v.clo; m.t32 = v.t32;
     m.q32 = v.q32; m.isqa32 = v.isqa32; m.n32 = v.n32;
+    m.sym = v.sym;
     return m;
 }
 
@@ -212,37 +213,100 @@ __device__ __forceinline__ cplx<T> col_adm(const DevFreq &f, int j, int bc) {
     return {(T)a.re, (T)a.im};
 }
 
+// ------------------------------------------------------------ symmetry images
+// Image tables (DevSym): one thread per (image, element).  The vertices go
+// through the reference's sequence of reflections (2 c - x per step, then the
+// node swap, NC_ReflectElement, NC_3dFunctions.cpp:357-452), so that each
+// image holds the coordinates the reference integrates over; the centre is
+// the global point at the local centre, as NC_GenerateSubelements computes
+// it for the level-0 test.
+__global__ void __launch_bounds__(256) k_image_tables(DevMeshView mv, ImageTables out) {
+    const DevMesh m = to_dev(mv);
+    const int n = m.n;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)(m.sym.nref - 1) * n) return;
+    const int k = (int)(t / n), j = (int)(t - (long long)k * n), kref = k + 1;
+    Elem64 e;
+    load_elem64(m, j, e);
+    double nr[3] = {m.n64[j], m.n64[n + j], m.n64[2 * n + j]};
+    for (int step = 1; step <= kref; ++step) {
+        const int d = m.sym.rdir[step];
+        const double c2 = 2.0 * m.sym.coord[d];
+        for (int a = 0; a < e.nv; ++a) e.p[a][d] = __dsub_rn(c2, e.p[a][d]);
+        nr[d] = -nr[d];
+        for (int q = 0; q < (e.nv == 4 ? 2 : 1); ++q)
+            for (int c = 0; c < 3; ++c) {
+                const double tmp = e.p[2 * q][c];
+                e.p[2 * q][c] = e.p[2 * q + 1][c];
+                e.p[2 * q + 1][c] = tmp;
+            }
+    }
+    const size_t nn = (size_t)n, ko = (size_t)k;
+    double *v64 = out.v64 + ko * 12 * nn, *c64 = out.c64 + ko * 3 * nn;
+    float *chi = out.chi + ko * 3 * nn, *clo = out.clo + ko * 3 * nn;
+    float *t32 = out.t32 + ko * 10 * nn, *q32 = out.q32 + ko * 12 * nn;
+    for (int a = 0; a < 4; ++a)
+        for (int c = 0; c < 3; ++c) v64[(3 * a + c) * nn + j] = a < e.nv ? e.p[a][c] : 0.0;
+    // local centre: (1 + 0 + 0) / 3 on triangles, 0 on quadrilaterals
+    const double sc = e.nv == 3 ? 1.0 / 3.0 : 0.0;
+    double cen[3];
+    global_point_exact(e, sc, sc, cen);
+    for (int c = 0; c < 3; ++c) {
+        c64[c * nn + j] = cen[c];
+        const float h = (float)cen[c];
+        chi[c * nn + j] = h;
+        clo[c * nn + j] = (float)(cen[c] - (double)h);
+    }
+    if (e.nv == 3) {
+        for (int c = 0; c < 3; ++c) {
+            t32[c * nn + j] = (float)(e.p[0][c] - e.p[2][c]);
+            t32[(3 + c) * nn + j] = (float)(e.p[1][c] - e.p[2][c]);
+            t32[(6 + c) * nn + j] = (float)nr[c];
+        }
+        t32[9 * nn + j] = m.t32[9 * nn + j];
+        for (int r = 0; r < 12; ++r) q32[r * nn + j] = 0.f;
+    } else {
+        for (int r = 0; r < 10; ++r) t32[r * nn + j] = 0.f;
+        for (int a = 0; a < 4; ++a)
+            for (int c = 0; c < 3; ++c) q32[(3 * a + c) * nn + j] = (float)(e.p[a][c] - cen[c]);
+    }
+}
+
 // ------------------------------------------------------------ near list
 // Pairs (row i, column j) that NumCalc integrates with subdivision (level-0
-// ratio distance/sqrt(area) < 1.3, exact FP64 test) plus the self pairs.
-// Depends on the geometry only, so it is built once per mesh.  Pass 1
-// (list == nullptr) counts, pass 2 fills; warp-aggregated atomics.
+// ratio distance/sqrt(area) < 1.3, exact FP64 test, for any image of j) plus
+// the self pairs.  Depends on the geometry only, so it is built once per
+// mesh.  Pass 1 (list == nullptr) counts, pass 2 fills; warp-aggregated
+// atomics.
 __global__ void __launch_bounds__(256) k_near_list(DevMeshView mv, int2 *list, unsigned long long *count) {
     const DevMesh m = to_dev(mv);
     const int lane = threadIdx.x, n = m.n;
     const int i = blockIdx.y * 8 + threadIdx.y;
     const int j = blockIdx.x * 32 + lane;
     if (i >= n) return;
-    bool near = false;
+    unsigned imask = 0;
     if (j < n) {
-        if (j == i) near = true;
-        else {
-            const float d0 = (m.chi[j] - m.chi[i]) + (m.clo[j] - m.clo[i]);
-            const float d1 = (m.chi[n + j] - m.chi[n + i]) + (m.clo[n + j] - m.clo[n + i]);
-            const float d2 = (m.chi[2 * n + j] - m.chi[2 * n + i]) + (m.clo[2 * n + j] - m.clo[2 * n + i]);
+        for (int kref = 0; kref < m.sym.nref; ++kref) {
+            if (kref == 0 && j == i) { imask |= 1u; continue; }
+            const DevMesh mk = image_mesh(m, kref);
+            const float d0 = (mk.chi[j] - m.chi[i]) + (mk.clo[j] - m.clo[i]);
+            const float d1 = (mk.chi[n + j] - m.chi[n + i]) + (mk.clo[n + j] - m.clo[n + i]);
+            const float d2 = (mk.chi[2 * n + j] - m.chi[2 * n + i]) + (mk.clo[2 * n + j] - m.clo[2 * n + i]);
             const float rf = sqrtf(d0 * d0 + d1 * d1 + d2 * d2) * m.isqa32[j];
             if (rf <= 1.3f * (1.0f + 1e-4f)) {
                 const double x[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
-                near = ratio0_exact(m, j, x) < kTolf;
+                if (ratio0_exact(mk, j, x) < kTolf) imask |= 1u << kref;
             }
         }
     }
+    const bool near = imask != 0;
     const unsigned mask = __ballot_sync(0xffffffffu, near);
     if (!mask) return;
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(mask));
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (near && list) list[base + __popc(mask & ((1u << lane) - 1u))] = make_int2(i, j);
+    if (near && list)
+        list[base + __popc(mask & ((1u << lane) - 1u))] = make_int2(i, j | (int)(imask << kNearColBits));
 }
 
 // ------------------------------------------------------------ regular pairs
@@ -271,10 +335,11 @@ __device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f
         for (int r = 0; r < kRowsPerThread; ++r) {
             const int i = i0 + r;
             if (i >= n) break;
-            if (i == j) continue;
+            // near and self entries: zero here, k_near adds their integrals
+            if (i == j) { A[(size_t)i * lda + j] = make_double2(0.0, 0.0); continue; }
             const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
             const double rd = ratio0_exact(m, j, x64);
-            if (rd < kTolf) continue;
+            if (rd < kTolf) { A[(size_t)i * lda + j] = make_double2(0.0, 0.0); continue; }
             const double nx64[3] = {m.n64[i], m.n64[n + i], m.n64[2 * n + i]};
             KVals<double> v = FarPair<double>::run(e, x64, nx64, gauss_order(rd), f.k, f.wr);
             const cplx<double> val = combine_entry(v, bcj, admj, PT);
@@ -298,7 +363,7 @@ __device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f
         for (int r = 0; r < kRowsPerThread; ++r) {
             const int i = i0 + r;
             if (i >= n) break;
-            if (i == j) continue;
+            if (i == j) { A[(size_t)i * lda + j] = make_float2(0.f, 0.f); continue; }
             for (int k = 0; k < 3; ++k) e.D[k] = (cjh[k] - m.chi[k * n + i]) + (cjl[k] - m.clo[k * n + i]);
             const float rf = sqrtf(e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * isq;
             bool near = false;
@@ -309,16 +374,102 @@ __device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f
                 near = rd < kTolf;
                 if (!near) order = gauss_order(rd);
             }
-            if (near) continue;
+            if (near) { A[(size_t)i * lda + j] = make_float2(0.f, 0.f); continue; }
             const float nx[3] = {m.n32[i], m.n32[n + i], m.n32[2 * n + i]};
             A[(size_t)i * lda + j] = far_entry_f(e, nx, order, fc);
         }
     }
 }
 
+// The same tile for a mesh with symmetry images: every entry sums the far
+// images of its column element (reflection factor applied, NC_AssembleTBEM,
+// NC_EquationSystem.cpp:181-206), in image order; near images and the self
+// pair are left to k_near, which adds them to the entry.
+template <typename T>
+__device__ __forceinline__ void far_tile_img(const DevMeshView &mv, const DevFreq &f,
+                                             typename Vec2<T>::type *__restrict__ A, size_t lda, int tx, int ty) {
+    const DevMesh m = to_dev(mv);
+    const int lane = threadIdx.x, n = m.n;
+    const int i0 = (ty * 8 + threadIdx.y) * kRowsPerThread;
+    const int j = tx * 32 + lane;
+    if (i0 >= n || j >= n) return;
+    Phys<T> PT;
+    if constexpr (std::is_same<T, double>::value) PT = {f.k, f.wr, f.tao, f.beta_im};
+    else PT = {f.kf, f.wrf, f.taof, f.beta_imf};
+    const int bcj = f.bc_type ? f.bc_type[j] : 0;
+    const cplx<T> admj = col_adm<T>(f, j, bcj);
+    T acc_re[kRowsPerThread], acc_im[kRowsPerThread];
+    for (int r = 0; r < kRowsPerThread; ++r) acc_re[r] = acc_im[r] = T(0);
+    for (int kref = 0; kref < m.sym.nref; ++kref) {
+        const DevMesh mk = image_mesh(m, kref);
+        const T sg = image_negated(m, kref) ? T(-1) : T(1);
+        if constexpr (std::is_same<T, double>::value) {
+            Elem64 e;
+            load_elem64(mk, j, e);
+            for (int r = 0; r < kRowsPerThread; ++r) {
+                const int i = i0 + r;
+                if (i >= n) break;
+                if (kref == 0 && i == j) continue;
+                const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
+                const double rd = ratio0_exact(mk, j, x64);
+                if (rd < kTolf) continue;
+                const double nx64[3] = {m.n64[i], m.n64[n + i], m.n64[2 * n + i]};
+                KVals<double> v = FarPair<double>::run(e, x64, nx64, gauss_order(rd), f.k, f.wr);
+                const cplx<double> val = combine_entry(v, bcj, admj, PT);
+                acc_re[r] += sg * val.re;
+                acc_im[r] += sg * val.im;
+            }
+        } else {
+            Elem32 e;
+            const float zero[3] = {0.f, 0.f, 0.f};
+            load_elem32(mk, j, zero, zero, e);
+            const float cjh[3] = {mk.chi[j], mk.chi[n + j], mk.chi[2 * n + j]};
+            const float cjl[3] = {mk.clo[j], mk.clo[n + j], mk.clo[2 * n + j]};
+            const float isq = m.isqa32[j];
+            FusedCol fc;
+            fc.bc = bcj;
+            fc.yr = admj.re;
+            fc.yi = admj.im;
+            fc.tau = PT.tao;
+            fc.b = PT.beta_im;
+            fc.k2 = PT.k * PT.k;
+            fc.wr = PT.wr;
+            for (int r = 0; r < kRowsPerThread; ++r) {
+                const int i = i0 + r;
+                if (i >= n) break;
+                if (kref == 0 && i == j) continue;
+                for (int k = 0; k < 3; ++k) e.D[k] = (cjh[k] - m.chi[k * n + i]) + (cjl[k] - m.clo[k * n + i]);
+                const float rf = sqrtf(e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * isq;
+                bool near = false;
+                int order = 2;
+                if (!classify_fast(rf, near, order)) {
+                    const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
+                    const double rd = ratio0_exact(mk, j, x64);
+                    near = rd < kTolf;
+                    if (!near) order = gauss_order(rd);
+                }
+                if (near) continue;
+                const float nx[3] = {m.n32[i], m.n32[n + i], m.n32[2 * n + i]};
+                const float2 v = far_entry_f(e, nx, order, fc);
+                acc_re[r] += sg * v.x;
+                acc_im[r] += sg * v.y;
+            }
+        }
+    }
+    for (int r = 0; r < kRowsPerThread; ++r) {
+        const int i = i0 + r;
+        if (i >= n) break;
+        typename Vec2<T>::type o;
+        o.x = acc_re[r];
+        o.y = acc_im[r];
+        A[(size_t)i * lda + j] = o;
+    }
+}
+
 // ONE: the batch holds a single system, whose table then stays in constant
-// operands instead of registers.
-template <typename T, bool ONE>
+// operands instead of registers.  IMG: some mesh of the batch has symmetry
+// images (meshes without take the plain tile).
+template <typename T, bool ONE, bool IMG>
 __global__ void __launch_bounds__(256, 3) k_far(const __grid_constant__ AsmBatch tb, unsigned *ctr) {
     __shared__ int item_s;
     const int total = tb.far_off[tb.B];
@@ -332,7 +483,10 @@ __global__ void __launch_bounds__(256, 3) k_far(const __grid_constant__ AsmBatch
         const AsmSys &S = tb.sys[ONE ? 0 : b];
         const int local = item - tb.far_off[b];
         const int ntx = (S.m.n + 31) / 32;
-        far_tile<T>(S.m, S.f, (typename Vec2<T>::type *)S.A, S.lda, local % ntx, local / ntx);
+        if (IMG && S.m.sym.nref > 1)
+            far_tile_img<T>(S.m, S.f, (typename Vec2<T>::type *)S.A, S.lda, local % ntx, local / ntx);
+        else
+            far_tile<T>(S.m, S.f, (typename Vec2<T>::type *)S.A, S.lda, local % ntx, local / ntx);
     }
     queue_exit(ctr);
 }
@@ -340,62 +494,74 @@ __global__ void __launch_bounds__(256, 3) k_far(const __grid_constant__ AsmBatch
 // ------------------------------------------------------------ near pairs
 // One warp per entry of the near list: the self pair by warp_singular (FP64,
 // plus NumCalc's free term), subdivided pairs by warp_subdivide with the
-// kernel arithmetic in T.
+// kernel arithmetic in T; with symmetry planes every image of the entry's
+// mask in image order.  The sum is added to the entry k_far wrote (its far
+// images, or zero).
 template <typename T>
 __device__ __forceinline__ void near_pair(const DevMeshView &mv, const DevFreq &f, int2 ij,
                                           typename Vec2<T>::type *__restrict__ A, size_t lda, int *status,
                                           WarpScratch &ws) {
     const DevMesh m = to_dev(mv);
     const int lane = threadIdx.x, n = m.n;
-    const int i = ij.x, j = ij.y;
+    const int i = ij.x, j = ij.y & kMaxElements;
+    const unsigned imask = (unsigned)ij.y >> kNearColBits;
     const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
     const double nx64[3] = {m.n64[i], m.n64[n + i], m.n64[2 * n + i]};
     Phys<double> P{f.k, f.wr, f.tao, f.beta_im};
     Phys<T> PT{(T)f.k, (T)f.wr, (T)f.tao, (T)f.beta_im};
     const int bcj = f.bc_type ? f.bc_type[j] : 0;
-    Elem64 e;
-    load_elem64(m, j, e);
-    cplx<T> entry;
+    cplx<T> sum = {T(0), T(0)};
     int err = kDevOk;
-    if (i == j) {
-        SingOut so = warp_singular(e, x64, nx64, P, 0, nullptr);
-        cplx<double> a = combine_entry(so.v, bcj, col_adm<double>(f, j, bcj), P);
-        // free term, NC_EquationSystem.cpp:220-231
-        const cplx<double> beta = {0.0, P.beta_im};
-        if (bcj == 1) a += beta * (-(0.5 * P.tao));
-        else a += (col_adm<double>(f, j, bcj) * beta - cplx<double>{1.0, 0.0}) * 0.5;
-        entry = {(T)a.re, (T)a.im};
-    } else if constexpr (std::is_same<T, double>::value) {
-        AsmSink<double> sink;
-        sink.e = &e; sink.x = x64; sink.nx = nx64; sink.k = f.k; sink.wr = f.wr;
-        sink.init();
-        err = warp_subdivide(e, m.area64[j], x64, ws, sink);
-        KVals<double> v = sink.reduce();
-        entry = combine_entry(v, bcj, col_adm<double>(f, j, bcj), PT);
-    } else {
-        const float xhi[3] = {m.chi[i], m.chi[n + i], m.chi[2 * n + i]};
-        const float xlo[3] = {m.clo[i], m.clo[n + i], m.clo[2 * n + i]};
-        const float nx32[3] = {(float)nx64[0], (float)nx64[1], (float)nx64[2]};
-        Elem32 e32;
-        load_elem32(m, j, xhi, xlo, e32);
-        AsmSink<float> sink;
-        sink.e = &e32; sink.nx = nx32; sink.k = PT.k; sink.wr = PT.wr;
-        sink.init();
-        err = warp_subdivide(e, m.area64[j], x64, ws, sink);
-        KVals<float> v = sink.reduce();
-        entry = combine_entry(v, bcj, col_adm<float>(f, j, bcj), PT);
+    for (int kref = 0; kref < 8; ++kref) {
+        if (!((imask >> kref) & 1u)) continue;
+        const DevMesh mk = image_mesh(m, kref);
+        Elem64 e;
+        load_elem64(mk, j, e);
+        cplx<T> entry;
+        if (kref == 0 && i == j) {
+            SingOut so = warp_singular(e, x64, nx64, P, 0, nullptr);
+            cplx<double> a = combine_entry(so.v, bcj, col_adm<double>(f, j, bcj), P);
+            // free term, NC_EquationSystem.cpp:220-231
+            const cplx<double> beta = {0.0, P.beta_im};
+            if (bcj == 1) a += beta * (-(0.5 * P.tao));
+            else a += (col_adm<double>(f, j, bcj) * beta - cplx<double>{1.0, 0.0}) * 0.5;
+            entry = {(T)a.re, (T)a.im};
+        } else if constexpr (std::is_same<T, double>::value) {
+            AsmSink<double> sink;
+            sink.e = &e; sink.x = x64; sink.nx = nx64; sink.k = f.k; sink.wr = f.wr;
+            sink.init();
+            const int rc = warp_subdivide(e, m.area64[j], x64, ws, sink);
+            if (rc != kDevOk) err = rc;
+            KVals<double> v = sink.reduce();
+            entry = combine_entry(v, bcj, col_adm<double>(f, j, bcj), PT);
+        } else {
+            const float xhi[3] = {m.chi[i], m.chi[n + i], m.chi[2 * n + i]};
+            const float xlo[3] = {m.clo[i], m.clo[n + i], m.clo[2 * n + i]};
+            const float nx32[3] = {(float)nx64[0], (float)nx64[1], (float)nx64[2]};
+            Elem32 e32;
+            load_elem32(mk, j, xhi, xlo, e32);
+            AsmSink<float> sink;
+            sink.e = &e32; sink.nx = nx32; sink.k = PT.k; sink.wr = PT.wr;
+            sink.init();
+            const int rc = warp_subdivide(e, m.area64[j], x64, ws, sink);
+            if (rc != kDevOk) err = rc;
+            KVals<float> v = sink.reduce();
+            entry = combine_entry(v, bcj, col_adm<float>(f, j, bcj), PT);
+        }
+        if (image_negated(m, kref)) entry = entry * T(-1);
+        sum += entry;
     }
     if (lane == 0) {
-        typename Vec2<T>::type o;
-        o.x = entry.re;
-        o.y = entry.im;
+        typename Vec2<T>::type o = A[(size_t)i * lda + j];
+        o.x += sum.re;
+        o.y += sum.im;
         A[(size_t)i * lda + j] = o;
         if (err != kDevOk) atomicMax(status, err);
     }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_near(const __grid_constant__ AsmBatch tb, unsigned *ctr) {
+__global__ void __launch_bounds__(256, 2) k_near(const __grid_constant__ AsmBatch tb, unsigned *ctr) {
     __shared__ WarpScratch ws_all[8];
     WarpScratch &ws = ws_all[threadIdx.y];
     const int total = tb.near_off[tb.B];
@@ -413,42 +579,71 @@ __global__ void __launch_bounds__(256) k_near(const __grid_constant__ AsmBatch t
     queue_exit(ctr);
 }
 
+// Images of the incident waves in the symmetry planes: step kref reflects a
+// plane-wave direction (negates one component) or a point source (2 c - x)
+// across the plane normal to axis rdir[kref]; the reflection factor of image
+// kref is the element images' (NC_ReflectPointVector, NC_3dFunctions.cpp:181-242).
+__device__ __forceinline__ void reflect_source(const DevSym &sy, int kref, double v[3], bool point) {
+    const int d = sy.rdir[kref];
+    if (point) v[d] = __dsub_rn(2.0 * sy.coord[d], v[d]);
+    else v[d] = -v[d];
+}
+
+// Plane waves take their phase at x minus the positions of the planes
+// present (NC_EquationSystem.cpp:1743-1748, NC_PostProcessing.cpp:794-799).
+__device__ __forceinline__ void plane_wave_origin(const DevSym &sy, const double x[3], double xs[3]) {
+    for (int k = 0; k < 3; ++k) xs[k] = ((sy.axes >> k) & 1u) ? x[k] - sy.coord[k] : x[k];
+}
+
 // Incident waves at a collocation point (NC_IncidentWaveRHS,
-// NC_EquationSystem.cpp:1731-1812), without symmetry planes.
-__device__ cplx<double> incident_rhs(const DevFreq &f, const double x[3], const double nx[3]) {
+// NC_EquationSystem.cpp:1731-1812), with their symmetry-plane images.
+__device__ cplx<double> incident_rhs(const DevSym &sy, const DevFreq &f, const double x[3], const double nx[3]) {
     cplx<double> zrc = {0.0, 0.0};
     const cplx<double> bt = {0.0, f.beta_im * f.tao};
+    double xs[3];
+    plane_wave_origin(sy, x, xs);
     for (int s = 0; s < f.n_plane; ++s) {
-        const double *d = f.pw_dir + 3 * s;
+        double d[3] = {f.pw_dir[3 * s], f.pw_dir[3 * s + 1], f.pw_dir[3 * s + 2]};
         const cplx<double> amp = ld_c(f.pw_amp, s);
-        const double ph = (d[0] * x[0] + d[1] * x[1] + d[2] * x[2]) * f.wr;
-        double sn, cs;
-        sincos(ph, &sn, &cs);
-        const cplx<double> zg = cplx<double>{cs, sn} * amp;
-        const double re1 = f.wr * (d[0] * nx[0] + d[1] * nx[1] + d[2] * nx[2]);
-        const cplx<double> zv = {-zg.im * re1, zg.re * re1};
-        zrc -= zg + zv * bt;
+        for (int kref = 0; kref < sy.nref; ++kref) {
+            if (kref > 0) reflect_source(sy, kref, d, false);
+            const double rf = ((sy.rneg >> kref) & 1u) ? -1.0 : 1.0;
+            const double ph = (d[0] * xs[0] + d[1] * xs[1] + d[2] * xs[2]) * f.wr;
+            double sn, cs;
+            sincos(ph, &sn, &cs);
+            const cplx<double> zg = cplx<double>{cs * rf, sn * rf} * amp;
+            const double re1 = f.wr * (d[0] * nx[0] + d[1] * nx[1] + d[2] * nx[2]);
+            const cplx<double> zv = {-zg.im * re1, zg.re * re1};
+            zrc -= zg + zv * bt;
+        }
     }
     for (int s = 0; s < f.n_point; ++s) {
-        const double *p = f.ps_xyz + 3 * s;
+        double p[3] = {f.ps_xyz[3 * s], f.ps_xyz[3 * s + 1], f.ps_xyz[3 * s + 2]};
         const cplx<double> amp = ld_c(f.ps_amp, s);
-        double d[3] = {x[0] - p[0], x[1] - p[1], x[2] - p[2]};
-        const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-        d[0] /= r; d[1] /= r; d[2] /= r;
-        double sn, cs;
-        sincos(f.wr * r, &sn, &cs);
-        const double re2 = 1.0 / kPI4 / r;
-        const cplx<double> zg = cplx<double>{cs * re2, sn * re2} * amp;
-        const double re1 = d[0] * nx[0] + d[1] * nx[1] + d[2] * nx[2];
-        const cplx<double> zv = cplx<double>{-re1 / r, f.wr * re1} * zg;
-        zrc -= zg + zv * bt;
+        for (int kref = 0; kref < sy.nref; ++kref) {
+            if (kref > 0) reflect_source(sy, kref, p, true);
+            const double rf = ((sy.rneg >> kref) & 1u) ? -1.0 : 1.0;
+            double d[3] = {x[0] - p[0], x[1] - p[1], x[2] - p[2]};
+            const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            d[0] /= r; d[1] /= r; d[2] /= r;
+            double sn, cs;
+            sincos(f.wr * r, &sn, &cs);
+            const double re2 = rf / kPI4 / r;
+            const cplx<double> zg = cplx<double>{cs * re2, sn * re2} * amp;
+            const double re1 = d[0] * nx[0] + d[1] * nx[1] + d[2] * nx[2];
+            const cplx<double> zv = cplx<double>{-re1 / r, f.wr * re1} * zg;
+            zrc -= zg + zv * bt;
+        }
     }
     return zrc;
 }
 
 // Right-hand side, one warp per row (FP64): free term of the prescribed value
 // (NC_EquationSystem.cpp:233-244), incident waves, and the columns whose
-// prescribed values are nonzero (Zrsintel[4], NC_EquationSystem.cpp:188-198).
+// prescribed values are nonzero (Zrsintel[4], NC_EquationSystem.cpp:188-198),
+// each with all its images: nodal values in the image's node order, velocity
+// values negated with the reflection factor, no factor on the term itself
+// (NC_ReflectElement, NC_3dFunctions.cpp:410-415; NC_AssembleTBEM).
 __global__ void __launch_bounds__(256) k_rhs(const __grid_constant__ AsmBatch tb) {
     __shared__ WarpScratch ws_all[8];
     const int sb = find_sys(tb.rhs_off, tb.B, blockIdx.x);
@@ -476,29 +671,35 @@ __global__ void __launch_bounds__(256) k_rhs(const __grid_constant__ AsmBatch tb
         zbvi = {zbvi.re / (double)nv, zbvi.im / (double)nv};
         if (bci != 1) z0 += ((zbvi * beta) * f.tao) * 0.5;
         else z0 += (zbvi * f.tao) * 0.5;
-        if (f.n_plane + f.n_point > 0) z0 += incident_rhs(f, x, nx);
+        if (f.n_plane + f.n_point > 0) z0 += incident_rhs(m.sym, f, x, nx);
     }
     int err = kDevOk;
     for (int c = 0; c < f.n_bc_cols; ++c) {
         const int jc = f.bc_cols[c];
         const int bcj = f.bc_type ? f.bc_type[jc] : 0;
-        Elem64 e;
-        load_elem64(m, jc, e);
-        cplx<double> bc[4];
-        for (int a = 0; a < 4; ++a) bc[a] = a < e.nv ? ld_c(f.bc_val, a * n + jc) : cplx<double>{0.0, 0.0};
-        cplx<double> contrib;
-        if (jc == i) {
-            SingOut so = warp_singular(e, x, nx, P, bcj == 1 ? 2 : 1, bc);
-            contrib = so.rhs;
-        } else {
-            RhsSink sink;
-            sink.e = &e; sink.x = x; sink.nx = nx; sink.bc = bc; sink.bctype = bcj == 1 ? 1 : 0; sink.P = P;
-            sink.init();
-            const int rc = warp_subdivide(e, m.area64[jc], x, ws, sink);
-            if (rc != kDevOk) err = rc;
-            contrib = sink.reduce();
+        const int nvj = m.nvert[jc];
+        for (int kref = 0; kref < m.sym.nref; ++kref) {
+            const DevMesh mk = image_mesh(m, kref);
+            Elem64 e;
+            load_elem64(mk, jc, e);
+            const double vs = (bcj != 1 && image_negated(m, kref)) ? -1.0 : 1.0;
+            cplx<double> bc[4];
+            for (int a = 0; a < 4; ++a)
+                bc[a] = a < nvj ? ld_c(f.bc_val, image_node(a, kref, nvj) * n + jc) * vs : cplx<double>{0.0, 0.0};
+            cplx<double> contrib;
+            if (kref == 0 && jc == i) {
+                SingOut so = warp_singular(e, x, nx, P, bcj == 1 ? 2 : 1, bc);
+                contrib = so.rhs;
+            } else {
+                RhsSink sink;
+                sink.e = &e; sink.x = x; sink.nx = nx; sink.bc = bc; sink.bctype = bcj == 1 ? 1 : 0; sink.P = P;
+                sink.init();
+                const int rc = warp_subdivide(e, m.area64[jc], x, ws, sink);
+                if (rc != kDevOk) err = rc;
+                contrib = sink.reduce();
+            }
+            if (lane == 0) z0 += contrib;
         }
-        if (lane == 0) z0 += contrib;
     }
     if (lane == 0) {
         b[i] = make_double2(z0.re, z0.im);
@@ -546,10 +747,35 @@ __global__ void __launch_bounds__(256) k_fields(const __grid_constant__ ProjBatc
     ivi[j] = any;
 }
 
-// Field projection, one warp per point: lanes sweep the elements 32 at a time;
-// regular pairs in the lane, subdivided pairs by the whole warp.
+// Element data of image kref for the projection: potential and nodal
+// velocities times the reflection factor, velocities in the image's node
+// order (NC_ContributionTBEM, NC_PostProcessing.cpp:925-940).
 template <typename T>
-__global__ void __launch_bounds__(256) k_project(const __grid_constant__ ProjBatch tb) {
+__device__ __forceinline__ void proj_elem_data(const double2 *phi, const double2 *vel, const float2 *phi32,
+                                               const float2 *vel32, int n, int j, int nv, bool iv, int kref,
+                                               bool neg, cplx<T> &ph, cplx<T> vl[4]) {
+    const T sg = neg ? T(-1) : T(1);
+    if constexpr (std::is_same<T, double>::value) {
+        ph = cplx<T>{phi[j].x, phi[j].y} * sg;
+        for (int a = 0; a < 4; ++a) {
+            const int src = image_node(a, kref, nv);
+            vl[a] = (iv && a < nv) ? cplx<T>{vel[src * n + j].x, vel[src * n + j].y} * sg : cplx<T>{0, 0};
+        }
+    } else {
+        const float2 p2 = phi32[j];
+        ph = cplx<T>{p2.x, p2.y} * sg;
+        for (int a = 0; a < 4; ++a) {
+            const float2 v2 = (iv && a < nv) ? vel32[image_node(a, kref, nv) * n + j] : make_float2(0.f, 0.f);
+            vl[a] = cplx<T>{v2.x, v2.y} * sg;
+        }
+    }
+}
+
+// Field projection, one warp per point: lanes sweep the elements (and their
+// symmetry images) 32 at a time; regular pairs in the lane, subdivided pairs
+// by the whole warp.
+template <typename T>
+__global__ void __launch_bounds__(256, 2) k_project(const __grid_constant__ ProjBatch tb) {
     __shared__ WarpScratch ws_all[8];
     const int sb = find_sys(tb.pt_off, tb.B, blockIdx.x);
     const ProjSys &S = tb.sys[sb];
@@ -577,111 +803,96 @@ __global__ void __launch_bounds__(256) k_project(const __grid_constant__ ProjBat
     acc.p = acc.g[0] = acc.g[1] = acc.g[2] = cmk(T(0), T(0));
     const T k = (T)f.k, wr = (T)f.wr;
     int err = kDevOk;
-    for (int base = 0; base < n; base += 32) {
-        const int j = base + lane;
-        const bool valid = j < n;
-        bool near = false;
-        int order = 2;
-        if (valid) {
-            // element data in T (float copies for the float path: no FP64 conversions)
-            const bool iv = ivi[j] != 0;
-            cplx<T> ph, vl[4];
-            if constexpr (std::is_same<T, double>::value) {
-                ph = {phi[j].x, phi[j].y};
-                for (int a = 0; a < 4; ++a) vl[a] = iv ? cplx<T>{vel[a * n + j].x, vel[a * n + j].y} : cplx<T>{0, 0};
-            } else {
-                const float2 p2 = phi32[j];
-                ph = {p2.x, p2.y};
-                for (int a = 0; a < 4; ++a) {
-                    const float2 v2 = iv ? vel32[a * n + j] : make_float2(0.f, 0.f);
-                    vl[a] = {v2.x, v2.y};
-                }
-            }
-            if constexpr (std::is_same<T, double>::value) {
-                const double rd = ratio0_exact(m, j, x64);
-                near = rd < kTolf;
-                if (!near) {
-                    order = gauss_order(rd);
-                    Elem64 e;
-                    load_elem64(m, j, e);
-                    const int np = e.nv == 3 ? tri_count(order) : quad_count(order);
-                    for (int g = 0; g < np; ++g) {
-                        double s, t, wq;
-                        sub_point(e.nv, order, g, 0.0, 0.0, 1.0, s, t, wq);
-                        QPoint<double> q;
-                        map_point(e, s, t, x64, wq, q);
-                        proj_point(q, ph, vl, e.nv, iv, k, wr, acc);
-                    }
-                }
-            } else {
-                Elem32 e;
-                load_elem32(m, j, xhi, xlo, e);
-                const float dist = sqrtf(e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]);
-                if (!classify_fast(dist * m.isqa32[j], near, order)) {
-                    const double rd = ratio0_exact(m, j, x64);
+    for (int kref = 0; kref < m.sym.nref; ++kref) {
+        const DevMesh mk = image_mesh(m, kref);
+        const bool neg = image_negated(m, kref);
+        for (int base = 0; base < n; base += 32) {
+            const int j = base + lane;
+            const bool valid = j < n;
+            bool near = false;
+            int order = 2;
+            if (valid) {
+                // element data in T (float copies for the float path: no FP64 conversions)
+                const bool iv = ivi[j] != 0;
+                const int nv = m.nvert[j];
+                cplx<T> ph, vl[4];
+                proj_elem_data<T>(phi, vel, phi32, vel32, n, j, nv, iv, kref, neg, ph, vl);
+                if constexpr (std::is_same<T, double>::value) {
+                    const double rd = ratio0_exact(mk, j, x64);
                     near = rd < kTolf;
-                    if (!near) order = gauss_order(rd);
-                }
-                if (!near) {
-                    const int np = e.nv == 3 ? tri_count(order) : quad_count(order);
-                    for (int g = 0; g < np; ++g) {
-                        float s, t, wq;
-                        if (e.nv == 3) {
-                            const int o = tri_offset(order) + g;
-                            s = c_trif[o][0]; t = c_trif[o][1]; wq = c_trif[o][2];
-                        } else {
-                            const int a = g / order, b = g - a * order;
-                            s = c_glxf[order][a]; t = c_glxf[order][b];
-                            wq = c_glwf[order][a] * c_glwf[order][b];
+                    if (!near) {
+                        order = gauss_order(rd);
+                        Elem64 e;
+                        load_elem64(mk, j, e);
+                        const int np = e.nv == 3 ? tri_count(order) : quad_count(order);
+                        for (int g = 0; g < np; ++g) {
+                            double s, t, wq;
+                            sub_point(e.nv, order, g, 0.0, 0.0, 1.0, s, t, wq);
+                            QPoint<double> q;
+                            map_point(e, s, t, x64, wq, q);
+                            proj_point(q, ph, vl, e.nv, iv, k, wr, acc);
                         }
-                        QPoint<float> q;
-                        map_point(e, s, t, wq, q);
-                        proj_point(q, ph, vl, e.nv, iv, k, wr, acc);
+                    }
+                } else {
+                    Elem32 e;
+                    load_elem32(mk, j, xhi, xlo, e);
+                    const float dist = sqrtf(e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]);
+                    if (!classify_fast(dist * m.isqa32[j], near, order)) {
+                        const double rd = ratio0_exact(mk, j, x64);
+                        near = rd < kTolf;
+                        if (!near) order = gauss_order(rd);
+                    }
+                    if (!near) {
+                        const int np = e.nv == 3 ? tri_count(order) : quad_count(order);
+                        for (int g = 0; g < np; ++g) {
+                            float s, t, wq;
+                            if (e.nv == 3) {
+                                const int o = tri_offset(order) + g;
+                                s = c_trif[o][0]; t = c_trif[o][1]; wq = c_trif[o][2];
+                            } else {
+                                const int a = g / order, b = g - a * order;
+                                s = c_glxf[order][a]; t = c_glxf[order][b];
+                                wq = c_glwf[order][a] * c_glwf[order][b];
+                            }
+                            QPoint<float> q;
+                            map_point(e, s, t, wq, q);
+                            proj_point(q, ph, vl, e.nv, iv, k, wr, acc);
+                        }
                     }
                 }
             }
-        }
-        unsigned todo = __ballot_sync(0xffffffffu, valid && near);
-        while (todo) {
-            const int L = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const int jl = base + L;
-            Elem64 e;
-            load_elem64(m, jl, e);
-            const bool iv = ivi[jl] != 0;
-            cplx<T> ph, vl[4];
-            if constexpr (std::is_same<T, double>::value) {
-                ph = {phi[jl].x, phi[jl].y};
-                for (int a = 0; a < 4; ++a) vl[a] = {vel[a * n + jl].x, vel[a * n + jl].y};
-            } else {
-                const float2 p2 = phi32[jl];
-                ph = {p2.x, p2.y};
-                for (int a = 0; a < 4; ++a) {
-                    const float2 v2 = vel32[a * n + jl];
-                    vl[a] = {v2.x, v2.y};
+            unsigned todo = __ballot_sync(0xffffffffu, valid && near);
+            while (todo) {
+                const int L = __ffs(todo) - 1;
+                todo &= todo - 1;
+                const int jl = base + L;
+                Elem64 e;
+                load_elem64(mk, jl, e);
+                const bool iv = ivi[jl] != 0;
+                cplx<T> ph, vl[4];
+                proj_elem_data<T>(phi, vel, phi32, vel32, n, jl, e.nv, true, kref, neg, ph, vl);
+                ProjAcc<T> r;
+                int rc;
+                if constexpr (std::is_same<T, double>::value) {
+                    ProjSink<double> sink;
+                    sink.e = &e; sink.x = x64; sink.phi = ph; sink.vel = vl; sink.ivi = iv; sink.k = k; sink.wr = wr;
+                    sink.init();
+                    rc = warp_subdivide(e, m.area64[jl], x64, ws, sink);
+                    r = sink.reduce();
+                } else {
+                    Elem32 e32;
+                    load_elem32(mk, jl, xhi, xlo, e32);
+                    ProjSink<float> sink;
+                    sink.e = &e32; sink.phi = ph; sink.vel = vl; sink.ivi = iv; sink.k = k; sink.wr = wr;
+                    sink.init();
+                    rc = warp_subdivide(e, m.area64[jl], x64, ws, sink);
+                    r = sink.reduce();
                 }
-            }
-            ProjAcc<T> r;
-            int rc;
-            if constexpr (std::is_same<T, double>::value) {
-                ProjSink<double> sink;
-                sink.e = &e; sink.x = x64; sink.phi = ph; sink.vel = vl; sink.ivi = iv; sink.k = k; sink.wr = wr;
-                sink.init();
-                rc = warp_subdivide(e, m.area64[jl], x64, ws, sink);
-                r = sink.reduce();
-            } else {
-                Elem32 e32;
-                load_elem32(m, jl, xhi, xlo, e32);
-                ProjSink<float> sink;
-                sink.e = &e32; sink.phi = ph; sink.vel = vl; sink.ivi = iv; sink.k = k; sink.wr = wr;
-                sink.init();
-                rc = warp_subdivide(e, m.area64[jl], x64, ws, sink);
-                r = sink.reduce();
-            }
-            if (rc != kDevOk) err = rc;
-            if (lane == 0) {
-                acc.p += r.p;
-                for (int kk = 0; kk < 3; ++kk) acc.g[kk] += r.g[kk];
+                if (rc != kDevOk) err = rc;
+                if (lane == 0) {
+                    acc.p += r.p;
+                    for (int kk = 0; kk < 3; ++kk) acc.g[kk] += r.g[kk];
+                }
             }
         }
     }
@@ -694,31 +905,43 @@ __global__ void __launch_bounds__(256) k_project(const __grid_constant__ ProjBat
             sp = sp * f.tao;
             for (int kk = 0; kk < 3; ++kk) sg[kk] = sg[kk] * f.tao;
         }
-        // incident field (NC_ContributionIncidentWaves, NC_PostProcessing.cpp:776-866)
+        // incident field with its images (NC_ContributionIncidentWaves,
+        // NC_PostProcessing.cpp:776-866)
         if (f.n_plane || f.n_point) {
+            const DevSym &sy = m.sym;
+            double xs[3];
+            plane_wave_origin(sy, x64, xs);
             for (int s = 0; s < f.n_plane; ++s) {
-                const double *d = f.pw_dir + 3 * s;
+                double d[3] = {f.pw_dir[3 * s], f.pw_dir[3 * s + 1], f.pw_dir[3 * s + 2]};
                 const cplx<double> amp = ld_c(f.pw_amp, s);
-                double sn, cs;
-                sincos((d[0] * x64[0] + d[1] * x64[1] + d[2] * x64[2]) * f.wr, &sn, &cs);
-                const cplx<double> zg = cplx<double>{cs, sn} * amp;
-                sp += zg;
-                const cplx<double> zv = {-zg.im * f.wr, zg.re * f.wr};
-                for (int kk = 0; kk < 3; ++kk) sg[kk] += zv * d[kk];
+                for (int kref = 0; kref < sy.nref; ++kref) {
+                    if (kref > 0) reflect_source(sy, kref, d, false);
+                    const double rf = ((sy.rneg >> kref) & 1u) ? -1.0 : 1.0;
+                    double sn, cs;
+                    sincos((d[0] * xs[0] + d[1] * xs[1] + d[2] * xs[2]) * f.wr, &sn, &cs);
+                    const cplx<double> zg = cplx<double>{cs * rf, sn * rf} * amp;
+                    sp += zg;
+                    const cplx<double> zv = {-zg.im * f.wr, zg.re * f.wr};
+                    for (int kk = 0; kk < 3; ++kk) sg[kk] += zv * d[kk];
+                }
             }
             for (int s = 0; s < f.n_point; ++s) {
-                const double *q = f.ps_xyz + 3 * s;
+                double q[3] = {f.ps_xyz[3 * s], f.ps_xyz[3 * s + 1], f.ps_xyz[3 * s + 2]};
                 const cplx<double> amp = ld_c(f.ps_amp, s);
-                double d[3] = {x64[0] - q[0], x64[1] - q[1], x64[2] - q[2]};
-                const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-                d[0] /= r; d[1] /= r; d[2] /= r;
-                double sn, cs;
-                sincos(f.wr * r, &sn, &cs);
-                const double re2 = 1.0 / kPI4 / r;
-                const cplx<double> zg = cplx<double>{cs * re2, sn * re2} * amp;
-                sp += zg;
-                const cplx<double> zv = cplx<double>{-1.0 / r, f.wr} * zg;
-                for (int kk = 0; kk < 3; ++kk) sg[kk] += zv * d[kk];
+                for (int kref = 0; kref < sy.nref; ++kref) {
+                    if (kref > 0) reflect_source(sy, kref, q, true);
+                    const double rf = ((sy.rneg >> kref) & 1u) ? -1.0 : 1.0;
+                    double d[3] = {x64[0] - q[0], x64[1] - q[1], x64[2] - q[2]};
+                    const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                    d[0] /= r; d[1] /= r; d[2] /= r;
+                    double sn, cs;
+                    sincos(f.wr * r, &sn, &cs);
+                    const double re2 = rf / kPI4 / r;
+                    const cplx<double> zg = cplx<double>{cs * re2, sn * re2} * amp;
+                    sp += zg;
+                    const cplx<double> zv = cplx<double>{-1.0 / r, f.wr} * zg;
+                    for (int kk = 0; kk < 3; ++kk) sg[kk] += zv * d[kk];
+                }
             }
         }
         pot[p] = make_double2(sp.re, sp.im);
@@ -835,6 +1058,14 @@ cudaError_t init_device_tables() {
     return e;
 }
 
+cudaError_t launch_image_tables(const DevMeshView &m, const ImageTables &out, cudaStream_t st) {
+    const long long total = (long long)(m.sym.nref - 1) * m.n;
+    if (total <= 0) return cudaSuccess;
+    count_launches(1);
+    k_image_tables<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(m, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long *count, cudaStream_t st) {
     dim3 block(32, 8), grid((m.n + 31) / 32, (m.n + 7) / 8);
     count_launches(1);
@@ -844,7 +1075,9 @@ cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long lon
 
 void asm_batch_finish(AsmBatch &t) {
     t.far_off[0] = t.near_off[0] = t.rhs_off[0] = 0;
+    t.img = 0;
     for (int b = 0; b < t.B; ++b) {
+        if (t.sys[b].m.sym.nref > 1) t.img = 1;
         const int n = t.sys[b].m.n;
         const int nt = (n + 31) / 32;
         t.far_off[b + 1] = t.far_off[b] + nt * ((n + 8 * kRowsPerThread - 1) / (8 * kRowsPerThread));
@@ -884,12 +1117,22 @@ cudaError_t launch_assemble(const AsmBatch &t, int prec, unsigned *ctr, cudaStre
     count_launches(near_items ? 2 : 1);
     const bool one = t.B == 1;
     if (prec == 0) {
-        if (one) k_far<double, true><<<gfar, block, 0, st>>>(t, ctr);
-        else k_far<double, false><<<gfar, block, 0, st>>>(t, ctr);
+        if (t.img) {
+            if (one) k_far<double, true, true><<<gfar, block, 0, st>>>(t, ctr);
+            else k_far<double, false, true><<<gfar, block, 0, st>>>(t, ctr);
+        } else {
+            if (one) k_far<double, true, false><<<gfar, block, 0, st>>>(t, ctr);
+            else k_far<double, false, false><<<gfar, block, 0, st>>>(t, ctr);
+        }
         if (near_items) k_near<double><<<gnear, block, 0, st>>>(t, ctr + 2);
     } else {
-        if (one) k_far<float, true><<<gfar, block, 0, st>>>(t, ctr);
-        else k_far<float, false><<<gfar, block, 0, st>>>(t, ctr);
+        if (t.img) {
+            if (one) k_far<float, true, true><<<gfar, block, 0, st>>>(t, ctr);
+            else k_far<float, false, true><<<gfar, block, 0, st>>>(t, ctr);
+        } else {
+            if (one) k_far<float, true, false><<<gfar, block, 0, st>>>(t, ctr);
+            else k_far<float, false, false><<<gfar, block, 0, st>>>(t, ctr);
+        }
         if (near_items) k_near<float><<<gnear, block, 0, st>>>(t, ctr + 2);
     }
     return cudaGetLastError();

@@ -39,17 +39,20 @@ struct bem_mesh_s {
     float *d_n32 = nullptr;
     int2 *d_near = nullptr;         // pairs integrated with subdivision + self pairs
     long long n_near = 0;
+    bem::DevSym sym{};              // symmetry-plane images (sym.nref = 1: none)
+    void *d_img = nullptr;          // one allocation holding the image tables
     bem::DevMeshView view() const {
         bem::DevMeshView v;
         v.n = n; v.nvert = d_nvert; v.v64 = d_v64; v.c64 = d_c64; v.n64 = d_n64; v.area64 = d_area;
         v.sqa64 = d_sqa; v.chi = d_chi; v.clo = d_clo; v.t32 = d_t32; v.q32 = d_q32; v.isqa32 = d_isqa;
         v.n32 = d_n32;
+        v.sym = sym;
         return v;
     }
     ~bem_mesh_s() {
         cudaFree(d_nvert); cudaFree(d_v64); cudaFree(d_c64); cudaFree(d_n64); cudaFree(d_area);
         cudaFree(d_sqa); cudaFree(d_chi); cudaFree(d_clo); cudaFree(d_t32); cudaFree(d_q32); cudaFree(d_isqa);
-        cudaFree(d_near); cudaFree(d_n32);
+        cudaFree(d_near); cudaFree(d_n32); cudaFree(d_img);
     }
 };
 

@@ -160,8 +160,6 @@ int run(int istart, int iend, bool estimate_ram, bool check_normals, int niterma
         nc::dump_tables(p, dump);
         return 0;
     }
-    if (p.n_sym > 0)
-        throw nc::NcExit{"symmetry planes are not supported by the GPU solver (NC.inp Main Parameters I, token 4)", 1};
     time(&ltim[2]);
 
     // boundary mesh and evaluation points for the device
@@ -198,7 +196,15 @@ int run(int istart, int iend, bool estimate_ram, bool check_normals, int niterma
         const char *dev_env = std::getenv("NUMCALC_GB300_DEVICE");
         bem_status st = bem_set_device(dev_env ? std::atoi(dev_env) : 0);
         if (st != BEM_OK) gpu_fail(out, "CUDA device", st);
-        bem_mesh_desc md{N, p.n_nodes, p.node_xyz.data(), conn.data(), nvert.data(), cen.data(), nor.data(), area.data()};
+        bem_mesh_desc md{N, p.n_nodes, p.node_xyz.data(), conn.data(), nvert.data(), cen.data(), nor.data(), area.data(),
+                         {0, 0, 0}, {0.0, 0.0, 0.0}};
+        // symmetry planes back to their NC.inp codes (the parser holds the
+        // reference's internal 1 / -1 / 2 / -2, NC_Input.cpp:474-487)
+        for (int k = 0; k < 3 && p.n_sym > 0; ++k) {
+            const int c = p.sym_planes[k];
+            md.sym_planes[k] = c == 1 ? 1 : c == -1 ? 2 : c == 2 ? 3 : c == -2 ? 4 : 0;
+            md.sym_coords[k] = p.sym_coords[k];
+        }
         st = bem_mesh_create(&md, &gpu.mesh);
         if (st != BEM_OK) gpu_fail(out, "mesh upload", st);
         bem_solver_params sp{};
