@@ -33,6 +33,7 @@ EXPORTED = [
     "bem_assemble", "bem_solve", "bem_get_solution", "bem_get_system", "bem_project",
     "bem_solve_frequency", "bem_project_static", "bem_solve_batch", "bem_solve_multi", "bem_footprint_multi",
     "bem_server_create", "bem_server_submit", "bem_server_wait", "bem_server_destroy",
+    "bem_mesh_footprint_bytes", "bem_device_memory",
 ]
 STATIC_MAX_ELEMENTS = 32768
 
@@ -108,6 +109,9 @@ def load(build_if_missing: bool = True):
     lib.bem_footprint_bytes.restype = C.c_double
     lib.bem_footprint_multi.argtypes = [i32, i32, i32, i32]
     lib.bem_footprint_multi.restype = C.c_double
+    lib.bem_mesh_footprint_bytes.argtypes = [i32, i32]
+    lib.bem_mesh_footprint_bytes.restype = C.c_double
+    lib.bem_device_memory.argtypes = [i32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.bem_solve_multi.argtypes = [vp, i32, vp, i32, vp, vp, vp, vp, vp]
     lib.bem_mesh_create.argtypes = [C.POINTER(MeshDesc), C.POINTER(vp)]
     lib.bem_mesh_destroy.argtypes = [vp]
@@ -128,7 +132,7 @@ def load(build_if_missing: bool = True):
     lib.bem_server_destroy.argtypes = [vp]
     for name in EXPORTED:
         if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes", "bem_footprint_multi",
-                        "bem_kernel_launches"):
+                        "bem_kernel_launches", "bem_mesh_footprint_bytes"):
             getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -382,3 +386,14 @@ class Server:
 
 def footprint_bytes(n_elem, precision=PREC_MIXED, restart=0):
     return load().bem_footprint_bytes(n_elem, precision, restart)
+
+
+def mesh_footprint_bytes(n_elem, n_sym_planes=0):
+    return load().bem_mesh_footprint_bytes(n_elem, n_sym_planes)
+
+
+def device_memory(device=0):
+    """(free, total) bytes of a device."""
+    fr, tot = C.c_double(), C.c_double()
+    _check(load().bem_device_memory(device, C.byref(fr), C.byref(tot)))
+    return fr.value, tot.value

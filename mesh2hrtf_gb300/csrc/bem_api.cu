@@ -605,6 +605,29 @@ double bem_footprint_multi(int32_t n_elem, int32_t precision, int32_t restart, i
     return (double)bem::solver_layout(std::max(n_elem, 1), prec, m, true, nullptr, nullptr, std::max(n_rhs, 1));
 }
 
+double bem_mesh_footprint_bytes(int32_t n_elem, int32_t n_sym_planes) {
+    const int n = std::max(n_elem, 1);
+    const int nref = 1 << std::min(std::max(n_sym_planes, 0), 3);
+    // element tables: 1 + 12 + 3 + 3 + 1 + 1 words of 8 B, 3 + 3 + 10 + 12 + 1 + 3 of 4 B
+    const double tables = (double)n * (4.0 + 20.0 * 8.0 + 32.0 * 4.0);
+    const double near = (double)n * 48.0 * sizeof(int2);
+    return tables + (double)bem::image_table_bytes(n, nref) + near;
+}
+
+bem_status bem_device_memory(int32_t device, double *free_bytes, double *total_bytes) {
+    if (!free_bytes || !total_bytes) return fail(BEM_ERR_INVALID, "null argument");
+    int cur = 0;
+    CU(cudaGetDevice(&cur));
+    CU(cudaSetDevice(device));
+    size_t fr = 0, tot = 0;
+    const cudaError_t e = cudaMemGetInfo(&fr, &tot);
+    cudaSetDevice(cur);
+    if (e != cudaSuccess) return fail(BEM_ERR_CUDA, "cudaMemGetInfo: %s", cudaGetErrorString(e));
+    *free_bytes = (double)fr;
+    *total_bytes = (double)tot;
+    return BEM_OK;
+}
+
 bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
     if (!d || !out) return fail(BEM_ERR_INVALID, "null argument");
     *out = nullptr;

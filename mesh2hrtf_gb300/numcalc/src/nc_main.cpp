@@ -36,6 +36,8 @@ using nc::cd;
 namespace {
 
 const mode_t kDirMode = S_IRUSR | S_IWUSR | S_IXUSR | S_IRGRP | S_IWGRP | S_IXGRP | S_IROTH | S_IXOTH;
+// Device memory a CUDA context of this process takes (MemoryGPU.txt).
+constexpr double kContextBytes = 0.6e9;
 
 void stamp(std::ostream &o, const char *what, const tm *d) {
     o << what << d->tm_mday << "/" << d->tm_mon + 1 << "/" << d->tm_year + 1900 << " " << d->tm_hour << ":"
@@ -142,8 +144,13 @@ int run(int istart, int iend, bool estimate_ram, bool check_normals, int niterma
         std::ofstream &out) {
     time_t ltim[7];
     time_t lti_eqa = 0, lti_sol = 0, lti_pos = 0;
-    std::ofstream est;
-    if (estimate_ram) est.open("Memory.txt");
+    std::ofstream est, est_gpu;
+    if (estimate_ram) {
+        est.open("Memory.txt");
+        // the same steps with this build's device memory per process, for
+        // GPU-aware scheduling (mesh2hrtf_gb300/manage_numcalc.py)
+        est_gpu.open("MemoryGPU.txt");
+    }
     time(&ltim[0]);
     FILE *inp = std::fopen("NC.inp", "r");
     if (!inp) throw nc::NcExit{"No input file found!", 1};
@@ -253,6 +260,10 @@ int run(int istart, int iend, bool estimate_ram, bool check_normals, int niterma
             const double gb = (double)(nint * sizeof(int) + ncmplx * 16) / 1000.0 / 1000.0 / 1000.0;
             std::cout << "RAM Estimation: " << gb << " GByte\n";
             est << step + 1 << " " << f << " " << gb << "\n";
+            // device: solver + mesh + evaluation points + a CUDA context
+            const double dev = bem_footprint_bytes(N, prec, 0) + bem_mesh_footprint_bytes(N, p.n_sym) +
+                               88.0 * (double)ev_nodes.size() + kContextBytes;
+            est_gpu << step + 1 << " " << f << " " << dev / 1e9 << "\n";
             continue;
         }
         nc::FreqState fs;

@@ -82,3 +82,28 @@ def test_istart_iend_keeps_other_steps(numcalc, tmp_path):
     assert os.path.exists(os.path.join(wd, "be.out", "be.2", "pEvalGrid"))
     out = open(os.path.join(wd, "NC1-1.out")).read()
     assert "Step 1," in out and "Step 2," not in out
+
+
+def test_manage_numcalc_runs_every_step_on_the_gpu(numcalc, tmp_path):
+    """The GPU-aware scheduler on a two-source project: both sources' steps
+    run as drop-in processes under device-memory admission, and every step's
+    be.out equals the reference's (source 1 is the sphere80 fixture)."""
+    from mesh2hrtf_gb300 import manage_numcalc as mn
+    c = gc.load("sphere80")
+    ps = c["point_sources"]
+    sh = [c.pts[:24], c.pts[24:]]
+    p = project.Project(root=str(tmp_path / "p"), nodes=c.nodes, elems=c.elems, eval_points=c.pts,
+                        eval_elems=meshes.shells_triangles(sh), freqs=list(c.freqs),
+                        point_sources=[tuple(ps[0])], boundary=["ELEM 0 TO 79 VELO 0.0 -1 0.0 -1"])
+    project.write_project(p, "source_1")
+    p.point_sources = [(-0.4, 0.2, 0.1, 1.0, 0.0)]
+    wd2 = project.write_project(p, "source_2")
+    open(os.path.join(str(tmp_path / "p"), "parameters.json"), "w").write("{}")
+    mn.manage_numcalc(str(tmp_path / "p"), numcalc, max_hbm_load=20.0, steps_per_instance=1, wait_time=0.05)
+    wd1 = os.path.join(str(tmp_path / "p"), "NumCalc", "source_1")
+    for s in range(1, len(c.freqs) + 1):
+        assert "End time:" in open(os.path.join(wd1, "NC%d-%d.out" % (s, s))).read()
+        ids, vals = project.read_result(os.path.join(wd1, "be.out", "be.%d" % s, "pEvalGrid"))
+        assert gc.rel_err(vals, c["s%d_pEvalGrid" % s]) < 1e-5
+        assert os.path.isfile(os.path.join(wd2, "be.out", "be.%d" % s, "pEvalGrid"))
+    assert os.path.isfile(os.path.join(wd1, "MemoryGPU.txt"))
