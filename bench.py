@@ -19,10 +19,11 @@ e2e       the same as value through the C ABI with host buffers: every step
 fp64      the plain FP64 GPU path on one batch of the same frequencies (also
           batched), with the mixed path's relative L2 boundary-pressure error
           against it.
-roofline  the dominant kernel (the complex64 matrix-vector product of the
-          solve), algorithmic bytes N^2*8 + 2*N*16 per product and system over
-          the CUDA-event time of the product launches, against the measured
-          HBM copy bandwidth.
+roofline  the dominant kernel (the matrix-vector products of the solve:
+          Krylov products from the fp16 copy of A, algorithmic bytes
+          N^2*4 + 2*N*16 per product and system; refinement residuals from
+          the complex64 matrix, N^2*8 + 2*N*16) over the CUDA-event time of
+          the product launches, against the measured HBM copy bandwidth.
 cpu_baseline  the FP64 C restatement of the reference path (oracle/, the
           "port") on the host cores, on a bounded sample: 2048 rows of the
           assembly, the dense matrix-vector product of those rows and 256
@@ -50,9 +51,9 @@ RHO, C0 = 1.21, 343.0
 N_TRI = 20480
 SEED = 20261204
 METRIC = "freq solves/s at <=1e-4 rel err, mixed vs plain FP64 GPU BEM; p50/p99 latency"
-# DRAM bytes (read + write) of one complex64 product at N = 20480, measured by
-# ncu on this workload: 3.3566 GB read + 13.2 MB of row partials written
-MV_TRAFFIC = 3.3698e9
+# DRAM bytes (read + write) of one Krylov product from the fp16 copy at
+# N = 20480, measured by ncu on this workload (k_mv_tma launch list)
+MV_TRAFFIC = 1.6863e9
 
 
 def workload():
@@ -263,14 +264,19 @@ def main():
     total_solves = args.steps * B * world
     value = total_solves / elapsed
 
-    # roofline of the dominant kernel: the complex64 matvec.  Each launch of
-    # the batched product covers every system still iterating; its bytes are
-    # counted per system and product (N^2*8 + 2*N*16), its time is the
-    # CUDA-event time of the launches inside the iteration bodies.
-    bytes_one = n * n * 8.0 + 2 * n * 16.0
+    # roofline of the dominant kernel: the matrix-vector products.  Each
+    # launch of the batched product covers every system still iterating; its
+    # bytes are counted per system and product (Krylov products read the fp16
+    # copy, N^2*4 + 2*N*16; refinement residuals the complex64 matrix,
+    # N^2*8 + 2*N*16), its time is the CUDA-event time of the launches inside
+    # the iteration bodies.
+    bytes_krylov = n * n * 4.0 + 2 * n * 16.0
+    bytes_resid = n * n * 8.0 + 2 * n * 16.0
     mv_ms = sum(step[0]["matvec_ms"] for step in infos)
     n_mv = sum(i["n_matvec"] for step in infos for i in step)
-    achieved = bytes_one * n_mv / (mv_ms / 1000.0) / 1e9 if mv_ms > 0 else None
+    n_kry = sum(i["iterations"] for step in infos for i in step)
+    mv_bytes = bytes_krylov * n_kry + bytes_resid * (n_mv - n_kry)
+    achieved = mv_bytes / (mv_ms / 1000.0) / 1e9 if mv_ms > 0 else None
     asm_ms = sum(step[0]["assemble_ms"] for step in infos)
     solve_ms = sum(step[0]["solve_ms"] for step in infos)
     proj_ms = sum(step[0]["project_ms"] for step in infos)
@@ -338,7 +344,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1000.0, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP32 assembly/matvec, FP64 singular + refinement)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (fp16 Krylov copy of A, complex64 residual matrix, FP64 singular terms + refinement)",
         "data": "synthetic", "config": cfg,
         "latency_ms": {"p50": float(np.percentile(lat, 50) * 1000), "p99": float(np.percentile(lat, 99) * 1000),
                        "mode": "one solve at a time (bem_solve_frequency), same frequencies"},
@@ -348,12 +354,14 @@ def main():
         "stage_ms_per_solve": {"assemble": asm_ms / n_solves, "solve": solve_ms / n_solves,
                                "project": proj_ms / n_solves, "matvec": mv_ms / n_solves,
                                "iterations": float(np.mean(iters))},
-        "roofline": {"bound": "hbm", "kernel": "k_mv<c64> (batched complex64 A x)", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "k_mv_tma (batched A x: fp16 Krylov copy, complex64 residuals)",
+                     "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if achieved else None,
                      "traffic": MV_TRAFFIC if n == N_TRI else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per k_mv_tma<0> launch, "
-                                       "same N (profiles/k_mv_tma_head20480.md)",
-                     "bytes_per_product": bytes_one, "products": n_mv,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per Krylov k_mv_tma<0> "
+                                       "launch from the fp16 copy, same N (profiles/k_mv_tma_fp16_head20480.md)",
+                     "bytes_per_krylov_product": bytes_krylov, "bytes_per_residual_product": bytes_resid,
+                     "krylov_products": n_kry, "residual_products": n_mv - n_kry,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),

@@ -108,6 +108,12 @@ typedef struct {
                                   1: none                                      */
     int32_t n_rhs;             /* right-hand sides the solver can hold for
                                   bem_solve_multi (0 or 1: one; at most 16)    */
+    int32_t complex64_krylov;  /* mixed precision with one right-hand side:
+                                  0 (default) the Krylov products read an fp16
+                                  copy of A (row-scaled; 4 bytes per entry,
+                                  +50 % matrix memory) and the refinement
+                                  residuals the complex64 matrix; 1 every
+                                  product reads the complex64 matrix          */
 } bem_solver_params;
 
 typedef struct {

@@ -61,7 +61,7 @@ class FreqDesc(C.Structure):
 class SolverParams(C.Structure):
     _fields_ = [("precision", C.c_int32), ("restart", C.c_int32), ("max_iter", C.c_int32),
                 ("tol", C.c_double), ("hbm_budget_bytes", C.c_double), ("no_precond", C.c_int32),
-                ("n_rhs", C.c_int32)]
+                ("n_rhs", C.c_int32), ("complex64_krylov", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -215,18 +215,20 @@ class Solver:
     """bem_solver_t: matrix + Krylov workspace for one mesh on the device."""
 
     def __init__(self, mesh: Mesh, precision=PREC_FP64, restart=0, max_iter=0, tol=0.0, hbm_budget=0.0,
-                 precond=True, n_rhs=1):
+                 precond=True, n_rhs=1, complex64_krylov=False):
+        """complex64_krylov: mixed precision without the fp16 Krylov copy of A."""
         lib = load()
         self.mesh = mesh
         self.n = mesh.n
-        p = SolverParams(precision, restart, max_iter, tol, hbm_budget, 0 if precond else 1, n_rhs)
+        p = SolverParams(precision, restart, max_iter, tol, hbm_budget, 0 if precond else 1, n_rhs,
+                         1 if complex64_krylov else 0)
         h = C.c_void_p()
         _check(lib.bem_solver_create(mesh.handle, C.byref(p), C.byref(h)))
         self.handle = h
         self.info = SolveInfo()
 
     def set_params(self, max_iter=0, tol=0.0):
-        p = SolverParams(0, 0, max_iter, tol, 0.0, 0, 0)
+        p = SolverParams(0, 0, max_iter, tol, 0.0, 0, 0, 0)
         _check(load().bem_solver_set_params(self.handle, C.byref(p)))
 
     def assemble(self, freq: Frequency):

@@ -133,7 +133,7 @@ namespace bem {
 // entries) receives right-hand sides 1..n_rhs-1, whose shared fields repeat
 // those of *o.
 size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, SolverBufs *o, int n_rhs,
-                     SolverBufs *extra) {
+                     SolverBufs *extra, bool half_copy) {
     size_t off = 0;
     auto take = [&](size_t bytes) -> void * {
         void *p = base ? (void *)(base + off) : nullptr;
@@ -144,6 +144,10 @@ size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, Solve
     const size_t esz = prec == 0 ? 16 : 8;
     SolverBufs d;
     d.A = take(N * lda * esz);
+    if (prec != 0 && n_rhs == 1 && half_copy) {
+        d.A16 = take(N * lda * 4);
+        d.rs = (float *)take(N * 4);
+    }
     if (pc) {
         const size_t pb = precond_bytes(n, prec);
         d.Minv = take(prec == 0 ? pb / 2 : pb);
@@ -405,8 +409,36 @@ bem_status assemble_group(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned *
     return first;
 }
 
+// fp16 copies of the complex64 matrices that have one (SplitBatch).
+cudaError_t split_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
+    std::unique_ptr<bem::SplitBatch> t(new bem::SplitBatch());
+    t->B = 0;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < cnt && e == cudaSuccess; ++i) {
+        const bem::SolverBufs &d = ss[i]->d;
+        if (!d.A16) continue;
+        bem::SplitSys &q = t->sys[t->B++];
+        q.A = d.A;
+        q.lda = ss[i]->lda;
+        q.n = ss[i]->n;
+        q.A16 = d.A16;
+        q.rs = d.rs;
+        if (t->B == bem::kMaxAsm) {
+            bem::split_batch_finish(*t);
+            e = bem::launch_split16(*t, st);
+            t->B = 0;
+        }
+    }
+    if (e == cudaSuccess && t->B > 0) {
+        bem::split_batch_finish(*t);
+        e = bem::launch_split16(*t, st);
+    }
+    return e;
+}
+
 bem_status precond_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
     const int prec = ss[0]->prec;
+    CU(split_group(ss, cnt, st));
     std::unique_ptr<bem::PcBatch> pt(new bem::PcBatch());
     std::vector<bem_solver_t> pcs;
     for (int i = 0; i < cnt; ++i) {
@@ -866,7 +898,8 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     const int prec = prm.precision == BEM_PREC_FP64 ? 0 : 1;
     const int n_rhs = prm.n_rhs > 0 ? prm.n_rhs : 1;
     if (n_rhs > bem::kMaxRhs) return fail(BEM_ERR_INVALID, "n_rhs %d above the limit %d", n_rhs, bem::kMaxRhs);
-    const size_t need = bem::solver_layout(n, prec, m, pc, nullptr, nullptr, n_rhs);
+    const bool half = prm.complex64_krylov == 0;
+    const size_t need = bem::solver_layout(n, prec, m, pc, nullptr, nullptr, n_rhs, nullptr, half);
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
     double budget = prm.hbm_budget_bytes > 0 ? prm.hbm_budget_bytes : (double)free_b - 1.0e9;
@@ -891,7 +924,7 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
         s->n_rhs = n_rhs;
         s->xr.resize(n_rhs - 1);
         s->xfreq.resize(n_rhs - 1);
-        bem::solver_layout(n, prec, m, pc, s->block, &s->d, n_rhs, s->xr.data());
+        bem::solver_layout(n, prec, m, pc, s->block, &s->d, n_rhs, s->xr.data(), half);
         e = cudaMemset(s->d.ctr, 0, 4 * sizeof(unsigned));
     }
     if (e != cudaSuccess)
@@ -925,8 +958,10 @@ bem_status bem_assemble(bem_solver_t s, const bem_frequency_desc *f) {
 // computed residual r = b - A x, so with BEM_PREC_MIXED every cycle is one
 // step of iterative refinement: the inner Arnoldi process (FP64 vectors,
 // classical Gram-Schmidt with one re-orthogonalisation, FP64 inner products)
-// uses the FP32 matrix-vector product and stops once it has gained five
-// digits, and the outer residual is evaluated with error-free products.
+// uses the FP32 product with the fp16 copy of A (or with the complex64 matrix)
+// and stops once it has gained three (five) digits; the outer residual is
+// evaluated from the complex64 matrix, with error-free products in the first
+// cycle and as r -= A d afterwards.
 bem_status bem_solve(bem_solver_t s, bem_solve_info *info) {
     if (!s) return fail(BEM_ERR_INVALID, "null solver");
     if (!s->have_freq) return fail(BEM_ERR_INVALID, "bem_solve before bem_assemble");

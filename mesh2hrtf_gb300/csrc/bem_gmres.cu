@@ -35,6 +35,7 @@
 // Inner products are summed in a fixed order (per block, then over blocks in
 // block order, every block computing the same sums), so results are
 // deterministic run to run.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -62,6 +63,27 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = a + b;
     const float bb = s - a;
     e = (a - (s - bb)) + (b - bb);
+}
+
+// Warp sums in FP32.  GB300's FP64 pipe is narrow (a warp instruction
+// occupies it for many cycles), so the products reduce their row sums in
+// FP32 and convert once per row; the butterfly leaves the same value on every
+// lane (a + b == b + a).
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// Float-float pairs (s, e): two-sum at every level, about twice-FP32 accurate.
+__device__ __forceinline__ void warp_sum_ff(float &s, float &e) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, o), e2 = __shfl_xor_sync(0xffffffffu, e, o);
+        float t, u;
+        two_sum(s, s2, t, u);
+        s = t;
+        e = (e + e2) + u;
+    }
 }
 __device__ __forceinline__ void acc_exact(float &s, float &e, float a, float b) {
     const float p = a * b;
@@ -115,7 +137,8 @@ __device__ void plan_build(KTable *tb, int which) {
     int c = 0;
     if (t < tb->B) {
         const KSys &S = tb->sys[t];
-        if (!S.shared && mv_active(S.st, which, tb->prec)) c = mv_items_of(S.n, tb->prec);
+        if (!S.shared && mv_active(S.st, which, tb->prec))
+            c = (which == 0 && S.A16) ? mv_items16(S.n) : mv_items_of(S.n, tb->prec);
     }
     cnt[t] = c;
     act[t] = c > 0;
@@ -234,20 +257,34 @@ __global__ void __launch_bounds__(256, 4) k_mv64(KTable *tb, int kind) {
 // each, one cp.async.bulk per segment) into shared memory; the chunk of x
 // (float hi parts, or hi/lo pairs for the refinement residual) goes into one
 // of two x buffers.  mbarriers carry the byte counts (full) and the
-// consumers' releases (empty).  Consumer warp w takes row w of a stage.
+// consumers' releases (empty).  Consumer warp w < 8 takes row w of a stage.
+// Krylov products of systems with an fp16 copy of A (KSys::A16) stream that
+// copy instead, with items of two column chunks so that row segments stay
+// 8 KB (the number of bulk copies an SM completes per second, not their
+// size, limits 4 KB segments); consumer warp w takes row w & 7 over chunk
+// w >> 3 of the item and scales its sum by the row's power-of-two scale.
 // Every wait is bounded (kWaitCycles); on expiry the kernel sets tb->err,
 // lets its own copies land and returns.
 constexpr int kTmaStages = 3;
-constexpr int kTmaConsumers = 8;
-static_assert(kTmaConsumers == kTmaRows, "one consumer warp per row of a stage");
+constexpr int kTmaConsumers = 16;
+static_assert(kTmaConsumers == 2 * kTmaRows, "one consumer warp per (row, chunk) of an fp16 stage");
 constexpr long long kWaitCycles = 4000000000LL;   // about 2 s at 2 GHz
 constexpr int kStageBytes = kTmaRows * kMvChunk * 8;   // 64 KB
 
 struct TmaMeta {
-    int b, chunk, row0, nrows, len, first, last, xslot;
+    int b, chunk, row0, nrows, len, first, last, xslot, h;
 };
+static_assert(kTmaRows * 2 * kMvChunk * 4 == kStageBytes, "an fp16 stage (two chunks) fills the stage buffer");
 
-__host__ __device__ constexpr int tma_x_bytes(bool exact) { return kMvChunk * (exact ? 16 : 8); }
+__device__ __forceinline__ float2 h2f(unsigned u) {
+    __half2 h;
+    *reinterpret_cast<unsigned *>(&h) = u;
+    return __half22float2(h);
+}
+
+// x buffers: hi/lo pairs of one chunk (refinement residual) or hi parts of
+// two chunks (fp16 Krylov items)
+__host__ __device__ constexpr int tma_x_bytes(bool) { return kMvChunk * 16; }
 __host__ __device__ constexpr int tma_smem_bytes(bool exact) {
     return kTmaStages * kStageBytes + 2 * tma_x_bytes(exact) + 256;
 }
@@ -317,75 +354,98 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
     plan_load(tb->plan[kind], pl);   // includes a block barrier
     int *err = &tb->err;
     if (warp == kTmaConsumers) {
-        // ---------------- producer (one lane)
-        if (lane != 0) return;
+        // ---------------- producer warp: lane 0 takes the items and keeps the
+        // barriers, lane r issues the bulk copy of row r of a stage (one
+        // thread issuing every copy caps the copy rate below HBM speed for
+        // the 4 KB fp16 segments)
+        const unsigned kAll = 0xffffffffu;
         const int total = pl.off[pl.n];
         int stage = 0, xs = 0;
         uint32_t eph = 1, xeph[2] = {1, 1};   // a fresh barrier's previous phase counts as complete
         int issued[kTmaStages] = {0, 0, 0};   // stage holds copies not yet seen complete by us
         uint32_t fph[kTmaStages] = {0, 0, 0};
         bool ok = true;
-        while (ok) {
-            if (total == 0) break;
-            const int item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+        while (ok && total > 0) {
+            int item = 0;
+            if (lane == 0) item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+            item = __shfl_sync(kAll, item, 0);
             if (item >= total) break;
             const int j = plan_find(pl.off, pl.n, item);
             const int sb = pl.sys[j], local = item - pl.off[j];
             const KSys &S = tb->sys[sb];
             const int n = S.n;
-            const int chunk = local % S.nchunk, strip = local / S.nchunk;
-            const int c0 = chunk * kMvChunk, len = min(kMvChunk, n - c0), lenp = (len + 1) & ~1;
+            const bool h = !EXACT && kind == 0 && S.A16 != nullptr;   // fp16 copy of A
+            const int span = h ? 2 * kMvChunk : kMvChunk;              // columns per item
+            const int nblk = h ? (S.nchunk + 1) / 2 : S.nchunk;
+            const int blk = local % nblk, strip = local / nblk;
+            const int chunk = h ? 2 * blk : blk;                       // first chunk of the item
+            const int c0 = blk * span, len = min(span, n - c0), lenp = (len + 1) & ~1;
             const int rbase = strip * kTmaStrip;
-            const int nst = min(kTmaStrip / kTmaRows, (n - rbase + kTmaRows - 1) / kTmaRows);
+            const int rps = kTmaRows;
+            const int nst = min(kTmaStrip / rps, (n - rbase + rps - 1) / rps);
+            // bytes per row segment: fp16 copies move whole 16-byte groups of 4 entries
+            const uint32_t seg = h ? (uint32_t)(((len + 3) & ~3) * 4) : (uint32_t)(lenp * 8);
+            const uint32_t pitch = kMvChunk * 8;
+            const size_t lda = (size_t)S.lda;
+            const unsigned char *abase = h ? (const unsigned char *)S.A16 : (const unsigned char *)S.A;
+            const size_t esz = h ? 4 : 8;
             // x chunk
-            if (!mbar_wait(xempty0 + 8 * xs, xeph[xs], err)) { ok = false; break; }
+            int w = 1;
+            if (lane == 0) w = mbar_wait(xempty0 + 8 * xs, xeph[xs], err);
+            if (!__shfl_sync(kAll, w, 0)) { ok = false; break; }
             xeph[xs] ^= 1;
-            const uint32_t xdst = smem_u32(xbuf + xs * tma_x_bytes(EXACT));
-            if (EXACT) {
-                mbar_expect_tx(xfull0 + 8 * xs, kMvChunk * 16);
-                bulk_g2s(xdst, S.xf + c0, kMvChunk * 16, xfull0 + 8 * xs);
-            } else {
-                mbar_expect_tx(xfull0 + 8 * xs, lenp * 8);
-                bulk_g2s(xdst, S.xh + c0, lenp * 8, xfull0 + 8 * xs);
+            if (lane == 0) {
+                const uint32_t xdst = smem_u32(xbuf + xs * tma_x_bytes(EXACT));
+                if (EXACT) {
+                    mbar_expect_tx(xfull0 + 8 * xs, kMvChunk * 16);
+                    bulk_g2s(xdst, S.xf + c0, kMvChunk * 16, xfull0 + 8 * xs);
+                } else {
+                    mbar_expect_tx(xfull0 + 8 * xs, lenp * 8);
+                    bulk_g2s(xdst, S.xh + c0, lenp * 8, xfull0 + 8 * xs);
+                }
             }
-            const float2 *A = (const float2 *)S.A;
-            for (int g = 0; g < nst && ok; ++g) {
-                if (!mbar_wait(empty0 + 8 * stage, eph, err)) { ok = false; break; }
-                const int row0 = rbase + g * kTmaRows, nrows = min(kTmaRows, n - row0);
-                TmaMeta mt;
-                mt.b = sb; mt.chunk = chunk; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
-                mt.first = g == 0; mt.last = g == nst - 1; mt.xslot = xs;
-                meta[stage] = mt;
-                mbar_expect_tx(full0 + 8 * stage, (uint32_t)(nrows * lenp * 8));
-                const uint32_t dst = smem_u32(ring + stage * kStageBytes);
-                for (int r = 0; r < nrows; ++r)
-                    bulk_g2s(dst + r * kMvChunk * 8, A + (size_t)(row0 + r) * S.lda + c0, lenp * 8,
-                             full0 + 8 * stage);
+            for (int g = 0; g < nst; ++g) {
+                if (lane == 0) w = mbar_wait(empty0 + 8 * stage, eph, err);
+                if (!__shfl_sync(kAll, w, 0)) { ok = false; break; }
+                const int row0 = rbase + g * rps, nrows = min(rps, n - row0);
+                if (lane == 0) {
+                    TmaMeta mt;
+                    mt.b = sb; mt.chunk = chunk; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
+                    mt.first = g == 0; mt.last = g == nst - 1; mt.xslot = xs; mt.h = h;
+                    meta[stage] = mt;
+                    mbar_expect_tx(full0 + 8 * stage, (uint32_t)nrows * seg);
+                }
+                __syncwarp();
+                if (lane < nrows)
+                    bulk_g2s(smem_u32(ring + stage * kStageBytes) + lane * pitch,
+                             abase + ((size_t)(row0 + lane) * lda + c0) * esz, seg, full0 + 8 * stage);
                 issued[stage] = 1;
                 fph[stage] ^= 1;
                 if (++stage == kTmaStages) { stage = 0; eph ^= 1; }
             }
             xs ^= 1;
         }
-        if (ok) {
-            // sentinel: consumers stop at the next stage
-            if (mbar_wait(empty0 + 8 * stage, eph, err)) {
-                meta[stage].b = -1;
-                mbar_arrive(full0 + 8 * stage);
-            } else {
-                ok = false;
+        if (lane == 0) {
+            if (ok) {
+                // sentinel: consumers stop at the next stage
+                if (mbar_wait(empty0 + 8 * stage, eph, err)) {
+                    meta[stage].b = -1;
+                    mbar_arrive(full0 + 8 * stage);
+                } else {
+                    ok = false;
+                }
             }
-        }
-        if (!ok) {
-            // a wait gave up: let this block's copies land before leaving
-            for (int s = 0; s < kTmaStages; ++s)
-                if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
-        }
-        __threadfence();
-        if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
-            tb->mv_ctr[0] = 0u;
-            tb->mv_ctr[1] = 0u;
+            if (!ok) {
+                // a wait gave up: let this block's copies land before leaving
+                for (int s = 0; s < kTmaStages; ++s)
+                    if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
+            }
             __threadfence();
+            if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
+                tb->mv_ctr[0] = 0u;
+                tb->mv_ctr[1] = 0u;
+                __threadfence();
+            }
         }
         return;
     }
@@ -401,7 +461,86 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
             if (!mbar_wait(xfull0 + 8 * mt.xslot, xph[mt.xslot], err)) return;
         }
         const unsigned char *xb = xbuf + mt.xslot * tma_x_bytes(EXACT);
-        if (warp < mt.nrows) {
+        // this warp's row sum as float-float (hi, lo) pairs of the real and
+        // imaginary parts, written after the stage is released
+        float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f);
+        int nout = 0;
+        float sca = 1.f;
+        bool released = false;   // stage handed back before the arithmetic
+        if (!EXACT && mt.h) {
+            // fp16: row w & 7 over the item's chunk w >> 3.  The warp copies its
+            // 4 KB of A into registers and releases the stage at once, so the
+            // slot refills while it computes; two accumulators per component
+            // (even / odd entries) shorten the dependency chains.
+            const int r = warp & (kTmaRows - 1), half = warp >> 3;
+            const int len = mt.len - half * kMvChunk;   // columns of this chunk
+            const bool act = r < mt.nrows && len > 0;
+            const int len2 = act ? min(len, kMvChunk) >> 1 : 0;
+            const uint2 *Aa = reinterpret_cast<const uint2 *>(ring + stage * kStageBytes + r * kMvChunk * 8 +
+                                                              half * kMvChunk * 4);
+            const bool full = len2 == kMvChunk / 2;   // whole chunk: no guards
+            uint2 av[kMvChunk / 64];
+            if (full) {
+#pragma unroll
+                for (int q = 0; q < kMvChunk / 64; ++q) av[q] = Aa[lane + 32 * q];
+            } else {
+#pragma unroll
+                for (int q = 0; q < kMvChunk / 64; ++q) {
+                    const int c = lane + 32 * q;
+                    av[q] = c < len2 ? Aa[c] : make_uint2(0u, 0u);
+                }
+            }
+            unsigned atail = 0u;
+            const bool tail = act && len < kMvChunk && (len & 1);
+            if (tail && lane == 0) atail = reinterpret_cast<const unsigned *>(Aa)[len - 1];
+            // every lane's loads have returned before the warp passes the
+            // barrier (the value below needs them), so the slot may be refilled
+            unsigned dep = atail;
+#pragma unroll
+            for (int q = 0; q < kMvChunk / 64; ++q) dep |= av[q].x | av[q].y;
+            asm volatile("" ::"r"(dep));
+            __syncwarp();
+            if (lane == 0) mbar_arrive(empty0 + 8 * stage);
+            released = true;
+            if (act) {
+                sca = S.rs[mt.row0 + r];
+                const float4 *x4 = reinterpret_cast<const float4 *>(xb + half * kMvChunk * 8);
+                float ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
+                if (full) {
+#pragma unroll
+                    for (int q = 0; q < kMvChunk / 64; ++q) {
+                        const float4 xv = x4[lane + 32 * q];
+                        const float2 a0 = h2f(av[q].x), a1 = h2f(av[q].y);
+                        ar = fmaf(a0.x, xv.x, ar); ar = fmaf(-a0.y, xv.y, ar);
+                        ai = fmaf(a0.x, xv.y, ai); ai = fmaf(a0.y, xv.x, ai);
+                        br = fmaf(a1.x, xv.z, br); br = fmaf(-a1.y, xv.w, br);
+                        bi = fmaf(a1.x, xv.w, bi); bi = fmaf(a1.y, xv.z, bi);
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < kMvChunk / 64; ++q) {
+                        const int c = lane + 32 * q;
+                        if (c < len2) {
+                            const float4 xv = x4[c];
+                            const float2 a0 = h2f(av[q].x), a1 = h2f(av[q].y);
+                            ar = fmaf(a0.x, xv.x, ar); ar = fmaf(-a0.y, xv.y, ar);
+                            ai = fmaf(a0.x, xv.y, ai); ai = fmaf(a0.y, xv.x, ai);
+                            br = fmaf(a1.x, xv.z, br); br = fmaf(-a1.y, xv.w, br);
+                            bi = fmaf(a1.x, xv.w, bi); bi = fmaf(a1.y, xv.z, bi);
+                        }
+                    }
+                }
+                if (tail && lane == 0) {
+                    const float2 xv = reinterpret_cast<const float2 *>(x4)[len - 1];
+                    const float2 at = h2f(atail);
+                    ar = fmaf(at.x, xv.x, ar); ar = fmaf(-at.y, xv.y, ar);
+                    ai = fmaf(at.x, xv.y, ai); ai = fmaf(at.y, xv.x, ai);
+                }
+                // power-of-two row scale: exact in float
+                o0 = make_float4(warp_sum_f(ar + br) * sca, 0.f, warp_sum_f(ai + bi) * sca, 0.f);
+                nout = 1;
+            }
+        } else if (warp < mt.nrows) {
             const float4 *A4 = reinterpret_cast<const float4 *>(ring + stage * kStageBytes) + warp * (kMvChunk / 2);
             const int len = mt.len, len2 = len >> 1;
             float sr = 0.f, si = 0.f, er = 0.f, ei = 0.f;
@@ -445,14 +584,27 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
                     ei = fmaf(a.x, x0.w, ei); ei = fmaf(a.y, x0.z, ei);
                 }
             }
-            const double tr = warp_sum_d((double)sr + (double)er);
-            const double ti = warp_sum_d((double)si + (double)ei);
-            if (lane == 0) S.mvp[(size_t)mt.chunk * S.n + mt.row0 + warp] = make_double2(tr, ti);
+            if (EXACT) {
+                warp_sum_ff(sr, er);
+                warp_sum_ff(si, ei);
+                o0 = make_float4(sr, er, si, ei);
+            } else {
+                o0 = make_float4(warp_sum_f(sr), 0.f, warp_sum_f(si), 0.f);
+            }
+            nout = 1;
         }
         __syncwarp();
         if (lane == 0) {
-            mbar_arrive(empty0 + 8 * stage);
+            if (!released) mbar_arrive(empty0 + 8 * stage);
             if (mt.last) mbar_arrive(xempty0 + 8 * mt.xslot);
+            double2 *out = S.mvp + (size_t)mt.chunk * S.n + mt.row0;
+            const double2 v = make_double2((double)o0.x + (double)o0.y, (double)o0.z + (double)o0.w);
+            if (!EXACT && mt.h) {
+                // chunk w >> 3 of the item, row w & 7
+                if (nout > 0) out[(size_t)(warp >> 3) * S.n + (warp & (kTmaRows - 1))] = v;
+            } else if (nout > 0) {
+                out[warp] = v;
+            }
         }
         if (mt.first) xph[mt.xslot] ^= 1;
         if (++stage == kTmaStages) { stage = 0; fph ^= 1; }

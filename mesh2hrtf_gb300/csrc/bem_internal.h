@@ -177,6 +177,27 @@ void pc_batch_finish(PcBatch &t);
 size_t precond_bytes(int n, int prec);
 cudaError_t launch_block_inverse(const PcBatch &t, int prec, cudaStream_t st);
 
+// ---------------------------------------------------------------- fp16 Krylov copy
+// A complex64 system may also hold A in fp16 pairs, every row scaled by a
+// power of two that puts its largest component in [2^14, 2^15).  The Krylov
+// products read that copy (4 bytes per entry instead of 8); the refinement
+// residuals read the complex64 matrix, so the solution still meets the
+// residual target with the complex64 system.
+struct SplitSys {
+    const void *A;          // complex64, leading dimension lda
+    size_t lda;
+    int n;
+    void *A16;              // fp16 pairs, the same leading dimension
+    float *rs;              // [n] row scales: A[i][j] ~ rs[i] * A16[i][j]
+};
+struct SplitBatch {
+    int B;
+    int off[kMaxAsm + 1];   // rows
+    SplitSys sys[kMaxAsm];
+};
+void split_batch_finish(SplitBatch &t);
+cudaError_t launch_split16(const SplitBatch &t, cudaStream_t st);
+
 // ---------------------------------------------------------------- Krylov engine
 // Restarted GMRES of one system as a state machine on the device.  An
 // iteration body (one captured graph) runs kSteps Arnoldi steps for every
@@ -215,6 +236,9 @@ struct KSys {
     int shared;             // 1: shares A with its neighbours in the table (one
                             // solver's right-hand sides; complex64 only); its
                             // product is one full-row partial (nchunk = 1)
+    const void *A16;        // complex64 systems: fp16 copy of A (leading
+                            // dimension lda) for the Krylov products, or nullptr
+    const float *rs;        // its row scales
     KState *st;
 };
 
@@ -270,6 +294,11 @@ constexpr int kTmaRows = 8;
 constexpr int kTmaStrip = 64;
 __host__ __device__ inline int mv_items_of(int n, int prec) {
     return ceil_div(n, prec == 0 ? kMvRows : kTmaStrip) * mv_chunks(n);
+}
+// Krylov products from the fp16 copy of A: items span two column chunks
+// (8 KB row segments, the size the complex64 items move).
+__host__ __device__ inline int mv_items16(int n) {
+    return ceil_div(n, kTmaStrip) * ceil_div(mv_chunks(n), 2);
 }
 // Rebuilds both launch plans of *d_tab from the systems' current phases.
 cudaError_t launch_plans(KTable *d_tab, cudaStream_t st);

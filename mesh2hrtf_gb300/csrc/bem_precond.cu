@@ -12,6 +12,7 @@
 // (128 KB); complex128 blocks are inverted in a global workspace (L2
 // resident).  Inverses are stored transposed so that the application (inside
 // the Krylov kernels, bem_gmres.cu) reads them coalesced.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "bem_internal.h"
@@ -173,7 +174,55 @@ __global__ void __launch_bounds__(512) k_binv64(const __grid_constant__ PcBatch 
     if (threadIdx.x == 0 && singular) atomicMax(S.status, 1);
 }
 
+// fp16 copy of complex64 rows (SplitBatch): one block per row; the row's
+// largest component m sets the scale 2^(15 - e) with m < 2^e, then every
+// component is scaled (exactly) and rounded to nearest.  Power-of-two scales
+// keep A16 * rs within one fp16 rounding of A.
+__global__ void __launch_bounds__(256) k_split16(const __grid_constant__ SplitBatch tb) {
+    __shared__ float red[8];
+    const int sb = find_blk(tb.off, tb.B, blockIdx.x);
+    const SplitSys &S = tb.sys[sb];
+    const int i = blockIdx.x - tb.off[sb];
+    const int n = S.n, n2 = n >> 1;
+    const float2 *row = (const float2 *)S.A + (size_t)i * S.lda;
+    const float4 *row4 = reinterpret_cast<const float4 *>(row);   // rows start 256-byte aligned
+    float m = 0.f;
+    for (int c = threadIdx.x; c < n2; c += blockDim.x) {
+        const float4 v = row4[c];
+        m = fmaxf(m, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+    }
+    if ((n & 1) && threadIdx.x == 0) m = fmaxf(m, fmaxf(fabsf(row[n - 1].x), fabsf(row[n - 1].y)));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    m = red[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+    int e = 0;
+    if (m > 0.f) frexpf(m, &e);   // m = f 2^e, 0.5 <= f < 1
+    const float scale = ldexpf(1.f, 15 - e);
+    if (threadIdx.x == 0) S.rs[i] = ldexpf(1.f, e - 15);
+    __half2 *out = (__half2 *)S.A16 + (size_t)i * S.lda;
+    for (int c = threadIdx.x; c < n2; c += blockDim.x) {
+        const float4 v = row4[c];
+        out[2 * c] = __floats2half2_rn(v.x * scale, v.y * scale);
+        out[2 * c + 1] = __floats2half2_rn(v.z * scale, v.w * scale);
+    }
+    if ((n & 1) && threadIdx.x == 0) out[n - 1] = __floats2half2_rn(row[n - 1].x * scale, row[n - 1].y * scale);
+}
+
 }  // namespace
+
+void split_batch_finish(SplitBatch &t) {
+    t.off[0] = 0;
+    for (int b = 0; b < t.B; ++b) t.off[b + 1] = t.off[b] + t.sys[b].n;
+}
+
+cudaError_t launch_split16(const SplitBatch &t, cudaStream_t st) {
+    if (t.B <= 0 || t.off[t.B] == 0) return cudaSuccess;
+    count_launches(1);
+    k_split16<<<t.off[t.B], 256, 0, st>>>(t);
+    return cudaGetLastError();
+}
 
 size_t precond_bytes(int n, int prec) {
     const size_t nb = (size_t)pc_blocks(n);

@@ -261,6 +261,7 @@ void bem_server_s::run() {
                     bem::pc_batch_finish(*pt);
                     e = bem::launch_block_inverse(*pt, prec01, st_a);
                 }
+                if (e == cudaSuccess) e = bem::split_group(ss.data(), cnt, st_a);
                 for (int i = 0; i < cnt && e == cudaSuccess; ++i)
                     e = cudaMemcpyAsync(&h_pool[2 * g.slot[i] + 1], ss[i]->d.status, sizeof(int),
                                         cudaMemcpyDeviceToHost, st_a);

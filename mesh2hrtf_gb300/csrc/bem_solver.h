@@ -64,6 +64,8 @@ constexpr int kInlineSources = 64;
 // Every per-solver device buffer, carved from one allocation.
 struct SolverBufs {
     void *A = nullptr;
+    void *A16 = nullptr;       // mixed precision, one right-hand side: fp16 copy of A
+    float *rs = nullptr;       // its row scales
     double2 *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *z = nullptr, *V = nullptr;
     double2 *mvp = nullptr, *dpa = nullptr, *dpb = nullptr;
     float2 *xh = nullptr;
@@ -82,8 +84,10 @@ struct SolverBufs {
 
 // Byte layout of a solver's block for n_rhs right-hand sides; base ==
 // nullptr only sizes it (bem_footprint_bytes is this size for one).
+// half_copy: complex64 solvers with one right-hand side keep the fp16 copy
+// of A that their Krylov products read.
 size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, SolverBufs *o, int n_rhs = 1,
-                     SolverBufs *extra = nullptr);
+                     SolverBufs *extra = nullptr, bool half_copy = true);
 
 }  // namespace bem
 
@@ -131,6 +135,8 @@ struct bem_solver_s {
         const bem::SolverBufs &d = buf(r);
         bem::KSys k{};
         k.A = d.A;
+        k.A16 = d.A16;
+        k.rs = d.rs;
         k.lda = (long long)lda;
         k.n = n;
         k.pc = have_precond ? 1 : 0;
@@ -150,7 +156,10 @@ struct bem_solver_s {
         q.m = restart;
         q.max_iter = max_iter;
         q.tol = tol;
-        q.floor_rel = prec == BEM_PREC_MIXED ? 1e-5 : 0.0;
+        // inner cycles stop at this fraction of the cycle's starting residual:
+        // with the fp16 Krylov copy (perturbation ~5e-4 relative) a cycle
+        // cannot gain more than about three digits on the complex64 system
+        q.floor_rel = prec == BEM_PREC_MIXED ? (d.A16 ? 1e-3 : 1e-5) : 0.0;
         return q;
     }
     bem::AsmSys asys(int r = 0) const {
@@ -209,6 +218,8 @@ bem_status assemble_group(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned *
                           cudaEvent_t e1, bem_status *rcs);
 // Block-Jacobi inverses of every preconditioned solver in ss and x = 0.
 bem_status precond_group(bem_solver_t *ss, int cnt, cudaStream_t st);
+// fp16 Krylov copies of the complex64 matrices of ss that keep one.
+cudaError_t split_group(bem_solver_t *ss, int cnt, cudaStream_t st);
 // Restarted GMRES of every solver in ss until all have finished.
 bem_status solve_group(bem_solver_t *ss, int cnt, Engine *eng, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1,
                        bem_status *rcs);

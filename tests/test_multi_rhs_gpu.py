@@ -45,7 +45,9 @@ def test_multi_rhs_equals_single(prec):
 def test_multi_rhs_footprint_and_limit():
     fp1 = capi.load().bem_footprint_multi(4000, capi.PREC_MIXED, 0, 1)
     fp8 = capi.load().bem_footprint_multi(4000, capi.PREC_MIXED, 0, 8)
-    assert fp8 > fp1 and fp8 < 2 * fp1   # the matrix is shared
+    # the complex64 matrix is shared (a single right-hand side also keeps its
+    # fp16 Krylov copy, several share the complex64 product)
+    assert fp8 > 4000 * 4000 * 8 and fp8 < 2 * fp1
     v, f = meshes.icosphere(320, 0.1)
     m = capi.Mesh(v, f)
     s = capi.Solver(m, precision=capi.PREC_MIXED, n_rhs=2)
