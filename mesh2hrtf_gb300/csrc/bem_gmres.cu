@@ -597,13 +597,16 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
         if (lane == 0) {
             if (!released) mbar_arrive(empty0 + 8 * stage);
             if (mt.last) mbar_arrive(xempty0 + 8 * mt.xslot);
-            double2 *out = S.mvp + (size_t)mt.chunk * S.n + mt.row0;
-            const double2 v = make_double2((double)o0.x + (double)o0.y, (double)o0.z + (double)o0.w);
-            if (!EXACT && mt.h) {
-                // chunk w >> 3 of the item, row w & 7
-                if (nout > 0) out[(size_t)(warp >> 3) * S.n + (warp & (kTmaRows - 1))] = v;
-            } else if (nout > 0) {
-                out[warp] = v;
+            // row partial of chunk (w >> 3 for fp16 items), row w (& 7): float for
+            // the Krylov products (summed in FP32 by k_dot1), FP64 for the
+            // residuals (summed in FP64 by k_resid)
+            const size_t o = (size_t)mt.chunk * S.n + mt.row0 +
+                             ((!EXACT && mt.h) ? (size_t)(warp >> 3) * S.n + (warp & (kTmaRows - 1)) : (size_t)warp);
+            if (nout > 0) {
+                if (!EXACT && kind == 0)
+                    reinterpret_cast<float2 *>(S.mvp)[o] = make_float2(o0.x + o0.y, o0.z + o0.w);
+                else
+                    S.mvp[o] = make_double2((double)o0.x + (double)o0.y, (double)o0.z + (double)o0.w);
             }
         }
         if (mt.first) xph[mt.xslot] ^= 1;
@@ -1095,8 +1098,13 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
                     yi += u[8 + q];
                 }
                 const int grow = orb * 16 + row;
-                if (grow < mt.nrows && ((mt.mask >> q) & 1))
-                    tb->sys[mt.first + q].mvp[mt.row0 + grow] = make_double2(yr, yi);
+                if (grow < mt.nrows && ((mt.mask >> q) & 1)) {
+                    double2 *mv = tb->sys[mt.first + q].mvp;
+                    if (kind == 0)   // Krylov partials are float (k_dot1)
+                        reinterpret_cast<float2 *>(mv)[mt.row0 + grow] = make_float2((float)yr, (float)yi);
+                    else
+                        mv[mt.row0 + grow] = make_double2(yr, yi);
+                }
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(redr);
@@ -1214,10 +1222,22 @@ __global__ void __launch_bounds__(kThreads) k_dot1(const KTable *tb) {
         const bool ok = row < n;
         double2 wv = make_double2(0.0, 0.0);
         if (ok) {
-            for (int c = 0; c < S.nchunk; ++c) {
-                const double2 p = S.mvp[(size_t)c * n + row];
-                wv.x += p.x;
-                wv.y += p.y;
+            if (tb->prec == 1) {
+                // complex64 products leave float partials: FP32 sum, one conversion
+                const float2 *mp = reinterpret_cast<const float2 *>(S.mvp);
+                float ax = 0.f, ay = 0.f;
+                for (int c = 0; c < S.nchunk; ++c) {
+                    const float2 p = mp[(size_t)c * n + row];
+                    ax += p.x;
+                    ay += p.y;
+                }
+                wv = make_double2((double)ax, (double)ay);
+            } else {
+                for (int c = 0; c < S.nchunk; ++c) {
+                    const double2 p = S.mvp[(size_t)c * n + row];
+                    wv.x += p.x;
+                    wv.y += p.y;
+                }
             }
             S.w[row] = wv;
         }
@@ -1278,9 +1298,39 @@ __global__ void __launch_bounds__(kThreads) k_axpy(const KTable *tb) {
 // RESTART = false: v_{k+1} = w / |w| (phase ARNOLDI).
 // RESTART = true:  v_0 = r / beta for systems that have just restarted.
 // Then z = M^{-1} v when the system is preconditioned.
+// complex64 systems: z = M^{-1} v only feeds the float input of the next
+// product, so it is formed in FP32 from a float copy of v (products in FP32,
+// chunks of 16 columns added in float-float pairs): no FP64-pipe work per
+// column.
+__device__ __forceinline__ float2 apply_minv_f(const void *Minv, int n, int blk, const float2 *vf) {
+    const int tid = threadIdx.x;
+    const int pb = blk * 2 + (tid >> 7), rr = tid & 127, r0 = pb * kBlock;
+    const int nb = min(kBlock, n - r0);
+    if (nb <= 0 || rr >= nb) return make_float2(0.f, 0.f);
+    const float2 *x = vf + (tid & 128);
+    const float2 *M = (const float2 *)Minv + (size_t)pb * kBlock * kBlock;
+    float sh = 0.f, sl = 0.f, th = 0.f, tl = 0.f;
+    for (int c0 = 0; c0 < nb; c0 += 16) {
+        float ar = 0.f, ai = 0.f;
+        const int ce = min(c0 + 16, nb);
+        for (int c = c0; c < ce; ++c) {
+            const float2 m = M[(size_t)c * kBlock + rr];
+            const float2 xv = x[c];
+            ar = fmaf(m.x, xv.x, ar); ar = fmaf(-m.y, xv.y, ar);
+            ai = fmaf(m.x, xv.y, ai); ai = fmaf(m.y, xv.x, ai);
+        }
+        float t, e;
+        two_sum(sh, ar, t, e); sh = t; sl += e;
+        two_sum(th, ai, t, e); th = t; tl += e;
+    }
+    return make_float2(sh + sl, th + tl);
+}
+
 template <bool C128, bool RESTART>
 __global__ void __launch_bounds__(kThreads) k_scale(const KTable *tb) {
     __shared__ double2 vs[kThreads];
+    __shared__ float2 vf[kThreads];
+    __shared__ double nrm_s;
     for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
         const int2 bi = tb->vb_items[it];
         const KSys &S = tb->sys[bi.x];
@@ -1288,7 +1338,12 @@ __global__ void __launch_bounds__(kThreads) k_scale(const KTable *tb) {
         if (st->phase != kPhaseArnoldi) continue;
         if (RESTART && st->k != 0) continue;
         const int n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x;
-        const double s = RESTART ? 1.0 / st->beta : 1.0 / sqrt(norm_total(S.nrmp, S.nvb));
+        if (!RESTART) {
+            // the norm once per block (same sum, same order as k_givens)
+            if (threadIdx.x == 0) nrm_s = norm_total(S.nrmp, S.nvb);
+            __syncthreads();
+        }
+        const double s = RESTART ? 1.0 / st->beta : 1.0 / sqrt(nrm_s);
         const int dst = RESTART ? 0 : st->k + 1;
         const double2 *src = RESTART ? S.r : S.w;
         double2 v = make_double2(0.0, 0.0);
@@ -1297,15 +1352,24 @@ __global__ void __launch_bounds__(kThreads) k_scale(const KTable *tb) {
             v = make_double2(a.x * s, a.y * s);
             S.V[(size_t)dst * S.ldv + row] = v;
         }
-        double2 u = v;   // input of the next product
-        if (S.pc) {
-            vs[threadIdx.x] = v;
-            __syncthreads();
-            u = apply_minv<C128>(S.Minv, n, blk, vs);
-            if (row < n) S.z[row] = u;
-            __syncthreads();
+        if (C128) {
+            double2 u = v;   // input of the next product
+            if (S.pc) {
+                vs[threadIdx.x] = v;
+                __syncthreads();
+                u = apply_minv<true>(S.Minv, n, blk, vs);
+                if (row < n) S.z[row] = u;
+            }
+        } else {
+            float2 u = make_float2((float)v.x, (float)v.y);
+            if (S.pc) {
+                vf[threadIdx.x] = u;
+                __syncthreads();
+                u = apply_minv_f(S.Minv, n, blk, vf);
+            }
+            if (row < n) S.xh[row] = u;
         }
-        if (!C128 && row < n) S.xh[row] = make_float2((float)u.x, (float)u.y);
+        __syncthreads();
     }
 }
 

@@ -177,18 +177,26 @@ __global__ void __launch_bounds__(512) k_binv64(const __grid_constant__ PcBatch 
 // fp16 copy of complex64 rows (SplitBatch): one block per row; the row's
 // largest component m sets the scale 2^(15 - e) with m < 2^e, then every
 // component is scaled (exactly) and rounded to nearest.  Power-of-two scales
-// keep A16 * rs within one fp16 rounding of A.
-__global__ void __launch_bounds__(256) k_split16(const __grid_constant__ SplitBatch tb) {
-    __shared__ float red[8];
+// keep A16 * rs within one fp16 rounding of A.  Rows of up to kSplitSmemMax
+// entries are staged in shared memory (one read of A); longer rows are read
+// twice.
+constexpr int kSplitThreads = 512;
+constexpr int kSplitSmemMax = 26624;   // entries: 208 KB of complex64
+
+__global__ void __launch_bounds__(kSplitThreads) k_split16(const __grid_constant__ SplitBatch tb, int staged) {
+    extern __shared__ __align__(16) float4 rowbuf[];
+    __shared__ float red[kSplitThreads / 32];
     const int sb = find_blk(tb.off, tb.B, blockIdx.x);
     const SplitSys &S = tb.sys[sb];
     const int i = blockIdx.x - tb.off[sb];
     const int n = S.n, n2 = n >> 1;
     const float2 *row = (const float2 *)S.A + (size_t)i * S.lda;
     const float4 *row4 = reinterpret_cast<const float4 *>(row);   // rows start 256-byte aligned
+    const bool st = staged && n <= kSplitSmemMax;
     float m = 0.f;
     for (int c = threadIdx.x; c < n2; c += blockDim.x) {
         const float4 v = row4[c];
+        if (st) rowbuf[c] = v;
         m = fmaxf(m, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
     }
     if ((n & 1) && threadIdx.x == 0) m = fmaxf(m, fmaxf(fabsf(row[n - 1].x), fabsf(row[n - 1].y)));
@@ -201,13 +209,15 @@ __global__ void __launch_bounds__(256) k_split16(const __grid_constant__ SplitBa
     if (m > 0.f) frexpf(m, &e);   // m = f 2^e, 0.5 <= f < 1
     const float scale = ldexpf(1.f, 15 - e);
     if (threadIdx.x == 0) S.rs[i] = ldexpf(1.f, e - 15);
-    __half2 *out = (__half2 *)S.A16 + (size_t)i * S.lda;
+    uint2 *out = reinterpret_cast<uint2 *>((__half2 *)S.A16 + (size_t)i * S.lda);
     for (int c = threadIdx.x; c < n2; c += blockDim.x) {
-        const float4 v = row4[c];
-        out[2 * c] = __floats2half2_rn(v.x * scale, v.y * scale);
-        out[2 * c + 1] = __floats2half2_rn(v.z * scale, v.w * scale);
+        const float4 v = st ? rowbuf[c] : row4[c];
+        const __half2 h0 = __floats2half2_rn(v.x * scale, v.y * scale);
+        const __half2 h1 = __floats2half2_rn(v.z * scale, v.w * scale);
+        out[c] = make_uint2(*reinterpret_cast<const unsigned *>(&h0), *reinterpret_cast<const unsigned *>(&h1));
     }
-    if ((n & 1) && threadIdx.x == 0) out[n - 1] = __floats2half2_rn(row[n - 1].x * scale, row[n - 1].y * scale);
+    if ((n & 1) && threadIdx.x == 0)
+        ((__half2 *)S.A16)[(size_t)i * S.lda + n - 1] = __floats2half2_rn(row[n - 1].x * scale, row[n - 1].y * scale);
 }
 
 }  // namespace
@@ -219,8 +229,16 @@ void split_batch_finish(SplitBatch &t) {
 
 cudaError_t launch_split16(const SplitBatch &t, cudaStream_t st) {
     if (t.B <= 0 || t.off[t.B] == 0) return cudaSuccess;
+    int nmax = 0;
+    for (int b = 0; b < t.B; ++b) nmax = nmax > t.sys[b].n ? nmax : t.sys[b].n;
+    const int staged = nmax <= kSplitSmemMax ? 1 : 0;
+    const size_t smem = staged ? (size_t)((nmax + 1) / 2) * sizeof(float4) : 0;
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(k_split16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     count_launches(1);
-    k_split16<<<t.off[t.B], 256, 0, st>>>(t);
+    k_split16<<<t.off[t.B], kSplitThreads, smem, st>>>(t, staged);
     return cudaGetLastError();
 }
 
