@@ -65,6 +65,12 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
+// FP64 row partial from a float-float pair; out of line so that the
+// conversions are not executed (predicated) on the float-partial path.
+__device__ __noinline__ void store_partial_f64(double2 *p, float4 o) {
+    *p = make_double2((double)o.x + (double)o.y, (double)o.z + (double)o.w);
+}
+
 // Warp sums in FP32.  GB300's FP64 pipe is narrow (a warp instruction
 // occupies it for many cycles), so the products reduce their row sums in
 // FP32 and convert once per row; the butterfly leaves the same value on every
@@ -606,7 +612,7 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
                 if (!EXACT && kind == 0)
                     reinterpret_cast<float2 *>(S.mvp)[o] = make_float2(o0.x + o0.y, o0.z + o0.w);
                 else
-                    S.mvp[o] = make_double2((double)o0.x + (double)o0.y, (double)o0.z + (double)o0.w);
+                    store_partial_f64(S.mvp + o, o0);
             }
         }
         if (mt.first) xph[mt.xslot] ^= 1;
