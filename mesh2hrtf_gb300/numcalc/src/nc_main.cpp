@@ -12,7 +12,11 @@
 // Environment: NUMCALC_GB300_PRECISION = mixed (default) | fp64,
 //              NUMCALC_GB300_DEVICE = CUDA device index (default 0),
 //              NUMCALC_GB300_WAIT_S = seconds to wait for device memory when
-//              other NumCalc processes hold it (default 3600).
+//              other NumCalc processes hold it (default 3600),
+//              NUMCALC_GB300_NPY = 1: every result file is also written as
+//              <name>.npy (complex128, the printed values at full precision,
+//              in the text file's row order) for post-processing without the
+//              7-digit text round trip (mesh2hrtf_gb300/output2hrtf.py).
 #include <sys/stat.h>
 #include <unistd.h>
 
@@ -62,6 +66,27 @@ struct Gpu {
     std::exit(1);
 }
 
+// complex128 array as a .npy file (format 1.0, little endian, C order)
+void write_npy(const std::string &path, const std::vector<cd> &v, const std::vector<size_t> &shape) {
+    if (!std::getenv("NUMCALC_GB300_NPY")) return;
+    std::string hdr = "{'descr': '<c16', 'fortran_order': False, 'shape': (";
+    for (size_t k = 0; k < shape.size(); ++k) hdr += std::to_string(shape[k]) + (shape.size() == 1 ? "," : k + 1 < shape.size() ? ", " : "");
+    hdr += "), }";
+    const size_t total = 10 + hdr.size() + 1;
+    hdr.append((64 - total % 64) % 64, ' ');
+    hdr += '\n';
+    FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) throw nc::NcExit{"Can not open the file " + path, 1};
+    const unsigned char magic[8] = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0};
+    const uint16_t hl = (uint16_t)hdr.size();
+    const unsigned char len[2] = {(unsigned char)(hl & 0xff), (unsigned char)(hl >> 8)};
+    std::fwrite(magic, 1, 8, f);
+    std::fwrite(len, 1, 2, f);
+    std::fwrite(hdr.data(), 1, hdr.size(), f);
+    std::fwrite(v.data(), sizeof(cd), v.size(), f);
+    std::fclose(f);
+}
+
 // pBoundary / vBoundary (NC_WriteResultsObjectMesh, NC_PostProcessing.cpp:
 // 367-578): element potentials and velocities at the collocation points.
 void write_boundary(const nc::Project &p, const nc::FreqState &fs, const std::vector<cd> &x,
@@ -84,6 +109,7 @@ void write_boundary(const nc::Project &p, const nc::FreqState &fs, const std::ve
             if (p.ibval[e] == 2) vel[e] -= (pot[e] * fs.zbval1[e]) * p.tao;
         }
     }
+    std::vector<cd> np_p, np_v;   // the printed values, for write_npy
     FILE *fp = std::fopen((dir + "/pBoundary").c_str(), "w");
     FILE *fv = std::fopen((dir + "/vBoundary").c_str(), "w");
     if (!fp || !fv) throw nc::NcExit{"Can not open the file " + dir + "/pBoundary", 1};
@@ -103,10 +129,14 @@ void write_boundary(const nc::Project &p, const nc::FreqState &fs, const std::ve
             const cd pr = mul_i(pot[e], fs.rpfact);
             std::fprintf(fp, "%5d % E % E\n", p.elem_ext[e], pr.real(), pr.imag());
             std::fprintf(fv, "%5d % E % E\n", p.elem_ext[e], vel[e].real(), vel[e].imag());
+            np_p.push_back(pr);
+            np_v.push_back(vel[e]);
         }
     }
     std::fclose(fp);
     std::fclose(fv);
+    write_npy(dir + "/pBoundary.npy", np_p, {np_p.size()});
+    write_npy(dir + "/vBoundary.npy", np_v, {np_v.size()});
 }
 
 // pEvalGrid / vEvalGrid (NC_WriteResultsEvaluationGrid,
@@ -132,12 +162,16 @@ void write_eval(const nc::Project &p, const nc::FreqState &fs, const std::vector
     }
     std::fprintf(fp, "%5d\n", ngrp);
     if (m > 0) std::fprintf(fp, "%5d %5d\n", group, m);
+    std::vector<cd> np_p(m);
     for (int i = 0; i < m; ++i) {
         const cd pr = mul_i(pot[i], fs.rpfact);
         std::fprintf(fp, "%5d % E % E\n", p.node_ext[ev_nodes[i]], pr.real(), pr.imag());
+        np_p[i] = pr;
     }
     std::fclose(fp);
     std::fclose(fv);
+    write_npy(dir + "/pEvalGrid.npy", np_p, {(size_t)m});
+    write_npy(dir + "/vEvalGrid.npy", std::vector<cd>(grad.begin(), grad.begin() + 3 * (size_t)m), {(size_t)m, 3});
 }
 
 int run(int istart, int iend, bool estimate_ram, bool check_normals, int nitermax, bool nitermax_given,

@@ -107,3 +107,33 @@ def test_manage_numcalc_runs_every_step_on_the_gpu(numcalc, tmp_path):
         assert gc.rel_err(vals, c["s%d_pEvalGrid" % s]) < 1e-5
         assert os.path.isfile(os.path.join(wd2, "be.out", "be.%d" % s, "pEvalGrid"))
     assert os.path.isfile(os.path.join(wd1, "MemoryGPU.txt"))
+
+
+def test_full_precision_results_and_hrtfs(numcalc, tmp_path):
+    """NUMCALC_GB300_NPY=1: every result file also as .npy (the printed
+    values at full precision); Output2HRTF's referencing reads them
+    (mesh2hrtf_gb300/output2hrtf.py)."""
+    import json
+
+    from mesh2hrtf_gb300 import output2hrtf as o2h
+    c, wd = _project(tmp_path)
+    env = dict(os.environ, NUMCALC_GB300_PRECISION="fp64", NUMCALC_GB300_NPY="1")
+    r = subprocess.run([numcalc], cwd=wd, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:]
+    for s in range(1, len(c.freqs) + 1):
+        d = os.path.join(wd, "be.out", "be.%d" % s)
+        for f in ("pBoundary", "vBoundary", "pEvalGrid", "vEvalGrid"):
+            ids, txt = project.read_result(os.path.join(d, f))
+            full = np.load(os.path.join(d, f + ".npy"))
+            assert full.shape == np.asarray(txt).shape
+            assert gc.rel_err(full, txt) < 1e-6                     # 7 printed digits
+            assert gc.rel_err(full, c["s%d_%s" % (s, f)]) < 2e-6     # the reference, 17 digits
+    root = str(tmp_path / "p")
+    json.dump({"Mesh2HRTF_Version": "1.0.0", "speedOfSound": 343.0, "densityOfMedium": 1.21,
+               "evaluationGrids": ["Grid"], "sourceType": "Point source", "numSources": 1,
+               "sourceCenter": [[0.5, 0.1, 0.0]], "sourceArea": [], "reference": True, "computeHRIRs": False,
+               "numFrequencies": len(c.freqs), "frequencies": [float(v) for v in c.freqs]},
+              open(os.path.join(root, "parameters.json"), "w"))
+    h = np.load(o2h.output2hrtf(root)[0])
+    hrtf = h["Data_Real"] + 1j * h["Data_Imag"]
+    assert hrtf.shape == (len(c.pts), 1, len(c.freqs)) and np.all(np.isfinite(hrtf))
