@@ -22,6 +22,9 @@
 //   k_dot1        w = sum parts; h1 = V^H w     per 256-row block
 //   k_axpy<1>     w -= V h1; h2 = V^H w         (classical Gram-Schmidt, twice)
 //   k_axpy<2>     w -= V h2; |w|^2 partials
+//                 (systems whose cycles gain only three digits, those with
+//                 the fp16 Krylov copy, skip the second pass: k_axpy<1>
+//                 passes them by and k_axpy<2> subtracts V h1)
 //   k_scale       v_{k+1} = w / |w|; z_{k+1} = M^{-1} v_{k+1}
 //   k_givens      column k of H, rotations, residual estimate, phase
 // End of cycle (6 launches):
@@ -1253,6 +1256,9 @@ __global__ void __launch_bounds__(kThreads) k_dot1(const KTable *tb) {
 
 // PASS 1: h = sum(dpa); w -= V h; hsum += h; dpb = V^H w.
 // PASS 2: h = sum(dpb); w -= V h; hsum += h; nrmp = |w|^2 partials.
+// Systems with one Gram-Schmidt pass (KSys::cgs1) skip PASS 1 and take dpa
+// in PASS 2: an inner cycle that stops after three digits keeps the basis
+// orthogonal to ~1e-10 with classical Gram-Schmidt in FP64.
 template <int PASS>
 __global__ void __launch_bounds__(kThreads) k_axpy(const KTable *tb) {
     __shared__ double2 hs[kMaxV];
@@ -1266,7 +1272,8 @@ __global__ void __launch_bounds__(kThreads) k_axpy(const KTable *tb) {
         const int n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x, nvb = S.nvb;
         const bool ok = row < n;
         const int nv = st->k + 1;
-        const double2 *dp = PASS == 1 ? S.dpa : S.dpb;
+        if (PASS == 1 && S.cgs1) continue;
+        const double2 *dp = (PASS == 1 || S.cgs1) ? S.dpa : S.dpb;
         for (int l = warp; l < nv; l += 8) {
             double re = 0.0, im = 0.0;
             for (int c = lane; c < nvb; c += 32) {

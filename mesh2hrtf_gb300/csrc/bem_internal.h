@@ -239,6 +239,7 @@ struct KSys {
     const void *A16;        // complex64 systems: fp16 copy of A (leading
                             // dimension lda) for the Krylov products, or nullptr
     const float *rs;        // its row scales
+    int cgs1;               // one classical Gram-Schmidt pass instead of two
     KState *st;
 };
 

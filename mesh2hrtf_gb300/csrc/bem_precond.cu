@@ -194,8 +194,9 @@ __global__ void __launch_bounds__(kSplitThreads) k_split16(const __grid_constant
     const float4 *row4 = reinterpret_cast<const float4 *>(row);   // rows start 256-byte aligned
     const bool st = staged && n <= kSplitSmemMax;
     float m = 0.f;
+#pragma unroll 4
     for (int c = threadIdx.x; c < n2; c += blockDim.x) {
-        const float4 v = row4[c];
+        const float4 v = __ldcs(row4 + c);   // streamed: A is read once here
         if (st) rowbuf[c] = v;
         m = fmaxf(m, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
     }
@@ -210,6 +211,7 @@ __global__ void __launch_bounds__(kSplitThreads) k_split16(const __grid_constant
     const float scale = ldexpf(1.f, 15 - e);
     if (threadIdx.x == 0) S.rs[i] = ldexpf(1.f, e - 15);
     uint2 *out = reinterpret_cast<uint2 *>((__half2 *)S.A16 + (size_t)i * S.lda);
+#pragma unroll 4
     for (int c = threadIdx.x; c < n2; c += blockDim.x) {
         const float4 v = st ? rowbuf[c] : row4[c];
         const __half2 h0 = __floats2half2_rn(v.x * scale, v.y * scale);

@@ -137,6 +137,7 @@ struct bem_solver_s {
         k.A = d.A;
         k.A16 = d.A16;
         k.rs = d.rs;
+        k.cgs1 = d.A16 ? 1 : 0;   // fp16 Krylov copy: cycles gain three digits
         k.lda = (long long)lda;
         k.n = n;
         k.pc = have_precond ? 1 : 0;
