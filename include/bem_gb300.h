@@ -146,13 +146,20 @@ double bem_footprint_bytes(int32_t n_elem, int32_t precision, int32_t restart);
 /* The same for a solver holding n_rhs right-hand sides (bem_solve_multi). */
 double bem_footprint_multi(int32_t n_elem, int32_t precision, int32_t restart, int32_t n_rhs);
 /* Bytes a mesh of n_elem elements with n_sym_planes symmetry planes holds on
- * the device: element tables, symmetry images and the near-pair list (an
- * estimate of 48 pairs per element; the list's real size depends on the
- * geometry).  Host arithmetic only, no device needed. */
+ * the device: element tables, symmetry images and the near-pair list (48
+ * pairs per element and image, grown to the exact count when the geometry
+ * needs more).  Host arithmetic only, no device needed. */
 double bem_mesh_footprint_bytes(int32_t n_elem, int32_t n_sym_planes);
 /* Free and total device memory of a device (cudaMemGetInfo; creates the
- * device's context in the calling process). */
+ * device's context in the calling process).  free_bytes counts the blocks
+ * the library keeps cached for reuse (see bem_release_cached_memory). */
 bem_status bem_device_memory(int32_t device, double *free_bytes, double *total_bytes);
+/* Meshes, solvers and point buffers release their device memory into a
+ * per-device cache that the next creation of about the same size reuses
+ * (cudaFree of GB-sized blocks synchronizes the device and takes
+ * milliseconds).  This returns the cached blocks to the driver.  Environment
+ * BEM_GB300_CACHE=0 turns the cache off. */
+bem_status bem_release_cached_memory(void);
 
 /* Mesh: upload and precompute element tables.
  * Replaces NC_ReadMesh's geometry part (NC_Input.cpp:522-602) and the per-pair

@@ -33,7 +33,7 @@ EXPORTED = [
     "bem_assemble", "bem_solve", "bem_get_solution", "bem_get_system", "bem_project",
     "bem_solve_frequency", "bem_project_static", "bem_solve_batch", "bem_solve_multi", "bem_footprint_multi",
     "bem_server_create", "bem_server_submit", "bem_server_wait", "bem_server_destroy",
-    "bem_mesh_footprint_bytes", "bem_device_memory",
+    "bem_mesh_footprint_bytes", "bem_device_memory", "bem_release_cached_memory",
 ]
 STATIC_MAX_ELEMENTS = 32768
 

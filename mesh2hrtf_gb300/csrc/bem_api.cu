@@ -9,6 +9,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <unordered_map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -67,7 +70,7 @@ bem_status ensure_device_init() {
 template <typename T> cudaError_t dalloc(T **p, size_t count) {
     *p = nullptr;
     if (count == 0) return cudaSuccess;
-    return cudaMalloc((void **)p, count * sizeof(T));
+    return bem::dev_malloc((void **)p, count * sizeof(T));
 }
 
 
@@ -132,6 +135,113 @@ namespace bem {
 // right-hand sides.  base == nullptr only sizes it.  extra (n_rhs - 1
 // entries) receives right-hand sides 1..n_rhs-1, whose shared fields repeat
 // those of *o.
+// ---------------------------------------------------------------- device memory cache
+namespace {
+struct DevCache {
+    std::mutex mu;
+    bool enabled = true;
+    std::unordered_map<void *, std::pair<int, size_t>> live;   // block -> (device, bytes)
+    std::map<int, std::multimap<size_t, void *>> idle;          // per device: bytes -> block
+    std::map<int, size_t> idle_bytes;
+};
+DevCache &dev_cache() {
+    static DevCache *c = [] {
+        DevCache *d = new DevCache();   // never destroyed: blocks may outlive static destructors
+        const char *v = std::getenv("BEM_GB300_CACHE");
+        d->enabled = !(v && std::string(v) == "0");
+        return d;
+    }();
+    return *c;
+}
+}  // namespace
+
+cudaError_t dev_malloc(void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return cudaSuccess;
+    const size_t gran = (size_t)2 << 20;
+    const size_t want = (bytes + gran - 1) / gran * gran;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    DevCache &C = dev_cache();
+    if (C.enabled) {
+        std::lock_guard<std::mutex> g(C.mu);
+        auto &m = C.idle[dev];
+        auto it = m.lower_bound(want);
+        if (it != m.end() && it->first <= want + want / 8) {
+            *p = it->second;
+            C.live[*p] = {dev, it->first};
+            C.idle_bytes[dev] -= it->first;
+            m.erase(it);
+            return cudaSuccess;
+        }
+    }
+    cudaError_t e = cudaMalloc(p, want);
+    if (e == cudaErrorMemoryAllocation && C.enabled) {
+        cudaGetLastError();
+        dev_release_cached(dev);
+        e = cudaMalloc(p, want);
+    }
+    if (e == cudaSuccess) {
+        std::lock_guard<std::mutex> g(C.mu);
+        C.live[*p] = {dev, want};
+    }
+    return e;
+}
+
+void dev_free(void *p) {
+    if (!p) return;
+    DevCache &C = dev_cache();
+    std::unique_lock<std::mutex> g(C.mu);
+    auto it = C.live.find(p);
+    if (it == C.live.end() || !C.enabled) {
+        if (it != C.live.end()) C.live.erase(it);
+        g.unlock();
+        cudaFree(p);
+        return;
+    }
+    const int dev = it->second.first;
+    const size_t bytes = it->second.second;
+    C.live.erase(it);
+    g.unlock();
+    // as cudaFree: no work still in flight may touch the block when it is reused
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (cur != dev) cudaSetDevice(dev);
+    cudaDeviceSynchronize();
+    if (cur != dev) cudaSetDevice(cur);
+    g.lock();
+    C.idle[dev].emplace(bytes, p);
+    C.idle_bytes[dev] += bytes;
+}
+
+size_t dev_cached_bytes(int device) {
+    DevCache &C = dev_cache();
+    std::lock_guard<std::mutex> g(C.mu);
+    auto it = C.idle_bytes.find(device);
+    return it == C.idle_bytes.end() ? 0 : it->second;
+}
+
+void dev_release_cached(int device) {
+    DevCache &C = dev_cache();
+    std::vector<std::pair<int, void *>> blocks;
+    {
+        std::lock_guard<std::mutex> g(C.mu);
+        for (auto &d : C.idle) {
+            if (device >= 0 && d.first != device) continue;
+            for (auto &b : d.second) blocks.push_back({d.first, b.second});
+            d.second.clear();
+            C.idle_bytes[d.first] = 0;
+        }
+    }
+    int cur = 0;
+    cudaGetDevice(&cur);
+    for (auto &b : blocks) {
+        if (b.first != cur) cudaSetDevice(b.first);
+        cudaFree(b.second);
+        if (b.first != cur) cudaSetDevice(cur);
+    }
+}
+
 size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, SolverBufs *o, int n_rhs,
                      SolverBufs *extra, bool half_copy) {
     size_t off = 0;
@@ -300,7 +410,7 @@ bem_status upload_freq(bem_solver_t s, const bem_frequency_desc *f, cudaStream_t
         if (f->n_point + f->n_plane > bem::kInlineSources) {
             if (rhs > 0) return fail(BEM_ERR_INVALID, "more than %d sources on right-hand side %d", bem::kInlineSources, rhs);
             CU(cudaStreamSynchronize(st));
-            cudaFree(s->src_extra);
+            bem::dev_free(s->src_extra);
             s->src_extra = nullptr;
             CU(dalloc(&s->src_extra, src.size()));
             dst = s->src_extra;
@@ -523,7 +633,7 @@ bem_status solve_group(bem_solver_t *ss, int cnt, bem::Engine *eng, cudaStream_t
 bem_status ensure_points(bem_solver_t s, int n_pts) {
     if (n_pts <= s->pts_cap) return BEM_OK;
     CU(cudaStreamSynchronize(s->st));
-    cudaFree(s->pts); cudaFree(s->pot); cudaFree(s->grad);
+    bem::dev_free(s->pts); bem::dev_free(s->pot); bem::dev_free(s->grad);
     s->pts = s->pot = s->grad = nullptr;
     s->pts_cap = 0;
     CU(dalloc(&s->pts, 3 * (size_t)n_pts));
@@ -642,8 +752,13 @@ double bem_mesh_footprint_bytes(int32_t n_elem, int32_t n_sym_planes) {
     const int nref = 1 << std::min(std::max(n_sym_planes, 0), 3);
     // element tables: 1 + 12 + 3 + 3 + 1 + 1 words of 8 B, 3 + 3 + 10 + 12 + 1 + 3 of 4 B
     const double tables = (double)n * (4.0 + 20.0 * 8.0 + 32.0 * 4.0);
-    const double near = (double)n * 48.0 * sizeof(int2);
+    const double near = (double)n * nref * 48.0 * sizeof(int2);   // the list's first allocation
     return tables + (double)bem::image_table_bytes(n, nref) + near;
+}
+
+bem_status bem_release_cached_memory(void) {
+    bem::dev_release_cached(-1);
+    return BEM_OK;
 }
 
 bem_status bem_device_memory(int32_t device, double *free_bytes, double *total_bytes) {
@@ -655,7 +770,7 @@ bem_status bem_device_memory(int32_t device, double *free_bytes, double *total_b
     const cudaError_t e = cudaMemGetInfo(&fr, &tot);
     cudaSetDevice(cur);
     if (e != cudaSuccess) return fail(BEM_ERR_CUDA, "cudaMemGetInfo: %s", cudaGetErrorString(e));
-    *free_bytes = (double)fr;
+    *free_bytes = (double)fr + (double)bem::dev_cached_bytes(device);
     *total_bytes = (double)tot;
     return BEM_OK;
 }
@@ -836,7 +951,7 @@ bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
     // symmetry images: one allocation, laid out as DevSym describes
     if (e == cudaSuccess && sym.nref > 1) {
         const size_t ni = (size_t)(sym.nref - 1) * (size_t)n;
-        e = cudaMalloc(&m->d_img, bem::image_table_bytes(n, sym.nref));
+        e = bem::dev_malloc(&m->d_img, bem::image_table_bytes(n, sym.nref));
         if (e == cudaSuccess) {
             bem::ImageTables it;
             it.v64 = (double *)m->d_img;
@@ -853,21 +968,26 @@ bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
     } else {
         m->sym = sym;
     }
-    // near list: count, allocate, fill (geometry only, reused by every frequency)
+    // near list (geometry only, reused by every frequency): one pass into a
+    // list sized for 48 pairs per element and image, a second with the exact
+    // size only if that was too small
     unsigned long long *d_cnt = nullptr, cnt = 0;
+    unsigned long long cap = 48ull * (unsigned long long)n * (unsigned long long)sym.nref;
     if (e == cudaSuccess) e = dalloc(&d_cnt, 1);
-    if (e == cudaSuccess) e = cudaMemset(d_cnt, 0, sizeof(unsigned long long));
-    if (e == cudaSuccess) e = bem::launch_near_list(m->view(), nullptr, d_cnt, 0);
-    if (e == cudaSuccess) e = cudaMemcpy(&cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = dalloc(&m->d_near, (size_t)cnt);
-    if (e == cudaSuccess) e = cudaMemset(d_cnt, 0, sizeof(unsigned long long));
-    if (e == cudaSuccess) e = bem::launch_near_list(m->view(), m->d_near, d_cnt, 0);
-    unsigned long long cnt2 = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(&cnt2, d_cnt, sizeof(cnt2), cudaMemcpyDeviceToHost);
-    cudaFree(d_cnt);
-    if (e == cudaSuccess && cnt2 != cnt) {
+    for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
+        if (e == cudaSuccess) e = dalloc(&m->d_near, (size_t)cap);
+        if (e == cudaSuccess) e = cudaMemset(d_cnt, 0, sizeof(unsigned long long));
+        if (e == cudaSuccess) e = bem::launch_near_list(m->view(), m->d_near, cap, d_cnt, 0);
+        if (e == cudaSuccess) e = cudaMemcpy(&cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess || cnt <= cap) break;
+        bem::dev_free(m->d_near);
+        m->d_near = nullptr;
+        cap = cnt;
+    }
+    bem::dev_free(d_cnt);
+    if (e == cudaSuccess && cnt > cap) {
         delete m;
-        return fail(BEM_ERR_CUDA, "near list: inconsistent counts %llu / %llu", cnt, cnt2);
+        return fail(BEM_ERR_CUDA, "near list: %llu pairs, list of %llu", cnt, cap);
     }
     m->n_near = (long long)cnt;
     if (e != cudaSuccess) {
@@ -902,6 +1022,9 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     const size_t need = bem::solver_layout(n, prec, m, pc, nullptr, nullptr, n_rhs, nullptr, half);
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
+    int dev = 0;
+    CU(cudaGetDevice(&dev));
+    free_b += bem::dev_cached_bytes(dev);   // cached blocks are free for this purpose
     double budget = prm.hbm_budget_bytes > 0 ? prm.hbm_budget_bytes : (double)free_b - 1.0e9;
     if ((double)need > budget)
         return fail(BEM_ERR_OUT_OF_HBM, "solver for %d unknowns needs %.3f GB, budget %.3f GB", n, need / 1e9,
@@ -918,7 +1041,7 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     for (auto &ev : s->ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);
-    if (e == cudaSuccess) e = cudaMalloc(&s->block, need);
+    if (e == cudaSuccess) e = bem::dev_malloc((void **)&s->block, need);
     if (e == cudaSuccess) {
         s->block_bytes = need;
         s->n_rhs = n_rhs;

@@ -87,6 +87,19 @@ inline int pc_blocks(int n) { return ceil_div(n, kBlock); }
 void count_launches(long long k);
 long long launches();
 
+// Device-memory cache for meshes, solvers and point buffers.  Released blocks
+// stay allocated per device and go to the next request of about the same size
+// (at most 1/8 larger): cudaFree synchronizes the device and takes
+// milliseconds for GB-sized blocks, so creating and destroying solvers per
+// request would otherwise cost as much as a small solve.  dev_free waits for
+// the device to be idle before keeping a block, as cudaFree does.  A failed
+// cudaMalloc releases the cached blocks and retries.  BEM_GB300_CACHE=0 turns
+// the cache off.
+cudaError_t dev_malloc(void **p, size_t bytes);
+void dev_free(void *p);
+size_t dev_cached_bytes(int device);
+void dev_release_cached(int device);   // device < 0: every device
+
 // Copies the quadrature tables into constant memory of the current device.
 cudaError_t init_device_tables();
 
@@ -113,8 +126,10 @@ struct AsmBatch {
 void asm_batch_finish(AsmBatch &t);
 
 // Pairs integrated with subdivision plus self pairs (row, column | image
-// mask << kNearColBits); list == nullptr only counts.
-cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long *count, cudaStream_t st);
+// mask << kNearColBits) into list[0, cap); *count (zero before) receives the
+// number of pairs, also when it exceeds cap.
+cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long cap, unsigned long long *count,
+                             cudaStream_t st);
 // Writable image tables of a mesh (DevSym's layout).
 struct ImageTables {
     double *v64, *c64;

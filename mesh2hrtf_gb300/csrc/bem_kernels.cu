@@ -276,9 +276,11 @@ __global__ void __launch_bounds__(256) k_image_tables(DevMeshView mv, ImageTable
 // Pairs (row i, column j) that NumCalc integrates with subdivision (level-0
 // ratio distance/sqrt(area) < 1.3, exact FP64 test, for any image of j) plus
 // the self pairs.  Depends on the geometry only, so it is built once per
-// mesh.  Pass 1 (list == nullptr) counts, pass 2 fills; warp-aggregated
-// atomics.
-__global__ void __launch_bounds__(256) k_near_list(DevMeshView mv, int2 *list, unsigned long long *count) {
+// mesh.  Entries go to list[0, cap) in any order (warp-aggregated atomics);
+// *count ends as the number of entries, which may exceed cap (the caller
+// then runs again with a larger list).
+__global__ void __launch_bounds__(256) k_near_list(DevMeshView mv, int2 *list, unsigned long long *count,
+                                                   unsigned long long cap) {
     const DevMesh m = to_dev(mv);
     const int lane = threadIdx.x, n = m.n;
     const int i = blockIdx.y * 8 + threadIdx.y;
@@ -305,8 +307,8 @@ __global__ void __launch_bounds__(256) k_near_list(DevMeshView mv, int2 *list, u
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(mask));
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (near && list)
-        list[base + __popc(mask & ((1u << lane) - 1u))] = make_int2(i, j | (int)(imask << kNearColBits));
+    const unsigned long long idx = base + __popc(mask & ((1u << lane) - 1u));
+    if (near && list && idx < cap) list[idx] = make_int2(i, j | (int)(imask << kNearColBits));
 }
 
 // ------------------------------------------------------------ regular pairs
@@ -1066,10 +1068,11 @@ cudaError_t launch_image_tables(const DevMeshView &m, const ImageTables &out, cu
     return cudaGetLastError();
 }
 
-cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long *count, cudaStream_t st) {
+cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long cap, unsigned long long *count,
+                             cudaStream_t st) {
     dim3 block(32, 8), grid((m.n + 31) / 32, (m.n + 7) / 8);
     count_launches(1);
-    k_near_list<<<grid, block, 0, st>>>(m, list, count);
+    k_near_list<<<grid, block, 0, st>>>(m, list, count, cap);
     return cudaGetLastError();
 }
 

@@ -429,6 +429,9 @@ bem_status bem_server_create(const bem_server_params *p, bem_server_t *out) {
     S->m = m;
     size_t free_b = 0, total_b = 0;
     BEM_CU(cudaMemGetInfo(&free_b, &total_b));
+    // the arena is one block: hand the library's cached blocks back first
+    bem::dev_release_cached(p->device);
+    BEM_CU(cudaMemGetInfo(&free_b, &total_b));
     double budget = p->hbm_budget_bytes > 0 ? p->hbm_budget_bytes : (double)free_b - 1.0e9;
     if (budget <= 0 || budget > (double)free_b)
         return bem::fail(BEM_ERR_OUT_OF_HBM, "server budget %.3f GB, device has %.3f GB free", budget / 1e9,

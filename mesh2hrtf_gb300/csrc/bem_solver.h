@@ -50,9 +50,10 @@ struct bem_mesh_s {
         return v;
     }
     ~bem_mesh_s() {
-        cudaFree(d_nvert); cudaFree(d_v64); cudaFree(d_c64); cudaFree(d_n64); cudaFree(d_area);
-        cudaFree(d_sqa); cudaFree(d_chi); cudaFree(d_clo); cudaFree(d_t32); cudaFree(d_q32); cudaFree(d_isqa);
-        cudaFree(d_near); cudaFree(d_n32); cudaFree(d_img);
+        for (void *p : {(void *)d_nvert, (void *)d_v64, (void *)d_c64, (void *)d_n64, (void *)d_area, (void *)d_sqa,
+                        (void *)d_chi, (void *)d_clo, (void *)d_t32, (void *)d_q32, (void *)d_isqa, (void *)d_near,
+                        (void *)d_n32, d_img})
+            bem::dev_free(p);
     }
 };
 
@@ -121,10 +122,10 @@ struct bem_solver_s {
         if (st) cudaStreamSynchronize(st);
         eng.reset();
         if (own_block) {
-            cudaFree(block);
-            cudaFree(pts); cudaFree(pot); cudaFree(grad);
+            bem::dev_free(block);
+            bem::dev_free(pts); bem::dev_free(pot); bem::dev_free(grad);
         }
-        cudaFree(src_extra);
+        bem::dev_free(src_extra);
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
         if (st) cudaStreamDestroy(st);
