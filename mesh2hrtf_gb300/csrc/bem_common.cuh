@@ -131,6 +131,23 @@ __device__ __forceinline__ int gauss_order(double ratdis) {
     return 6;
 }
 
+// Approximate decision (split, Gauss order) in float; returns false if the ratio lies too
+// close to a threshold to decide without the exact FP64 value.
+__device__ __forceinline__ bool classify_fast(float rf, bool &near, int &order) {
+    const float tol = 2e-5f;
+    if (fabsf(rf - 1.3f) <= tol * 1.3f) return false;
+    near = rf < 1.3f;
+    if (near) return true;
+#pragma unroll
+    for (int mm = 2; mm <= 5; ++mm) {
+        const float t = c_quad.order_thrf[mm];
+        if (fabsf(rf - t) <= tol * t) return false;
+        if (rf >= t) { order = mm; return true; }
+    }
+    order = 6;
+    return true;
+}
+
 // ------------------------------------------------------------ mesh tables
 // Device element tables, structure of arrays (index [row * n + element]).
 struct DevMesh {

@@ -64,23 +64,6 @@ __device__ __forceinline__ cplx<double> ld_c(const double *p, int idx) {
     return {v.x, v.y};
 }
 
-// Approximate level-0 decision in float; returns false if the ratio lies too
-// close to a threshold to decide without the exact FP64 value.
-__device__ __forceinline__ bool classify_fast(float rf, bool &near, int &order) {
-    const float tol = 2e-5f;
-    if (fabsf(rf - 1.3f) <= tol * 1.3f) return false;
-    near = rf < 1.3f;
-    if (near) return true;
-#pragma unroll
-    for (int mm = 2; mm <= 5; ++mm) {
-        const float t = c_quad.order_thrf[mm];
-        if (fabsf(rf - t) <= tol * t) return false;
-        if (rf >= t) { order = mm; return true; }
-    }
-    order = 6;
-    return true;
-}
-
 // Regular pair in precision T with a fixed Gauss order (no subdivision):
 // the single-subelement case of NC_RegularIntegration.
 template <typename T> struct FarPair;
@@ -529,10 +512,15 @@ __device__ __forceinline__ void near_pair(const DevMeshView &mv, const DevFreq &
             else a += (col_adm<double>(f, j, bcj) * beta - cplx<double>{1.0, 0.0}) * 0.5;
             entry = {(T)a.re, (T)a.im};
         } else if constexpr (std::is_same<T, double>::value) {
+            // float tables only for the subdivision's fast decisions
+            const float xhi[3] = {m.chi[i], m.chi[n + i], m.chi[2 * n + i]};
+            const float xlo[3] = {m.clo[i], m.clo[n + i], m.clo[2 * n + i]};
+            Elem32 ef;
+            load_elem32(mk, j, xhi, xlo, ef);
             AsmSink<double> sink;
             sink.e = &e; sink.x = x64; sink.nx = nx64; sink.k = f.k; sink.wr = f.wr;
             sink.init();
-            const int rc = warp_subdivide(e, m.area64[j], x64, ws, sink);
+            const int rc = warp_subdivide(e, m.area64[j], x64, ws, sink, &ef, m.isqa32[j]);
             if (rc != kDevOk) err = rc;
             KVals<double> v = sink.reduce();
             entry = combine_entry(v, bcj, col_adm<double>(f, j, bcj), PT);
@@ -545,7 +533,7 @@ __device__ __forceinline__ void near_pair(const DevMeshView &mv, const DevFreq &
             AsmSink<float> sink;
             sink.e = &e32; sink.nx = nx32; sink.k = PT.k; sink.wr = PT.wr;
             sink.init();
-            const int rc = warp_subdivide(e, m.area64[j], x64, ws, sink);
+            const int rc = warp_subdivide(e, m.area64[j], x64, ws, sink, &e32, m.isqa32[j]);
             if (rc != kDevOk) err = rc;
             KVals<float> v = sink.reduce();
             entry = combine_entry(v, bcj, col_adm<float>(f, j, bcj), PT);
@@ -882,12 +870,12 @@ __global__ void __launch_bounds__(256, 2) k_project(const __grid_constant__ Proj
                     rc = warp_subdivide(e, m.area64[jl], x64, ws, sink);
                     r = sink.reduce();
                 } else {
-                    Elem32 e32;
+                    Elem32 e32;   // float tables: the arithmetic and the fast decisions
                     load_elem32(mk, jl, xhi, xlo, e32);
                     ProjSink<float> sink;
                     sink.e = &e32; sink.phi = ph; sink.vel = vl; sink.ivi = iv; sink.k = k; sink.wr = wr;
                     sink.init();
-                    rc = warp_subdivide(e, m.area64[jl], x64, ws, sink);
+                    rc = warp_subdivide(e, m.area64[jl], x64, ws, sink, &e32, m.isqa32[jl]);
                     r = sink.reduce();
                 }
                 if (rc != kDevOk) err = rc;

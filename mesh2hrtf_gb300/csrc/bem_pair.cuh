@@ -187,8 +187,18 @@ __device__ __forceinline__ int sub_npts(int nv, int order) {
 // stored ones are integrated immediately (points spread over the lanes).
 // Returns kDevOk or an error code; all lanes return the same value and every
 // lane's sink holds a partial sum (the caller reduces).
+// Fast decisions: with ef (the element's float tables for this point, D =
+// centre - x in double-float) and isqa = 1/sqrt(area) in float, levels up to
+// kFastLevels decide "split" and the Gauss order from a float ratio, and take
+// the exact FP64 test only within 2e-5 of a threshold; deeper levels (points
+// within an eighth of the element from it) always take the exact test.  The
+// decisions are the exact ones either way: the float ratio is accurate to
+// ~1e-6 relative there.
+constexpr int kFastLevels = 3;
+
 template <class Sink>
-__device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], WarpScratch &ws, Sink &sink) {
+__device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], WarpScratch &ws, Sink &sink,
+                              const Elem32 *ef = nullptr, float isqa = 0.f) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int nv = e.nv;
@@ -207,21 +217,57 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
             const int idi = base + lane;
             const bool active = idi < nsel;
             bool split = false;
+            int ordf = 0;   // Gauss order from the float test (0: not decided there)
             double ratdis = 0.0, scent = 0.0, tcent = 0.0;
             double vs[4] = {0, 0, 0, 0}, vt[4] = {0, 0, 0, 0};
             if (active) {
                 for (int v = 0; v < nv; ++v) {
                     vs[v] = ws.lv[cur][idi][v][0];
                     vt[v] = ws.lv[cur][idi][v][1];
-                    scent = __dadd_rn(scent, vs[v]);
-                    tcent = __dadd_rn(tcent, vt[v]);
                 }
-                scent = __ddiv_rn(scent, (double)nv);
-                tcent = __ddiv_rn(tcent, (double)nv);
-                double cp[3];
-                global_point_exact(e, scent, tcent, cp);
-                ratdis = __ddiv_rn(dist_exact(cp, x), sqa);
-                split = ratdis < kTolf;
+                bool decided = false;
+                if (ef && level <= kFastLevels) {
+                    float sc = 0.f, tc = 0.f;
+                    for (int v = 0; v < nv; ++v) {
+                        sc += (float)vs[v];
+                        tc += (float)vt[v];
+                    }
+                    sc /= (float)nv;
+                    tc /= (float)nv;
+                    float d[3];
+                    if (nv == 3) {
+                        const float ss = sc - (1.0f / 3.0f), tt = tc - (1.0f / 3.0f);
+                        for (int k = 0; k < 3; ++k) d[k] = ef->D[k] + ss * ef->a[k] + tt * ef->b[k];
+                    } else {
+                        const float s1 = 0.25f * (sc + 1.0f), s2 = 0.25f * (sc - 1.0f), t1 = tc + 1.0f, t2 = tc - 1.0f;
+                        const float sh[4] = {s1 * t1, -s2 * t1, s2 * t2, -s1 * t2};
+                        for (int k = 0; k < 3; ++k)
+                            d[k] = ef->D[k] + sh[0] * ef->q[0][k] + sh[1] * ef->q[1][k] + sh[2] * ef->q[2][k] +
+                                   sh[3] * ef->q[3][k];
+                    }
+                    const float rf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * isqa / (float)faclin;
+                    bool nr = false;
+                    int o = 2;
+                    if (classify_fast(rf, nr, o)) {
+                        split = nr;
+                        ordf = nr ? 0 : o;
+                        decided = true;
+                    }
+                }
+                if (!decided || split) {
+                    for (int v = 0; v < nv; ++v) {
+                        scent = __dadd_rn(scent, vs[v]);
+                        tcent = __dadd_rn(tcent, vt[v]);
+                    }
+                    scent = __ddiv_rn(scent, (double)nv);
+                    tcent = __ddiv_rn(tcent, (double)nv);
+                }
+                if (!decided) {
+                    double cp[3];
+                    global_point_exact(e, scent, tcent, cp);
+                    ratdis = __ddiv_rn(dist_exact(cp, x), sqa);
+                    split = ratdis < kTolf;
+                }
             }
             const unsigned smask = __ballot_sync(0xffffffffu, split);
             if (split) {
@@ -279,7 +325,7 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
                     ox = vs[jr]; oy = vt[jr];
                     fac = dxi >= 0.0 ? faclin : -faclin;
                 }
-                const int ord = gauss_order(ratdis);
+                const int ord = ordf ? ordf : gauss_order(ratdis);
                 ws.sxi[r] = (float)ox; ws.seta[r] = (float)oy; ws.sfac[r] = (float)fac;
                 ws.sord[r] = ord;
             }
