@@ -737,6 +737,49 @@ __global__ void __launch_bounds__(256) k_fields(const __grid_constant__ ProjBatc
     ivi[j] = any;
 }
 
+// Far-pair projection of a flat triangle without velocity terms, fused
+// (NC_IntegrationTBEM, NC_PostProcessing.cpp:1217-1322, with phi factored out
+// of the quadrature sum): per point Gw = w J e^{i wr r}/(4 pi r), Gi =
+// Gw (-1/r + i wr), r^.n_y = (D.n_y)/r (constant numerator on a flat
+// element);
+//   P  += Gi (r^.n_y)
+//   U  += Gw [(r^.n_y)(k^2 - 3/r^2) + i 3 wr (r^.n_y)/r] / r * (y - x)
+//   T  -= Gi / r
+// and the element adds phi P to the potential and phi (U + T n_y) to the
+// gradient.
+template <int NP, int O0>
+__device__ __forceinline__ void proj_tri_points(const Elem32 &e, float dny, float k2, float wr, float2 &P,
+                                                float2 (&U)[3], float2 &T) {
+#pragma unroll
+    for (int g = 0; g < NP; ++g) {
+        const float ss = c_trif[O0 + g][0] - (1.0f / 3.0f), tt = c_trif[O0 + g][1] - (1.0f / 3.0f);
+        const float wj = c_trif[O0 + g][2] * e.J * (float)(1.0 / kPI4);
+        float d[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) d[k] = fmaf(tt, e.b[k], fmaf(ss, e.a[k], e.D[k]));
+        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const float ir = rsqrtf(r2), r = r2 * ir;
+        float sn, cs;
+        phase_sincos(wr * r, &sn, &cs);
+        const float amp = wj * ir;
+        const float gr = cs * amp, gi = sn * amp;                              // Gw
+        const float hr = fmaf(-gr, ir, -gi * wr), hi = fmaf(gr, wr, -gi * ir);   // Gi
+        const float dn = dny * ir;                                           // r^.n_y
+        P.x = fmaf(hr, dn, P.x);
+        P.y = fmaf(hi, dn, P.y);
+        const float ir2 = ir * ir;
+        const float f1r = dn * (k2 - 3.0f * ir2), f1i = 3.0f * wr * dn * ir;
+        const float ur = (gr * f1r - gi * f1i) * ir, ui = (gr * f1i + gi * f1r) * ir;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            U[k].x = fmaf(ur, d[k], U[k].x);
+            U[k].y = fmaf(ui, d[k], U[k].y);
+        }
+        T.x = fmaf(-hr, ir, T.x);
+        T.y = fmaf(-hi, ir, T.y);
+    }
+}
+
 // Element data of image kref for the projection: potential and nodal
 // velocities times the reflection factor, velocities in the image's node
 // order (NC_ContributionTBEM, NC_PostProcessing.cpp:925-940).
@@ -832,7 +875,25 @@ __global__ void __launch_bounds__(256, 2) k_project(const __grid_constant__ Proj
                         near = rd < kTolf;
                         if (!near) order = gauss_order(rd);
                     }
-                    if (!near) {
+                    if (!near && e.nv == 3 && !iv) {
+                        // fused flat-triangle path (no velocity terms)
+                        float2 P = make_float2(0.f, 0.f), U[3], T = make_float2(0.f, 0.f);
+                        U[0] = U[1] = U[2] = make_float2(0.f, 0.f);
+                        const float dny = e.D[0] * e.n[0] + e.D[1] * e.n[1] + e.D[2] * e.n[2];
+                        const float k2 = (float)k * (float)k;
+                        if (order <= 2) proj_tri_points<4, 0>(e, dny, k2, (float)wr, P, U, T);
+                        else if (order == 3) proj_tri_points<7, 4>(e, dny, k2, (float)wr, P, U, T);
+                        else proj_tri_points<13, 11>(e, dny, k2, (float)wr, P, U, T);
+                        const cplx<float> pp = ph * cplx<float>{P.x, P.y};
+                        acc.p.re += pp.re;
+                        acc.p.im += pp.im;
+#pragma unroll
+                        for (int kk = 0; kk < 3; ++kk) {
+                            const cplx<float> gg = ph * cplx<float>{fmaf(T.x, e.n[kk], U[kk].x), fmaf(T.y, e.n[kk], U[kk].y)};
+                            acc.g[kk].re += gg.re;
+                            acc.g[kk].im += gg.im;
+                        }
+                    } else if (!near) {
                         const int np = e.nv == 3 ? tri_count(order) : quad_count(order);
                         for (int g = 0; g < np; ++g) {
                             float s, t, wq;
