@@ -85,6 +85,10 @@ struct QuadTables {
     // order is 6.  Computed on the host by bisection over doubles.
     double order_thr[8];
     float order_thrf[8];
+    // squared ratio beyond which the float test alone gives order 2 (the
+    // order-2 threshold with a 3e-5 margin): skips the square root and the
+    // threshold scan for most regular pairs
+    float far2_sq;
 };
 // Defined here: exactly one translation unit (bem_kernels.cu) includes this
 // header.

@@ -336,7 +336,7 @@ __device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f
         load_elem32(m, j, zero, zero, e);
         const float cjh[3] = {m.chi[j], m.chi[n + j], m.chi[2 * n + j]};
         const float cjl[3] = {m.clo[j], m.clo[n + j], m.clo[2 * n + j]};
-        const float isq = m.isqa32[j];
+        const float isq2 = m.isqa32[j] * m.isqa32[j];
         FusedCol fc;
         fc.bc = bcj;
         fc.yr = admj.re;
@@ -350,10 +350,10 @@ __device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f
             if (i >= n) break;
             if (i == j) { A[(size_t)i * lda + j] = make_float2(0.f, 0.f); continue; }
             for (int k = 0; k < 3; ++k) e.D[k] = (cjh[k] - m.chi[k * n + i]) + (cjl[k] - m.clo[k * n + i]);
-            const float rf = sqrtf(e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * isq;
+            const float q2 = (e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * isq2;
             bool near = false;
             int order = 2;
-            if (!classify_fast(rf, near, order)) {
+            if (q2 <= c_quad.far2_sq && !classify_fast(sqrtf(q2), near, order)) {
                 const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
                 const double rd = ratio0_exact(m, j, x64);
                 near = rd < kTolf;
@@ -410,7 +410,7 @@ __device__ __forceinline__ void far_tile_img(const DevMeshView &mv, const DevFre
             load_elem32(mk, j, zero, zero, e);
             const float cjh[3] = {mk.chi[j], mk.chi[n + j], mk.chi[2 * n + j]};
             const float cjl[3] = {mk.clo[j], mk.clo[n + j], mk.clo[2 * n + j]};
-            const float isq = m.isqa32[j];
+            const float isq2 = m.isqa32[j] * m.isqa32[j];
             FusedCol fc;
             fc.bc = bcj;
             fc.yr = admj.re;
@@ -424,10 +424,10 @@ __device__ __forceinline__ void far_tile_img(const DevMeshView &mv, const DevFre
                 if (i >= n) break;
                 if (kref == 0 && i == j) continue;
                 for (int k = 0; k < 3; ++k) e.D[k] = (cjh[k] - m.chi[k * n + i]) + (cjl[k] - m.clo[k * n + i]);
-                const float rf = sqrtf(e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * isq;
+                const float q2 = (e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * isq2;
                 bool near = false;
                 int order = 2;
-                if (!classify_fast(rf, near, order)) {
+                if (q2 <= c_quad.far2_sq && !classify_fast(sqrtf(q2), near, order)) {
                     const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
                     const double rd = ratio0_exact(mk, j, x64);
                     near = rd < kTolf;
@@ -869,8 +869,8 @@ __global__ void __launch_bounds__(256, 2) k_project(const __grid_constant__ Proj
                 } else {
                     Elem32 e;
                     load_elem32(mk, j, xhi, xlo, e);
-                    const float dist = sqrtf(e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]);
-                    if (!classify_fast(dist * m.isqa32[j], near, order)) {
+                    const float q2 = (e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * (m.isqa32[j] * m.isqa32[j]);
+                    if (q2 <= c_quad.far2_sq && !classify_fast(sqrtf(q2), near, order)) {
                         const double rd = ratio0_exact(mk, j, x64);
                         near = rd < kTolf;
                         if (!near) order = gauss_order(rd);
@@ -1102,6 +1102,7 @@ cudaError_t init_device_tables() {
         q.order_thr[m] = order_threshold(m);
         q.order_thrf[m] = (float)q.order_thr[m];
     }
+    q.far2_sq = (float)((q.order_thr[2] * (1.0 + 3e-5)) * (q.order_thr[2] * (1.0 + 3e-5)));
     cudaError_t e = cudaMemcpyToSymbol(c_quad, &q, sizeof(q));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_trif, trif, sizeof(trif));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_glxf, glxf, sizeof(glxf));
