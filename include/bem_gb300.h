@@ -104,8 +104,11 @@ typedef struct {
     double tol;                /* relative residual target (0 = 1e-9)          */
     double hbm_budget_bytes;   /* admission budget for this solver (0 = all
                                   free device memory minus a reserve)          */
-    int32_t no_precond;        /* 0: block-Jacobi preconditioner (default),
-                                  1: none                                      */
+    int32_t no_precond;        /* 0 (default): block-Jacobi inverse X of the
+                                  128-unknown diagonal blocks with one
+                                  correction step over 1024-unknown diagonal
+                                  windows A_w, M = X (2 I - A_w X);
+                                  1: none; 2: block-Jacobi only (M = X)       */
     int32_t n_rhs;             /* right-hand sides the solver can hold for
                                   bem_solve_multi (0 or 1: one; at most 16)    */
     int32_t complex64_krylov;  /* mixed precision with one right-hand side:

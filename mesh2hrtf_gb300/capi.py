@@ -216,11 +216,19 @@ class Solver:
 
     def __init__(self, mesh: Mesh, precision=PREC_FP64, restart=0, max_iter=0, tol=0.0, hbm_budget=0.0,
                  precond=True, n_rhs=1, complex64_krylov=False):
-        """complex64_krylov: mixed precision without the fp16 Krylov copy of A."""
+        """complex64_krylov: mixed precision without the fp16 Krylov copy of A.
+        precond: True (block-Jacobi with its window correction), "block-jacobi"
+        (block-Jacobi alone) or False (none)."""
         lib = load()
         self.mesh = mesh
         self.n = mesh.n
-        p = SolverParams(precision, restart, max_iter, tol, hbm_budget, 0 if precond else 1, n_rhs,
+        if precond == "block-jacobi":
+            npc = 2
+        elif precond is True or precond is False:
+            npc = 0 if precond else 1
+        else:
+            raise ValueError("precond must be True, False or 'block-jacobi', not %r" % (precond,))
+        p = SolverParams(precision, restart, max_iter, tol, hbm_budget, npc, n_rhs,
                          1 if complex64_krylov else 0)
         h = C.c_void_p()
         _check(lib.bem_solver_create(mesh.handle, C.byref(p), C.byref(h)))

@@ -279,6 +279,10 @@ size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, Solve
             q.xh = (float2 *)take(xsplit_elems(n) * 8);
             q.xf = (float4 *)take(xsplit_elems(n) * 16);
         }
+        if (pc) {
+            q.pcy = take(N * 16);
+            q.pcz = take(N * 16);
+        }
         q.dpa = (double2 *)take(dp_elems(n) * 16);
         q.dpb = (double2 *)take(dp_elems(n) * 16);
         q.nrmp = (double *)take((size_t)vec_blocks(n) * 8);
@@ -1014,7 +1018,9 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     const int m = prm.restart > 0 ? prm.restart : 60;
     if (m > bem::kMaxRestart) return fail(BEM_ERR_INVALID, "restart length %d above the limit %d", m, bem::kMaxRestart);
     const int n = mesh->n;
-    const bool pc = prm.no_precond == 0;
+    if (prm.no_precond < 0 || prm.no_precond > 2)
+        return fail(BEM_ERR_INVALID, "no_precond %d is not 0, 1 or 2", prm.no_precond);
+    const bool pc = prm.no_precond != 1;
     const int prec = prm.precision == BEM_PREC_FP64 ? 0 : 1;
     const int n_rhs = prm.n_rhs > 0 ? prm.n_rhs : 1;
     if (n_rhs > bem::kMaxRhs) return fail(BEM_ERR_INVALID, "n_rhs %d above the limit %d", n_rhs, bem::kMaxRhs);
@@ -1038,6 +1044,7 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     s->tol = prm.tol > 0 ? prm.tol : 1e-9;
     s->lda = round_up((size_t)n, 32);
     s->precond = pc;
+    s->pc_window = prm.no_precond == 0;
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     for (auto &ev : s->ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);

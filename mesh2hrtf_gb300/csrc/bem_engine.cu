@@ -71,6 +71,7 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
         h_tab_->sys[b] = sys[b];
         h_tab_->sys[b].st = d_st_ + b;
         h_tab_->sys[b].shared = 0;
+        h_tab_->pcw_any |= sys[b].pcw;
         h_st_[b] = init[b];
     }
     // complex64 systems next to each other on the same matrix (the right-hand

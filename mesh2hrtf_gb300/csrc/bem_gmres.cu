@@ -3,9 +3,10 @@
 //
 // Counterpart of NumCalc's NC_IterativeSolverCGS with its preconditioners
 // and matrix-vector product (NC_CommonFunctions.cpp:1066-1245, 1322-1721).
-// The method is different (GMRES with a block-Jacobi preconditioner and
-// refinement instead of CGS with a threshold ILU); the system solved and the
-// stopping rule (relative residual below 1e-9 by default) are NumCalc's.
+// The method is different (GMRES with a block-Jacobi preconditioner, its
+// window correction and refinement instead of CGS with a threshold ILU); the
+// system solved and the stopping rule (relative residual below 1e-9 by
+// default) are NumCalc's.
 //
 // Every system of the batch carries a small state machine (KState) in device
 // memory.  An iteration body runs kSteps Arnoldi steps for each system in
@@ -16,7 +17,7 @@
 // replays.  The per-system arithmetic does not depend on the other systems of
 // the batch, so a system's result is the same alone and in any mix.
 //
-// Arnoldi step k (6 launches):
+// Arnoldi step k (8 launches):
 //   k_mv_tma      w_parts = A z_k               complex64: bulk-copy pipeline
 //   (k_mv64)                                    complex128: persistent tiles
 //   k_dot1        w = sum parts; h1 = V^H w     per 256-row block
@@ -26,14 +27,17 @@
 //                 the fp16 Krylov copy, skip the second pass: k_axpy<1>
 //                 passes them by and k_axpy<2> subtracts V h1)
 //   k_scale       v_{k+1} = w / |w|; z_{k+1} = M^{-1} v_{k+1}
+//   k_pcwin,      the preconditioner's window correction:
+//   k_pcfin       M^{-1} = X (2 I - A_w X), X block-Jacobi (2 launches)
 //   k_givens      column k of H, rotations, residual estimate, phase
-// End of cycle (6 launches):
+// End of cycle (8 launches):
 //   k_trisolve    y = H^{-1} g                   warp per system
-//   k_xupdate     x += M^{-1} (V y)
+//   k_xupdate     x += M^{-1} (V y)              (+ k_pcwin, k_pcfin)
 //   k_mv_tma      b - A x with error-free products (the refinement residual)
 //   k_resid       r, |r|^2 partials
 //   k_decide      convergence / stagnation / limit, restart set-up
 //   k_scale       v_0 = r / |r|; z_0 = M^{-1} v_0 (restarted systems)
+//                 (+ k_pcwin, k_pcfin)
 //
 // Inner products are summed in a fixed order (per block, then over blocks in
 // block order, every block computing the same sums), so results are
@@ -1365,13 +1369,15 @@ __global__ void __launch_bounds__(kThreads) k_scale(const KTable *tb) {
             v = make_double2(a.x * s, a.y * s);
             S.V[(size_t)dst * S.ldv + row] = v;
         }
+        // with the window correction, X v goes to pcy and k_pcwin / k_pcfin
+        // form the product's input
         if (C128) {
             double2 u = v;   // input of the next product
             if (S.pc) {
                 vs[threadIdx.x] = v;
                 __syncthreads();
                 u = apply_minv<true>(S.Minv, n, blk, vs);
-                if (row < n) S.z[row] = u;
+                if (row < n) (S.pcw ? (double2 *)S.pcy : S.z)[row] = u;
             }
         } else {
             float2 u = make_float2((float)v.x, (float)v.y);
@@ -1380,7 +1386,7 @@ __global__ void __launch_bounds__(kThreads) k_scale(const KTable *tb) {
                 __syncthreads();
                 u = apply_minv_f(S.Minv, n, blk, vf);
             }
-            if (row < n) S.xh[row] = u;
+            if (row < n) (S.pcw ? (float2 *)S.pcy : S.xh)[row] = u;
         }
         __syncthreads();
     }
@@ -1474,6 +1480,28 @@ __global__ void __launch_bounds__(128) k_trisolve(const KTable *tb) {
     }
 }
 
+// x += d for the thread's row; complex64 systems also keep the float forms
+// of x (first cycle) or d (later cycles) that the residual products read
+template <bool C128>
+__device__ __forceinline__ void xupdate_finish(const KSys &S, const KState *st, int row, double2 t) {
+    double2 xv = S.x[row];
+    xv.x += t.x;
+    xv.y += t.y;
+    S.x[row] = xv;
+    if (!C128 && st->cycles == 1) {
+        // first residual: (hi, lo) float split of x, stored so that
+        // chunk entries 2c and 2c + 1 land in the chunk's first and
+        // second half (conflict-free reads in the product)
+        const float hr = (float)xv.x, hi = (float)xv.y;
+        const int c = row & (kMvChunk - 1);
+        S.xf[(size_t)(row - c) + (c & 1) * (kMvChunk / 2) + (c >> 1)] =
+            make_float4(hr, hi, (float)(xv.x - (double)hr), (float)(xv.y - (double)hi));
+    } else if (!C128) {
+        // later residuals: r -= A d, with the float copy of d
+        S.xh[row] = make_float2((float)t.x, (float)t.y);
+    }
+}
+
 // x += M^{-1} (V y)
 template <bool C128>
 __global__ void __launch_bounds__(kThreads) k_xupdate(const KTable *tb) {
@@ -1502,21 +1530,157 @@ __global__ void __launch_bounds__(kThreads) k_xupdate(const KTable *tb) {
             t = apply_minv<C128>(S.Minv, n, blk, vs);
         }
         if (row < n) {
-            double2 xv = S.x[row];
-            xv.x += t.x;
-            xv.y += t.y;
-            S.x[row] = xv;
-            if (!C128 && st->cycles == 1) {
-                // first residual: (hi, lo) float split of x, stored so that
-                // chunk entries 2c and 2c + 1 land in the chunk's first and
-                // second half (conflict-free reads in the product)
-                const float hr = (float)xv.x, hi = (float)xv.y;
-                const int c = row & (kMvChunk - 1);
-                S.xf[(size_t)(row - c) + (c & 1) * (kMvChunk / 2) + (c >> 1)] =
-                    make_float4(hr, hi, (float)(xv.x - (double)hr), (float)(xv.y - (double)hi));
-            } else if (!C128) {
-                // later residuals: r -= A d, with the float copy of d
-                S.xh[row] = make_float2((float)t.x, (float)t.y);
+            if (!S.pcw) xupdate_finish<C128>(S, st, row, t);
+            else if (C128) ((double2 *)S.pcy)[row] = t;   // k_pcfin adds the corrected d
+            else ((float2 *)S.pcy)[row] = make_float2((float)t.x, (float)t.y);
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ window correction
+// M v = X (2 I - A_w X) v with X the block-Jacobi inverse and A_w the
+// diagonal windows of kPcWin rows of A: after y = X v (k_scale, k_xupdate),
+// k_pcwin forms z = A_w y and k_pcfin u = 2 y - X z.  A Neumann step towards
+// the inverse of the window blocks: it takes about a sixth of the Krylov
+// iterations off block-Jacobi alone on the head-like meshes, for one read
+// of the diagonal windows (kPcWin / N of the matrix) per application.
+// mode 0: after an Arnoldi step (phase ARNOLDI); 1: after a restart (phase
+// ARNOLDI, k = 0); 2: the update at the end of a cycle (phase UPDATE).
+__device__ __forceinline__ bool pcw_active(const KSys &S, int mode) {
+    const KState *st = S.st;
+    if (!S.pcw) return false;
+    if (mode == 2) return st->phase == kPhaseUpdate && st->k != 0;
+    return st->phase == kPhaseArnoldi && (mode == 0 || st->k == 0);
+}
+
+constexpr int kPcRows = 32;                  // rows per k_pcwin item
+constexpr int kPcItems = kThreads / kPcRows; // items per vector block
+static_assert(kPcWin % kThreads == 0, "windows hold whole vector blocks");
+
+__device__ __forceinline__ void cmac(float &sr, float &si, float2 a, float2 y) {
+    sr = fmaf(a.x, y.x, sr); sr = fmaf(-a.y, y.y, sr);
+    si = fmaf(a.x, y.y, si); si = fmaf(a.y, y.x, si);
+}
+
+// z = A_w y, one warp per row; the window's y staged in shared memory.
+// Reads the fp16 copy of A when the system keeps one (scaled by the row's
+// power of two), else the complex64 or complex128 matrix.
+template <bool C128>
+__global__ void __launch_bounds__(kThreads) k_pcwin(const KTable *tb, int mode) {
+    __shared__ __align__(16) double2 ysh[kPcWin];
+    if (!tb->pcw_any) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int it = blockIdx.x; it < tb->vb_total * kPcItems; it += gridDim.x) {
+        const int2 bi = tb->vb_items[it / kPcItems];
+        const KSys &S = tb->sys[bi.x];
+        if (!pcw_active(S, mode)) continue;
+        const int n = S.n, r0 = bi.y * kThreads + (it % kPcItems) * kPcRows;
+        if (r0 >= n) continue;
+        const int c0 = r0 / kPcWin * kPcWin, nw = min(kPcWin, n - c0);
+        const int r1 = min(r0 + kPcRows, n);
+        __syncthreads();   // the previous item's rows are done with ysh
+        if (C128) {
+            const double2 *y = (const double2 *)S.pcy + c0;
+            for (int c = threadIdx.x; c < nw; c += kThreads) ysh[c] = y[c];
+        } else {
+            const float2 *y = (const float2 *)S.pcy + c0;
+            float2 *yf = reinterpret_cast<float2 *>(ysh);
+            for (int c = threadIdx.x; c < nw; c += kThreads) yf[c] = y[c];
+        }
+        __syncthreads();
+        for (int r = r0 + warp; r < r1; r += kThreads / 32) {
+            if (C128) {
+                const double2 *a = (const double2 *)S.A + (size_t)r * S.lda + c0;
+                double sr = 0.0, si = 0.0;
+#pragma unroll 4
+                for (int c = lane; c < nw; c += 32) {
+                    const double2 av = a[c], yv = ysh[c];
+                    sr = fma(av.x, yv.x, sr); sr = fma(-av.y, yv.y, sr);
+                    si = fma(av.x, yv.y, si); si = fma(av.y, yv.x, si);
+                }
+                sr = warp_sum_d(sr);
+                si = warp_sum_d(si);
+                if (lane == 0) ((double2 *)S.pcz)[r] = make_double2(sr, si);
+            } else {
+                const float2 *yf = reinterpret_cast<const float2 *>(ysh);
+                float sr = 0.f, si = 0.f, scale = 1.f;
+                if (S.A16) {
+                    // 16-byte loads of 4 entries; full windows unrolled
+                    const __half2 *a = (const __half2 *)S.A16 + (size_t)r * S.lda + c0;
+                    if (nw == kPcWin) {
+                        uint4 q[kPcWin / 128];
+#pragma unroll
+                        for (int p = 0; p < kPcWin / 128; ++p) q[p] = reinterpret_cast<const uint4 *>(a)[lane + 32 * p];
+#pragma unroll
+                        for (int p = 0; p < kPcWin / 128; ++p) {
+                            const int c = 4 * (lane + 32 * p);
+                            const __half2 *h = reinterpret_cast<const __half2 *>(&q[p]);
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) cmac(sr, si, __half22float2(h[e]), yf[c + e]);
+                        }
+                    } else {
+                        for (int c = lane; c < nw; c += 32) cmac(sr, si, __half22float2(a[c]), yf[c]);
+                    }
+                    scale = S.rs[r];
+                } else {
+                    const float2 *a = (const float2 *)S.A + (size_t)r * S.lda + c0;
+                    if (nw == kPcWin) {
+                        float4 q[kPcWin / 64];
+#pragma unroll
+                        for (int p = 0; p < kPcWin / 64; ++p) q[p] = reinterpret_cast<const float4 *>(a)[lane + 32 * p];
+#pragma unroll
+                        for (int p = 0; p < kPcWin / 64; ++p) {
+                            const int c = 2 * (lane + 32 * p);
+                            cmac(sr, si, make_float2(q[p].x, q[p].y), yf[c]);
+                            cmac(sr, si, make_float2(q[p].z, q[p].w), yf[c + 1]);
+                        }
+                    } else {
+                        for (int c = lane; c < nw; c += 32) cmac(sr, si, a[c], yf[c]);
+                    }
+                }
+                sr = warp_sum_f(sr);
+                si = warp_sum_f(si);
+                if (lane == 0) ((float2 *)S.pcz)[r] = make_float2(sr * scale, si * scale);
+            }
+        }
+    }
+}
+
+// u = 2 y - X z: the product's input (mode 0, 1) or the cycle's update of x
+// (mode 2).
+template <bool C128>
+__global__ void __launch_bounds__(kThreads) k_pcfin(const KTable *tb, int mode) {
+    __shared__ double2 vs[kThreads];
+    __shared__ float2 vf[kThreads];
+    if (!tb->pcw_any) return;
+    for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
+        const int2 bi = tb->vb_items[it];
+        const KSys &S = tb->sys[bi.x];
+        if (!pcw_active(S, mode)) continue;
+        const int n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x;
+        const bool ok = row < n;
+        if (C128) {
+            const double2 *Y = (const double2 *)S.pcy, *Z = (const double2 *)S.pcz;
+            vs[threadIdx.x] = ok ? Z[row] : make_double2(0.0, 0.0);
+            __syncthreads();
+            const double2 q = apply_minv<true>(S.Minv, n, blk, vs);
+            if (ok) {
+                const double2 y = Y[row];
+                const double2 u = make_double2(2.0 * y.x - q.x, 2.0 * y.y - q.y);
+                if (mode == 2) xupdate_finish<true>(S, S.st, row, u);
+                else S.z[row] = u;
+            }
+        } else {
+            const float2 *Y = (const float2 *)S.pcy, *Z = (const float2 *)S.pcz;
+            vf[threadIdx.x] = ok ? Z[row] : make_float2(0.f, 0.f);
+            __syncthreads();
+            const float2 q = apply_minv_f(S.Minv, n, blk, vf);
+            if (ok) {
+                const float2 y = Y[row];
+                const float2 u = make_float2(2.f * y.x - q.x, 2.f * y.y - q.y);
+                if (mode == 2) xupdate_finish<false>(S, S.st, row, make_double2((double)u.x, (double)u.y));
+                else S.xh[row] = u;
             }
         }
         __syncthreads();
@@ -1620,6 +1784,7 @@ __global__ void __launch_bounds__(kMaxSys) k_plans(KTable *tb) {
 
 int g_mv_grid[2] = {0, 0};
 int g_vec_grid = 0;
+int g_pcw_grid = 0;   // k_pcwin: every block it can keep resident (loads in flight)
 std::atomic<long long> g_launches{0};
 
 }  // namespace
@@ -1652,7 +1817,15 @@ cudaError_t krylov_prepare() {
         g_mv_grid[1] = sms;   // one bulk-copy block per SM
         if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mv64<false>, 256, 0);
         g_mv_grid[0] = sms * (per > 0 ? per : 1);
-        g_vec_grid = 2 * sms;
+        // vector kernels: as many blocks as stay resident, so that a batch's
+        // row blocks are all in flight at once (their loops are latency bound)
+        per = 0;
+        if (err == cudaSuccess)
+            err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scale<false, false>, kThreads, 0);
+        g_vec_grid = sms * (per > 2 ? per : 2);
+        per = 0;
+        if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcwin<false>, kThreads, 0);
+        g_pcw_grid = sms * (per > 0 ? per : 1);
     });
     return err;
 }
@@ -1661,6 +1834,17 @@ cudaError_t launch_plans(KTable *d_tab, cudaStream_t st) {
     count_launches(1);
     k_plans<<<1, kMaxSys, 0, st>>>(d_tab);
     return cudaGetLastError();
+}
+
+// the two launches of the preconditioner's window correction
+static void pc_window(bool c128, const KTable *d_tab, int mode, int gv, cudaStream_t st) {
+    if (c128) {
+        k_pcwin<true><<<g_pcw_grid, kThreads, 0, st>>>(d_tab, mode);
+        k_pcfin<true><<<gv, kThreads, 0, st>>>(d_tab, mode);
+    } else {
+        k_pcwin<false><<<g_pcw_grid, kThreads, 0, st>>>(d_tab, mode);
+        k_pcfin<false><<<gv, kThreads, 0, st>>>(d_tab, mode);
+    }
 }
 
 cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev, cudaStream_t st,
@@ -1686,12 +1870,14 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
         k_axpy<2><<<gv, kThreads, 0, st>>>(d_tab);
         if (c128) k_scale<true, false><<<gv, kThreads, 0, st>>>(d_tab);
         else k_scale<false, false><<<gv, kThreads, 0, st>>>(d_tab);
+        pc_window(c128, d_tab, 0, gv, st);
         k_givens<<<1, kMaxSys, 0, st>>>(tb);
-        nl += 6;
+        nl += 8;
     }
     k_trisolve<<<(kMaxSys + 3) / 4, 128, 0, st>>>(d_tab);
     if (c128) k_xupdate<true><<<gv, kThreads, 0, st>>>(d_tab);
     else k_xupdate<false><<<gv, kThreads, 0, st>>>(d_tab);
+    pc_window(c128, d_tab, 2, gv, st);
     if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * kSteps], st, cudaEventRecordExternal);
     if (c128) k_mv64<true><<<gmv, 256, 0, st>>>(tb, 1);
     else {
@@ -1707,7 +1893,8 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
     k_decide<<<1, kMaxSys, 0, st>>>(tb);
     if (c128) k_scale<true, true><<<gv, kThreads, 0, st>>>(d_tab);
     else k_scale<false, true><<<gv, kThreads, 0, st>>>(d_tab);
-    nl += 6;
+    pc_window(c128, d_tab, 1, gv, st);
+    nl += 10;
     e = cudaGetLastError();
     if (launches_out) *launches_out = nl;
     return e;

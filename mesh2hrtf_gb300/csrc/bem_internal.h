@@ -66,6 +66,10 @@ struct DevFreq {
 
 // Unknowns per diagonal block of the block-Jacobi preconditioner.
 constexpr int kBlock = 128;
+// Rows of a window of the preconditioner's correction step (8 blocks): the
+// preconditioner is M = X (2 I - A_w X), X the block-Jacobi inverse and A_w
+// the diagonal windows of A (one Neumann step towards the inverse of A_w).
+constexpr int kPcWin = 1024;
 // Rows per block of the vector kernels (two preconditioner blocks).
 constexpr int kVecBlock = 256;
 // Matrix-vector product tile: kMvRows rows x kMvChunk columns.
@@ -255,6 +259,9 @@ struct KSys {
                             // dimension lda) for the Krylov products, or nullptr
     const float *rs;        // its row scales
     int cgs1;               // one classical Gram-Schmidt pass instead of two
+    int pcw;                // window correction of the preconditioner (needs pc)
+    void *pcy, *pcz;        // its vectors X v and A_w X v: float2 for complex64
+                            // systems, double2 for complex128
     KState *st;
 };
 
@@ -278,6 +285,7 @@ struct KTable {
     int prec;               // 0: complex128 tiles, 1: complex64 strips
     int vb_total;           // vector blocks of all systems
     int err;                // set when a bounded device wait gave up
+    int pcw_any;            // some system applies the window correction
     unsigned mv_ctr[2];     // work queue of the persistent matvec
     KPlan plan[3];          // [0] Krylov product, [1] refinement residual with
                             // error-free products, [2] recursive residual update

@@ -6,6 +6,9 @@
 // preconditioner is the block diagonal of A with blocks of kBlock unknowns,
 // inverted once per frequency; NumCalc's own preconditioner is a threshold
 // ILU on the same near-field entries (NC_CommonFunctions.cpp:1357-1721).
+// By default the Krylov kernels apply it with one correction step over
+// windows of kPcWin unknowns, M = X (2 I - A_w X) (bem_gmres.cu), which
+// needs no further set-up.
 //
 // Inversion: one CTA per block of any system in the batch, in-place
 // Gauss-Jordan with partial pivoting.  complex64 blocks live in shared memory

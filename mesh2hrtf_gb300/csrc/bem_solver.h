@@ -74,6 +74,7 @@ struct SolverBufs {
     double *nrmp = nullptr;
     double2 *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr, *hsum = nullptr;
     void *Minv = nullptr, *Mwork = nullptr;
+    void *pcy = nullptr, *pcz = nullptr;   // window correction vectors
     int *status = nullptr;
     unsigned *ctr = nullptr;   // 4 words: work queues of the persistent assembly kernels
     double *phi = nullptr, *vel = nullptr;
@@ -101,6 +102,7 @@ struct bem_solver_s {
     double tol = 1e-9;
     size_t lda = 0;
     bool precond = true, have_precond = false;
+    bool pc_window = true;   // block-Jacobi with the window correction step
     cudaStream_t st = nullptr;
     cudaEvent_t ev[8] = {};
     unsigned char *block = nullptr;
@@ -142,6 +144,9 @@ struct bem_solver_s {
         k.lda = (long long)lda;
         k.n = n;
         k.pc = have_precond ? 1 : 0;
+        k.pcw = have_precond && pc_window ? 1 : 0;
+        k.pcy = d.pcy;
+        k.pcz = d.pcz;
         k.nchunk = bem::mv_chunks(n);
         k.nvb = bem::vec_blocks(n);
         k.Minv = d.Minv;
