@@ -271,9 +271,11 @@ size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, Solve
         q.b = (double2 *)take(N * 16);
         q.x = (double2 *)take(N * 16);
         q.r = (double2 *)take(N * 16);
-        q.w = (double2 *)take(N * 16);
+        // complex64 systems keep w and the Krylov basis in float pairs
+        const size_t vsz = prec == 0 ? 16 : 8;
+        q.w = (double2 *)take(N * vsz);
         q.z = (double2 *)take(N * 16);
-        q.V = (double2 *)take((size_t)(m + 1) * N * 16);
+        q.V = (double2 *)take((size_t)(m + 1) * N * vsz);
         q.mvp = (double2 *)take(mvp_elems(n) * 16);
         if (prec != 0) {   // complex64: float copies of the product's input
             q.xh = (float2 *)take(xsplit_elems(n) * 8);

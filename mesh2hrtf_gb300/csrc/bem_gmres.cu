@@ -23,9 +23,8 @@
 //   k_dot1        w = sum parts; h1 = V^H w     per 256-row block
 //   k_axpy<1>     w -= V h1; h2 = V^H w         (classical Gram-Schmidt, twice)
 //   k_axpy<2>     w -= V h2; |w|^2 partials
-//                 (systems whose cycles gain only three digits, those with
-//                 the fp16 Krylov copy, skip the second pass: k_axpy<1>
-//                 passes them by and k_axpy<2> subtracts V h1)
+//                 (a system flagged cgs1 takes one pass: k_axpy<1> passes
+//                 it by and k_axpy<2> subtracts V h1)
 //   k_scale       v_{k+1} = w / |w|; z_{k+1} = M^{-1} v_{k+1}
 //   k_pcwin,      the preconditioner's window correction:
 //   k_pcfin       M^{-1} = X (2 I - A_w X), X block-Jacobi (2 launches)
@@ -42,6 +41,13 @@
 // Inner products are summed in a fixed order (per block, then over blocks in
 // block order, every block computing the same sums), so results are
 // deterministic run to run.
+//
+// complex128 systems run the Arnoldi vectors in FP64.  complex64 systems
+// keep w and the basis V in float pairs with FP32 products and sums (GMRES
+// in working precision inside the refinement, whose residuals stay FP64):
+// an inner cycle needs three to five digits, and GB300's narrow FP64 pipe
+// bounded the FP64 inner products and updates of these kernels.  H, the
+// rotations and x stay FP64.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -1184,6 +1190,55 @@ __device__ __forceinline__ double norm_total(const double *__restrict__ nrmp, in
     return t;
 }
 
+// The same for the float Krylov basis of complex64 systems: FP32 products
+// and sums (GB300's FP64 pipe would bound these loops), one float2 inner-
+// product partial per block and vector, the norm partial converted once.
+__device__ void block_dots_f(const float2 *__restrict__ V, long long ldv, int nv, float2 wv, bool ok, int row,
+                             float2 *__restrict__ dp, int nvb, int blk, float (*red)[16]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int l0 = 0; l0 < nv; l0 += 8) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            float re = 0.f, im = 0.f;
+            if (ok && l0 + q < nv) {
+                const float2 a = V[(size_t)(l0 + q) * ldv + row];
+                re = fmaf(a.x, wv.x, a.y * wv.y);
+                im = fmaf(a.x, wv.y, -a.y * wv.x);
+            }
+            re = warp_sum_f(re);
+            im = warp_sum_f(im);
+            if (lane == 0) {
+                red[warp][2 * q] = re;
+                red[warp][2 * q + 1] = im;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 16) {
+            float t = 0.f;
+#pragma unroll
+            for (int w8 = 0; w8 < 8; ++w8) t += red[w8][threadIdx.x];
+            const int q = threadIdx.x >> 1;
+            if (l0 + q < nv) reinterpret_cast<float *>(dp + (size_t)(l0 + q) * nvb + blk)[threadIdx.x & 1] = t;
+        }
+        __syncthreads();
+    }
+}
+
+__device__ void block_norm_f(float2 wv, bool ok, double *__restrict__ nrmp, int blk, float (*red)[16]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float t = ok ? fmaf(wv.x, wv.x, wv.y * wv.y) : 0.f;
+    t = warp_sum_f(t);
+    if (lane == 0) red[warp][0] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.f;
+#pragma unroll
+        for (int w8 = 0; w8 < 8; ++w8) s += red[w8][0];
+        nrmp[blk] = (double)s;
+    }
+    __syncthreads();
+}
+
 // (M^{-1} v)[row] for the thread's own row: vs holds the block's 256 values
 // of v; the thread's 128-row preconditioner block is rows (tid & 128) .. +127.
 // Inverse blocks are stored transposed ([col][row]), so the loads coalesce.
@@ -1223,9 +1278,12 @@ __device__ __forceinline__ double2 apply_minv(const void *Minv, int n, int blk, 
 }
 
 // ------------------------------------------------------------ Arnoldi step
-// w = sum of the matvec partials; dpa = V^H w
+// w = sum of the matvec partials; dpa = V^H w.  complex64 systems keep w and
+// V in float (C128 = false).
+template <bool C128>
 __global__ void __launch_bounds__(kThreads) k_dot1(const KTable *tb) {
     __shared__ double red[8][16];
+    __shared__ float redf[8][16];
     for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
         const int2 bi = tb->vb_items[it];
         const KSys &S = tb->sys[bi.x];
@@ -1233,40 +1291,46 @@ __global__ void __launch_bounds__(kThreads) k_dot1(const KTable *tb) {
         if (st->phase != kPhaseArnoldi) continue;
         const int n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x;
         const bool ok = row < n;
-        double2 wv = make_double2(0.0, 0.0);
-        if (ok) {
-            if (tb->prec == 1) {
-                // complex64 products leave float partials: FP32 sum, one conversion
+        if (!C128) {
+            // complex64 products leave float partials: FP32 sum
+            float2 wv = make_float2(0.f, 0.f);
+            if (ok) {
                 const float2 *mp = reinterpret_cast<const float2 *>(S.mvp);
-                float ax = 0.f, ay = 0.f;
                 for (int c = 0; c < S.nchunk; ++c) {
                     const float2 p = mp[(size_t)c * n + row];
-                    ax += p.x;
-                    ay += p.y;
+                    wv.x += p.x;
+                    wv.y += p.y;
                 }
-                wv = make_double2((double)ax, (double)ay);
-            } else {
+                reinterpret_cast<float2 *>(S.w)[row] = wv;
+            }
+            block_dots_f(reinterpret_cast<const float2 *>(S.V), S.ldv, st->k + 1, wv, ok, row,
+                         reinterpret_cast<float2 *>(S.dpa), S.nvb, blk, redf);
+        } else {
+            double2 wv = make_double2(0.0, 0.0);
+            if (ok) {
                 for (int c = 0; c < S.nchunk; ++c) {
                     const double2 p = S.mvp[(size_t)c * n + row];
                     wv.x += p.x;
                     wv.y += p.y;
                 }
+                S.w[row] = wv;
             }
-            S.w[row] = wv;
+            block_dots(S.V, S.ldv, st->k + 1, wv, ok, row, S.dpa, S.nvb, blk, red);
         }
-        block_dots(S.V, S.ldv, st->k + 1, wv, ok, row, S.dpa, S.nvb, blk, red);
     }
 }
 
 // PASS 1: h = sum(dpa); w -= V h; hsum += h; dpb = V^H w.
 // PASS 2: h = sum(dpb); w -= V h; hsum += h; nrmp = |w|^2 partials.
 // Systems with one Gram-Schmidt pass (KSys::cgs1) skip PASS 1 and take dpa
-// in PASS 2: an inner cycle that stops after three digits keeps the basis
-// orthogonal to ~1e-10 with classical Gram-Schmidt in FP64.
-template <int PASS>
+// in PASS 2.  complex64 systems (C128 = false): float basis, FP32 sums of
+// the block partials and FP32 updates; H accumulates in FP64.
+template <int PASS, bool C128>
 __global__ void __launch_bounds__(kThreads) k_axpy(const KTable *tb) {
     __shared__ double2 hs[kMaxV];
+    __shared__ float2 hsf[kMaxV];
     __shared__ double red[8][16];
+    __shared__ float redf[8][16];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
         const int2 bi = tb->vb_items[it];
@@ -1278,37 +1342,74 @@ __global__ void __launch_bounds__(kThreads) k_axpy(const KTable *tb) {
         const int nv = st->k + 1;
         if (PASS == 1 && S.cgs1) continue;
         const double2 *dp = (PASS == 1 || S.cgs1) ? S.dpa : S.dpb;
-        for (int l = warp; l < nv; l += 8) {
-            double re = 0.0, im = 0.0;
-            for (int c = lane; c < nvb; c += 32) {
-                const double2 p = dp[(size_t)l * nvb + c];
-                re += p.x;
-                im += p.y;
+        if constexpr (!C128) {
+            const float2 *dpf = reinterpret_cast<const float2 *>(dp);
+            for (int l = warp; l < nv; l += 8) {
+                float re = 0.f, im = 0.f;
+                for (int c = lane; c < nvb; c += 32) {
+                    const float2 p = dpf[(size_t)l * nvb + c];
+                    re += p.x;
+                    im += p.y;
+                }
+                re = warp_sum_f(re);
+                im = warp_sum_f(im);
+                if (lane == 0) hsf[l] = make_float2(re, im);
             }
-            re = warp_sum_d(re);
-            im = warp_sum_d(im);
-            if (lane == 0) hs[l] = make_double2(re, im);
-        }
-        __syncthreads();
-        if (blk == 0 && threadIdx.x < nv) {
-            double2 hh = S.hsum[threadIdx.x];
-            hh.x += hs[threadIdx.x].x;
-            hh.y += hs[threadIdx.x].y;
-            S.hsum[threadIdx.x] = hh;
-        }
-        double2 wv = make_double2(0.0, 0.0);
-        if (ok) {
-            wv = S.w[row];
+            __syncthreads();
+            if (blk == 0 && threadIdx.x < nv) {
+                double2 hh = S.hsum[threadIdx.x];
+                hh.x += (double)hsf[threadIdx.x].x;
+                hh.y += (double)hsf[threadIdx.x].y;
+                S.hsum[threadIdx.x] = hh;
+            }
+            float2 wv = make_float2(0.f, 0.f);
+            float2 *wf = reinterpret_cast<float2 *>(S.w);
+            const float2 *Vf = reinterpret_cast<const float2 *>(S.V);
+            if (ok) {
+                wv = wf[row];
 #pragma unroll 8
-            for (int l = 0; l < nv; ++l) {
-                const double2 v = S.V[(size_t)l * S.ldv + row], c = hs[l];
-                wv.x -= c.x * v.x - c.y * v.y;
-                wv.y -= c.x * v.y + c.y * v.x;
+                for (int l = 0; l < nv; ++l) {
+                    const float2 v = Vf[(size_t)l * S.ldv + row], c = hsf[l];
+                    wv.x = fmaf(-c.x, v.x, fmaf(c.y, v.y, wv.x));
+                    wv.y = fmaf(-c.x, v.y, fmaf(-c.y, v.x, wv.y));
+                }
+                wf[row] = wv;
             }
-            S.w[row] = wv;
+            if (PASS == 1) block_dots_f(Vf, S.ldv, nv, wv, ok, row, reinterpret_cast<float2 *>(S.dpb), nvb, blk, redf);
+            else block_norm_f(wv, ok, S.nrmp, blk, redf);
+        } else {
+            for (int l = warp; l < nv; l += 8) {
+                double re = 0.0, im = 0.0;
+                for (int c = lane; c < nvb; c += 32) {
+                    const double2 p = dp[(size_t)l * nvb + c];
+                    re += p.x;
+                    im += p.y;
+                }
+                re = warp_sum_d(re);
+                im = warp_sum_d(im);
+                if (lane == 0) hs[l] = make_double2(re, im);
+            }
+            __syncthreads();
+            if (blk == 0 && threadIdx.x < nv) {
+                double2 hh = S.hsum[threadIdx.x];
+                hh.x += hs[threadIdx.x].x;
+                hh.y += hs[threadIdx.x].y;
+                S.hsum[threadIdx.x] = hh;
+            }
+            double2 wv = make_double2(0.0, 0.0);
+            if (ok) {
+                wv = S.w[row];
+#pragma unroll 8
+                for (int l = 0; l < nv; ++l) {
+                    const double2 v = S.V[(size_t)l * S.ldv + row], c = hs[l];
+                    wv.x -= c.x * v.x - c.y * v.y;
+                    wv.y -= c.x * v.y + c.y * v.x;
+                }
+                S.w[row] = wv;
+            }
+            if (PASS == 1) block_dots(S.V, S.ldv, nv, wv, ok, row, S.dpb, nvb, blk, red);
+            else block_norm(wv, ok, S.nrmp, blk, red);
         }
-        if (PASS == 1) block_dots(S.V, S.ldv, nv, wv, ok, row, S.dpb, nvb, blk, red);
-        else block_norm(wv, ok, S.nrmp, blk, red);
     }
 }
 
@@ -1362,16 +1463,16 @@ __global__ void __launch_bounds__(kThreads) k_scale(const KTable *tb) {
         }
         const double s = RESTART ? 1.0 / st->beta : 1.0 / sqrt(nrm_s);
         const int dst = RESTART ? 0 : st->k + 1;
-        const double2 *src = RESTART ? S.r : S.w;
-        double2 v = make_double2(0.0, 0.0);
-        if (row < n) {
-            const double2 a = src[row];
-            v = make_double2(a.x * s, a.y * s);
-            S.V[(size_t)dst * S.ldv + row] = v;
-        }
         // with the window correction, X v goes to pcy and k_pcwin / k_pcfin
         // form the product's input
         if (C128) {
+            const double2 *src = RESTART ? S.r : S.w;
+            double2 v = make_double2(0.0, 0.0);
+            if (row < n) {
+                const double2 a = src[row];
+                v = make_double2(a.x * s, a.y * s);
+                S.V[(size_t)dst * S.ldv + row] = v;
+            }
             double2 u = v;   // input of the next product
             if (S.pc) {
                 vs[threadIdx.x] = v;
@@ -1380,7 +1481,19 @@ __global__ void __launch_bounds__(kThreads) k_scale(const KTable *tb) {
                 if (row < n) (S.pcw ? (double2 *)S.pcy : S.z)[row] = u;
             }
         } else {
-            float2 u = make_float2((float)v.x, (float)v.y);
+            // float basis: v = w / |w| in FP32 (v_0 = r / beta from the FP64 r)
+            float2 u = make_float2(0.f, 0.f);
+            if (row < n) {
+                if (RESTART) {
+                    const double2 a = S.r[row];
+                    u = make_float2((float)(a.x * s), (float)(a.y * s));
+                } else {
+                    const float2 a = reinterpret_cast<const float2 *>(S.w)[row];
+                    const float sf = (float)s;
+                    u = make_float2(a.x * sf, a.y * sf);
+                }
+                reinterpret_cast<float2 *>(S.V)[(size_t)dst * S.ldv + row] = u;
+            }
             if (S.pc) {
                 vf[threadIdx.x] = u;
                 __syncthreads();
@@ -1507,12 +1620,40 @@ template <bool C128>
 __global__ void __launch_bounds__(kThreads) k_xupdate(const KTable *tb) {
     __shared__ double2 ys[kMaxV];
     __shared__ double2 vs[kThreads];
+    __shared__ float2 ysf[kMaxV];
+    __shared__ float2 vf[kThreads];
     for (int it = blockIdx.x; it < tb->vb_total; it += gridDim.x) {
         const int2 bi = tb->vb_items[it];
         const KSys &S = tb->sys[bi.x];
         const KState *st = S.st;
         if (st->phase != kPhaseUpdate || st->k == 0) continue;
         const int kk = st->k, n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x;
+        if (!C128) {
+            // float basis: d = M^{-1} V y in FP32, added to x in FP64
+            if (threadIdx.x < kk) ysf[threadIdx.x] = make_float2((float)S.y[threadIdx.x].x, (float)S.y[threadIdx.x].y);
+            __syncthreads();
+            const float2 *Vf = reinterpret_cast<const float2 *>(S.V);
+            float2 tf = make_float2(0.f, 0.f);
+            if (row < n) {
+#pragma unroll 8
+                for (int l = 0; l < kk; ++l) {
+                    const float2 v = Vf[(size_t)l * S.ldv + row], c = ysf[l];
+                    tf.x = fmaf(c.x, v.x, fmaf(-c.y, v.y, tf.x));
+                    tf.y = fmaf(c.x, v.y, fmaf(c.y, v.x, tf.y));
+                }
+            }
+            if (S.pc) {
+                vf[threadIdx.x] = tf;
+                __syncthreads();
+                tf = apply_minv_f(S.Minv, n, blk, vf);
+            }
+            if (row < n) {
+                if (!S.pcw) xupdate_finish<false>(S, st, row, make_double2((double)tf.x, (double)tf.y));
+                else reinterpret_cast<float2 *>(S.pcy)[row] = tf;   // k_pcfin adds the corrected d
+            }
+            __syncthreads();
+            continue;
+        }
         if (threadIdx.x < kk) ys[threadIdx.x] = S.y[threadIdx.x];
         __syncthreads();
         double2 t = make_double2(0.0, 0.0);
@@ -1865,9 +2006,15 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
             ++nl;
         }
         if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q + 1], st, cudaEventRecordExternal);
-        k_dot1<<<gv, kThreads, 0, st>>>(d_tab);
-        k_axpy<1><<<gv, kThreads, 0, st>>>(d_tab);
-        k_axpy<2><<<gv, kThreads, 0, st>>>(d_tab);
+        if (c128) {
+            k_dot1<true><<<gv, kThreads, 0, st>>>(d_tab);
+            k_axpy<1, true><<<gv, kThreads, 0, st>>>(d_tab);
+            k_axpy<2, true><<<gv, kThreads, 0, st>>>(d_tab);
+        } else {
+            k_dot1<false><<<gv, kThreads, 0, st>>>(d_tab);
+            k_axpy<1, false><<<gv, kThreads, 0, st>>>(d_tab);
+            k_axpy<2, false><<<gv, kThreads, 0, st>>>(d_tab);
+        }
         if (c128) k_scale<true, false><<<gv, kThreads, 0, st>>>(d_tab);
         else k_scale<false, false><<<gv, kThreads, 0, st>>>(d_tab);
         pc_window(c128, d_tab, 0, gv, st);

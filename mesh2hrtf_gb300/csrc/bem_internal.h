@@ -244,7 +244,9 @@ struct KSys {
     int n, pc;              // pc: apply Minv
     int nchunk, nvb;        // mv_chunks(n), vec_blocks(n)
     const void *Minv;
-    double2 *x, *b, *r, *w, *z, *V;   // V: kMaxRestart + 1 vectors, stride ldv
+    double2 *x, *b, *r, *w, *z, *V;   // V: kMaxRestart + 1 vectors, stride ldv;
+                                      // complex64 systems: w, V (and the inner-
+                                      // product partials) hold float pairs
     float2 *xh;             // complex64 systems: float copy of the next product's input
     float4 *xf;             // complex64 systems: x as (hi, lo) floats, chunk-permuted
     long long ldv;

@@ -140,7 +140,7 @@ struct bem_solver_s {
         k.A = d.A;
         k.A16 = d.A16;
         k.rs = d.rs;
-        k.cgs1 = d.A16 ? 1 : 0;   // fp16 Krylov copy: cycles gain three digits
+        k.cgs1 = 0;   // the float basis of complex64 systems needs the second pass
         k.lda = (long long)lda;
         k.n = n;
         k.pc = have_precond ? 1 : 0;
