@@ -256,7 +256,7 @@ size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, Solve
     d.A = take(N * lda * esz);
     if (prec != 0 && n_rhs == 1 && half_copy) {
         d.A16 = take(N * lda * 4);
-        d.rs = (float *)take(N * 4);
+        d.rs = (float *)take(N * (size_t)mv_chunks(n) * 4);
     }
     if (pc) {
         const size_t pb = precond_bytes(n, prec);

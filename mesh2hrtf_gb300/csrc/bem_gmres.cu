@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
             if (lane == 0) mbar_arrive(empty0 + 8 * stage);
             released = true;
             if (act) {
-                sca = S.rs[mt.row0 + r];
+                sca = S.rs[(size_t)(mt.row0 + r) * mv_chunks(S.n) + mt.chunk + half];
                 const float4 *x4 = reinterpret_cast<const float4 *>(xb + half * kMvChunk * 8);
                 float ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
                 if (full) {
@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
                     ar = fmaf(at.x, xv.x, ar); ar = fmaf(-at.y, xv.y, ar);
                     ai = fmaf(at.x, xv.y, ai); ai = fmaf(at.y, xv.x, ai);
                 }
-                // power-of-two row scale: exact in float
+                // power-of-two segment scale: exact in float
                 o0 = make_float4(warp_sum_f(ar + br) * sca, 0.f, warp_sum_f(ai + bi) * sca, 0.f);
                 nout = 1;
             }
@@ -1698,6 +1698,7 @@ __device__ __forceinline__ bool pcw_active(const KSys &S, int mode) {
 constexpr int kPcRows = 32;                  // rows per k_pcwin item
 constexpr int kPcItems = kThreads / kPcRows; // items per vector block
 static_assert(kPcWin % kThreads == 0, "windows hold whole vector blocks");
+static_assert(kPcWin == kMvChunk, "a window is one column chunk: one fp16 segment scale per row");
 
 __device__ __forceinline__ void cmac(float &sr, float &si, float2 a, float2 y) {
     sr = fmaf(a.x, y.x, sr); sr = fmaf(-a.y, y.y, sr);
@@ -1763,7 +1764,7 @@ __global__ void __launch_bounds__(kThreads) k_pcwin(const KTable *tb, int mode) 
                     } else {
                         for (int c = lane; c < nw; c += 32) cmac(sr, si, __half22float2(a[c]), yf[c]);
                     }
-                    scale = S.rs[r];
+                    scale = S.rs[(size_t)r * mv_chunks(n) + c0 / kMvChunk];
                 } else {
                     const float2 *a = (const float2 *)S.A + (size_t)r * S.lda + c0;
                     if (nw == kPcWin) {

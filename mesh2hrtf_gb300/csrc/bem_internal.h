@@ -197,8 +197,9 @@ size_t precond_bytes(int n, int prec);
 cudaError_t launch_block_inverse(const PcBatch &t, int prec, cudaStream_t st);
 
 // ---------------------------------------------------------------- fp16 Krylov copy
-// A complex64 system may also hold A in fp16 pairs, every row scaled by a
-// power of two that puts its largest component in [2^14, 2^15).  The Krylov
+// A complex64 system may also hold A in fp16 pairs, every row segment of
+// kMvChunk columns scaled by a power of two that puts its largest component
+// in [2^14, 2^15).  The Krylov
 // products read that copy (4 bytes per entry instead of 8); the refinement
 // residuals read the complex64 matrix, so the solution still meets the
 // residual target with the complex64 system.
@@ -207,11 +208,12 @@ struct SplitSys {
     size_t lda;
     int n;
     void *A16;              // fp16 pairs, the same leading dimension
-    float *rs;              // [n] row scales: A[i][j] ~ rs[i] * A16[i][j]
+    float *rs;              // [n][mv_chunks(n)] segment scales:
+                            // A[i][j] ~ rs[i * mv_chunks(n) + j / kMvChunk] * A16[i][j]
 };
 struct SplitBatch {
     int B;
-    int off[kMaxAsm + 1];   // rows
+    int off[kMaxAsm + 1];   // blocks (kSplitWarps segments each)
     SplitSys sys[kMaxAsm];
 };
 void split_batch_finish(SplitBatch &t);
@@ -259,7 +261,7 @@ struct KSys {
                             // product is one full-row partial (nchunk = 1)
     const void *A16;        // complex64 systems: fp16 copy of A (leading
                             // dimension lda) for the Krylov products, or nullptr
-    const float *rs;        // its row scales
+    const float *rs;        // its segment scales (SplitSys::rs)
     int cgs1;               // one classical Gram-Schmidt pass instead of two
     int pcw;                // window correction of the preconditioner (needs pc)
     void *pcy, *pcz;        // its vectors X v and A_w X v: float2 for complex64

@@ -177,73 +177,69 @@ __global__ void __launch_bounds__(512) k_binv64(const __grid_constant__ PcBatch 
     if (threadIdx.x == 0 && singular) atomicMax(S.status, 1);
 }
 
-// fp16 copy of complex64 rows (SplitBatch): one block per row; the row's
-// largest component m sets the scale 2^(15 - e) with m < 2^e, then every
-// component is scaled (exactly) and rounded to nearest.  Power-of-two scales
-// keep A16 * rs within one fp16 rounding of A.  Rows of up to kSplitSmemMax
-// entries are staged in shared memory (one read of A); longer rows are read
-// twice.
-constexpr int kSplitThreads = 512;
-constexpr int kSplitSmemMax = 26624;   // entries: 208 KB of complex64
+// fp16 copy of complex64 rows (SplitBatch): one warp per (row, column
+// chunk of kMvChunk entries).  The segment's largest component m sets the
+// scale 2^(15 - e) with m < 2^e; every component is scaled (exactly) and
+// rounded to nearest.  Power-of-two scales keep A16 * rs within one fp16
+// rounding of A.  The warp holds its 8 KB segment in registers, so A is
+// read once and no block-wide step is needed.
+constexpr int kSplitThreads = 256;
+constexpr int kSplitWarps = kSplitThreads / 32;
 
-__global__ void __launch_bounds__(kSplitThreads) k_split16(const __grid_constant__ SplitBatch tb, int staged) {
-    extern __shared__ __align__(16) float4 rowbuf[];
-    __shared__ float red[kSplitThreads / 32];
+__global__ void __launch_bounds__(kSplitThreads) k_split16(const __grid_constant__ SplitBatch tb) {
     const int sb = find_blk(tb.off, tb.B, blockIdx.x);
     const SplitSys &S = tb.sys[sb];
-    const int i = blockIdx.x - tb.off[sb];
-    const int n = S.n, n2 = n >> 1;
-    const float2 *row = (const float2 *)S.A + (size_t)i * S.lda;
-    const float4 *row4 = reinterpret_cast<const float4 *>(row);   // rows start 256-byte aligned
-    const bool st = staged && n <= kSplitSmemMax;
+    const int n = S.n, nch = mv_chunks(n), lane = threadIdx.x & 31;
+    const long long item = (long long)(blockIdx.x - tb.off[sb]) * kSplitWarps + (threadIdx.x >> 5);
+    if (item >= (long long)n * nch) return;
+    const int i = (int)(item / nch), c = (int)(item - (long long)i * nch);
+    const int c0 = c * kMvChunk, len = min(kMvChunk, n - c0), len2 = len >> 1;
+    const float2 *seg = (const float2 *)S.A + (size_t)i * S.lda + c0;   // 8 KB aligned within the row
+    const float4 *seg4 = reinterpret_cast<const float4 *>(seg);
+    float4 v[kMvChunk / 64];
     float m = 0.f;
-#pragma unroll 4
-    for (int c = threadIdx.x; c < n2; c += blockDim.x) {
-        const float4 v = __ldcs(row4 + c);   // streamed: A is read once here
-        if (st) rowbuf[c] = v;
-        m = fmaxf(m, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+#pragma unroll
+    for (int q = 0; q < kMvChunk / 64; ++q) {
+        const int k = lane + 32 * q;
+        v[q] = k < len2 ? __ldcs(seg4 + k) : make_float4(0.f, 0.f, 0.f, 0.f);   // A is streamed
+        m = fmaxf(m, fmaxf(fmaxf(fabsf(v[q].x), fabsf(v[q].y)), fmaxf(fabsf(v[q].z), fabsf(v[q].w))));
     }
-    if ((n & 1) && threadIdx.x == 0) m = fmaxf(m, fmaxf(fabsf(row[n - 1].x), fabsf(row[n - 1].y)));
+    float2 last = make_float2(0.f, 0.f);
+    if (len & 1) {
+        last = seg[len - 1];
+        m = fmaxf(m, fmaxf(fabsf(last.x), fabsf(last.y)));
+    }
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-    __syncthreads();
-    m = red[0];
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
     int e = 0;
     if (m > 0.f) frexpf(m, &e);   // m = f 2^e, 0.5 <= f < 1
     const float scale = ldexpf(1.f, 15 - e);
-    if (threadIdx.x == 0) S.rs[i] = ldexpf(1.f, e - 15);
-    uint2 *out = reinterpret_cast<uint2 *>((__half2 *)S.A16 + (size_t)i * S.lda);
-#pragma unroll 4
-    for (int c = threadIdx.x; c < n2; c += blockDim.x) {
-        const float4 v = st ? rowbuf[c] : row4[c];
-        const __half2 h0 = __floats2half2_rn(v.x * scale, v.y * scale);
-        const __half2 h1 = __floats2half2_rn(v.z * scale, v.w * scale);
-        out[c] = make_uint2(*reinterpret_cast<const unsigned *>(&h0), *reinterpret_cast<const unsigned *>(&h1));
+    if (lane == 0) S.rs[(size_t)i * nch + c] = ldexpf(1.f, e - 15);
+    __half2 *h = (__half2 *)S.A16 + (size_t)i * S.lda + c0;
+    uint2 *out = reinterpret_cast<uint2 *>(h);
+#pragma unroll
+    for (int q = 0; q < kMvChunk / 64; ++q) {
+        const int k = lane + 32 * q;
+        if (k < len2) {
+            const __half2 h0 = __floats2half2_rn(v[q].x * scale, v[q].y * scale);
+            const __half2 h1 = __floats2half2_rn(v[q].z * scale, v[q].w * scale);
+            out[k] = make_uint2(*reinterpret_cast<const unsigned *>(&h0), *reinterpret_cast<const unsigned *>(&h1));
+        }
     }
-    if ((n & 1) && threadIdx.x == 0)
-        ((__half2 *)S.A16)[(size_t)i * S.lda + n - 1] = __floats2half2_rn(row[n - 1].x * scale, row[n - 1].y * scale);
+    if ((len & 1) && lane == 0) h[len - 1] = __floats2half2_rn(last.x * scale, last.y * scale);
 }
 
 }  // namespace
 
 void split_batch_finish(SplitBatch &t) {
     t.off[0] = 0;
-    for (int b = 0; b < t.B; ++b) t.off[b + 1] = t.off[b] + t.sys[b].n;
+    for (int b = 0; b < t.B; ++b)
+        t.off[b + 1] = t.off[b] + ceil_div((long long)t.sys[b].n * mv_chunks(t.sys[b].n), kSplitWarps);
 }
 
 cudaError_t launch_split16(const SplitBatch &t, cudaStream_t st) {
     if (t.B <= 0 || t.off[t.B] == 0) return cudaSuccess;
-    int nmax = 0;
-    for (int b = 0; b < t.B; ++b) nmax = nmax > t.sys[b].n ? nmax : t.sys[b].n;
-    const int staged = nmax <= kSplitSmemMax ? 1 : 0;
-    const size_t smem = staged ? (size_t)((nmax + 1) / 2) * sizeof(float4) : 0;
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(k_split16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
     count_launches(1);
-    k_split16<<<t.off[t.B], kSplitThreads, smem, st>>>(t, staged);
+    k_split16<<<t.off[t.B], kSplitThreads, 0, st>>>(t);
     return cudaGetLastError();
 }
 
