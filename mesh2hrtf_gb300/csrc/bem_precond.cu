@@ -113,6 +113,80 @@ __device__ void gauss_jordan(typename C2<T>::t *W, int ld, int nb, typename C2<T
     }
 }
 
+// The same on a full kBlock x kBlock block by NT threads, with compile-time
+// indexing and three barriers per pivot: warp 0 finds the pivot (largest
+// |a|^2, lowest row on ties) and gathers the pivot column with the rows
+// interchanged, the first kBlock threads interchange the rows and scale the
+// pivot row, then thread t updates column t % kBlock of rows t / kBlock,
+// + NT / kBlock, ...
+template <typename T, int NT>
+__device__ void gauss_jordan_full(typename C2<T>::t *W, typename C2<T>::t *colk, int *piv, int *pivrow,
+                                  int *singular) {
+    using V = typename C2<T>::t;
+    constexpr int kG = NT / kBlock;
+    static_assert(NT % kBlock == 0 && kBlock % 32 == 0, "threads cover whole columns");
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int j = tid % kBlock, g = tid / kBlock;
+    for (int k = 0; k < kBlock; ++k) {
+        if (tid < 32) {
+            T best = -1;
+            int bi = k;
+            for (int i = k + lane; i < kBlock; i += 32) {
+                const V a = W[i * kBlock + k];
+                const T m = a.x * a.x + a.y * a.y;
+                if (m > best) { best = m; bi = i; }
+            }
+            // butterfly: every lane ends with the same (best, bi)
+            for (int o = 16; o > 0; o >>= 1) {
+                const T ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            for (int i = lane; i < kBlock; i += 32) {
+                const int src = i == k ? bi : (i == bi ? k : i);
+                colk[i] = W[src * kBlock + k];
+            }
+            if (lane == 0) {
+                *pivrow = bi;
+                piv[k] = bi;
+                if (!(best > 0)) *singular = 1;
+            }
+        }
+        __syncthreads();
+        const int p = *pivrow;
+        if (tid < kBlock) {
+            const V inv = cinv2(colk[k]);
+            const V tk = W[k * kBlock + j], tp = W[p * kBlock + j];
+            if (p != k) W[p * kBlock + j] = tk;
+            const V a = j == k ? V{1, 0} : tp;
+            W[k * kBlock + j] = cmul2(a, inv);
+        }
+        __syncthreads();
+        const V r = W[k * kBlock + j];
+#pragma unroll 4
+        for (int i = g; i < kBlock; i += kG) {
+            if (i == k) continue;
+            const V f = colk[i];
+            V a = j == k ? V{0, 0} : W[i * kBlock + j];
+            a.x -= f.x * r.x - f.y * r.y;
+            a.y -= f.x * r.y + f.y * r.x;
+            W[i * kBlock + j] = a;
+        }
+        __syncthreads();
+    }
+    // undo the row interchanges as column interchanges, last first
+    for (int k = kBlock - 1; k >= 0; --k) {
+        const int p = piv[k];
+        if (p != k)
+            for (int i = tid; i < kBlock; i += NT) {
+                V t = W[i * kBlock + k];
+                W[i * kBlock + k] = W[i * kBlock + p];
+                W[i * kBlock + p] = t;
+            }
+        __syncthreads();
+    }
+}
+
 __device__ __forceinline__ int find_blk(const int *off, int B, int item) {
     int lo = 0, hi = B - 1;
     while (lo < hi) {
@@ -123,7 +197,8 @@ __device__ __forceinline__ int find_blk(const int *off, int B, int item) {
 }
 
 // complex64: block in shared memory
-__global__ void __launch_bounds__(512) k_binv32(const __grid_constant__ PcBatch tb) {
+constexpr int kBinv32Threads = 1024;
+__global__ void __launch_bounds__(kBinv32Threads) k_binv32(const __grid_constant__ PcBatch tb) {
     extern __shared__ float2 smem[];
     __shared__ float2 colk[kBlock];
     __shared__ int piv[kBlock];
@@ -135,12 +210,19 @@ __global__ void __launch_bounds__(512) k_binv32(const __grid_constant__ PcBatch 
     const int b = blockIdx.x - tb.off[sb], r0 = b * kBlock;
     const int nb = min(kBlock, S.n - r0);
     if (threadIdx.x == 0) singular = 0;
-    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-        const int i = e / nb, j = e - i * nb;
-        smem[i * kBlock + j] = A[(size_t)(r0 + i) * lda + r0 + j];
+    if (nb == kBlock) {
+        for (int e = threadIdx.x; e < kBlock * kBlock; e += kBinv32Threads)
+            smem[e] = A[(size_t)(r0 + e / kBlock) * lda + r0 + e % kBlock];
+        __syncthreads();
+        gauss_jordan_full<float, kBinv32Threads>(smem, colk, piv, &pivrow, &singular);
+    } else {   // the last, partial block of a system
+        for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+            const int i = e / nb, j = e - i * nb;
+            smem[i * kBlock + j] = A[(size_t)(r0 + i) * lda + r0 + j];
+        }
+        __syncthreads();
+        gauss_jordan<float>(smem, kBlock, nb, colk, piv, &pivrow, &singular);
     }
-    __syncthreads();
-    gauss_jordan<float>(smem, kBlock, nb, colk, piv, &pivrow, &singular);
     // store transposed: Minv[b][c][r] = inv[r][c]
     float2 *out = (float2 *)S.Minv + (size_t)b * kBlock * kBlock;
     for (int e = threadIdx.x; e < kBlock * kBlock; e += blockDim.x) {
@@ -163,12 +245,19 @@ __global__ void __launch_bounds__(512) k_binv64(const __grid_constant__ PcBatch 
     const int nb = min(kBlock, S.n - r0);
     double2 *w = (double2 *)S.work + (size_t)b * kBlock * kBlock;
     if (threadIdx.x == 0) singular = 0;
-    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-        const int i = e / nb, j = e - i * nb;
-        w[i * kBlock + j] = A[(size_t)(r0 + i) * lda + r0 + j];
+    if (nb == kBlock) {
+        for (int e = threadIdx.x; e < kBlock * kBlock; e += 512)
+            w[e] = A[(size_t)(r0 + e / kBlock) * lda + r0 + e % kBlock];
+        __syncthreads();
+        gauss_jordan_full<double, 512>(w, colk, piv, &pivrow, &singular);
+    } else {
+        for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+            const int i = e / nb, j = e - i * nb;
+            w[i * kBlock + j] = A[(size_t)(r0 + i) * lda + r0 + j];
+        }
+        __syncthreads();
+        gauss_jordan<double>(w, kBlock, nb, colk, piv, &pivrow, &singular);
     }
-    __syncthreads();
-    gauss_jordan<double>(w, kBlock, nb, colk, piv, &pivrow, &singular);
     double2 *out = (double2 *)S.Minv + (size_t)b * kBlock * kBlock;
     for (int e = threadIdx.x; e < kBlock * kBlock; e += blockDim.x) {
         const int c = e / kBlock, r = e - c * kBlock;
@@ -263,7 +352,7 @@ cudaError_t launch_block_inverse(const PcBatch &t, int prec, cudaStream_t st) {
         const int smem = kBlock * kBlock * sizeof(float2);
         cudaError_t e = cudaFuncSetAttribute(k_binv32, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_binv32<<<t.off[t.B], 512, smem, st>>>(t);
+        k_binv32<<<t.off[t.B], kBinv32Threads, smem, st>>>(t);
     }
     return cudaGetLastError();
 }
