@@ -756,8 +756,8 @@ double bem_footprint_multi(int32_t n_elem, int32_t precision, int32_t restart, i
 double bem_mesh_footprint_bytes(int32_t n_elem, int32_t n_sym_planes) {
     const int n = std::max(n_elem, 1);
     const int nref = 1 << std::min(std::max(n_sym_planes, 0), 3);
-    // element tables: 1 + 12 + 3 + 3 + 1 + 1 words of 8 B, 3 + 3 + 10 + 12 + 1 + 3 of 4 B
-    const double tables = (double)n * (4.0 + 20.0 * 8.0 + 32.0 * 4.0);
+    // element tables: 1 + 12 + 3 + 3 + 1 + 1 words of 8 B, 3 + 3 + 10 + 12 + 1 + 3 + 12 of 4 B
+    const double tables = (double)n * (4.0 + 20.0 * 8.0 + 44.0 * 4.0);
     const double near = (double)n * nref * 48.0 * sizeof(int2);   // the list's first allocation
     return tables + (double)bem::image_table_bytes(n, nref) + near;
 }
@@ -954,6 +954,15 @@ bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
     if (e == cudaSuccess) e = up(&m->d_q32, q32);
     if (e == cudaSuccess) e = up(&m->d_isqa, isqa);
     if (e == cudaSuccess) e = up(&m->d_n32, n32);
+    if (e == cudaSuccess) {
+        std::vector<float4> row4(3 * (size_t)n);
+        for (int i = 0; i < n; ++i) {
+            row4[3 * (size_t)i] = make_float4(chi[i], chi[(size_t)n + i], chi[2 * (size_t)n + i], 0.f);
+            row4[3 * (size_t)i + 1] = make_float4(clo[i], clo[(size_t)n + i], clo[2 * (size_t)n + i], 0.f);
+            row4[3 * (size_t)i + 2] = make_float4(n32[i], n32[(size_t)n + i], n32[2 * (size_t)n + i], 0.f);
+        }
+        e = up(&m->d_row4, row4);
+    }
     // symmetry images: one allocation, laid out as DevSym describes
     if (e == cudaSuccess && sym.nref > 1) {
         const size_t ni = (size_t)(sym.nref - 1) * (size_t)n;

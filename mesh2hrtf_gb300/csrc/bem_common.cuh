@@ -94,6 +94,9 @@ struct QuadTables {
 // header.
 __constant__ QuadTables c_quad;
 __constant__ float c_trif[24][3];
+// The 4-point rule's (s - 1/3, t - 1/3, 2 (s - 1/3), 2 (t - 1/3)): operands of
+// the expanded squared distance of the order-2 far pairs.
+__constant__ float c_far4[4][4];
 __constant__ float c_glxf[7][6];
 __constant__ float c_glwf[7][6];
 // local node coordinates of 6-/8-noded parents, NC_Arrays.h:126-129
@@ -168,6 +171,8 @@ struct DevMesh {
     const float *q32;       // 12 rows (quads): vertex offsets from the centre
     const float *isqa32;    // 1 / sqrt(areael) in float (approximate ratios)
     const float *n32;       // 3 rows: centre normal in float
+    const float4 *row4;     // [n][3]: (chi, 0), (clo, 0), (n32, 0): a collocation
+                            // row's data in three 16-byte loads
     DevSym sym;             // symmetry-plane images (sym.nref = 1: none)
 };
 

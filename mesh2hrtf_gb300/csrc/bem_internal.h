@@ -39,6 +39,7 @@ struct DevMeshView {
     const int *nvert;
     const double *v64, *c64, *n64, *area64, *sqa64;
     const float *chi, *clo, *t32, *q32, *isqa32, *n32;
+    const float4 *row4;     // [n][3]: (chi, 0), (clo, 0), (n32, 0) of each element
     DevSym sym;
 };
 

@@ -30,7 +30,7 @@ __device__ __forceinline__ DevMesh to_dev(const DevMeshView &v) {
     DevMesh m;
     m.n = v.n; m.nvert = v.nvert; m.v64 = v.v64; m.c64 = v.c64; m.n64 = v.n64;
     m.area64 = v.area64; m.sqa64 = v.sqa64; m.chi = v.chi; m.clo = v.clo; m.t32 = v.t32;
-    m.q32 = v.q32; m.isqa32 = v.isqa32; m.n32 = v.n32;
+    m.q32 = v.q32; m.isqa32 = v.isqa32; m.n32 = v.n32; m.row4 = v.row4;
     m.sym = v.sym;
     return m;
 }
@@ -189,6 +189,85 @@ __device__ __forceinline__ float2 far_entry_f(const Elem32 &e, const float nx[3]
     return make_float2(ar, ai);
 }
 
+// Order-2 far pair on a flat triangle (the 4-point rule) with the column
+// element's data hoisted out of the row loop: point g's squared distance is
+// |D|^2 + 2 s_g D.a + 2 t_g D.b + C_g with C_g = |s_g a + t_g b|^2 (at the
+// order-2 ratio, |D| > 4 sqrt(area), the terms do not cancel), and the
+// kernel terms of fused_point regrouped around u = 1/r.
+struct FarCol4 {
+    float a[3], b[3], n[3];
+    float C[4];    // |s_g a + t_g b|^2
+    float J4;      // J / (4 pi)
+};
+
+__device__ __forceinline__ void far_col4(const DevMesh &m, int j, FarCol4 &e) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        e.a[k] = m.t32[k * m.n + j];
+        e.b[k] = m.t32[(3 + k) * m.n + j];
+        e.n[k] = m.t32[(6 + k) * m.n + j];
+    }
+    const float J = m.t32[9 * m.n + j];
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+        float c = 0.f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float d = fmaf(c_far4[g][1], e.b[k], c_far4[g][0] * e.a[k]);
+            c = fmaf(d, d, c);
+        }
+        e.C[g] = c;
+    }
+    e.J4 = J * (float)(1.0 / kPI4);
+}
+
+__device__ __forceinline__ float2 far_entry_tri2(const FarCol4 &e, const float D[3], float D2, const float nx[3],
+                                                 const FusedCol &c) {
+    const float dny = D[0] * e.n[0] + D[1] * e.n[1] + D[2] * e.n[2];
+    const float dnx0 = D[0] * nx[0] + D[1] * nx[1] + D[2] * nx[2];
+    const float anx = e.a[0] * nx[0] + e.a[1] * nx[1] + e.a[2] * nx[2];
+    const float bnx = e.b[0] * nx[0] + e.b[1] * nx[1] + e.b[2] * nx[2];
+    const float nn = e.n[0] * nx[0] + e.n[1] * nx[1] + e.n[2] * nx[2];
+    const float Da = D[0] * e.a[0] + D[1] * e.a[1] + D[2] * e.a[2];
+    const float Db = D[0] * e.b[0] + D[1] * e.b[1] + D[2] * e.b[2];
+    const float ct = -c.tau * dny;          // velocity: -tau d.n_y / r^2
+    const float cw = c.tau * c.wr * dny;    // velocity: tau wr d.n_y / r
+    const float bwr = c.b * c.wr;
+    float ar = 0.f, ai = 0.f;
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+        const float r2 = fmaf(c_far4[g][2], Da, fmaf(c_far4[g][3], Db, D2 + e.C[g]));
+        const float dnx = fmaf(c_far4[g][1], bnx, fmaf(c_far4[g][0], anx, dnx0));
+        const float u = rsqrtf(r2);
+        float sn, cs;
+        phase_sincos(c.wr * (r2 * u), &sn, &cs);
+        float fr, fi;
+        if (c.bc == 1) {
+            // -tau - i b z1 re2, z1 = -1/r + i wr, re2 = -d.n_x / r
+            const float du = dnx * u;
+            fr = fmaf(-bwr, du, -c.tau);
+            fi = -c.b * du * u;
+        } else {
+            // tau z1 re1 + i b ze1 (re1 = d.n_y / r)
+            const float u2 = u * u;
+            const float rq = -(dny * dnx) * u2;
+            fr = fmaf(bwr * u, fmaf(3.f, rq, nn), ct * u2);
+            fi = fmaf(c.b, fmaf(fmaf(3.f, u2, -c.k2), rq, nn * u2), cw * u);
+            if (c.bc == 2) {
+                // + Y (1 + i b tau z1 re2)
+                const float du = dnx * u, bt = c.b * c.tau;
+                const float pr = fmaf(bt * c.wr, du, 1.f), pi = bt * u * du;
+                fr += c.yr * pr - c.yi * pi;
+                fi += c.yr * pi + c.yi * pr;
+            }
+        }
+        const float amp = c_trif[g][2] * e.J4 * u;
+        ar = fmaf(amp, fmaf(cs, fr, -sn * fi), ar);
+        ai = fmaf(amp, fmaf(cs, fi, sn * fr), ai);
+    }
+    return make_float2(ar, ai);
+}
+
 template <typename T>
 __device__ __forceinline__ cplx<T> col_adm(const DevFreq &f, int j, int bc) {
     if (bc != 2 || f.adm == nullptr) return {T(0), T(0)};
@@ -301,6 +380,29 @@ __global__ void __launch_bounds__(256) k_near_list(DevMeshView mv, int2 *list, u
 // and self pairs are skipped here and written by k_near.
 constexpr int kRowsPerThread = 4;
 
+// Out-of-line parts of the float tile, taken by few pairs: keeping them out
+// of the row loop keeps the mesh pointers they read out of its registers.
+// Exact (FP64) decision for a pair within the float test's margin of a
+// threshold: 0 for a near pair, else the Gauss order.
+__device__ __noinline__ int far_order_exact(const DevMeshView *mv, int i, int j) {
+    const DevMesh m = to_dev(*mv);
+    const int n = m.n;
+    const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
+    const double rd = ratio0_exact(m, j, x64);
+    return rd < kTolf ? 0 : gauss_order(rd);
+}
+// Entry of a quadrilateral column or of a Gauss order above 2.
+__device__ __noinline__ float2 far_entry_general(const DevMeshView *mv, int j, float D0, float D1, float D2,
+                                                 float nx0, float nx1, float nx2, int order, FusedCol fc) {
+    const DevMesh m = to_dev(*mv);
+    Elem32 e;
+    const float zero[3] = {0.f, 0.f, 0.f};
+    load_elem32(m, j, zero, zero, e);
+    e.D[0] = D0; e.D[1] = D1; e.D[2] = D2;
+    const float nx[3] = {nx0, nx1, nx2};
+    return far_entry_f(e, nx, order, fc);
+}
+
 template <typename T>
 __device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f,
                                          typename Vec2<T>::type *__restrict__ A, size_t lda, int tx, int ty) {
@@ -331,9 +433,9 @@ __device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f
             A[(size_t)i * lda + j] = make_double2(val.re, val.im);
         }
     } else {
-        Elem32 e;
-        const float zero[3] = {0.f, 0.f, 0.f};
-        load_elem32(m, j, zero, zero, e);
+        const bool tri = m.nvert[j] == 3;
+        FarCol4 e4;
+        if (tri) far_col4(m, j, e4);
         const float cjh[3] = {m.chi[j], m.chi[n + j], m.chi[2 * n + j]};
         const float cjl[3] = {m.clo[j], m.clo[n + j], m.clo[2 * n + j]};
         const float isq2 = m.isqa32[j] * m.isqa32[j];
@@ -345,23 +447,29 @@ __device__ __forceinline__ void far_tile(const DevMeshView &mv, const DevFreq &f
         fc.b = PT.beta_im;
         fc.k2 = PT.k * PT.k;
         fc.wr = PT.wr;
+        #pragma unroll 1
         for (int r = 0; r < kRowsPerThread; ++r) {
             const int i = i0 + r;
             if (i >= n) break;
             if (i == j) { A[(size_t)i * lda + j] = make_float2(0.f, 0.f); continue; }
-            for (int k = 0; k < 3; ++k) e.D[k] = (cjh[k] - m.chi[k * n + i]) + (cjl[k] - m.clo[k * n + i]);
-            const float q2 = (e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * isq2;
+            // the row's data (the same for the warp's 32 columns)
+            const float4 rh = m.row4[3 * (size_t)i], rl = m.row4[3 * (size_t)i + 1], rn = m.row4[3 * (size_t)i + 2];
+            const float D[3] = {(cjh[0] - rh.x) + (cjl[0] - rl.x), (cjh[1] - rh.y) + (cjl[1] - rl.y),
+                                (cjh[2] - rh.z) + (cjl[2] - rl.z)};
+            const float D2 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+            const float q2 = D2 * isq2;
             bool near = false;
             int order = 2;
             if (q2 <= c_quad.far2_sq && !classify_fast(sqrtf(q2), near, order)) {
-                const double x64[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
-                const double rd = ratio0_exact(m, j, x64);
-                near = rd < kTolf;
-                if (!near) order = gauss_order(rd);
+                order = far_order_exact(&mv, i, j);
+                near = order == 0;
             }
             if (near) { A[(size_t)i * lda + j] = make_float2(0.f, 0.f); continue; }
-            const float nx[3] = {m.n32[i], m.n32[n + i], m.n32[2 * n + i]};
-            A[(size_t)i * lda + j] = far_entry_f(e, nx, order, fc);
+            const float nx[3] = {rn.x, rn.y, rn.z};
+            if (tri && order <= 2)
+                A[(size_t)i * lda + j] = far_entry_tri2(e4, D, D2, nx, fc);
+            else
+                A[(size_t)i * lda + j] = far_entry_general(&mv, j, D[0], D[1], D[2], nx[0], nx[1], nx[2], order, fc);
         }
     }
 }
@@ -451,11 +559,13 @@ __device__ __forceinline__ void far_tile_img(const DevMeshView &mv, const DevFre
     }
 }
 
+constexpr int kFarPerSm = 3;   // resident k_far blocks per SM (launch bounds and persistent grid)
+
 // ONE: the batch holds a single system, whose table then stays in constant
 // operands instead of registers.  IMG: some mesh of the batch has symmetry
 // images (meshes without take the plain tile).
 template <typename T, bool ONE, bool IMG>
-__global__ void __launch_bounds__(256, 3) k_far(const __grid_constant__ AsmBatch tb, unsigned *ctr) {
+__global__ void __launch_bounds__(256, kFarPerSm) k_far(const __grid_constant__ AsmBatch tb, unsigned *ctr) {
     __shared__ int item_s;
     const int total = tb.far_off[tb.B];
     while (true) {
@@ -877,19 +987,19 @@ __global__ void __launch_bounds__(256, 2) k_project(const __grid_constant__ Proj
                     }
                     if (!near && e.nv == 3 && !iv) {
                         // fused flat-triangle path (no velocity terms)
-                        float2 P = make_float2(0.f, 0.f), U[3], T = make_float2(0.f, 0.f);
+                        float2 P = make_float2(0.f, 0.f), U[3], Tn = make_float2(0.f, 0.f);
                         U[0] = U[1] = U[2] = make_float2(0.f, 0.f);
                         const float dny = e.D[0] * e.n[0] + e.D[1] * e.n[1] + e.D[2] * e.n[2];
                         const float k2 = (float)k * (float)k;
-                        if (order <= 2) proj_tri_points<4, 0>(e, dny, k2, (float)wr, P, U, T);
-                        else if (order == 3) proj_tri_points<7, 4>(e, dny, k2, (float)wr, P, U, T);
-                        else proj_tri_points<13, 11>(e, dny, k2, (float)wr, P, U, T);
+                        if (order <= 2) proj_tri_points<4, 0>(e, dny, k2, (float)wr, P, U, Tn);
+                        else if (order == 3) proj_tri_points<7, 4>(e, dny, k2, (float)wr, P, U, Tn);
+                        else proj_tri_points<13, 11>(e, dny, k2, (float)wr, P, U, Tn);
                         const cplx<float> pp = ph * cplx<float>{P.x, P.y};
                         acc.p.re += pp.re;
                         acc.p.im += pp.im;
 #pragma unroll
                         for (int kk = 0; kk < 3; ++kk) {
-                            const cplx<float> gg = ph * cplx<float>{fmaf(T.x, e.n[kk], U[kk].x), fmaf(T.y, e.n[kk], U[kk].y)};
+                            const cplx<float> gg = ph * cplx<float>{fmaf(Tn.x, e.n[kk], U[kk].x), fmaf(Tn.y, e.n[kk], U[kk].y)};
                             acc.g[kk].re += gg.re;
                             acc.g[kk].im += gg.im;
                         }
@@ -1105,6 +1215,14 @@ cudaError_t init_device_tables() {
     q.far2_sq = (float)((q.order_thr[2] * (1.0 + 3e-5)) * (q.order_thr[2] * (1.0 + 3e-5)));
     cudaError_t e = cudaMemcpyToSymbol(c_quad, &q, sizeof(q));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_trif, trif, sizeof(trif));
+    float far4[4][4];
+    for (int g = 0; g < 4; ++g) {
+        far4[g][0] = trif[g][0] - (1.0f / 3.0f);
+        far4[g][1] = trif[g][1] - (1.0f / 3.0f);
+        far4[g][2] = 2.0f * far4[g][0];
+        far4[g][3] = 2.0f * far4[g][1];
+    }
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_far4, far4, sizeof(far4));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_glxf, glxf, sizeof(glxf));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_glwf, glwf, sizeof(glwf));
     return e;
@@ -1164,8 +1282,8 @@ cudaError_t launch_assemble(const AsmBatch &t, int prec, unsigned *ctr, cudaStre
     if (t.B <= 0) return cudaSuccess;
     dim3 block(32, 8);
     const int far_items = t.far_off[t.B], near_items = t.near_off[t.B];
-    // persistent grids: 3 resident blocks of k_far per SM (launch bounds), 4 of k_near
-    const int gfar = std::max(1, std::min(far_items, 3 * sm_count()));
+    // persistent grids: kFarPerSm resident blocks of k_far per SM (launch bounds), 4 of k_near
+    const int gfar = std::max(1, std::min(far_items, kFarPerSm * sm_count()));
     const int gnear = std::max(1, std::min((near_items + 7) / 8, 4 * sm_count()));
     count_launches(near_items ? 2 : 1);
     const bool one = t.B == 1;

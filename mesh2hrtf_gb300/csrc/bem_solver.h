@@ -37,6 +37,7 @@ struct bem_mesh_s {
     double *d_v64 = nullptr, *d_c64 = nullptr, *d_n64 = nullptr, *d_area = nullptr, *d_sqa = nullptr;
     float *d_chi = nullptr, *d_clo = nullptr, *d_t32 = nullptr, *d_q32 = nullptr, *d_isqa = nullptr;
     float *d_n32 = nullptr;
+    float4 *d_row4 = nullptr;
     int2 *d_near = nullptr;         // pairs integrated with subdivision + self pairs
     long long n_near = 0;
     bem::DevSym sym{};              // symmetry-plane images (sym.nref = 1: none)
@@ -46,13 +47,14 @@ struct bem_mesh_s {
         v.n = n; v.nvert = d_nvert; v.v64 = d_v64; v.c64 = d_c64; v.n64 = d_n64; v.area64 = d_area;
         v.sqa64 = d_sqa; v.chi = d_chi; v.clo = d_clo; v.t32 = d_t32; v.q32 = d_q32; v.isqa32 = d_isqa;
         v.n32 = d_n32;
+        v.row4 = d_row4;
         v.sym = sym;
         return v;
     }
     ~bem_mesh_s() {
         for (void *p : {(void *)d_nvert, (void *)d_v64, (void *)d_c64, (void *)d_n64, (void *)d_area, (void *)d_sqa,
                         (void *)d_chi, (void *)d_clo, (void *)d_t32, (void *)d_q32, (void *)d_isqa, (void *)d_near,
-                        (void *)d_n32, d_img})
+                        (void *)d_n32, (void *)d_row4, d_img})
             bem::dev_free(p);
     }
 };
