@@ -104,6 +104,11 @@ __constant__ double c_csi8[8] = {1.0, -1.0, -1.0, 1.0, 0.0, -1.0, 0.0, 1.0};
 __constant__ double c_eta8[8] = {1.0, 1.0, -1.0, -1.0, 1.0, 0.0, -1.0, 0.0};
 __constant__ double c_csi6[6] = {1.0, 0.0, 0.0, 0.5, 0.0, 0.5};
 __constant__ double c_eta6[6] = {0.0, 1.0, 0.0, 0.5, 0.5, 0.0};
+// the same corner and mid-side points in float (FP32 singular rule)
+__constant__ float c_csi8f[8] = {1.f, -1.f, -1.f, 1.f, 0.f, -1.f, 0.f, 1.f};
+__constant__ float c_eta8f[8] = {1.f, 1.f, -1.f, -1.f, 1.f, 0.f, -1.f, 0.f};
+__constant__ float c_csi6f[6] = {1.f, 0.f, 0.f, 0.5f, 0.f, 0.5f};
+__constant__ float c_eta6f[6] = {0.f, 1.f, 0.f, 0.5f, 0.5f, 0.f};
 
 __host__ __device__ constexpr int tri_offset(int order) { return order <= 2 ? 0 : (order == 3 ? 4 : 11); }
 __host__ __device__ constexpr int tri_count(int order) { return order <= 2 ? 4 : (order == 3 ? 7 : 13); }

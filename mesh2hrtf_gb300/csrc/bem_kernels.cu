@@ -587,8 +587,9 @@ __global__ void __launch_bounds__(256, kFarPerSm) k_far(const __grid_constant__ 
 }
 
 // ------------------------------------------------------------ near pairs
-// One warp per entry of the near list: the self pair by warp_singular (FP64,
-// plus NumCalc's free term), subdivided pairs by warp_subdivide with the
+// One warp per entry of the near list: the self pair by warp_singular (FP64;
+// warp_singular_f in FP32 for complex64 systems) plus NumCalc's free term,
+// subdivided pairs by warp_subdivide with the
 // kernel arithmetic in T; with symmetry planes every image of the entry's
 // mask in image order.  The sum is added to the entry k_far wrote (its far
 // images, or zero).
@@ -614,8 +615,24 @@ __device__ __forceinline__ void near_pair(const DevMeshView &mv, const DevFreq &
         load_elem64(mk, j, e);
         cplx<T> entry;
         if (kref == 0 && i == j) {
-            SingOut so = warp_singular(e, x64, nx64, P, 0, nullptr);
-            cplx<double> a = combine_entry(so.v, bcj, col_adm<double>(f, j, bcj), P);
+            KVals<double> sv;
+            if constexpr (std::is_same<T, float>::value) {
+                // FP32 rule on the vertices relative to the collocation point
+                float pl[4][3];
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) pl[a][k] = a < e.nv ? (float)(e.p[a][k] - x64[k]) : 0.f;
+                const float nxf[3] = {(float)nx64[0], (float)nx64[1], (float)nx64[2]};
+                const KVals<float> vf = warp_singular_f(e.nv, pl, nxf, f.kf, f.wrf);
+                sv.G = {vf.G.re, vf.G.im};
+                sv.H = {vf.H.re, vf.H.im};
+                sv.HT = {vf.HT.re, vf.HT.im};
+                sv.E = {vf.E.re, vf.E.im};
+            } else {
+                sv = warp_singular(e, x64, nx64, P, 0, nullptr).v;
+            }
+            cplx<double> a = combine_entry(sv, bcj, col_adm<double>(f, j, bcj), P);
             // free term, NC_EquationSystem.cpp:220-231
             const cplx<double> beta = {0.0, P.beta_im};
             if (bcj == 1) a += beta * (-(0.5 * P.tao));

@@ -473,4 +473,109 @@ __device__ __forceinline__ SingOut warp_singular(const Elem64 &e, const double x
     return o;
 }
 
+// FP32 form of warp_singular's G, H, H^T and E (no right-hand-side terms)
+// for the mixed-precision assembly.  p holds the element's vertices minus
+// the collocation point (differences taken in FP64, then rounded), so no
+// large coordinate enters the float arithmetic.  The rule subtracts no
+// static part anywhere (Stokes contour form for E, Duffy-collapsed
+// sub-triangles for G, H, H^T), so FP32 keeps about 1e-6 relative accuracy
+// on the self entry, below the complex64 storage of A it is added to.  The
+// FP64 rule made the near-pair kernel FP64-pipe bound on GB300.
+__device__ __forceinline__ KVals<float> warp_singular_f(int nv, const float p[4][3], const float nx[3], float k,
+                                                        float wr) {
+    const int lane = threadIdx.x & 31;
+    const float wnu2 = k * k;
+    const float i4pi = (float)(1.0 / kPI4);
+    cplx<float> zG = {0.f, 0.f}, zH = zG, zHT = zG, zE = zG;
+    const int n_edge = nv * 12, n_area = nv * 32;
+    for (int f = lane; f < n_edge + n_area; f += 32) {
+        if (f < n_edge) {
+            // contour term of E: 4 sections x 3-point Gauss per edge
+            const int ieg = f / 12, rem = f - ieg * 12, isec = rem / 3, ig = rem - isec * 3;
+            const int ig1 = ieg + 1 == nv ? 0 : ieg + 1;
+            float dif[3], len2 = 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { dif[c] = p[ig1][c] - p[ieg][c]; len2 = fmaf(dif[c], dif[c], len2); }
+            const float len = sqrtf(len2), il = 1.f / len;
+            const float sga = (-0.75f + 0.5f * (float)isec) + 0.25f * c_glxf[3][ig];
+            const float wga = c_glwf[3][ig] * (0.125f * len);
+            float d[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) d[c] = fmaf(dif[c], 0.5f * (sga + 1.f), p[ieg][c]);
+            const float r = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]), ir = 1.f / r;
+            float sn, cs;
+            phase_sincos(wr * r, &sn, &cs);
+            // grad G = G (-1/r + i wr) r^, crossed with the edge direction
+            const cplx<float> zg = cplx<float>{cs * i4pi * ir, sn * i4pi * ir} * cplx<float>{-ir, wr};
+            const float t0 = (d[1] * dif[2] - d[2] * dif[1]) * ir * il;
+            const float t1 = (d[2] * dif[0] - d[0] * dif[2]) * ir * il;
+            const float t2 = (d[0] * dif[1] - d[1] * dif[0]) * ir * il;
+            zE += zg * ((t0 * nx[0] + t1 * nx[1] + t2 * nx[2]) * wga);
+        } else {
+            // G, H, H^T and the k^2 part of E: 2 sub-triangles per edge from
+            // the centre, 4 x 4 Gauss collapsed at the centre (weight 1 + s)
+            const int fa = f - n_edge;
+            const int ieg = fa / 32, rem = fa - ieg * 32, isec = rem / 16, g = rem - isec * 16;
+            const int ig1 = ieg + 1 == nv ? 0 : ieg + 1, ig2 = ieg + nv;
+            float ss[3], ts[3], aresub;
+            if (nv == 3) {
+                aresub = 1.f / 48.f;
+                ss[0] = ts[0] = 1.f / 3.f;
+                if (isec == 0) { ss[1] = c_csi6f[ieg]; ss[2] = c_csi6f[ig2]; ts[1] = c_eta6f[ieg]; ts[2] = c_eta6f[ig2]; }
+                else { ss[1] = c_csi6f[ig2]; ss[2] = c_csi6f[ig1]; ts[1] = c_eta6f[ig2]; ts[2] = c_eta6f[ig1]; }
+            } else {
+                aresub = 0.125f;
+                ss[0] = ts[0] = 0.f;
+                if (isec == 0) { ss[1] = c_csi8f[ieg]; ss[2] = c_csi8f[ig2]; ts[1] = c_eta8f[ieg]; ts[2] = c_eta8f[ig2]; }
+                else { ss[1] = c_csi8f[ig2]; ss[2] = c_csi8f[ig1]; ts[1] = c_eta8f[ig2]; ts[2] = c_eta8f[ig1]; }
+            }
+            const int gi = g >> 2, gj = g & 3;
+            const float sga = c_glxf[4][gi], tga = c_glxf[4][gj];
+            const float wq = c_glwf[4][gi] * c_glwf[4][gj] * (1.f + sga) * aresub;
+            const float s = 0.5f * (1.f - sga) * ss[0] + 0.25f * (1.f + sga) * ((1.f - tga) * ss[1] + (1.f + tga) * ss[2]);
+            const float t = 0.5f * (1.f - sga) * ts[0] + 0.25f * (1.f + sga) * ((1.f - tga) * ts[1] + (1.f + tga) * ts[2]);
+            // shape functions and their derivatives (NC_ComputeParameters)
+            float sh[4], ds[4], dt[4];
+            if (nv == 3) {
+                sh[0] = s; sh[1] = t; sh[2] = 1.f - s - t; sh[3] = 0.f;
+                ds[0] = 1.f; ds[1] = 0.f; ds[2] = -1.f; ds[3] = 0.f;
+                dt[0] = 0.f; dt[1] = 1.f; dt[2] = -1.f; dt[3] = 0.f;
+            } else {
+                const float s1 = 0.25f * (s + 1.f), s2 = 0.25f * (s - 1.f), t1 = t + 1.f, t2 = t - 1.f;
+                sh[0] = s1 * t1; sh[1] = -s2 * t1; sh[2] = s2 * t2; sh[3] = -s1 * t2;
+                ds[0] = 0.25f * (t + 1.f); ds[2] = 0.25f * (t - 1.f); ds[1] = -ds[0]; ds[3] = -ds[2];
+                dt[0] = 0.25f * (s + 1.f); dt[2] = 0.25f * (s - 1.f); dt[1] = -dt[2]; dt[3] = -dt[0];
+            }
+            float d[3], dxs[3], dxt[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                d[c] = 0.f; dxs[c] = 0.f; dxt[c] = 0.f;
+                for (int a = 0; a < nv; ++a) {
+                    d[c] = fmaf(sh[a], p[a][c], d[c]);
+                    dxs[c] = fmaf(ds[a], p[a][c], dxs[c]);
+                    dxt[c] = fmaf(dt[a], p[a][c], dxt[c]);
+                }
+            }
+            const float n0 = dxs[1] * dxt[2] - dxt[1] * dxs[2];
+            const float n1 = dxs[2] * dxt[0] - dxt[2] * dxs[0];
+            const float n2 = dxs[0] * dxt[1] - dxt[0] * dxs[1];
+            const float jl = sqrtf(n0 * n0 + n1 * n1 + n2 * n2), ijl = 1.f / jl;
+            const float ny[3] = {n0 * ijl, n1 * ijl, n2 * ijl};
+            const float r = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]), ir = 1.f / r;
+            float sn, cs;
+            phase_sincos(wr * r, &sn, &cs);
+            const float re2 = wq * jl * i4pi * ir;
+            const cplx<float> zg = {cs * re2, sn * re2};
+            const cplx<float> zh = zg * cplx<float>{-ir, wr};
+            const float re1 = (d[0] * ny[0] + d[1] * ny[1] + d[2] * ny[2]) * ir;
+            const float rr2 = -(d[0] * nx[0] + d[1] * nx[1] + d[2] * nx[2]) * ir;
+            zG += zg;
+            zH += zh * re1;
+            zHT += zh * rr2;
+            zE += zg * (wnu2 * (nx[0] * ny[0] + nx[1] * ny[1] + nx[2] * ny[2]));
+        }
+    }
+    return {warp_sum(zG), warp_sum(zH), warp_sum(zHT), warp_sum(zE)};
+}
+
 }  // namespace bem
