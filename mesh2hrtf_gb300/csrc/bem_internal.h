@@ -166,11 +166,17 @@ struct ProjSys {
     const double *pts;      // [npts][3]
     double *pot, *grad;     // [npts], [npts][3] complex; grad may be nullptr
     int *status;
+    float4 *part;           // float projection: partial sums [slice][point][2]
+                            // (the Krylov basis, idle once the system is solved)
+    long long part_cap;     // its capacity in float4
+    int nslice;             // element slices (proj_batch_finish; 0: one warp per point)
 };
 struct ProjBatch {
     int B;
     int fld_off[kMaxAsm + 1];    // blocks of 256 elements
     int pt_off[kMaxAsm + 1];     // blocks of 8 points
+    int lp_off[kMaxAsm + 1];     // blocks of 8 (32-point group, element slice) warps
+    int ps_off[kMaxAsm + 1];     // blocks of 256 points (slice sums)
     ProjSys sys[kMaxAsm];
 };
 void proj_batch_finish(ProjBatch &t);

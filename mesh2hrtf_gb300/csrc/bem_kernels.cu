@@ -931,6 +931,57 @@ __device__ __forceinline__ void proj_elem_data(const double2 *phi, const double2
     }
 }
 
+// Potential and gradient of point p from the element sums (FP64): the tau
+// factor, then the incident field with its images (NC_ContributionIncidentWaves,
+// NC_PostProcessing.cpp:776-866).
+__device__ void project_finish(const DevMesh &m, const DevFreq &f, const double x64[3], int p, cplx<double> sp,
+                               cplx<double> sg[3], double2 *pot, double2 *grad) {
+    if (f.tao != 1.0) {
+        sp = sp * f.tao;
+        for (int kk = 0; kk < 3; ++kk) sg[kk] = sg[kk] * f.tao;
+    }
+    if (f.n_plane || f.n_point) {
+        const DevSym &sy = m.sym;
+        double xs[3];
+        plane_wave_origin(sy, x64, xs);
+        for (int s = 0; s < f.n_plane; ++s) {
+            double d[3] = {f.pw_dir[3 * s], f.pw_dir[3 * s + 1], f.pw_dir[3 * s + 2]};
+            const cplx<double> amp = ld_c(f.pw_amp, s);
+            for (int kref = 0; kref < sy.nref; ++kref) {
+                if (kref > 0) reflect_source(sy, kref, d, false);
+                const double rf = ((sy.rneg >> kref) & 1u) ? -1.0 : 1.0;
+                double sn, cs;
+                sincos((d[0] * xs[0] + d[1] * xs[1] + d[2] * xs[2]) * f.wr, &sn, &cs);
+                const cplx<double> zg = cplx<double>{cs * rf, sn * rf} * amp;
+                sp += zg;
+                const cplx<double> zv = {-zg.im * f.wr, zg.re * f.wr};
+                for (int kk = 0; kk < 3; ++kk) sg[kk] += zv * d[kk];
+            }
+        }
+        for (int s = 0; s < f.n_point; ++s) {
+            double q[3] = {f.ps_xyz[3 * s], f.ps_xyz[3 * s + 1], f.ps_xyz[3 * s + 2]};
+            const cplx<double> amp = ld_c(f.ps_amp, s);
+            for (int kref = 0; kref < sy.nref; ++kref) {
+                if (kref > 0) reflect_source(sy, kref, q, true);
+                const double rf = ((sy.rneg >> kref) & 1u) ? -1.0 : 1.0;
+                double d[3] = {x64[0] - q[0], x64[1] - q[1], x64[2] - q[2]};
+                const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                d[0] /= r; d[1] /= r; d[2] /= r;
+                double sn, cs;
+                sincos(f.wr * r, &sn, &cs);
+                const double re2 = rf / kPI4 / r;
+                const cplx<double> zg = cplx<double>{cs * re2, sn * re2} * amp;
+                sp += zg;
+                const cplx<double> zv = cplx<double>{-1.0 / r, f.wr} * zg;
+                for (int kk = 0; kk < 3; ++kk) sg[kk] += zv * d[kk];
+            }
+        }
+    }
+    pot[p] = make_double2(sp.re, sp.im);
+    if (grad)
+        for (int kk = 0; kk < 3; ++kk) grad[3 * p + kk] = make_double2(sg[kk].re, sg[kk].im);
+}
+
 // Field projection, one warp per point: lanes sweep the elements (and their
 // symmetry images) 32 at a time; regular pairs in the lane, subdivided pairs
 // by the whole warp.
@@ -1079,54 +1130,171 @@ __global__ void __launch_bounds__(256, 2) k_project(const __grid_constant__ Proj
     cplx<double> sg[3];
     for (int kk = 0; kk < 3; ++kk) sg[kk] = warp_sum(cplx<double>{(double)acc.g[kk].re, (double)acc.g[kk].im});
     if (lane == 0) {
-        if (f.tao != 1.0) {
-            sp = sp * f.tao;
-            for (int kk = 0; kk < 3; ++kk) sg[kk] = sg[kk] * f.tao;
-        }
-        // incident field with its images (NC_ContributionIncidentWaves,
-        // NC_PostProcessing.cpp:776-866)
-        if (f.n_plane || f.n_point) {
-            const DevSym &sy = m.sym;
-            double xs[3];
-            plane_wave_origin(sy, x64, xs);
-            for (int s = 0; s < f.n_plane; ++s) {
-                double d[3] = {f.pw_dir[3 * s], f.pw_dir[3 * s + 1], f.pw_dir[3 * s + 2]};
-                const cplx<double> amp = ld_c(f.pw_amp, s);
-                for (int kref = 0; kref < sy.nref; ++kref) {
-                    if (kref > 0) reflect_source(sy, kref, d, false);
-                    const double rf = ((sy.rneg >> kref) & 1u) ? -1.0 : 1.0;
-                    double sn, cs;
-                    sincos((d[0] * xs[0] + d[1] * xs[1] + d[2] * xs[2]) * f.wr, &sn, &cs);
-                    const cplx<double> zg = cplx<double>{cs * rf, sn * rf} * amp;
-                    sp += zg;
-                    const cplx<double> zv = {-zg.im * f.wr, zg.re * f.wr};
-                    for (int kk = 0; kk < 3; ++kk) sg[kk] += zv * d[kk];
-                }
-            }
-            for (int s = 0; s < f.n_point; ++s) {
-                double q[3] = {f.ps_xyz[3 * s], f.ps_xyz[3 * s + 1], f.ps_xyz[3 * s + 2]};
-                const cplx<double> amp = ld_c(f.ps_amp, s);
-                for (int kref = 0; kref < sy.nref; ++kref) {
-                    if (kref > 0) reflect_source(sy, kref, q, true);
-                    const double rf = ((sy.rneg >> kref) & 1u) ? -1.0 : 1.0;
-                    double d[3] = {x64[0] - q[0], x64[1] - q[1], x64[2] - q[2]};
-                    const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-                    d[0] /= r; d[1] /= r; d[2] /= r;
-                    double sn, cs;
-                    sincos(f.wr * r, &sn, &cs);
-                    const double re2 = rf / kPI4 / r;
-                    const cplx<double> zg = cplx<double>{cs * re2, sn * re2} * amp;
-                    sp += zg;
-                    const cplx<double> zv = cplx<double>{-1.0 / r, f.wr} * zg;
-                    for (int kk = 0; kk < 3; ++kk) sg[kk] += zv * d[kk];
-                }
-            }
-        }
-        pot[p] = make_double2(sp.re, sp.im);
-        if (grad)
-            for (int kk = 0; kk < 3; ++kk) grad[3 * p + kk] = make_double2(sg[kk].re, sg[kk].im);
+        project_finish(m, f, x64, p, sp, sg, pot, grad);
         if (err != kDevOk) atomicMax(status, err);
     }
+}
+
+// Float projection with the roles of lanes and elements exchanged: a warp
+// takes 32 evaluation points (one per lane) and a slice of the elements,
+// and sweeps the slice one element at a time, so every element's data is a
+// warp-uniform load shared by 32 points instead of 32 loads of different
+// elements.  Partial sums go to ProjSys::part per (slice, point);
+// k_project_sum adds the slices in slice order (FP64) and finishes the
+// point.  Pair arithmetic as in k_project<float>: the fused flat-triangle
+// rule, the general rule, and the warp-wide subdivision for near pairs, here
+// one near lane at a time.
+constexpr int kProjSlice = 256;   // elements per slice (fewer slices if the scratch is short)
+
+__global__ void __launch_bounds__(256, 2) k_project_pts(const __grid_constant__ ProjBatch tb) {
+    __shared__ WarpScratch ws_all[8];
+    const int sb = find_sys(tb.lp_off, tb.B, blockIdx.x);
+    const ProjSys &S = tb.sys[sb];
+    const DevMesh m = to_dev(S.m);
+    const DevFreq &f = S.f;
+    const int lane = threadIdx.x, w = threadIdx.y, n = m.n, npts = S.npts;
+    const int G = (npts + 31) >> 5, nsl = S.nslice;
+    const int item = (blockIdx.x - tb.lp_off[sb]) * 8 + w;
+    if (item >= G * nsl) return;
+    const int g = item % G, sl = item / G;
+    const int per = (n + nsl - 1) / nsl;
+    const int j0 = sl * per, j1 = min(n, j0 + per);
+    const int p = g * 32 + lane;
+    const bool pv = p < npts;
+    const int pp = pv ? p : g * 32;   // idle lanes shadow the group's first point
+    WarpScratch &ws = ws_all[w];
+    // The point as float hi/lo pair and the wave numbers in float, made opaque
+    // to the compiler: under register pressure it otherwise recomputes them
+    // from the FP64 values at every pair, and GB300 issues those conversions
+    // (and the FP64 subtraction) on its narrow FP64 pipe.
+    float xhi[3], xlo[3];
+    for (int c = 0; c < 3; ++c) {
+        const double xv = S.pts[3 * pp + c];
+        xhi[c] = (float)xv;
+        xlo[c] = (float)(xv - (double)xhi[c]);
+        asm volatile("" : "+f"(xhi[c]), "+f"(xlo[c]));
+    }
+    const double2 *phi = (const double2 *)S.phi, *vel = (const double2 *)S.vel;
+    const float2 *phi32 = (const float2 *)S.phi32, *vel32 = (const float2 *)S.vel32;
+    ProjAcc<float> acc;
+    acc.p = acc.g[0] = acc.g[1] = acc.g[2] = cmk(0.f, 0.f);
+    float k = (float)f.k, wr = (float)f.wr;
+    asm volatile("" : "+f"(k), "+f"(wr));
+    const float k2 = k * k;
+    int err = kDevOk;
+    for (int kref = 0; kref < m.sym.nref; ++kref) {
+        const DevMesh mk = image_mesh(m, kref);
+        const bool neg = image_negated(m, kref);
+        for (int j = j0; j < j1; ++j) {
+            const bool iv = S.ivi[j] != 0;
+            const int nv = m.nvert[j];
+            cplx<float> ph, vl[4];
+            proj_elem_data<float>(phi, vel, phi32, vel32, n, j, nv, iv, kref, neg, ph, vl);
+            Elem32 e;
+            load_elem32(mk, j, xhi, xlo, e);
+            const float isq = m.isqa32[j];
+            const float q2 = (e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * (isq * isq);
+            bool near = false;
+            int order = 2;
+            if (q2 <= c_quad.far2_sq && !classify_fast(sqrtf(q2), near, order)) {
+                const double xp[3] = {S.pts[3 * pp], S.pts[3 * pp + 1], S.pts[3 * pp + 2]};
+                const double rd = ratio0_exact(mk, j, xp);
+                near = rd < kTolf;
+                if (!near) order = gauss_order(rd);
+            }
+            if (!near && e.nv == 3 && !iv) {
+                float2 P = make_float2(0.f, 0.f), U[3], Tn = make_float2(0.f, 0.f);
+                U[0] = U[1] = U[2] = make_float2(0.f, 0.f);
+                const float dny = e.D[0] * e.n[0] + e.D[1] * e.n[1] + e.D[2] * e.n[2];
+                if (order <= 2) proj_tri_points<4, 0>(e, dny, k2, wr, P, U, Tn);
+                else if (order == 3) proj_tri_points<7, 4>(e, dny, k2, wr, P, U, Tn);
+                else proj_tri_points<13, 11>(e, dny, k2, wr, P, U, Tn);
+                const cplx<float> pq = ph * cplx<float>{P.x, P.y};
+                acc.p.re += pq.re;
+                acc.p.im += pq.im;
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk) {
+                    const cplx<float> gg = ph * cplx<float>{fmaf(Tn.x, e.n[kk], U[kk].x), fmaf(Tn.y, e.n[kk], U[kk].y)};
+                    acc.g[kk].re += gg.re;
+                    acc.g[kk].im += gg.im;
+                }
+            } else if (!near) {
+                const int np = e.nv == 3 ? tri_count(order) : quad_count(order);
+                for (int gq = 0; gq < np; ++gq) {
+                    float s, t, wq;
+                    if (e.nv == 3) {
+                        const int o = tri_offset(order) + gq;
+                        s = c_trif[o][0]; t = c_trif[o][1]; wq = c_trif[o][2];
+                    } else {
+                        const int a = gq / order, b = gq - a * order;
+                        s = c_glxf[order][a]; t = c_glxf[order][b];
+                        wq = c_glwf[order][a] * c_glwf[order][b];
+                    }
+                    QPoint<float> q;
+                    map_point(e, s, t, wq, q);
+                    proj_point(q, ph, vl, e.nv, iv, k, wr, acc);
+                }
+            }
+            // near pairs: the whole warp subdivides for one lane's point at a time
+            unsigned todo = __ballot_sync(0xffffffffu, pv && near);
+            if (todo) {
+                Elem64 e64;
+                load_elem64(mk, j, e64);
+                cplx<float> phn, vln[4];
+                proj_elem_data<float>(phi, vel, phi32, vel32, n, j, nv, true, kref, neg, phn, vln);
+                while (todo) {
+                    const int L = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    double xl[3];
+                    float lh[3], ll[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        xl[c] = S.pts[3 * (g * 32 + L) + c];   // lane L's point, a uniform load
+                        lh[c] = __shfl_sync(0xffffffffu, xhi[c], L);
+                        ll[c] = __shfl_sync(0xffffffffu, xlo[c], L);
+                    }
+                    Elem32 e32;
+                    load_elem32(mk, j, lh, ll, e32);
+                    ProjSink<float> sink;
+                    sink.e = &e32; sink.phi = phn; sink.vel = vln; sink.ivi = iv; sink.k = k; sink.wr = wr;
+                    sink.init();
+                    const int rc = warp_subdivide(e64, m.area64[j], xl, ws, sink, &e32, isq);
+                    if (rc != kDevOk) err = rc;
+                    const ProjAcc<float> r = sink.reduce();
+                    if (lane == L) {
+                        acc.p += r.p;
+                        for (int kk = 0; kk < 3; ++kk) acc.g[kk] += r.g[kk];
+                    }
+                }
+            }
+        }
+    }
+    float4 *out = S.part + 2 * ((size_t)(sl * G + g) * 32 + lane);
+    out[0] = make_float4(acc.p.re, acc.p.im, acc.g[0].re, acc.g[0].im);
+    out[1] = make_float4(acc.g[1].re, acc.g[1].im, acc.g[2].re, acc.g[2].im);
+    if (err != kDevOk && lane == 0) atomicMax(S.status, err);
+}
+
+// Thread per point: the slices' partial sums in slice order (FP64), then the
+// point's tau factor and incident field.
+__global__ void __launch_bounds__(256) k_project_sum(const __grid_constant__ ProjBatch tb) {
+    const int sb = find_sys(tb.ps_off, tb.B, blockIdx.x);
+    const ProjSys &S = tb.sys[sb];
+    const int p = (blockIdx.x - tb.ps_off[sb]) * 256 + threadIdx.x;
+    if (p >= S.npts) return;
+    const DevMesh m = to_dev(S.m);
+    const int G = (S.npts + 31) >> 5;
+    cplx<double> sp = {0.0, 0.0}, sg[3] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+    for (int sl = 0; sl < S.nslice; ++sl) {
+        const float4 *in = S.part + 2 * ((size_t)sl * G * 32 + p);
+        const float4 a = in[0], b = in[1];
+        sp += cplx<double>{(double)a.x, (double)a.y};
+        sg[0] += cplx<double>{(double)a.z, (double)a.w};
+        sg[1] += cplx<double>{(double)b.x, (double)b.y};
+        sg[2] += cplx<double>{(double)b.z, (double)b.w};
+    }
+    const double x64[3] = {S.pts[3 * p], S.pts[3 * p + 1], S.pts[3 * p + 2]};
+    project_finish(m, S.f, x64, p, sp, sg, (double2 *)S.pot, (double2 *)S.grad);
 }
 
 // ---------------------------------------------------------------- tables
@@ -1275,10 +1443,18 @@ void asm_batch_finish(AsmBatch &t) {
 }
 
 void proj_batch_finish(ProjBatch &t) {
-    t.fld_off[0] = t.pt_off[0] = 0;
+    t.fld_off[0] = t.pt_off[0] = t.lp_off[0] = t.ps_off[0] = 0;
     for (int b = 0; b < t.B; ++b) {
-        t.fld_off[b + 1] = t.fld_off[b] + (t.sys[b].m.n + 255) / 256;
-        t.pt_off[b + 1] = t.pt_off[b] + (t.sys[b].npts + 7) / 8;
+        ProjSys &S = t.sys[b];
+        t.fld_off[b + 1] = t.fld_off[b] + (S.m.n + 255) / 256;
+        t.pt_off[b + 1] = t.pt_off[b] + (S.npts + 7) / 8;
+        // element slices of the float projection, as many as the scratch holds
+        const long long G = (S.npts + 31) / 32;
+        const long long want = (S.m.n + kProjSlice - 1) / kProjSlice;
+        const long long fit = G > 0 ? S.part_cap / (2 * 32 * G) : 0;
+        S.nslice = S.part ? (int)std::min(want, fit) : 0;
+        t.lp_off[b + 1] = t.lp_off[b] + (int)((G * S.nslice + 7) / 8);
+        t.ps_off[b + 1] = t.ps_off[b] + (S.npts + 255) / 256;
     }
 }
 
@@ -1345,10 +1521,18 @@ cudaError_t launch_project(const ProjBatch &t, int prec, cudaStream_t st) {
     if (t.B <= 0 || t.pt_off[t.B] == 0) return cudaSuccess;
     dim3 block(32, 8);
     count_launches(1);
-    if (prec == 0)
+    bool sliced = prec != 0;
+    for (int b = 0; b < t.B; ++b)
+        if (t.sys[b].npts > 0 && t.sys[b].nslice == 0) sliced = false;   // scratch too short
+    if (prec == 0) {
         k_project<double><<<t.pt_off[t.B], block, 0, st>>>(t);
-    else
+    } else if (!sliced) {
         k_project<float><<<t.pt_off[t.B], block, 0, st>>>(t);
+    } else {
+        count_launches(1);
+        k_project_pts<<<t.lp_off[t.B], block, 0, st>>>(t);
+        k_project_sum<<<t.ps_off[t.B], 256, 0, st>>>(t);
+    }
     return cudaGetLastError();
 }
 

@@ -210,6 +210,8 @@ struct bem_solver_s {
         q.pot = pot_dev;
         q.grad = grad_dev;
         q.status = d.status;
+        q.part = reinterpret_cast<float4 *>(d.V);
+        q.part_cap = (long long)((size_t)(restart + 1) * (size_t)n * (prec == BEM_PREC_FP64 ? 16 : 8) / 16);
         return q;
     }
 };
