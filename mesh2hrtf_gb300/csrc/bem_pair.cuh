@@ -25,6 +25,7 @@ struct WarpScratch {
 template <typename T> struct AsmSink;
 
 template <> struct AsmSink<double> {
+    static constexpr bool kFloatPoints = false;   // quadrature points in FP64
     const Elem64 *e;
     const double *x, *nx;
     double k, wr;
@@ -42,17 +43,19 @@ template <> struct AsmSink<double> {
 };
 
 template <> struct AsmSink<float> {
+    static constexpr bool kFloatPoints = true;    // quadrature points in float (addf)
     const Elem32 *e;
     const float *nx;
     float k, wr;
     KVals<float> acc;
     __device__ void init() { acc.G = acc.H = acc.HT = acc.E = cmk(0.f, 0.f); }
-    __device__ void add(double s, double t, double w) {
+    __device__ void addf(float s, float t, float w) {
         QPoint<float> q;
-        map_point(*e, (float)s, (float)t, (float)w, q);
+        map_point(*e, s, t, w, q);
         KVals<float> v = kernel_values(q, nx, k, wr);
         acc.G += v.G; acc.H += v.H; acc.HT += v.HT; acc.E += v.E;
     }
+    __device__ void add(double s, double t, double w) { addf((float)s, (float)t, (float)w); }
     __device__ KVals<float> reduce() {
         return {warp_sum(acc.G), warp_sum(acc.H), warp_sum(acc.HT), warp_sum(acc.E)};
     }
@@ -61,6 +64,7 @@ template <> struct AsmSink<float> {
 // Right-hand side contribution of a column with prescribed nonzero boundary
 // values (Zrsintel[4] of NC_RegularIntegration, NC_EquationSystem.cpp:1719-1725).
 struct RhsSink {
+    static constexpr bool kFloatPoints = false;
     const Elem64 *e;
     const double *x, *nx;
     const cplx<double> *bc;   // nodal values
@@ -116,6 +120,7 @@ __device__ __forceinline__ void proj_point(const QPoint<T> &q, cplx<T> phi, cons
 template <typename T> struct ProjSink;
 
 template <> struct ProjSink<double> {
+    static constexpr bool kFloatPoints = false;
     const Elem64 *e;
     const double *x;
     cplx<double> phi;
@@ -138,6 +143,7 @@ template <> struct ProjSink<double> {
 };
 
 template <> struct ProjSink<float> {
+    static constexpr bool kFloatPoints = true;
     const Elem32 *e;
     cplx<float> phi;
     const cplx<float> *vel;
@@ -145,11 +151,12 @@ template <> struct ProjSink<float> {
     float k, wr;
     ProjAcc<float> acc;
     __device__ void init() { acc.p = acc.g[0] = acc.g[1] = acc.g[2] = cmk(0.f, 0.f); }
-    __device__ void add(double s, double t, double w) {
+    __device__ void addf(float s, float t, float w) {
         QPoint<float> q;
-        map_point(*e, (float)s, (float)t, (float)w, q);
+        map_point(*e, s, t, w, q);
         proj_point(q, phi, vel, e->nv, ivi, k, wr, acc);
     }
+    __device__ void add(double s, double t, double w) { addf((float)s, (float)t, (float)w); }
     __device__ ProjAcc<float> reduce() {
         ProjAcc<float> r;
         r.p = warp_sum(acc.p);
@@ -174,6 +181,24 @@ __device__ __forceinline__ void sub_point(int nv, int order, int g, double xice,
     }
     if (fabs(fase - 1.0) < kEPSY) { s = cs; t = ct; w = cw; }
     else { s = xice + cs * fase; t = etce + ct * fase; w = cw * (fase * fase); }
+}
+
+// The same in float for the float sinks: the stored origin and scale are
+// exact floats (dyadic), the rule's tables float; the point moves by float
+// rounding only (~1e-7 of the element), below the float kernel arithmetic.
+__device__ __forceinline__ void sub_point_f(int nv, int order, int g, float xice, float etce, float fase,
+                                            float &s, float &t, float &w) {
+    float cs, ct, cw;
+    if (nv == 3) {
+        const int o = tri_offset(order) + g;
+        cs = c_trif[o][0]; ct = c_trif[o][1]; cw = c_trif[o][2];
+    } else {
+        const int i = g / order, jj = g - i * order;
+        cs = c_glxf[order][i]; ct = c_glxf[order][jj];
+        cw = c_glwf[order][i] * c_glwf[order][jj];
+    }
+    if (fase == 1.0f) { s = cs; t = ct; w = cw; }   // |fase - 1| < 1e-14 for dyadic fase
+    else { s = fmaf(cs, fase, xice); t = fmaf(ct, fase, etce); w = cw * (fase * fase); }
 }
 
 __device__ __forceinline__ int sub_npts(int nv, int order) {
@@ -211,6 +236,7 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
     double faclin = 2.0;
     for (int level = 0; level <= kMaxLevel; ++level) {
         faclin *= 0.5;
+        const float faclinf = (float)faclin;   // a power of two
         const double sqa = __dsqrt_rn(__dmul_rn(__dmul_rn(area, faclin), faclin));
         int ndie = 0;
         for (int base = 0; base < nsel; base += 32) {
@@ -219,18 +245,20 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
             bool split = false;
             int ordf = 0;   // Gauss order from the float test (0: not decided there)
             double ratdis = 0.0, scent = 0.0, tcent = 0.0;
-            double vs[4] = {0, 0, 0, 0}, vt[4] = {0, 0, 0, 0};
+            // vertices as stored (exact floats); FP64 copies only where the
+            // exact arithmetic needs them
+            float vsf[4] = {0.f, 0.f, 0.f, 0.f}, vtf[4] = {0.f, 0.f, 0.f, 0.f};
             if (active) {
                 for (int v = 0; v < nv; ++v) {
-                    vs[v] = ws.lv[cur][idi][v][0];
-                    vt[v] = ws.lv[cur][idi][v][1];
+                    vsf[v] = ws.lv[cur][idi][v][0];
+                    vtf[v] = ws.lv[cur][idi][v][1];
                 }
                 bool decided = false;
                 if (ef && level <= kFastLevels) {
                     float sc = 0.f, tc = 0.f;
                     for (int v = 0; v < nv; ++v) {
-                        sc += (float)vs[v];
-                        tc += (float)vt[v];
+                        sc += vsf[v];
+                        tc += vtf[v];
                     }
                     sc /= (float)nv;
                     tc /= (float)nv;
@@ -245,7 +273,7 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
                             d[k] = ef->D[k] + sh[0] * ef->q[0][k] + sh[1] * ef->q[1][k] + sh[2] * ef->q[2][k] +
                                    sh[3] * ef->q[3][k];
                     }
-                    const float rf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * isqa / (float)faclin;
+                    const float rf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * isqa / faclinf;
                     bool nr = false;
                     int o = 2;
                     if (classify_fast(rf, nr, o)) {
@@ -256,8 +284,8 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
                 }
                 if (!decided || split) {
                     for (int v = 0; v < nv; ++v) {
-                        scent = __dadd_rn(scent, vs[v]);
-                        tcent = __dadd_rn(tcent, vt[v]);
+                        scent = __dadd_rn(scent, (double)vsf[v]);
+                        tcent = __dadd_rn(tcent, (double)vtf[v]);
                     }
                     scent = __ddiv_rn(scent, (double)nv);
                     tcent = __ddiv_rn(tcent, (double)nv);
@@ -275,27 +303,28 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
                 if (rank + 1 > 15) {
                     err = kDevSplitLimit;
                 } else {
-                    double ms[8], mt[8];
+                    // midpoints of dyadic vertices: exact in float
+                    float ms[8], mt[8];
                     for (int v = 0; v < nv; ++v) {
                         int v1 = v + 1 == nv ? 0 : v + 1;
-                        ms[v] = vs[v]; mt[v] = vt[v];
-                        ms[v + nv] = (vs[v] + vs[v1]) / 2.0;
-                        mt[v + nv] = (vt[v] + vt[v1]) / 2.0;
+                        ms[v] = vsf[v]; mt[v] = vtf[v];
+                        ms[v + nv] = (vsf[v] + vsf[v1]) * 0.5f;
+                        mt[v + nv] = (vtf[v] + vtf[v1]) * 0.5f;
                     }
                     const int nxt = cur ^ 1, c0 = rank * 4;
                     for (int v = 0; v < nv; ++v) {
                         const int nsu = c0 + v, j1 = v + nv;
                         int j2 = j1 - 1;
                         if (j2 < nv) j2 += nv;
-                        ws.lv[nxt][nsu][0][0] = (float)ms[v];  ws.lv[nxt][nsu][0][1] = (float)mt[v];
-                        ws.lv[nxt][nsu][1][0] = (float)ms[j1]; ws.lv[nxt][nsu][1][1] = (float)mt[j1];
+                        ws.lv[nxt][nsu][0][0] = ms[v];  ws.lv[nxt][nsu][0][1] = mt[v];
+                        ws.lv[nxt][nsu][1][0] = ms[j1]; ws.lv[nxt][nsu][1][1] = mt[j1];
                         if (nv == 4) {
                             ws.lv[nxt][nsu][2][0] = (float)scent;  ws.lv[nxt][nsu][2][1] = (float)tcent;
-                            ws.lv[nxt][nsu][3][0] = (float)ms[j2]; ws.lv[nxt][nsu][3][1] = (float)mt[j2];
+                            ws.lv[nxt][nsu][3][0] = ms[j2]; ws.lv[nxt][nsu][3][1] = mt[j2];
                         } else {
-                            ws.lv[nxt][nsu][2][0] = (float)ms[j2]; ws.lv[nxt][nsu][2][1] = (float)mt[j2];
-                            ws.lv[nxt][c0 + 3][v][0] = (float)ms[j1];
-                            ws.lv[nxt][c0 + 3][v][1] = (float)mt[j1];
+                            ws.lv[nxt][nsu][2][0] = ms[j2]; ws.lv[nxt][nsu][2][1] = mt[j2];
+                            ws.lv[nxt][c0 + 3][v][0] = ms[j1];
+                            ws.lv[nxt][c0 + 3][v][1] = mt[j1];
                         }
                     }
                 }
@@ -308,6 +337,8 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
                 const int r = __popc(stmask & lt);
                 if (nsbe + r >= kMSBE) err = kDevSubLimit;
                 double ox, oy, fac;
+                double vs[4], vt[4];
+                for (int v = 0; v < 4; ++v) { vs[v] = (double)vsf[v]; vt[v] = (double)vtf[v]; }
                 if (nv == 4) {
                     ox = (vs[0] + vs[1] + vs[2] + vs[3]) / 4.0;
                     oy = (vt[0] + vt[1] + vt[2] + vt[3]) / 4.0;
@@ -345,10 +376,16 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
                 int sidx = 0;
                 while (ws.soff[sidx + 1] <= f) ++sidx;
                 const int g = f - ws.soff[sidx];
-                double s, t, w;
-                sub_point(nv, ws.sord[sidx], g, (double)ws.sxi[sidx], (double)ws.seta[sidx],
-                          (double)ws.sfac[sidx], s, t, w);
-                sink.add(s, t, w);
+                if constexpr (Sink::kFloatPoints) {
+                    float s, t, w;
+                    sub_point_f(nv, ws.sord[sidx], g, ws.sxi[sidx], ws.seta[sidx], ws.sfac[sidx], s, t, w);
+                    sink.addf(s, t, w);
+                } else {
+                    double s, t, w;
+                    sub_point(nv, ws.sord[sidx], g, (double)ws.sxi[sidx], (double)ws.seta[sidx],
+                              (double)ws.sfac[sidx], s, t, w);
+                    sink.add(s, t, w);
+                }
             }
             nsbe += nst;
             __syncwarp();
