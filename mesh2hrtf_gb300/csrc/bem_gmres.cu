@@ -1428,6 +1428,25 @@ __device__ __forceinline__ float2 apply_minv_f(const void *Minv, int n, int blk,
     const float2 *x = vf + (tid & 128);
     const float2 *M = (const float2 *)Minv + (size_t)pb * kBlock * kBlock;
     float sh = 0.f, sl = 0.f, th = 0.f, tl = 0.f;
+    if (nb == kBlock) {
+        // full block: each chunk's 16 loads issued before its arithmetic
+        for (int c0 = 0; c0 < kBlock; c0 += 16) {
+            float2 mv[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) mv[u] = M[(size_t)(c0 + u) * kBlock + rr];
+            float ar = 0.f, ai = 0.f;
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const float2 xv = x[c0 + u];
+                ar = fmaf(mv[u].x, xv.x, ar); ar = fmaf(-mv[u].y, xv.y, ar);
+                ai = fmaf(mv[u].x, xv.y, ai); ai = fmaf(mv[u].y, xv.x, ai);
+            }
+            float t, e;
+            two_sum(sh, ar, t, e); sh = t; sl += e;
+            two_sum(th, ai, t, e); th = t; tl += e;
+        }
+        return make_float2(sh + sl, th + tl);
+    }
     for (int c0 = 0; c0 < nb; c0 += 16) {
         float ar = 0.f, ai = 0.f;
         const int ce = min(c0 + 16, nb);
