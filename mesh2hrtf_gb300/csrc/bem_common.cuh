@@ -49,19 +49,40 @@ template <typename T> __device__ __forceinline__ cplx<T> warp_sum(cplx<T> v) {
     return {warp_sum(v.re), warp_sum(v.im)};
 }
 
+// The hardware approximations (PTX sin/cos/rsqrt.approx) with denormal
+// inputs flushed to zero: without .ftz the compiler wraps each in a
+// denormal test and rescaling (the library build keeps IEEE denormals).
+// Normal inputs give the same results as the non-ftz forms.
+__device__ __forceinline__ float sin_approx(float x) {
+    float y;
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float cos_approx(float x) {
+    float y;
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+// 1/sqrt(x) for squared distances (never denormal: >= 1e-12 m^2 here)
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // sin and cos of a float phase k*r: Cody & Waite reduction by 2 pi (2 pi
 // split into two floats, x / 2 pi rounded with the 1.5 * 2^23 shifter, which
 // needs no float-to-integer conversion: on GB300 those issue on the narrow
-// FP64 pipe), then the hardware approximations __sinf / __cosf, accurate to
-// about 2^-21 absolute on [-pi, pi].  The mixed-precision path's error budget
-// is 1e-4 against FP64; this keeps it near 3e-6.
+// FP64 pipe), then the hardware approximations, accurate to about 2^-21
+// absolute on [-pi, pi].  The mixed-precision path's error budget is 1e-4
+// against FP64; this keeps it near 3e-6.
 __device__ __forceinline__ void phase_sincos(float x, float *s, float *c) {
     const float sh = fmaf(x, 0.159154943f, 12582912.0f);   // 1 / (2 pi), 1.5 * 2^23
     const float q = sh - 12582912.0f;
     float r = fmaf(q, -6.28318548202514648f, x);
     r = fmaf(q, 1.74845553146951e-07f, r);
-    *s = __sinf(r);
-    *c = __cosf(r);
+    *s = sin_approx(r);
+    *c = cos_approx(r);
 }
 
 __device__ __forceinline__ void sincos_t(double x, double *s, double *c) { sincos(x, s, c); }
@@ -384,7 +405,7 @@ __device__ __forceinline__ void map_point(const Elem32 &e, float s, float t, flo
         for (int a = 0; a < 4; ++a) q.sh[a] = sh[a];
     }
     const float r2 = q.d[0] * q.d[0] + q.d[1] * q.d[1] + q.d[2] * q.d[2];
-    q.ir = rsqrtf(r2);
+    q.ir = rsqrt_approx(r2);
     q.r = r2 * q.ir;
 }
 

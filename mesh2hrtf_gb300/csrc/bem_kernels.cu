@@ -111,7 +111,7 @@ struct FusedCol {
 
 __device__ __forceinline__ void fused_point(const FusedCol &c, float dny, float dnx, float nn, float r2, float w,
                                             float &acc_re, float &acc_im) {
-    const float ir = rsqrtf(r2);
+    const float ir = rsqrt_approx(r2);
     const float r = r2 * ir;
     float sn, cs;
     phase_sincos(c.wr * r, &sn, &cs);
@@ -238,7 +238,7 @@ __device__ __forceinline__ float2 far_entry_tri2(const FarCol4 &e, const float D
     for (int g = 0; g < 4; ++g) {
         const float r2 = fmaf(c_far4[g][2], Da, fmaf(c_far4[g][3], Db, D2 + e.C[g]));
         const float dnx = fmaf(c_far4[g][1], bnx, fmaf(c_far4[g][0], anx, dnx0));
-        const float u = rsqrtf(r2);
+        const float u = rsqrt_approx(r2);
         float sn, cs;
         phase_sincos(c.wr * (r2 * u), &sn, &cs);
         float fr, fi;
@@ -885,7 +885,7 @@ __device__ __forceinline__ void proj_tri_points(const Elem32 &e, float dny, floa
 #pragma unroll
         for (int k = 0; k < 3; ++k) d[k] = fmaf(tt, e.b[k], fmaf(ss, e.a[k], e.D[k]));
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        const float ir = rsqrtf(r2), r = r2 * ir;
+        const float ir = rsqrt_approx(r2), r = r2 * ir;
         float sn, cs;
         phase_sincos(wr * r, &sn, &cs);
         const float amp = wj * ir;
