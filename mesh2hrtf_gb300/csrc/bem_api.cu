@@ -988,11 +988,13 @@ bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
     // size only if that was too small
     unsigned long long *d_cnt = nullptr, cnt = 0;
     unsigned long long cap = 48ull * (unsigned long long)n * (unsigned long long)sym.nref;
+    void *d_nls = nullptr;   // bounding spheres of the near-list column blocks
+    if (e == cudaSuccess) e = bem::dev_malloc(&d_nls, bem::near_list_scratch_bytes(n, sym.nref));
     if (e == cudaSuccess) e = dalloc(&d_cnt, 1);
     for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
         if (e == cudaSuccess) e = dalloc(&m->d_near, (size_t)cap);
         if (e == cudaSuccess) e = cudaMemset(d_cnt, 0, sizeof(unsigned long long));
-        if (e == cudaSuccess) e = bem::launch_near_list(m->view(), m->d_near, cap, d_cnt, 0);
+        if (e == cudaSuccess) e = bem::launch_near_list(m->view(), d_nls, m->d_near, cap, d_cnt, 0);
         if (e == cudaSuccess) e = cudaMemcpy(&cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess || cnt <= cap) break;
         bem::dev_free(m->d_near);
@@ -1000,6 +1002,7 @@ bem_status bem_mesh_create(const bem_mesh_desc *d, bem_mesh_t *out) {
         cap = cnt;
     }
     bem::dev_free(d_cnt);
+    bem::dev_free(d_nls);
     if (e == cudaSuccess && cnt > cap) {
         delete m;
         return fail(BEM_ERR_CUDA, "near list: %llu pairs, list of %llu", cnt, cap);

@@ -132,9 +132,11 @@ void asm_batch_finish(AsmBatch &t);
 
 // Pairs integrated with subdivision plus self pairs (row, column | image
 // mask << kNearColBits) into list[0, cap); *count (zero before) receives the
-// number of pairs, also when it exceeds cap.
-cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long cap, unsigned long long *count,
-                             cudaStream_t st);
+// number of pairs, also when it exceeds cap.  scratch: device memory of
+// near_list_scratch_bytes(n, nref) for the column blocks' bounding spheres.
+size_t near_list_scratch_bytes(int n, int nref);
+cudaError_t launch_near_list(const DevMeshView &m, void *scratch, int2 *list, unsigned long long cap,
+                             unsigned long long *count, cudaStream_t st);
 // Writable image tables of a mesh (DevSym's layout).
 struct ImageTables {
     double *v64, *c64;

@@ -341,36 +341,101 @@ __global__ void __launch_bounds__(256) k_image_tables(DevMeshView mv, ImageTable
 // mesh.  Entries go to list[0, cap) in any order (warp-aggregated atomics);
 // *count ends as the number of entries, which may exceed cap (the caller
 // then runs again with a larger list).
-__global__ void __launch_bounds__(256) k_near_list(DevMeshView mv, int2 *list, unsigned long long *count,
-                                                   unsigned long long cap) {
+//
+// Bounding spheres of the column blocks (32 consecutive elements, Morton
+// order) of every image, and each block's largest sqrt(area): warp per
+// (image, block).  Radii are inflated past float rounding, so the block test
+// of k_near_list never drops a pair the element test would keep.
+__global__ void __launch_bounds__(256) k_block_spheres(DevMeshView mv, float4 *sph, float *bsq) {
     const DevMesh m = to_dev(mv);
-    const int lane = threadIdx.x, n = m.n;
-    const int i = blockIdx.y * 8 + threadIdx.y;
-    const int j = blockIdx.x * 32 + lane;
-    if (i >= n) return;
-    unsigned imask = 0;
-    if (j < n) {
-        for (int kref = 0; kref < m.sym.nref; ++kref) {
-            if (kref == 0 && j == i) { imask |= 1u; continue; }
-            const DevMesh mk = image_mesh(m, kref);
-            const float d0 = (mk.chi[j] - m.chi[i]) + (mk.clo[j] - m.clo[i]);
-            const float d1 = (mk.chi[n + j] - m.chi[n + i]) + (mk.clo[n + j] - m.clo[n + i]);
-            const float d2 = (mk.chi[2 * n + j] - m.chi[2 * n + i]) + (mk.clo[2 * n + j] - m.clo[2 * n + i]);
-            const float rf = sqrtf(d0 * d0 + d1 * d1 + d2 * d2) * m.isqa32[j];
-            if (rf <= 1.3f * (1.0f + 1e-4f)) {
-                const double x[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
-                if (ratio0_exact(mk, j, x) < kTolf) imask |= 1u << kref;
-            }
+    const int lane = threadIdx.x, n = m.n, nb = (n + 31) / 32;
+    const int gw = blockIdx.x * 8 + threadIdx.y;
+    if (gw >= nb * m.sym.nref) return;
+    const int kref = gw / nb, b = gw - kref * nb;
+    const DevMesh mk = image_mesh(m, kref);
+    const int j = b * 32 + lane, jj = j < n ? j : b * 32;   // idle lanes repeat the block's first element
+    float c[3], lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        c[k] = mk.chi[k * n + jj] + mk.clo[k * n + jj];
+        lo[k] = c[k];
+        hi[k] = c[k];
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
         }
     }
-    const bool near = imask != 0;
-    const unsigned mask = __ballot_sync(0xffffffffu, near);
-    if (!mask) return;
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(mask));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    const unsigned long long idx = base + __popc(mask & ((1u << lane) - 1u));
-    if (near && list && idx < cap) list[idx] = make_int2(i, j | (int)(imask << kNearColBits));
+    const float cx = 0.5f * (lo[0] + hi[0]), cy = 0.5f * (lo[1] + hi[1]), cz = 0.5f * (lo[2] + hi[2]);
+    float r = sqrtf((c[0] - cx) * (c[0] - cx) + (c[1] - cy) * (c[1] - cy) + (c[2] - cz) * (c[2] - cz));
+    float sq = (float)m.sqa64[jj];
+    for (int o = 16; o > 0; o >>= 1) {
+        r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
+        sq = fmaxf(sq, __shfl_xor_sync(0xffffffffu, sq, o));
+    }
+    if (lane == 0) {
+        const float cmax = fmaxf(fabsf(cx), fmaxf(fabsf(cy), fabsf(cz)));
+        sph[gw] = make_float4(cx, cy, cz, r * (1.f + 1e-5f) + 1e-6f * cmax);
+        if (kref == 0) bsq[b] = sq * (1.f + 1e-5f);
+    }
+}
+
+// Near list: warp per row, lanes over 32 column blocks at a time.  A block
+// whose sphere (of any image) lies farther from the row's centre than 1.31
+// times its largest sqrt(area) holds no pair below the subdivision threshold
+// 1.3 (the element test below keeps pairs up to 1.3 (1 + 1e-4) for the exact
+// decision); the other blocks get the element test, image by image as the
+// reference loops them, with one entry per (row, column) carrying the mask of
+// near images (the self pair always).
+__global__ void __launch_bounds__(256) k_near_list(DevMeshView mv, const float4 *sph, const float *bsq, int2 *list,
+                                                   unsigned long long *count, unsigned long long cap) {
+    const DevMesh m = to_dev(mv);
+    const int lane = threadIdx.x, n = m.n, nb = (n + 31) / 32, nref = m.sym.nref;
+    const int i = blockIdx.x * 8 + threadIdx.y;
+    if (i >= n) return;
+    const float ci[3] = {m.chi[i] + m.clo[i], m.chi[n + i] + m.clo[n + i], m.chi[2 * n + i] + m.clo[2 * n + i]};
+    const float cn = fmaxf(fabsf(ci[0]), fmaxf(fabsf(ci[1]), fabsf(ci[2])));
+    for (int cb0 = 0; cb0 < nb; cb0 += 32) {
+        const int cb = cb0 + lane;
+        bool cand = false;
+        if (cb < nb) {
+            const float thr = 1.31f * bsq[cb];
+            for (int kref = 0; kref < nref; ++kref) {
+                const float4 sp = sph[kref * nb + cb];
+                const float d0 = ci[0] - sp.x, d1 = ci[1] - sp.y, d2 = ci[2] - sp.z;
+                const float slack = 1e-6f * (cn + fmaxf(fabsf(sp.x), fmaxf(fabsf(sp.y), fabsf(sp.z))));
+                if (sqrtf(d0 * d0 + d1 * d1 + d2 * d2) - sp.w <= thr + slack) cand = true;
+            }
+        }
+        unsigned cm = __ballot_sync(0xffffffffu, cand);
+        while (cm) {
+            const int bl = __ffs(cm) - 1;
+            cm &= cm - 1;
+            const int j = (cb0 + bl) * 32 + lane;
+            unsigned imask = 0;
+            if (j < n) {
+                for (int kref = 0; kref < nref; ++kref) {
+                    if (kref == 0 && j == i) { imask |= 1u; continue; }
+                    const DevMesh mk = image_mesh(m, kref);
+                    const float d0 = (mk.chi[j] - m.chi[i]) + (mk.clo[j] - m.clo[i]);
+                    const float d1 = (mk.chi[n + j] - m.chi[n + i]) + (mk.clo[n + j] - m.clo[n + i]);
+                    const float d2 = (mk.chi[2 * n + j] - m.chi[2 * n + i]) + (mk.clo[2 * n + j] - m.clo[2 * n + i]);
+                    const float rf = sqrtf(d0 * d0 + d1 * d1 + d2 * d2) * m.isqa32[j];
+                    if (rf <= 1.3f * (1.0f + 1e-4f)) {
+                        const double x[3] = {m.c64[i], m.c64[n + i], m.c64[2 * n + i]};
+                        if (ratio0_exact(mk, j, x) < kTolf) imask |= 1u << kref;
+                    }
+                }
+            }
+            const bool near = imask != 0;
+            const unsigned mask = __ballot_sync(0xffffffffu, near);
+            if (!mask) continue;
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            const unsigned long long idx = base + __popc(mask & ((1u << lane) - 1u));
+            if (near && list && idx < cap) list[idx] = make_int2(i, j | (int)(imask << kNearColBits));
+        }
+    }
 }
 
 // ------------------------------------------------------------ regular pairs
@@ -1421,11 +1486,20 @@ cudaError_t launch_image_tables(const DevMeshView &m, const ImageTables &out, cu
     return cudaGetLastError();
 }
 
-cudaError_t launch_near_list(const DevMeshView &m, int2 *list, unsigned long long cap, unsigned long long *count,
-                             cudaStream_t st) {
-    dim3 block(32, 8), grid((m.n + 31) / 32, (m.n + 7) / 8);
-    count_launches(1);
-    k_near_list<<<grid, block, 0, st>>>(m, list, count, cap);
+size_t near_list_scratch_bytes(int n, int nref) {
+    const size_t nb = (size_t)(n + 31) / 32;
+    return nb * (size_t)nref * sizeof(float4) + nb * sizeof(float);
+}
+
+cudaError_t launch_near_list(const DevMeshView &m, void *scratch, int2 *list, unsigned long long cap,
+                             unsigned long long *count, cudaStream_t st) {
+    const int nb = (m.n + 31) / 32;
+    float4 *sph = (float4 *)scratch;
+    float *bsq = (float *)(sph + (size_t)nb * m.sym.nref);
+    dim3 block(32, 8);
+    count_launches(2);
+    k_block_spheres<<<(nb * m.sym.nref + 7) / 8, block, 0, st>>>(m, sph, bsq);
+    k_near_list<<<(m.n + 7) / 8, block, 0, st>>>(m, sph, bsq, list, count, cap);
     return cudaGetLastError();
 }
 
