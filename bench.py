@@ -344,7 +344,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1000.0, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (fp16 Krylov copy of A, complex64 residual matrix, FP64 singular terms + refinement)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (fp16 Krylov copy of A, complex64 residual matrix, FP64-accurate refinement residuals)",
         "data": "synthetic", "config": cfg,
         "latency_ms": {"p50": float(np.percentile(lat, 50) * 1000), "p99": float(np.percentile(lat, 99) * 1000),
                        "mode": "one solve at a time (bem_solve_frequency), same frequencies"},

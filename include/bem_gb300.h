@@ -42,10 +42,11 @@ typedef enum {
 
 typedef enum {
     BEM_PREC_FP64 = 0,   /* FP64 assembly, complex128 matrix, FP64 GMRES        */
-    BEM_PREC_MIXED = 1   /* FP32 regular/near assembly, FP64 singular terms,     */
-                         /* complex64 matrix, compensated FP32 matvec inside a   */
-                         /* restarted GMRES with FP64 Arnoldi and an FP64 outer  */
-                         /* residual (iterative refinement)                      */
+    BEM_PREC_MIXED = 1   /* FP32 assembly (FP64 free terms and exact            */
+                         /* subdivision decisions), complex64 matrix with an    */
+                         /* fp16 Krylov copy, restarted GMRES in FP32 inside an */
+                         /* iterative refinement whose residuals reach FP64     */
+                         /* accuracy (compensated products)                     */
 } bem_precision;
 
 typedef struct bem_mesh_s *bem_mesh_t;

@@ -3,7 +3,7 @@
 Tolerances: the FP64 path assembles and projects in FP64 and solves with
 GMRES to a relative residual of 1e-12, so entries agree with the reference to
 1e-12 of the matrix scale and the solution with the reference's dense solve
-to 1e-9.  The mixed path (FP32 regular/near assembly, FP64 singular terms,
+to 1e-9.  The mixed path (FP32 assembly with exact subdivision decisions,
 refined solve) must meet the metric's bar: boundary pressure within 1e-4
 relative L2 of the FP64 solution.
 """
