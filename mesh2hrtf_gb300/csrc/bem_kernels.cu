@@ -13,6 +13,7 @@
 // entries of the per-mesh near lists from a second queue and integrate them
 // cooperatively (warp_subdivide / warp_singular).
 #include <algorithm>
+#include <memory>
 #include <type_traits>
 
 #include "bem_internal.h"
@@ -1552,26 +1553,49 @@ cudaError_t launch_assemble(const AsmBatch &t, int prec, unsigned *ctr, cudaStre
     // persistent grids: kFarPerSm resident blocks of k_far per SM (launch bounds), 4 of k_near
     const int gfar = std::max(1, std::min(far_items, kFarPerSm * sm_count()));
     const int gnear = std::max(1, std::min((near_items + 7) / 8, 4 * sm_count()));
-    count_launches(near_items ? 2 : 1);
-    const bool one = t.B == 1;
-    if (prec == 0) {
-        if (t.img) {
-            if (one) k_far<double, true, true><<<gfar, block, 0, st>>>(t, ctr);
-            else k_far<double, false, true><<<gfar, block, 0, st>>>(t, ctr);
+    // Systems that fill the GPU on their own take one single-system launch
+    // each: the single-system kernel keeps the table in constant operands
+    // (fewer registers, no spills), which beat the shared work queue.
+    bool split = t.B > 1;
+    for (int b = 0; b < t.B && split; ++b)
+        if (t.far_off[b + 1] - t.far_off[b] < kFarPerSm * sm_count()) split = false;
+    std::unique_ptr<AsmBatch> one_sys;
+    if (split) one_sys.reset(new AsmBatch());
+    count_launches((split ? t.B : 1) + (near_items ? 1 : 0));
+    auto far = [&](const AsmBatch &a, int grid) {
+        const bool one = a.B == 1;
+        if (prec == 0) {
+            if (a.img) {
+                if (one) k_far<double, true, true><<<grid, block, 0, st>>>(a, ctr);
+                else k_far<double, false, true><<<grid, block, 0, st>>>(a, ctr);
+            } else {
+                if (one) k_far<double, true, false><<<grid, block, 0, st>>>(a, ctr);
+                else k_far<double, false, false><<<grid, block, 0, st>>>(a, ctr);
+            }
         } else {
-            if (one) k_far<double, true, false><<<gfar, block, 0, st>>>(t, ctr);
-            else k_far<double, false, false><<<gfar, block, 0, st>>>(t, ctr);
+            if (a.img) {
+                if (one) k_far<float, true, true><<<grid, block, 0, st>>>(a, ctr);
+                else k_far<float, false, true><<<grid, block, 0, st>>>(a, ctr);
+            } else {
+                if (one) k_far<float, true, false><<<grid, block, 0, st>>>(a, ctr);
+                else k_far<float, false, false><<<grid, block, 0, st>>>(a, ctr);
+            }
         }
-        if (near_items) k_near<double><<<gnear, block, 0, st>>>(t, ctr + 2);
+    };
+    if (split) {
+        // launches run in order on st; each ends by resetting the queue counter
+        for (int b = 0; b < t.B; ++b) {
+            one_sys->B = 1;
+            one_sys->sys[0] = t.sys[b];
+            asm_batch_finish(*one_sys);
+            far(*one_sys, std::max(1, std::min(one_sys->far_off[1], kFarPerSm * sm_count())));
+        }
     } else {
-        if (t.img) {
-            if (one) k_far<float, true, true><<<gfar, block, 0, st>>>(t, ctr);
-            else k_far<float, false, true><<<gfar, block, 0, st>>>(t, ctr);
-        } else {
-            if (one) k_far<float, true, false><<<gfar, block, 0, st>>>(t, ctr);
-            else k_far<float, false, false><<<gfar, block, 0, st>>>(t, ctr);
-        }
-        if (near_items) k_near<float><<<gnear, block, 0, st>>>(t, ctr + 2);
+        far(t, gfar);
+    }
+    if (near_items) {
+        if (prec == 0) k_near<double><<<gnear, block, 0, st>>>(t, ctr + 2);
+        else k_near<float><<<gnear, block, 0, st>>>(t, ctr + 2);
     }
     return cudaGetLastError();
 }
@@ -1594,16 +1618,17 @@ cudaError_t launch_fields(const ProjBatch &t, cudaStream_t st) {
 cudaError_t launch_project(const ProjBatch &t, int prec, cudaStream_t st) {
     if (t.B <= 0 || t.pt_off[t.B] == 0) return cudaSuccess;
     dim3 block(32, 8);
-    count_launches(1);
     bool sliced = prec != 0;
     for (int b = 0; b < t.B; ++b)
         if (t.sys[b].npts > 0 && t.sys[b].nslice == 0) sliced = false;   // scratch too short
     if (prec == 0) {
+        count_launches(1);
         k_project<double><<<t.pt_off[t.B], block, 0, st>>>(t);
     } else if (!sliced) {
+        count_launches(1);
         k_project<float><<<t.pt_off[t.B], block, 0, st>>>(t);
     } else {
-        count_launches(1);
+        count_launches(2);
         k_project_pts<<<t.lp_off[t.B], block, 0, st>>>(t);
         k_project_sum<<<t.ps_off[t.B], 256, 0, st>>>(t);
     }
