@@ -170,31 +170,44 @@ __device__ void plan_build(KTable *tb, int which) {
     }
     gm[t] = mask;
     __syncthreads();
-    if (t == 0) {   // serial scans over at most kMaxSys slots
-        KPlan &p = tb->plan[which];
-        int n = 0, off = 0;
-        for (int j = 0; j < kMaxSys; ++j)
-            if (act[j]) {
-                p.sys[n] = j;
-                p.off[n] = off;
-                off += cnt[j];
-                ++n;
-            }
-        p.off[n] = off;
-        p.n = n;
-        KPlan &gp = tb->gplan[which];
-        n = 0;
-        off = 0;
-        for (int j = 0; j < tb->n_groups; ++j)
-            if (gm[j]) {
-                gp.sys[n] = j;
-                gp.off[n] = off;
-                tb->gmask[which][n] = gm[j];
-                off += ceil_div(tb->sys[tb->grp[j].first].n, which == 1 ? kGrpRowsExact : kGrpRowsInner);
-                ++n;
-            }
-        gp.off[n] = off;
-        gp.n = n;
+    // exclusive prefix sums over the kMaxSys slots (warp scans, then the
+    // warps' totals in order): the plan entries in slot order
+    __shared__ int wsum[kMaxSys / 32][4];
+    const int lane = t & 31, wp = t >> 5;
+    const int ga = gm[t] ? 1 : 0;
+    const int gc = ga ? ceil_div(tb->sys[tb->grp[t].first].n, which == 1 ? kGrpRowsExact : kGrpRowsInner) : 0;
+    int v[4] = {act[t], cnt[t], ga, gc};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, v[q], o);
+            if (lane >= o) v[q] += y;
+        }
+        if (lane == 31) wsum[wp][q] = v[q];
+    }
+    __syncthreads();
+    int base[4] = {0, 0, 0, 0};
+    for (int w = 0; w < wp; ++w)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) base[q] += wsum[w][q];
+    const int pos = base[0] + v[0] - act[t], off = base[1] + v[1] - cnt[t];
+    const int gpos = base[2] + v[2] - ga, goff = base[3] + v[3] - gc;
+    KPlan &p = tb->plan[which];
+    KPlan &gp = tb->gplan[which];
+    if (act[t]) {
+        p.sys[pos] = t;
+        p.off[pos] = off;
+    }
+    if (ga) {
+        gp.sys[gpos] = t;
+        gp.off[gpos] = goff;
+        tb->gmask[which][gpos] = gm[t];
+    }
+    if (t == kMaxSys - 1) {
+        p.n = base[0] + v[0];
+        p.off[p.n] = base[1] + v[1];
+        gp.n = base[2] + v[2];
+        gp.off[gp.n] = base[3] + v[3];
     }
     __syncthreads();
 }
@@ -1186,6 +1199,7 @@ __device__ void block_norm(double2 wv, bool ok, double *__restrict__ nrmp, int b
 // sum of the squared-norm partials, in block order
 __device__ __forceinline__ double norm_total(const double *__restrict__ nrmp, int nvb) {
     double t = 0.0;
+#pragma unroll 8
     for (int c = 0; c < nvb; ++c) t += nrmp[c];
     return t;
 }
@@ -1532,16 +1546,17 @@ __device__ void givens_step(const KSys &S) {
     KState *st = S.st;
     const int k = st->k, m = st->m;
     double2 *H = S.H, *cs = S.cs, *sn = S.sn, *g = S.g, *hsum = S.hsum;
-    for (int l = 0; l <= k; ++l) {
-        H[(size_t)l * m + k] = hsum[l];
-        hsum[l] = make_double2(0.0, 0.0);
-    }
     const double hn = sqrt(norm_total(S.nrmp, S.nvb));
-    // previous rotations: [a; b] <- [[conj(c), conj(s)], [-s, c]] [a; b];
-    // the running entry stays in registers
-    double2 a = H[k];
+    // column k of H from hsum (cleared for the next step) with the previous
+    // rotations applied on the way: [a; b] <- [[conj(c), conj(s)], [-s, c]]
+    // [a; b]; the running entry stays in registers, the loads do not depend
+    // on it
+    double2 a = hsum[0];
+    hsum[0] = make_double2(0.0, 0.0);
+#pragma unroll 4
     for (int l = 0; l < k; ++l) {
-        const double2 bb = H[(size_t)(l + 1) * m + k];
+        const double2 bb = hsum[l + 1];
+        hsum[l + 1] = make_double2(0.0, 0.0);
         const double2 c = cs[l], s = sn[l];
         H[(size_t)l * m + k] = make_double2(c.x * a.x + c.y * a.y + s.x * bb.x + s.y * bb.y,
                                             c.x * a.y - c.y * a.x + s.x * bb.y - s.y * bb.x);
