@@ -593,8 +593,11 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
                     si = fmaf(a.x, xv.y, si); si = fmaf(a.y, xv.x, si);
                 }
             } else {
-                // x chunk permuted: entry 2c at xa[c], entry 2c + 1 at xb2[c]
+                // x chunk permuted: entry 2c at xa[c], entry 2c + 1 at xb2[c].
+                // Even and odd entries accumulate into separate float-float
+                // pairs (half the dependency chain per pair), merged below.
                 const float4 *xa = reinterpret_cast<const float4 *>(xb), *xb2 = xa + kMvChunk / 2;
+                float sr2 = 0.f, si2 = 0.f, er2 = 0.f, ei2 = 0.f;
 #pragma unroll 2
                 for (int c = lane; c < len2; c += 32) {
                     const float4 a = A4[c], x0 = xa[c], x1 = xb2[c];
@@ -602,10 +605,15 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
                     acc_exact(si, ei, a.x, x0.y); acc_exact(si, ei, a.y, x0.x);
                     er = fmaf(a.x, x0.z, er); er = fmaf(-a.y, x0.w, er);
                     ei = fmaf(a.x, x0.w, ei); ei = fmaf(a.y, x0.z, ei);
-                    acc_exact(sr, er, a.z, x1.x); acc_exact(sr, er, -a.w, x1.y);
-                    acc_exact(si, ei, a.z, x1.y); acc_exact(si, ei, a.w, x1.x);
-                    er = fmaf(a.z, x1.z, er); er = fmaf(-a.w, x1.w, er);
-                    ei = fmaf(a.z, x1.w, ei); ei = fmaf(a.w, x1.z, ei);
+                    acc_exact(sr2, er2, a.z, x1.x); acc_exact(sr2, er2, -a.w, x1.y);
+                    acc_exact(si2, ei2, a.z, x1.y); acc_exact(si2, ei2, a.w, x1.x);
+                    er2 = fmaf(a.z, x1.z, er2); er2 = fmaf(-a.w, x1.w, er2);
+                    ei2 = fmaf(a.z, x1.w, ei2); ei2 = fmaf(a.w, x1.z, ei2);
+                }
+                {
+                    float t, u;
+                    two_sum(sr, sr2, t, u); sr = t; er += er2 + u;
+                    two_sum(si, si2, t, u); si = t; ei += ei2 + u;
                 }
                 if ((len & 1) && lane == 0) {
                     const float2 a = reinterpret_cast<const float2 *>(A4)[len - 1];
