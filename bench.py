@@ -5,7 +5,7 @@ seeded Gaussian bumps, 20480 triangles graded toward bump 1), reciprocal point
 source 1 mm off bump 1, evaluation grid of 1730 points on a 1.2 m sphere,
 frequencies 100 Hz .. 20 kHz in 100 Hz steps (200 solves).  One solve =
 assemble A(k) and b, GMRES to a relative residual of 1e-9, project onto the
-1730 points.  A step is one batch of --batch frequencies (default 8) taken
+1730 points.  A step is one batch of --batch frequencies (default 16) taken
 from a seeded permutation of the 200, so K steps sample the whole band.
 
 value     mixed-precision solves/s with the mesh resident on the device; a
@@ -165,7 +165,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     args = ap.parse_args()
     if args.warmup < 3:
