@@ -222,8 +222,11 @@ __device__ __forceinline__ void far_col4(const DevMesh &m, int j, FarCol4 &e) {
     e.J4 = J * (float)(1.0 / kPI4);
 }
 
-__device__ __forceinline__ float2 far_entry_tri2(const FarCol4 &e, const float D[3], float D2, const float nx[3],
-                                                 const FusedCol &c) {
+// BC: the column's boundary condition (0 velocity, 1 pressure, 2 velocity
+// with admittance), fixed per instantiation so the point loop has no branch
+template <int BC>
+__device__ __forceinline__ float2 far_entry_tri2_bc(const FarCol4 &e, const float D[3], float D2, const float nx[3],
+                                                    const FusedCol &c) {
     const float dny = D[0] * e.n[0] + D[1] * e.n[1] + D[2] * e.n[2];
     const float dnx0 = D[0] * nx[0] + D[1] * nx[1] + D[2] * nx[2];
     const float anx = e.a[0] * nx[0] + e.a[1] * nx[1] + e.a[2] * nx[2];
@@ -243,7 +246,7 @@ __device__ __forceinline__ float2 far_entry_tri2(const FarCol4 &e, const float D
         float sn, cs;
         phase_sincos(c.wr * (r2 * u), &sn, &cs);
         float fr, fi;
-        if (c.bc == 1) {
+        if (BC == 1) {
             // -tau - i b z1 re2, z1 = -1/r + i wr, re2 = -d.n_x / r
             const float du = dnx * u;
             fr = fmaf(-bwr, du, -c.tau);
@@ -254,7 +257,7 @@ __device__ __forceinline__ float2 far_entry_tri2(const FarCol4 &e, const float D
             const float rq = -(dny * dnx) * u2;
             fr = fmaf(bwr * u, fmaf(3.f, rq, nn), ct * u2);
             fi = fmaf(c.b, fmaf(fmaf(3.f, u2, -c.k2), rq, nn * u2), cw * u);
-            if (c.bc == 2) {
+            if (BC == 2) {
                 // + Y (1 + i b tau z1 re2)
                 const float du = dnx * u, bt = c.b * c.tau;
                 const float pr = fmaf(bt * c.wr, du, 1.f), pi = bt * u * du;
@@ -267,6 +270,13 @@ __device__ __forceinline__ float2 far_entry_tri2(const FarCol4 &e, const float D
         ai = fmaf(amp, fmaf(cs, fi, sn * fr), ai);
     }
     return make_float2(ar, ai);
+}
+
+__device__ __forceinline__ float2 far_entry_tri2(const FarCol4 &e, const float D[3], float D2, const float nx[3],
+                                                 const FusedCol &c) {
+    if (c.bc == 0) return far_entry_tri2_bc<0>(e, D, D2, nx, c);
+    if (c.bc == 1) return far_entry_tri2_bc<1>(e, D, D2, nx, c);
+    return far_entry_tri2_bc<2>(e, D, D2, nx, c);
 }
 
 template <typename T>
