@@ -282,7 +282,9 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
                         decided = true;
                     }
                 }
-                if (!decided || split) {
+                // the FP64 centre: for the exact test, and for the children of
+                // a split quadrilateral (the centre is one of their vertices)
+                if (!decided || (split && nv == 4)) {
                     for (int v = 0; v < nv; ++v) {
                         scent = __dadd_rn(scent, (double)vsf[v]);
                         tcent = __dadd_rn(tcent, (double)vtf[v]);
@@ -336,28 +338,30 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
             if (store) {
                 const int r = __popc(stmask & lt);
                 if (nsbe + r >= kMSBE) err = kDevSubLimit;
-                double ox, oy, fac;
-                double vs[4], vt[4];
-                for (int v = 0; v < 4; ++v) { vs[v] = (double)vsf[v]; vt[v] = (double)vtf[v]; }
+                float ox, oy, fac;
                 if (nv == 4) {
-                    ox = (vs[0] + vs[1] + vs[2] + vs[3]) / 4.0;
-                    oy = (vt[0] + vt[1] + vt[2] + vt[3]) / 4.0;
-                    fac = faclin;
+                    const double vs[4] = {vsf[0], vsf[1], vsf[2], vsf[3]}, vt[4] = {vtf[0], vtf[1], vtf[2], vtf[3]};
+                    ox = (float)((vs[0] + vs[1] + vs[2] + vs[3]) / 4.0);
+                    oy = (float)((vt[0] + vt[1] + vt[2] + vt[3]) / 4.0);
+                    fac = faclinf;
                 } else {
-                    const double xi = (vs[0] + vs[1] + vs[2]) / 3.0;
-                    const double et = (vt[0] + vt[1] + vt[2]) / 3.0;
+                    // the vertex whose offset to the centroid is equal in s and
+                    // t (NC_GenerateSubelements): with dyadic vertices the sums
+                    // and 3 v are exact in float, so the reference's test
+                    // |(c_s - s_v) - (c_t - t_v)| < 1e-8 is exact equality here
+                    const float ssum = vsf[0] + vsf[1] + vsf[2], tsum = vtf[0] + vtf[1] + vtf[2];
                     int jr = 0;
-                    double dxi = 0.0;
+                    float dxi = 0.f;
                     for (int v = 0; v < 3; ++v) {
-                        dxi = xi - vs[v];
-                        const double det = et - vt[v];
-                        if (fabs(dxi - det) < 1.0e-8) { jr = v; break; }
+                        dxi = ssum - 3.f * vsf[v];
+                        const float det = tsum - 3.f * vtf[v];
+                        if (dxi == det) { jr = v; break; }
                     }
-                    ox = vs[jr]; oy = vt[jr];
-                    fac = dxi >= 0.0 ? faclin : -faclin;
+                    ox = vsf[jr]; oy = vtf[jr];
+                    fac = dxi >= 0.f ? faclinf : -faclinf;
                 }
                 const int ord = ordf ? ordf : gauss_order(ratdis);
-                ws.sxi[r] = (float)ox; ws.seta[r] = (float)oy; ws.sfac[r] = (float)fac;
+                ws.sxi[r] = ox; ws.seta[r] = oy; ws.sfac[r] = fac;
                 ws.sord[r] = ord;
             }
             __syncwarp();
