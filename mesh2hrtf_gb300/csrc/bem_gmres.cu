@@ -594,24 +594,31 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
                 }
             } else {
                 // x chunk permuted: entry 2c at xa[c], entry 2c + 1 at xb2[c].
-                // Even and odd entries accumulate into separate float-float
-                // pairs (half the dependency chain per pair), merged below.
+                // Even and odd entries, and the two terms of each component,
+                // accumulate into separate float-float pairs (one exact
+                // product per pair and iteration), merged below.
                 const float4 *xa = reinterpret_cast<const float4 *>(xb), *xb2 = xa + kMvChunk / 2;
-                float sr2 = 0.f, si2 = 0.f, er2 = 0.f, ei2 = 0.f;
+                float sr2 = 0.f, si2 = 0.f, er2 = 0.f, ei2 = 0.f;   // odd entries
+                float sr3 = 0.f, si3 = 0.f, er3 = 0.f, ei3 = 0.f;   // second terms, even
+                float sr4 = 0.f, si4 = 0.f, er4 = 0.f, ei4 = 0.f;   // second terms, odd
 #pragma unroll 2
                 for (int c = lane; c < len2; c += 32) {
                     const float4 a = A4[c], x0 = xa[c], x1 = xb2[c];
-                    acc_exact(sr, er, a.x, x0.x); acc_exact(sr, er, -a.y, x0.y);
-                    acc_exact(si, ei, a.x, x0.y); acc_exact(si, ei, a.y, x0.x);
-                    er = fmaf(a.x, x0.z, er); er = fmaf(-a.y, x0.w, er);
-                    ei = fmaf(a.x, x0.w, ei); ei = fmaf(a.y, x0.z, ei);
-                    acc_exact(sr2, er2, a.z, x1.x); acc_exact(sr2, er2, -a.w, x1.y);
-                    acc_exact(si2, ei2, a.z, x1.y); acc_exact(si2, ei2, a.w, x1.x);
-                    er2 = fmaf(a.z, x1.z, er2); er2 = fmaf(-a.w, x1.w, er2);
-                    ei2 = fmaf(a.z, x1.w, ei2); ei2 = fmaf(a.w, x1.z, ei2);
+                    acc_exact(sr, er, a.x, x0.x); acc_exact(sr3, er3, -a.y, x0.y);
+                    acc_exact(si, ei, a.x, x0.y); acc_exact(si3, ei3, a.y, x0.x);
+                    er = fmaf(a.x, x0.z, er); er3 = fmaf(-a.y, x0.w, er3);
+                    ei = fmaf(a.x, x0.w, ei); ei3 = fmaf(a.y, x0.z, ei3);
+                    acc_exact(sr2, er2, a.z, x1.x); acc_exact(sr4, er4, -a.w, x1.y);
+                    acc_exact(si2, ei2, a.z, x1.y); acc_exact(si4, ei4, a.w, x1.x);
+                    er2 = fmaf(a.z, x1.z, er2); er4 = fmaf(-a.w, x1.w, er4);
+                    ei2 = fmaf(a.z, x1.w, ei2); ei4 = fmaf(a.w, x1.z, ei4);
                 }
                 {
                     float t, u;
+                    two_sum(sr, sr3, t, u); sr = t; er += er3 + u;
+                    two_sum(si, si3, t, u); si = t; ei += ei3 + u;
+                    two_sum(sr2, sr4, t, u); sr2 = t; er2 += er4 + u;
+                    two_sum(si2, si4, t, u); si2 = t; ei2 += ei4 + u;
                     two_sum(sr, sr2, t, u); sr = t; er += er2 + u;
                     two_sum(si, si2, t, u); si = t; ei += ei2 + u;
                 }
