@@ -228,16 +228,18 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
     const unsigned lt = (1u << lane) - 1u;
     const int nv = e.nv;
     if (lane < nv) {
-        ws.lv[0][0][lane][0] = (float)(nv == 3 ? c_csi6[lane] : c_csi8[lane]);
-        ws.lv[0][0][lane][1] = (float)(nv == 3 ? c_eta6[lane] : c_eta8[lane]);
+        ws.lv[0][0][lane][0] = nv == 3 ? c_csi6f[lane] : c_csi8f[lane];
+        ws.lv[0][0][lane][1] = nv == 3 ? c_eta6f[lane] : c_eta8f[lane];
     }
     __syncwarp();
     int cur = 0, nsel = 1, nsbe = 0, err = kDevOk;
+    // NumCalc's sqrt(area faclin^2) equals sqrt(area) faclin exactly (faclin
+    // is a power of two): one FP64 square root per pair, not per level
+    const double sqa0 = __dsqrt_rn(area);
     double faclin = 2.0;
     for (int level = 0; level <= kMaxLevel; ++level) {
         faclin *= 0.5;
         const float faclinf = (float)faclin;   // a power of two
-        const double sqa = __dsqrt_rn(__dmul_rn(__dmul_rn(area, faclin), faclin));
         int ndie = 0;
         for (int base = 0; base < nsel; base += 32) {
             const int idi = base + lane;
@@ -295,7 +297,7 @@ __device__ int warp_subdivide(const Elem64 &e, double area, const double x[3], W
                 if (!decided) {
                     double cp[3];
                     global_point_exact(e, scent, tcent, cp);
-                    ratdis = __ddiv_rn(dist_exact(cp, x), sqa);
+                    ratdis = __ddiv_rn(dist_exact(cp, x), __dmul_rn(sqa0, faclin));
                     split = ratdis < kTolf;
                 }
             }
