@@ -1268,10 +1268,10 @@ __device__ void block_norm_f(float2 wv, bool ok, double *__restrict__ nrmp, int 
     __syncthreads();
 }
 
-// (M^{-1} v)[row] for the thread's own row: vs holds the block's 256 values
-// of v; the thread's 128-row preconditioner block is rows (tid & 128) .. +127.
-// Inverse blocks are stored transposed ([col][row]), so the loads coalesce.
-template <bool C128>
+// (M^{-1} v)[row] for the thread's own row of a complex128 system: vs holds
+// the block's 256 values of v; the thread's 128-row preconditioner block is
+// rows (tid & 128) .. +127.  Inverse blocks are stored transposed
+// ([col][row]), so the loads coalesce.  (complex64 systems: apply_minv_f.)
 __device__ __forceinline__ double2 apply_minv(const void *Minv, int n, int blk, const double2 *vs) {
     const int tid = threadIdx.x;
     const int pb = blk * 2 + (tid >> 7), rr = tid & 127, r0 = pb * kBlock;
@@ -1279,29 +1279,12 @@ __device__ __forceinline__ double2 apply_minv(const void *Minv, int n, int blk, 
     if (nb <= 0 || rr >= nb) return make_double2(0.0, 0.0);
     const double2 *x = vs + (tid & 128);
     double sr = 0.0, si = 0.0;
-    if (C128) {
-        const double2 *M = (const double2 *)Minv + (size_t)pb * kBlock * kBlock;
-        for (int c = 0; c < nb; ++c) {
-            const double2 m = M[(size_t)c * kBlock + rr];
-            const double2 xv = x[c];
-            sr = fma(m.x, xv.x, sr); sr = fma(-m.y, xv.y, sr);
-            si = fma(m.x, xv.y, si); si = fma(m.y, xv.x, si);
-        }
-    } else {
-        // FP32 products, FP64 accumulation in chunks of 16
-        const float2 *M = (const float2 *)Minv + (size_t)pb * kBlock * kBlock;
-        for (int c0 = 0; c0 < nb; c0 += 16) {
-            float ar = 0.f, ai = 0.f;
-            const int ce = min(c0 + 16, nb);
-            for (int c = c0; c < ce; ++c) {
-                const float2 m = M[(size_t)c * kBlock + rr];
-                const float xr = (float)x[c].x, xi = (float)x[c].y;
-                ar += m.x * xr - m.y * xi;
-                ai += m.x * xi + m.y * xr;
-            }
-            sr += (double)ar;
-            si += (double)ai;
-        }
+    const double2 *M = (const double2 *)Minv + (size_t)pb * kBlock * kBlock;
+    for (int c = 0; c < nb; ++c) {
+        const double2 m = M[(size_t)c * kBlock + rr];
+        const double2 xv = x[c];
+        sr = fma(m.x, xv.x, sr); sr = fma(-m.y, xv.y, sr);
+        si = fma(m.x, xv.y, si); si = fma(m.y, xv.x, si);
     }
     return make_double2(sr, si);
 }
@@ -1525,7 +1508,7 @@ __global__ void __launch_bounds__(kThreads) k_scale(const KTable *tb) {
             if (S.pc) {
                 vs[threadIdx.x] = v;
                 __syncthreads();
-                u = apply_minv<true>(S.Minv, n, blk, vs);
+                u = apply_minv(S.Minv, n, blk, vs);
                 if (row < n) (S.pcw ? (double2 *)S.pcy : S.z)[row] = u;
             }
         } else {
@@ -1677,7 +1660,7 @@ __global__ void __launch_bounds__(kThreads) k_xupdate(const KTable *tb) {
         const KState *st = S.st;
         if (st->phase != kPhaseUpdate || st->k == 0) continue;
         const int kk = st->k, n = S.n, blk = bi.y, row = blk * kThreads + threadIdx.x;
-        if (!C128) {
+        if constexpr (!C128) {
             // float basis: d = M^{-1} V y in FP32, added to x in FP64
             if (threadIdx.x < kk) ysf[threadIdx.x] = make_float2((float)S.y[threadIdx.x].x, (float)S.y[threadIdx.x].y);
             __syncthreads();
@@ -1701,30 +1684,29 @@ __global__ void __launch_bounds__(kThreads) k_xupdate(const KTable *tb) {
                 else reinterpret_cast<float2 *>(S.pcy)[row] = tf;   // k_pcfin adds the corrected d
             }
             __syncthreads();
-            continue;
-        }
-        if (threadIdx.x < kk) ys[threadIdx.x] = S.y[threadIdx.x];
-        __syncthreads();
-        double2 t = make_double2(0.0, 0.0);
-        if (row < n) {
-#pragma unroll 8
-            for (int l = 0; l < kk; ++l) {
-                const double2 v = S.V[(size_t)l * S.ldv + row], c = ys[l];
-                t.x += c.x * v.x - c.y * v.y;
-                t.y += c.x * v.y + c.y * v.x;
-            }
-        }
-        if (S.pc) {
-            vs[threadIdx.x] = t;
+        } else {
+            if (threadIdx.x < kk) ys[threadIdx.x] = S.y[threadIdx.x];
             __syncthreads();
-            t = apply_minv<C128>(S.Minv, n, blk, vs);
+            double2 t = make_double2(0.0, 0.0);
+            if (row < n) {
+#pragma unroll 8
+                for (int l = 0; l < kk; ++l) {
+                    const double2 v = S.V[(size_t)l * S.ldv + row], c = ys[l];
+                    t.x += c.x * v.x - c.y * v.y;
+                    t.y += c.x * v.y + c.y * v.x;
+                }
+            }
+            if (S.pc) {
+                vs[threadIdx.x] = t;
+                __syncthreads();
+                t = apply_minv(S.Minv, n, blk, vs);
+            }
+            if (row < n) {
+                if (!S.pcw) xupdate_finish<true>(S, st, row, t);
+                else ((double2 *)S.pcy)[row] = t;   // k_pcfin adds the corrected d
+            }
+            __syncthreads();
         }
-        if (row < n) {
-            if (!S.pcw) xupdate_finish<C128>(S, st, row, t);
-            else if (C128) ((double2 *)S.pcy)[row] = t;   // k_pcfin adds the corrected d
-            else ((float2 *)S.pcy)[row] = make_float2((float)t.x, (float)t.y);
-        }
-        __syncthreads();
     }
 }
 
@@ -1855,7 +1837,7 @@ __global__ void __launch_bounds__(kThreads) k_pcfin(const KTable *tb, int mode) 
             const double2 *Y = (const double2 *)S.pcy, *Z = (const double2 *)S.pcz;
             vs[threadIdx.x] = ok ? Z[row] : make_double2(0.0, 0.0);
             __syncthreads();
-            const double2 q = apply_minv<true>(S.Minv, n, blk, vs);
+            const double2 q = apply_minv(S.Minv, n, blk, vs);
             if (ok) {
                 const double2 y = Y[row];
                 const double2 u = make_double2(2.0 * y.x - q.x, 2.0 * y.y - q.y);
