@@ -57,13 +57,9 @@ MV_TRAFFIC = 1.6863e9
 
 
 def workload():
-    from mesh2hrtf_gb300 import meshes
+    from mesh2hrtf_gb300 import workloads
 
-    v, f, info = meshes.head_like(32, seed=SEED)
-    pts = meshes.equal_angle_grid(1.2, 5.0, 24)
-    freqs = np.arange(1, 201) * 100.0
-    order = np.random.default_rng(SEED).permutation(len(freqs))
-    return v, f, info["source"], pts, freqs[order]
+    return workloads.head_workload(SEED)
 
 
 def freq_desc(capi, n, fr, src):

@@ -229,14 +229,23 @@ bem_status bem_project(bem_solver_t solver, int32_t n_pts, const double *pts,
  *
  * Limits and rules:
  *  - at most BEM_STATIC_MAX_ELEMENTS boundary elements (larger solvers get
- *    BEM_ERR_INVALID); the scratch array (about 4.1 MB) is held on every
- *    device that loads the library until the process exits;
- *  - the first call on a device looks up the array's device address; make
- *    that first call before any stream capture;
+ *    BEM_ERR_INVALID); the scratch array (about 12.4 MB: 4.1 MB of element
+ *    data plus 8 MB of partial sums) is held on every device that loads the
+ *    library until the process exits;
+ *  - the first call on a device looks up the array's device address;
+ *  - the call is synchronous: it runs on `stream` (a cudaStream_t, NULL for
+ *    the legacy default stream), reads the status word back and returns
+ *    after the stream has finished, so it cannot be recorded into a CUDA
+ *    graph;
+ *  - the calling thread's current device, the stream's device and the
+ *    solver's device must be the same (else BEM_ERR_INVALID);
  *  - all calls share the one array, so calls that overlap on the GPU (other
- *    streams, other threads) race: serialize them;
- *  - the call runs on `stream` (a cudaStream_t, NULL for the legacy default
- *    stream) and returns after it has finished;
+ *    streams, other threads) race: serialize them.  The call reads the
+ *    solver's solution and mesh tables and writes none of its buffers, but
+ *    it must not overlap a bem_assemble or bem_solve of the same solver;
+ *  - with many points and elements the partial sums take wider element
+ *    slices than bem_project's (a different FP32 summation order in mixed
+ *    precision, same quadrature);
  *  - pts_dev [n_pts][3] FP64, pot_dev [n_pts] complex, grad_dev [n_pts][3]
  *    complex or NULL, all device memory. */
 #define BEM_STATIC_MAX_ELEMENTS 32768

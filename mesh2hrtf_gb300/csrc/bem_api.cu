@@ -1398,8 +1398,9 @@ namespace bem {
 
 // Inputs of the projection kernels held by a solved solver (for
 // bem_project_static in bem_static.cu).
-bool solver_projection_inputs(bem_solver_t s, int max_elem, ProjSys *out, int *prec) {
+bool solver_projection_inputs(bem_solver_t s, int max_elem, ProjSys *out, int *prec, int *device) {
     if (!s) { g_err = "null solver"; return false; }
+    *device = s->mesh->device;
     if (s->n > max_elem) {
         char buf[160];
         snprintf(buf, sizeof(buf), "bem_project_static: %d boundary elements, limit BEM_STATIC_MAX_ELEMENTS = %d",

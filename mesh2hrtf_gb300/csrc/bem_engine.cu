@@ -2,11 +2,24 @@
 // work-item lists, graph capture and replay.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
 #include <cstring>
 
 #include "bem_engine.h"
 
 namespace bem {
+
+namespace {
+// BEM_GB300_TEST_WAIT_CYCLES: a bound (clock cycles) for the products'
+// mbarrier waits in place of the default of about 2 s.  Only for tests that
+// make a wait run out; read whenever a batch is set up.
+long long test_wait_cycles() {
+    const char *v = std::getenv("BEM_GB300_TEST_WAIT_CYCLES");
+    if (!v || !*v) return 0;
+    const long long c = std::atoll(v);
+    return c > 0 ? c : 0;
+}
+}  // namespace
 
 Engine::~Engine() {
     if (st_) cudaStreamSynchronize(st_);
@@ -67,6 +80,7 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
     h_tab_->prec = prec_;
     h_tab_->vb_total = vb_total;
     h_tab_->vb_items = d_items_;
+    h_tab_->wait_cycles = test_wait_cycles();
     for (int b = 0; b < B; ++b) {
         h_tab_->sys[b] = sys[b];
         h_tab_->sys[b].st = d_st_ + b;

@@ -342,12 +342,38 @@ __device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// bounded wait for the completion of the phase with the given parity
-__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, int *err) {
+// non-blocking test of the same
+__device__ __forceinline__ bool mbar_test(uint32_t a, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for the completion of the phase with the given parity; lim
+// is the bound in clock cycles.  try_wait may suspend the thread for a
+// system-dependent time before it reports an incomplete phase, so a bound
+// shorter than the default (set by a test that makes a wait run out) polls
+// with the non-blocking test instead.
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, int *err, long long lim = kWaitCycles) {
+    if (lim < kWaitCycles) {
+        const long long t0 = clock64();
+        while (!mbar_test(a, parity)) {
+            if (clock64() - t0 > lim) {
+                atomicExch(err, 1);
+                return false;
+            }
+        }
+        return true;
+    }
     if (mbar_try(a, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try(a, parity)) {
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > lim) {
             atomicExch(err, 1);
             return false;
         }
@@ -385,6 +411,8 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
     __shared__ PlanSmem pl;
     plan_load(tb->plan[kind], pl);   // includes a block barrier
     int *err = &tb->err;
+    // bound of the waits (the drains of in-flight copies keep the full bound)
+    const long long lim = tb->wait_cycles > 0 ? tb->wait_cycles : kWaitCycles;
     if (warp == kTmaConsumers) {
         // ---------------- producer warp: lane 0 takes the items and keeps the
         // barriers, lane r issues the bulk copy of row r of a stage (one
@@ -396,6 +424,8 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
         uint32_t eph = 1, xeph[2] = {1, 1};   // a fresh barrier's previous phase counts as complete
         int issued[kTmaStages] = {0, 0, 0};   // stage holds copies not yet seen complete by us
         uint32_t fph[kTmaStages] = {0, 0, 0};
+        int xiss[2] = {0, 0};                 // the same for the two x buffers
+        uint32_t xfp[2] = {0, 0};
         bool ok = true;
         while (ok && total > 0) {
             int item = 0;
@@ -423,7 +453,7 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
             const size_t esz = h ? 4 : 8;
             // x chunk
             int w = 1;
-            if (lane == 0) w = mbar_wait(xempty0 + 8 * xs, xeph[xs], err);
+            if (lane == 0) w = mbar_wait(xempty0 + 8 * xs, xeph[xs], err, lim);
             if (!__shfl_sync(kAll, w, 0)) { ok = false; break; }
             xeph[xs] ^= 1;
             if (lane == 0) {
@@ -436,8 +466,10 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
                     bulk_g2s(xdst, S.xh + c0, lenp * 8, xfull0 + 8 * xs);
                 }
             }
+            xiss[xs] = 1;
+            xfp[xs] ^= 1;
             for (int g = 0; g < nst; ++g) {
-                if (lane == 0) w = mbar_wait(empty0 + 8 * stage, eph, err);
+                if (lane == 0) w = mbar_wait(empty0 + 8 * stage, eph, err, lim);
                 if (!__shfl_sync(kAll, w, 0)) { ok = false; break; }
                 const int row0 = rbase + g * rps, nrows = min(rps, n - row0);
                 if (lane == 0) {
@@ -460,7 +492,7 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
         if (lane == 0) {
             if (ok) {
                 // sentinel: consumers stop at the next stage
-                if (mbar_wait(empty0 + 8 * stage, eph, err)) {
+                if (mbar_wait(empty0 + 8 * stage, eph, err, lim)) {
                     meta[stage].b = -1;
                     mbar_arrive(full0 + 8 * stage);
                 } else {
@@ -468,9 +500,12 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
                 }
             }
             if (!ok) {
-                // a wait gave up: let this block's copies land before leaving
+                // a wait gave up: let this block's copies (stages and x
+                // buffers) land before leaving
                 for (int s = 0; s < kTmaStages; ++s)
                     if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
+                for (int q = 0; q < 2; ++q)
+                    if (xiss[q]) mbar_wait(xfull0 + 8 * q, xfp[q] ^ 1, err);
             }
             __threadfence();
             if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
@@ -485,12 +520,12 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
     int stage = 0;
     uint32_t fph = 0, xph[2] = {0, 0};
     while (true) {
-        if (!mbar_wait(full0 + 8 * stage, fph, err)) return;
+        if (!mbar_wait(full0 + 8 * stage, fph, err, lim)) return;
         const TmaMeta mt = meta[stage];
         if (mt.b < 0) return;
         const KSys &S = tb->sys[mt.b];
         if (mt.first) {
-            if (!mbar_wait(xfull0 + 8 * mt.xslot, xph[mt.xslot], err)) return;
+            if (!mbar_wait(xfull0 + 8 * mt.xslot, xph[mt.xslot], err, lim)) return;
         }
         const unsigned char *xb = xbuf + mt.xslot * tma_x_bytes(EXACT);
         // this warp's row sum as float-float (hi, lo) pairs of the real and
@@ -712,6 +747,8 @@ __global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(
     __shared__ PlanSmem pl;
     plan_load(tb->gplan[kind], pl);   // includes a block barrier
     int *err = &tb->err;
+    // bound of the waits (the drains of in-flight copies keep the full bound)
+    const long long lim = tb->wait_cycles > 0 ? tb->wait_cycles : kWaitCycles;
     if (warp == NW) {
         // ---------------- producer (one lane)
         if (lane != 0) return;
@@ -746,7 +783,7 @@ __global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(
                 }
             }
             for (int ck = 0; ck < nck && ok; ++ck) {
-                if (!mbar_wait(empty0 + 8 * stage, eph, err)) { ok = false; break; }
+                if (!mbar_wait(empty0 + 8 * stage, eph, err, lim)) { ok = false; break; }
                 const int c0 = ck * kGrpCols, len = min(kGrpCols, n - c0), lenp = (len + 1) & ~1;
                 GrpMeta mt;
                 mt.first = g.first; mt.chunk = ck; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
@@ -778,7 +815,7 @@ __global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(
             }
         }
         if (ok) {
-            if (mbar_wait(empty0 + 8 * stage, eph, err)) {
+            if (mbar_wait(empty0 + 8 * stage, eph, err, lim)) {
                 meta[stage].first = -1;
                 mbar_arrive(full0 + 8 * stage);
             } else {
@@ -805,7 +842,7 @@ __global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(
     int stage = 0;
     uint32_t fph = 0;
     while (true) {
-        if (!mbar_wait(full0 + 8 * stage, fph, err)) return;
+        if (!mbar_wait(full0 + 8 * stage, fph, err, lim)) return;
         const GrpMeta mt = meta[stage];
         if (mt.first < 0) return;
         if (mt.chunk == 0) {
@@ -974,6 +1011,8 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
     __shared__ PlanSmem pl;
     plan_load(tb->gplan[kind], pl);   // includes a block barrier
     int *err = &tb->err;
+    // bound of the waits (the drains of in-flight copies keep the full bound)
+    const long long lim = tb->wait_cycles > 0 ? tb->wait_cycles : kWaitCycles;
     if (warp == kTcWarps) {
         // ---------------- producer (one lane)
         if (lane != 0) return;
@@ -1006,7 +1045,7 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
                 }
             }
             for (int ck = 0; ck < nck && ok; ++ck) {
-                if (!mbar_wait(empty0 + 8 * stage, eph, err)) { ok = false; break; }
+                if (!mbar_wait(empty0 + 8 * stage, eph, err, lim)) { ok = false; break; }
                 const int c0 = ck * kGrpCols, len = min(kGrpCols, n - c0), lenp = (len + 1) & ~1;
                 GrpMeta mt;
                 mt.first = g.first; mt.chunk = ck; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
@@ -1026,7 +1065,7 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
             }
         }
         if (ok) {
-            if (mbar_wait(empty0 + 8 * stage, eph, err)) {
+            if (mbar_wait(empty0 + 8 * stage, eph, err, lim)) {
                 meta[stage].first = -1;
                 mbar_arrive(full0 + 8 * stage);
             } else {
@@ -1054,7 +1093,7 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
     int stage = 0;
     uint32_t fph = 0, rph = 0;
     while (true) {
-        if (!mbar_wait(full0 + 8 * stage, fph, err)) return;
+        if (!mbar_wait(full0 + 8 * stage, fph, err, lim)) return;
         const GrpMeta mt = meta[stage];
         if (mt.first < 0) return;
         if (mt.chunk == 0) {
@@ -1131,7 +1170,7 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
             t[(gid + 8) * 16 + 8 + 2 * tig + 1] = (double)sh[7] + (double)sl[7];
             __syncwarp();
             if (lane == 0) mbar_arrive(redw);
-            if (!mbar_wait(redw, rph, err)) return;
+            if (!mbar_wait(redw, rph, err, lim)) return;
             // outputs (row block, row, member) = consumer thread index < 256; the
             // sum of the slices of its row block (warps rb, rb + 2, ...)
             const int ot = warp * 32 + lane;
@@ -1155,7 +1194,7 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(redr);
-            if (!mbar_wait(redr, rph, err)) return;   // the tile is free for the next strip
+            if (!mbar_wait(redr, rph, err, lim)) return;   // the tile is free for the next strip
             rph ^= 1;
         }
         if (++stage == kTcStages) { stage = 0; fph ^= 1; }

@@ -300,6 +300,9 @@ struct KTable {
     int vb_total;           // vector blocks of all systems
     int err;                // set when a bounded device wait gave up
     int pcw_any;            // some system applies the window correction
+    long long wait_cycles;  // bound of the products' mbarrier waits in clock
+                            // cycles (0: the default of about 2 s); a test
+                            // sets it low to make a wait run out
     unsigned mv_ctr[2];     // work queue of the persistent matvec
     KPlan plan[3];          // [0] Krylov product, [1] refinement residual with
                             // error-free products, [2] recursive residual update

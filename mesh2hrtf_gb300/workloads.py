@@ -1,5 +1,10 @@
 """Seeded synthetic workloads of the batched and served configurations.
 
+head_workload       the head-like scatterer of the benchmark: ellipsoid
+                    0.09/0.075/0.11 m with two seeded Gaussian bumps, 20480
+                    triangles graded toward bump 1, source 1 mm off bump 1,
+                    1730-point equal-angle grid on a 1.2 m sphere, 200
+                    frequencies 100 Hz .. 20 kHz in a seeded order.
 batched_instances   (mesh, frequency) pairs: perturbed ellipsoids
                     (0.09/0.075/0.11 m, smooth radial noise of 3 mm standard
                     deviation), element counts drawn log-uniform and rounded
@@ -21,6 +26,16 @@ from . import meshes
 C0, RHO = 343.0, 1.21
 SEED_BATCH = 20261205
 SEED_STREAM = 20261206
+SEED_HEAD = 20261204
+
+
+def head_workload(seed=SEED_HEAD):
+    """(nodes, elems, source, points, frequencies in a seeded order)."""
+    v, f, info = meshes.head_like(32, seed=seed)
+    pts = meshes.equal_angle_grid(1.2, 5.0, 24)
+    freqs = np.arange(1, 201) * 100.0
+    order = np.random.default_rng(seed).permutation(len(freqs))
+    return v, f, info["source"], pts, freqs[order]
 
 
 def _instance(rng, i, seed, n_min, n_max, f_min, f_max):

@@ -811,3 +811,343 @@ int or_project(const or_mesh *m, const double *centers, const double *normals, c
     }
     return err ? -1 : 0;
 }
+
+/* ------------------------------------------------------- iterative solver */
+/* Complex division as the reference's Complex::operator/ does it
+ * (NC_TypeDefinition.h). */
+static inline cx cdiv(cx a, cx b)
+{
+    double t = b.re * b.re + b.im * b.im;
+    return cmk((a.re * b.re + a.im * b.im) / t, (a.im * b.re - a.re * b.im) / t);
+}
+
+/* Unconjugated dot product Vector<Complex>::operator* (NC_TypeDefinition.h:
+ * 403-410), summed in index order. */
+static cx cdot(int n, const cx *a, const cx *b)
+{
+    cx d = cmk(0.0, 0.0);
+    for (int i = 0; i < n; ++i) d = cadd(d, cmul(a[i], b[i]));
+    return d;
+}
+
+/* Threshold ILU of the TBEM branch of NC_IncompleteLUDecomposition
+ * (NC_CommonFunctions.cpp:1357-1659): L by rows (diagonal last), U by
+ * columns (unit diagonal implied).  The reference finds each product term
+ * by scanning boolean masks over all m < i; here the same terms are found by
+ * merging the sorted index lists, in the same increasing m, so every entry
+ * sees the same operations in the same order. */
+typedef struct {
+    int n;
+    int *lp, *lc;   /* L: row pointers, column indices */
+    int *up, *ur;   /* U: column pointers, row indices */
+    cx *lv, *uv;
+} ilu_t;
+
+static void ilu_free(ilu_t *F)
+{
+    free(F->lp); free(F->lc); free(F->up); free(F->ur); free(F->lv); free(F->uv);
+    memset(F, 0, sizeof(*F));
+}
+
+/* dot of L row k (columns < i) with U column c (rows < i), merged in
+ * increasing index; the running value z is updated term by term */
+static cx ilu_merge(const ilu_t *F, int k, int c, int i, cx z)
+{
+    int a = F->lp[k], ae = F->lp[k + 1], b = F->up[c], be = F->up[c + 1];
+    while (a < ae && b < be) {
+        int ca = F->lc[a], rb = F->ur[b];
+        if (ca >= i || rb >= i) break;
+        if (ca == rb) { z = csub(z, cmul(F->lv[a], F->uv[b])); ++a; ++b; }
+        else if (ca < rb) ++a;
+        else ++b;
+    }
+    return z;
+}
+
+static int find_idx(const int *idx, int lo, int hi, int v)
+{
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (idx[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+/* Scales the rows of A and b in place (1410-1423) and factors. */
+static int ilu_build(int n, cx *A, cx *b, int scan, ilu_t *F)
+{
+    static const double thresh[4] = {1.2, 1.0, 0.8, 0.6};
+    const double tf = thresh[scan < 0 ? 0 : (scan > 3 ? 3 : scan)];
+    memset(F, 0, sizeof(*F));
+    F->n = n;
+    int *rcnt = (int *)calloc((size_t)n + 1, sizeof(int));
+    int *ccnt = (int *)calloc((size_t)n + 1, sizeof(int));
+    if (!rcnt || !ccnt) { free(rcnt); free(ccnt); return -1; }
+    /* row scaling and the pattern ("trues"): |a_ij| > tf or i == j */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i = 0; i < n; ++i) {
+        cx *row = A + (size_t)i * n;
+        double dw1 = 0.0;
+        for (int j = 0; j < n; ++j) dw1 += row[j].re * row[j].re + row[j].im * row[j].im;
+        double dwk = sqrt((double)n / dw1);
+        int c = 0;
+        for (int j = 0; j < n; ++j) {
+            row[j] = cscl(row[j], dwk);
+            if (cabs_(row[j]) > tf || i == j) ++c;
+        }
+        b[i] = cscl(b[i], dwk);
+        rcnt[i] = c;
+    }
+    /* L: row i's pattern entries with j <= i; U: column c's entries with
+     * row < c.  Count, then fill (rows in increasing order per column). */
+    F->lp = (int *)malloc(sizeof(int) * ((size_t)n + 1));
+    F->up = (int *)malloc(sizeof(int) * ((size_t)n + 1));
+    int *lcnt = (int *)calloc((size_t)n, sizeof(int));
+    if (!F->lp || !F->up || !lcnt) { free(rcnt); free(ccnt); free(lcnt); ilu_free(F); return -1; }
+    for (int i = 0; i < n; ++i) {
+        const cx *row = A + (size_t)i * n;
+        for (int j = 0; j < n; ++j) {
+            if (!(cabs_(row[j]) > tf || i == j)) continue;
+            if (j <= i) ++lcnt[i];
+            else ++ccnt[j];
+        }
+    }
+    F->lp[0] = F->up[0] = 0;
+    for (int i = 0; i < n; ++i) {
+        F->lp[i + 1] = F->lp[i] + lcnt[i];
+        F->up[i + 1] = F->up[i] + ccnt[i];
+    }
+    size_t nl = (size_t)F->lp[n], nu = (size_t)F->up[n];
+    F->lc = (int *)malloc(sizeof(int) * (nl ? nl : 1));
+    F->lv = (cx *)malloc(sizeof(cx) * (nl ? nl : 1));
+    F->ur = (int *)malloc(sizeof(int) * (nu ? nu : 1));
+    F->uv = (cx *)malloc(sizeof(cx) * (nu ? nu : 1));
+    if (!F->lc || !F->lv || !F->ur || !F->uv) { free(rcnt); free(ccnt); free(lcnt); ilu_free(F); return -1; }
+    memset(ccnt, 0, sizeof(int) * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const cx *row = A + (size_t)i * n;
+        int q = F->lp[i];
+        for (int j = 0; j < n; ++j) {
+            if (!(cabs_(row[j]) > tf || i == j)) continue;
+            if (j <= i) { F->lc[q] = j; F->lv[q] = row[j]; ++q; }
+            else { int p = F->up[j] + ccnt[j]++; F->ur[p] = i; F->uv[p] = row[j]; }
+        }
+    }
+    free(rcnt); free(ccnt); free(lcnt);
+    /* transposed position lists: per column c the L entries (k, c), k >= c,
+     * and per row r the U entries (r, k), k > r, each in increasing k */
+    int *ltp = (int *)calloc((size_t)n + 1, sizeof(int)), *utp = (int *)calloc((size_t)n + 1, sizeof(int));
+    int *ltq = (int *)malloc(sizeof(int) * (nl ? nl : 1)), *utq = (int *)malloc(sizeof(int) * (nu ? nu : 1));
+    if (!ltp || !utp || !ltq || !utq) { free(ltp); free(utp); free(ltq); free(utq); ilu_free(F); return -1; }
+    for (size_t q = 0; q < nl; ++q) ++ltp[F->lc[q] + 1];
+    for (size_t q = 0; q < nu; ++q) ++utp[F->ur[q] + 1];
+    for (int i = 0; i < n; ++i) { ltp[i + 1] += ltp[i]; utp[i + 1] += utp[i]; }
+    {
+        int *fl = (int *)malloc(sizeof(int) * (size_t)n), *fu = (int *)malloc(sizeof(int) * (size_t)n);
+        if (!fl || !fu) { free(fl); free(fu); free(ltp); free(utp); free(ltq); free(utq); ilu_free(F); return -1; }
+        memcpy(fl, ltp, sizeof(int) * (size_t)n);
+        memcpy(fu, utp, sizeof(int) * (size_t)n);
+        for (int k = 0; k < n; ++k)                       /* rows in increasing k */
+            for (int q = F->lp[k]; q < F->lp[k + 1]; ++q) ltq[fl[F->lc[q]]++] = q;
+        for (int k = 0; k < n; ++k)                       /* columns in increasing k */
+            for (int q = F->up[k]; q < F->up[k + 1]; ++q) utq[fu[F->ur[q]]++] = q;
+        free(fl); free(fu);
+    }
+    /* factorization, loop I of 1611-1658: column i of L (rows k >= i of the
+     * pattern), then row i of U (columns k > i) divided by L_ii */
+    for (int i = 0; i < n; ++i) {
+        const int l0 = ltp[i], l1 = ltp[i + 1];
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) if (l1 - l0 > 256)
+#endif
+        for (int t = l0; t < l1; ++t) {
+            const int q = ltq[t];
+            int k = find_idx(F->lp, 0, n + 1, q + 1) - 1;   /* row of entry q */
+            while (F->lp[k + 1] <= q) ++k;
+            F->lv[q] = ilu_merge(F, k, i, i, F->lv[q]);
+        }
+        const cx dia = F->lv[F->lp[i + 1] - 1];
+        const int u0 = utp[i], u1 = utp[i + 1];
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) if (u1 - u0 > 256)
+#endif
+        for (int t = u0; t < u1; ++t) {
+            const int p = utq[t];
+            int k = find_idx(F->up, 0, n + 1, p + 1) - 1;   /* column of entry p */
+            while (F->up[k + 1] <= p) ++k;
+            cx z = F->uv[p];
+            /* L row i (columns < i) with U column k (rows < i) */
+            int a = F->lp[i], ae = F->lp[i + 1], bb = F->up[k], be = F->up[k + 1];
+            while (a < ae && bb < be) {
+                int ca = F->lc[a], rb = F->ur[bb];
+                if (ca >= i || rb >= i) break;
+                if (ca == rb) { z = csub(z, cmul(F->lv[a], F->uv[bb])); ++a; ++bb; }
+                else if (ca < rb) ++a;
+                else ++bb;
+            }
+            F->uv[p] = cdiv(z, dia);
+        }
+    }
+    free(ltp); free(utp); free(ltq); free(utq);
+    return 0;
+}
+
+/* NC_IncompleteLUForBack (NC_CommonFunctions.cpp:1673-1721): y = (LU)^-1 v. */
+static void ilu_apply(const ilu_t *F, const cx *v, cx *y)
+{
+    const int n = F->n;
+    for (int i = 0; i < n; ++i) y[i] = v[i];
+    y[0] = cdiv(y[0], F->lv[0]);
+    for (int i = 1; i < n; ++i) {
+        int k = F->lp[i + 1] - 1;
+        for (int j = F->lp[i]; j < k; ++j) y[i] = csub(y[i], cmul(F->lv[j], y[F->lc[j]]));
+        y[i] = cdiv(y[i], F->lv[k]);
+    }
+    for (int i = n - 1; i > 0; --i)
+        for (int j = F->up[i]; j < F->up[i + 1]; ++j) y[F->ur[j]] = csub(y[F->ur[j]], cmul(F->uv[j], y[i]));
+}
+
+/* y = A (M^-1 v): NC_MatrixVectorMultiplication case 0 (1211-1245); each row
+ * summed in column order, rows split over threads. */
+static void precond_matvec(int n, const cx *A, int precond, const ilu_t *F, const double *dsc, const cx *v,
+                           cx *t, cx *y)
+{
+    if (precond == 0) ilu_apply(F, v, t);
+    else if (precond == 1) for (int i = 0; i < n; ++i) t[i] = cscl(v[i], dsc[i]);
+    else for (int i = 0; i < n; ++i) t[i] = v[i];
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i = 0; i < n; ++i) {
+        const cx *row = A + (size_t)i * n;
+        cx s = cmk(0.0, 0.0);
+        for (int j = 0; j < n; ++j) s = cadd(s, cmul(row[j], t[j]));
+        y[i] = s;
+    }
+}
+
+/* Tfactor_usy / Tfbelim (NC_TypeDefinition.h:543-594): LU without pivoting
+ * in place, then the solve; b is overwritten by the solution. */
+static void dense_lu_nopivot(int n, cx *A, cx *b)
+{
+    for (int i = 0; i < n - 1; ++i) {
+        const cx dia = A[(size_t)i * n + i];
+        const cx *ri = A + (size_t)i * n;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+        for (int j = i + 1; j < n; ++j) {
+            cx *rj = A + (size_t)j * n;
+            rj[i] = cdiv(rj[i], dia);
+            const cx cji = rj[i];
+            for (int k = i + 1; k < n; ++k) rj[k] = csub(rj[k], cmul(ri[k], cji));
+        }
+        for (int k = i + 1; k < n; ++k) A[(size_t)i * n + k] = cdiv(A[(size_t)i * n + k], dia);
+    }
+    for (int i = 1; i < n; ++i)
+        for (int j = 0; j < i; ++j) b[i] = csub(b[i], cmul(A[(size_t)i * n + j], b[j]));
+    for (int i = 0; i < n; ++i) b[i] = cdiv(b[i], A[(size_t)i * n + i]);
+    for (int i = n - 1; i > 0; --i)
+        for (int j = 0; j < i; ++j) b[j] = csub(b[j], cmul(b[i], A[(size_t)j * n + i]));
+}
+
+#include <time.h>
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+int or_solve_cgs(int n, double *Ad, double *bd, int precond, int scan, int niter_max, double tol, double *xd,
+                 int *iters, double *rel_err, int nthreads, double *stage_s)
+{
+    cx *A = (cx *)Ad, *b = (cx *)bd, *x = (cx *)xd;
+    double t0 = now_s();
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    if (stage_s) stage_s[0] = stage_s[1] = stage_s[2] = 0.0;
+    ilu_t F;
+    memset(&F, 0, sizeof(F));
+    double *dsc = NULL;
+    /* preconditioner set-up (1078-1087) */
+    if (precond == 0) {
+        if (ilu_build(n, A, b, scan, &F) != 0) return -1;
+    } else if (precond == 1) {
+        /* NC_ComputeScalingVector, 1322-1354 */
+        dsc = (double *)malloc(sizeof(double) * (size_t)n);
+        if (!dsc) return -1;
+        for (int i = 0; i < n; ++i) {
+            double dwk = 0.0;
+            const cx *row = A + (size_t)i * n;
+            for (int j = 0; j < n; ++j) dwk += row[j].re * row[j].re + row[j].im * row[j].im;
+            dsc[i] = sqrt((double)n / dwk);
+        }
+    }
+    double t1 = now_s();
+    cx *w = (cx *)malloc(sizeof(cx) * (size_t)n * 10);
+    if (!w) { ilu_free(&F); free(dsc); return -1; }
+    cx *X = w, *R0 = w + n, *R = w + 2 * (size_t)n, *P = w + 3 * (size_t)n, *V = w + 4 * (size_t)n;
+    cx *Q = w + 5 * (size_t)n, *U = w + 6 * (size_t)n, *UQ = w + 7 * (size_t)n, *AUQ = w + 8 * (size_t)n;
+    cx *T = w + 9 * (size_t)n;
+    for (int j = 0; j < n; ++j) X[j] = cmk(0.0, 0.0);
+    precond_matvec(n, A, precond, &F, dsc, X, T, V);
+    int direct = 0;
+    if (precond == 0)   /* ILU nearly singular (1102-1122): TBEM goes to the direct solver */
+        for (int i = 0; i < n; ++i) if (cabs_(V[i]) > 1.0e8) { direct = 1; break; }
+    double err_ori = 0.0, err_rel = 1.0;
+    int j = 0;
+    if (!direct) {
+        for (int i = 0; i < n; ++i) U[i] = R[i] = P[i] = R0[i] = csub(b[i], V[i]);
+        cx zrjr0 = cmk(0.0, 0.0), zrjr1 = cmk(0.0, 0.0);
+        for (j = 0; j <= niter_max; ++j) {
+            precond_matvec(n, A, precond, &F, dsc, P, T, V);
+            zrjr0 = j == 0 ? cdot(n, R, R0) : zrjr1;
+            cx zalph = cdiv(zrjr0, cdot(n, V, R0));
+            for (int i = 0; i < n; ++i) Q[i] = csub(U[i], cmul(zalph, V[i]));
+            for (int i = 0; i < n; ++i) UQ[i] = cadd(U[i], Q[i]);
+            precond_matvec(n, A, precond, &F, dsc, UQ, T, AUQ);
+            double dwk1 = 0.0;
+            for (int i = 0; i < n; ++i) {
+                X[i] = cadd(X[i], cmul(zalph, UQ[i]));
+                R[i] = csub(R[i], cmul(zalph, AUQ[i]));
+                dwk1 += R[i].re * R[i].re + R[i].im * R[i].im;
+            }
+            if (j == 0) err_ori = sqrt(dwk1);
+            else err_rel = sqrt(dwk1) / err_ori;
+            if (err_rel < tol || j == niter_max) {
+                for (int i = 0; i < n; ++i) b[i] = X[i];
+                break;
+            }
+            zrjr1 = cdot(n, R, R0);
+            cx zbet = cdiv(zrjr1, zrjr0);
+            for (int i = 0; i < n; ++i) U[i] = cadd(R[i], cmul(zbet, Q[i]));
+            for (int i = 0; i < n; ++i) P[i] = cadd(U[i], cmul(zbet, cadd(Q[i], cmul(zbet, P[i]))));
+        }
+        if (j >= niter_max) direct = 1;   /* 1181-1191 */
+    }
+    double t2 = now_s();
+    if (direct) {
+        /* the reference factors the (scaled) matrix and solves for its
+         * (scaled) right-hand side */
+        dense_lu_nopivot(n, A, b);
+        for (int i = 0; i < n; ++i) x[i] = b[i];
+    } else if (precond == 0) {
+        ilu_apply(&F, b, x);   /* 1194-1199 */
+    } else if (precond == 1) {
+        for (int i = 0; i < n; ++i) x[i] = cscl(b[i], dsc[i]);
+    } else {
+        for (int i = 0; i < n; ++i) x[i] = b[i];
+    }
+    double t3 = now_s();
+    if (stage_s) { stage_s[0] = t1 - t0; stage_s[1] = t2 - t1; stage_s[2] = t3 - t2; }
+    if (iters) *iters = j;
+    if (rel_err) *rel_err = err_rel;
+    ilu_free(&F);
+    free(dsc);
+    free(w);
+    return direct ? 1 : 0;
+}

@@ -63,6 +63,22 @@ int or_assemble(const or_mesh *m, const double *centers, const double *normals,
 /* Dense complex LU with partial pivoting, overwriting A; x = A^{-1} b. */
 int or_solve_dense(int n, double *A, const double *b, double *x);
 
+/* NumCalc's iterative solver: CGS with right preconditioning and unconjugated
+ * inner products, stopped at err_rel < tol (relative to the residual after
+ * the first update) or at niter_max (NC_IterativeSolverCGS,
+ * NC_CommonFunctions.cpp:1066-1208), on y = A M^-1 x products
+ * (NC_MatrixVectorMultiplication case 0, 1211-1245).  precond 0: threshold
+ * ILU of scanning degree scan (NC_IncompleteLUDecomposition TBEM branch and
+ * NC_IncompleteLUForBack, 1357-1721; it scales the rows of A and b in place);
+ * 1: row scaling (NC_ComputeScalingVector, 1322-1354); 2: none.  On
+ * iteration failure it runs the reference's dense LU without pivoting
+ * (Tfactor_usy / Tfbelim, NC_TypeDefinition.h:543-594).  A and b are
+ * overwritten.  stage_s (may be NULL): seconds of preconditioner set-up,
+ * iterations, and the final (un)preconditioning or direct solve.  Returns 0,
+ * 1 when the direct solver ran, -1 on allocation failure. */
+int or_solve_cgs(int n, double *A, double *b, int precond, int scan, int niter_max, double tol, double *x,
+                 int *iters, double *rel_err, int nthreads, double *stage_s);
+
 /* Potential and its gradient at points: NC_ContributionTBEM /
  * NC_IntegrationTBEM / NC_ContributionIncidentWaves,
  * NC_PostProcessing.cpp:776-975,1217-1322 (with the element and source

@@ -33,6 +33,9 @@ def lib():
         _lib.or_solve_dense.argtypes = [C.c_int, dp, dp, dp]
         _lib.or_project.argtypes = [C.c_void_p, dp, dp, dp, C.c_void_p, dp, dp, C.c_int, dp, dp, dp, C.c_int]
         _lib.or_project.restype = C.c_int
+        _lib.or_solve_cgs.argtypes = [C.c_int, dp, dp, C.c_int, C.c_int, C.c_int, C.c_double, dp, ip, dp,
+                                      C.c_int, dp]
+        _lib.or_solve_cgs.restype = C.c_int
         _lib.or_subelements.argtypes = [C.c_void_p, C.c_int, dp, C.c_double, dp, dp, dp, ip]
         _lib.or_subelements.restype = C.c_int
     return _lib
@@ -116,6 +119,28 @@ def solve_dense(A, b):
     if lib().or_solve_dense(len(b), _p(A), _p(b), _p(x)) != 0:
         raise RuntimeError("singular matrix")
     return x
+
+
+def solve_cgs(A, b, precond=0, scan=0, niter_max=250, tol=1e-9, nthreads=0, overwrite=False):
+    """NumCalc's CGS with its preconditioners (or_solve_cgs).  A and b are
+    copied unless overwrite (then A must be C-contiguous complex128; it is
+    row-scaled and, on the direct fallback, factored in place).  Returns x,
+    iterations, relative error, whether the direct fallback ran, and the
+    stage seconds (set-up, iterations, final step)."""
+    if overwrite:
+        assert A.dtype == np.complex128 and A.flags.c_contiguous
+    else:
+        A = np.array(A, dtype=np.complex128, order="C", copy=True)
+    b = np.array(b, dtype=np.complex128, copy=True)
+    x = np.zeros_like(b)
+    it = C.c_int(0)
+    err = C.c_double(0.0)
+    st = np.zeros(3)
+    rc = lib().or_solve_cgs(len(b), _p(A), _p(b), precond, scan, niter_max, tol, _p(x), C.byref(it),
+                            C.byref(err), nthreads, _p(st))
+    if rc < 0:
+        raise RuntimeError("or_solve_cgs: allocation failed")
+    return x, it.value, err.value, rc == 1, st
 
 
 def boundary_fields(mesh: OracleMesh, x, tao=1.0):

@@ -14,7 +14,19 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 REF_NUMCALC = os.path.join(REF_DIR, "NumCalc")
 REF_NUMCALC_DUMP = os.path.join(REF_DIR, "NumCalc_dump")
-DEFAULT_REFSRC = "/root/reference/mesh2hrtf/NumCalc/src"
+# Root of a Mesh2HRTF checkout holding the reference sources, from the
+# environment; unset means the reference is absent and build() skips.
+REFERENCE_ENV = "MESH2HRTF_REFERENCE"
+
+
+def reference_root():
+    root = os.environ.get(REFERENCE_ENV, "")
+    return root if root and os.path.isdir(root) else None
+
+
+def default_refsrc():
+    root = reference_root()
+    return os.path.join(root, "mesh2hrtf", "NumCalc", "src") if root else None
 
 _DT = {"f8": (np.float64, 8), "i4": (np.int32, 4), "c16": (np.complex128, 16)}
 
@@ -23,9 +35,10 @@ def available() -> bool:
     return os.path.isfile(REF_NUMCALC_DUMP) and os.access(REF_NUMCALC_DUMP, os.X_OK)
 
 
-def build(refsrc: str = DEFAULT_REFSRC) -> bool:
+def build(refsrc: str | None = None) -> bool:
     """Build oracle/_ref when the reference sources are present."""
-    if not os.path.isfile(os.path.join(refsrc, "NC_Main.cpp")):
+    refsrc = refsrc or default_refsrc()
+    if not refsrc or not os.path.isfile(os.path.join(refsrc, "NC_Main.cpp")):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "-j8", "REFSRC=" + refsrc], check=True)
     return available()

@@ -5,7 +5,8 @@ oracle/Makefile) on small projects and stores, per case, the inputs (mesh,
 evaluation points, frequency data), the reference's assembled matrix (full
 or sampled rows/entries), right-hand side, CGS solution, a dense FP64 solve of
 the same system, and the full-precision be.out results.  Needs the reference
-sources; the committed .npz files are what the tests read.
+sources (MESH2HRTF_REFERENCE = root of a Mesh2HRTF checkout); the committed
+.npz files are what the tests read.
 
     python tests/golden/make_golden.py [case ...]
 """
@@ -25,7 +26,14 @@ sys.path.insert(0, ROOT)
 from mesh2hrtf_gb300 import meshes, project  # noqa: E402
 from oracle import refdump  # noqa: E402
 
-REF_FIXTURES = "/root/reference/tests/resources/test_numcalc"
+
+
+def ref_fixtures() -> str:
+    """The reference's test_numcalc resources (needs MESH2HRTF_REFERENCE)."""
+    root = refdump.reference_root()
+    if not root:
+        raise SystemExit("set %s to the root of a Mesh2HRTF checkout" % refdump.REFERENCE_ENV)
+    return os.path.join(root, "tests", "resources", "test_numcalc")
 
 
 def cube_sphere(n, radius):
@@ -140,7 +148,7 @@ def _load_ref_mesh(folder):
 def case_pspw():
     """The reference's own TBEM fixture: 2412-element sphere (a = 0.0875 m),
     point source at 0.2 m, 4 kHz, 7560 evaluation points from 0.09 m."""
-    base = os.path.join(REF_FIXTURES, "project_folder_pspw")
+    base = os.path.join(ref_fixtures(), "project_folder_pspw")
     v, f = _load_ref_mesh(os.path.join(base, "ObjectMeshes", "Reference"))
     pts, ptri = _load_ref_mesh(os.path.join(base, "EvaluationGrids", "HorPlane"))
     p = project.Project(root="", nodes=v, elems=f, eval_points=pts, eval_elems=ptri, freqs=[4000.0],

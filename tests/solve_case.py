@@ -1,12 +1,12 @@
 """Solve one synthetic scattering case on the GPU and print a JSON summary.
 
-    python -m mesh2hrtf_gb300.solve_case [--n-tri 8000] [--freq 5000]
+    python -m tests.solve_case [--n-tri 8000] [--freq 5000]
         [--precision mixed|fp64] [--repeat 2] [--head]
 
 Sphere (radius 0.1 m, geodesic mesh with --n-tri = 20 n^2 triangles) or the
 head-like scatterer (--head), point source at 1 m, 1000 evaluation points at
-1.2 m.  Useful for quick checks of a device and as a small, fixed workload for
-profilers.
+1.2 m.  A small, fixed workload for profilers (the commands under profiles/) and
+quick checks of a device; not part of the library.
 """
 from __future__ import annotations
 
@@ -16,7 +16,7 @@ import time
 
 import numpy as np
 
-from . import capi, meshes
+from mesh2hrtf_gb300 import capi, meshes
 
 
 def main():

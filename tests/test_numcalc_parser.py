@@ -86,7 +86,7 @@ def test_output_naming_estimate_mode(args, name, numcalc, tmp_path):
     assert [int(l.split()[0]) for l in mem] == list(range(first, last + 1))
 
 
-@pytest.mark.skipif(not os.path.isdir(refdump.DEFAULT_REFSRC), reason="reference sources not present")
+@pytest.mark.skipif(not (refdump.available() or refdump.default_refsrc()), reason="reference build and sources not present")
 @pytest.mark.parametrize("case", sorted(REF))
 def test_live_reference_agrees(case, numcalc, tmp_path):
     """Where the reference builds (this container), compare directly."""

@@ -82,6 +82,22 @@ def test_dense_solve_matches_reference_cgs():
     assert gc.rel_err(x, c["s1_x_cgs"]) < 1e-8
 
 
+@pytest.mark.parametrize("name", ["sphere80", "sphere1280_1k", "pspw2412_4k"])
+def test_cgs_ilu_reproduces_reference_cgs(name):
+    """The restatement of NumCalc's solver (threshold ILU of scanning degree 0,
+    CGS to 1e-9, NC_CommonFunctions.cpp:1066-1721) on the oracle's matrix
+    gives the reference's own CGS solution bit for bit, at any thread count."""
+    c = gc.load(name)
+    m = _mesh(c)
+    st = c.step(1)
+    A, b = op.assemble(m, _freq(st), nthreads=8)
+    x1, it, err, direct, _ = op.solve_cgs(A, b, precond=0, scan=0, nthreads=1)
+    x8, it8, _, _, _ = op.solve_cgs(A, b, precond=0, scan=0, nthreads=8)
+    assert not direct and err < 1e-9 and it == it8
+    assert np.array_equal(x1, x8)
+    assert np.array_equal(x1, c["s1_x_cgs"])
+
+
 def test_analytic_series_vs_reference_bem():
     """Discretisation error of the reference BEM on the 1280-triangle sphere
     (a = 0.1 m, 1 kHz, point source at 1 m) against the FP64 series."""

@@ -37,10 +37,16 @@ def test_static_projection_matches_bem_project_twice(prec):
     pts_d = torch.tensor(pts, dtype=torch.float64, device=dev).contiguous()
     stream = torch.cuda.current_stream(dev).cuda_stream
     results = []
-    for _ in range(2):
+    for call in range(2):
         pot_d = torch.full((len(pts), 2), float("nan"), dtype=torch.float64, device=dev)
         grad_d = torch.full((len(pts), 3, 2), float("nan"), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize(dev)
+        free0 = torch.cuda.mem_get_info(dev)[0]
         s.project_static(len(pts), pts_d.data_ptr(), pot_d.data_ptr(), grad_d.data_ptr(), stream)
+        if call > 0:
+            # the defining property: once the first call on the device has
+            # looked up the scratch array, a call takes no device memory
+            assert torch.cuda.mem_get_info(dev)[0] == free0
         pot = pot_d.cpu().numpy().view(np.complex128).reshape(-1)
         grad = grad_d.cpu().numpy().view(np.complex128).reshape(len(pts), 3)
         results.append((pot, grad))
