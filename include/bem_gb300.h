@@ -139,6 +139,13 @@ const char *bem_version(void);
 /* Number of CUDA kernels this library has launched in this process (all
  * devices).  Diagnostic with no counterpart in the reference. */
 int64_t bem_kernel_launches(void);
+/* Measured issue rates of a device, in operations per second over the whole
+ * device: rates[0] FP32 FMA, rates[1] special-function approximations
+ * (sin / cos / rsqrt), rates[2] FP64 FMA.  Micro-kernels of independent
+ * dependency chains in every lane, timed with CUDA events (best of three);
+ * they are the denominators of the compute-bound stages' rooflines.
+ * Diagnostic with no counterpart in the reference.  Sets the device. */
+bem_status bem_measure_issue_peaks(int32_t device, double *rates);
 /* Select the CUDA device for this thread's subsequent calls. */
 bem_status bem_set_device(int32_t device);
 /* Bytes a solver for n_elem unknowns holds on the device (matrix, Krylov
@@ -195,6 +202,18 @@ bem_status bem_assemble(bem_solver_t solver, const bem_frequency_desc *freq);
  * and direct fallback (NC_CommonFunctions.cpp:1066-1208,1322-1721) by a
  * restarted GMRES (see bem_precision). */
 bem_status bem_solve(bem_solver_t solver, bem_solve_info *info);
+
+/* Solve A x = b directly: LU factorisation without pivoting in place, then
+ * forward and back substitution, for every right-hand side the solver holds.
+ * Replaces Tfactor_usy / Tfbelim (NC_TypeDefinition.h:543-594), which NumCalc
+ * runs for ISOLVER 4 (NC_Main.cpp:833-866) and after a failed CGS
+ * (NC_CommonFunctions.cpp:1181-1191).  The factorisation runs in the matrix's
+ * precision (complex128 for BEM_PREC_FP64, complex64 for BEM_PREC_MIXED), the
+ * substitutions in FP64.  A holds the factors afterwards: bem_solve and a
+ * second bem_solve_direct need a new bem_assemble, and bem_get_system returns
+ * the factors (L unit lower, U upper).  info gets no iterations and a
+ * residual of 0 (not computed); a zero pivot gives BEM_ERR_INVALID. */
+bem_status bem_solve_direct(bem_solver_t solver, bem_solve_info *info);
 
 /* Copy the solution (complex, n_elem) to host memory. */
 bem_status bem_get_solution(bem_solver_t solver, double *x_host);

@@ -33,7 +33,8 @@ EXPORTED = [
     "bem_assemble", "bem_solve", "bem_get_solution", "bem_get_system", "bem_project",
     "bem_solve_frequency", "bem_project_static", "bem_solve_batch", "bem_solve_multi", "bem_footprint_multi",
     "bem_server_create", "bem_server_submit", "bem_server_wait", "bem_server_destroy",
-    "bem_mesh_footprint_bytes", "bem_device_memory", "bem_release_cached_memory",
+    "bem_mesh_footprint_bytes", "bem_device_memory", "bem_release_cached_memory", "bem_measure_issue_peaks",
+    "bem_solve_direct",
 ]
 STATIC_MAX_ELEMENTS = 32768
 
@@ -130,6 +131,8 @@ def load(build_if_missing: bool = True):
     lib.bem_server_submit.argtypes = [vp, vp, C.POINTER(FreqDesc), i32, vp, C.POINTER(C.c_uint64)]
     lib.bem_server_wait.argtypes = [vp, C.c_uint64, C.c_double, vp, vp, vp, C.POINTER(RequestInfo)]
     lib.bem_server_destroy.argtypes = [vp]
+    lib.bem_measure_issue_peaks.argtypes = [i32, dp]
+    lib.bem_solve_direct.argtypes = [vp, C.POINTER(SolveInfo)]
     for name in EXPORTED:
         if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes", "bem_footprint_multi",
                         "bem_kernel_launches", "bem_mesh_footprint_bytes"):
@@ -245,6 +248,12 @@ class Solver:
     def solve(self, allow_not_converged=False):
         allow = (BEM_ERR_NOT_CONVERGED,) if allow_not_converged else ()
         _check(load().bem_solve(self.handle, C.byref(self.info)), allow)
+        return self.info.as_dict()
+
+    def solve_direct(self):
+        """bem_solve_direct: LU without pivoting in place (the matrix is
+        consumed until the next assemble)."""
+        _check(load().bem_solve_direct(self.handle, C.byref(self.info)))
         return self.info.as_dict()
 
     def solution(self):
@@ -392,6 +401,14 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def issue_peaks(device=0):
+    """bem_measure_issue_peaks: measured FP32 FMA, special-function and FP64
+    FMA rates of the device (operations per second)."""
+    r = np.zeros(3)
+    _check(load().bem_measure_issue_peaks(device, r.ctypes.data_as(C.POINTER(C.c_double))))
+    return {"fp32_fma_per_s": float(r[0]), "sfu_per_s": float(r[1]), "fp64_fma_per_s": float(r[2])}
 
 
 def footprint_bytes(n_elem, precision=PREC_MIXED, restart=0):

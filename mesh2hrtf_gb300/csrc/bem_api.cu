@@ -515,6 +515,7 @@ bem_status assemble_group(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned *
         s->info.assemble_ms = ms;
         s->info.n_near_pairs = (int64_t)(s->mesh->n_near - s->n);   // subdivided pairs (self pairs excluded)
         s->have_freq = true;
+        s->factored = false;
         s->solved = false;
         rcs[i] = BEM_OK;
         if (code[i] != 0) {
@@ -1109,6 +1110,7 @@ bem_status bem_assemble(bem_solver_t s, const bem_frequency_desc *f) {
 bem_status bem_solve(bem_solver_t s, bem_solve_info *info) {
     if (!s) return fail(BEM_ERR_INVALID, "null solver");
     if (!s->have_freq) return fail(BEM_ERR_INVALID, "bem_solve before bem_assemble");
+    if (s->factored) return fail(BEM_ERR_INVALID, "bem_solve: the matrix was factored by bem_solve_direct; assemble again");
     bem_status one = BEM_OK;
     bem_status rc = solve_group(&s, 1, solver_engine(s), s->st, s->ev[2], s->ev[3], &one);
     if (info) *info = s->info;
@@ -1222,6 +1224,7 @@ bem_status bem_solve_multi(bem_solver_t s, int32_t R, const bem_frequency_desc *
     s->info.n_near_pairs = (int64_t)(s->mesh->n_near - s->n);
     if (code != 0) return fail(BEM_ERR_SUBDIVISION, "%s", subdivision_message(code));
     s->have_freq = true;
+    s->factored = false;
     s->solved = false;
     // preconditioner of the shared matrix, x = 0, then the R systems in lockstep
     CU(cudaEventRecord(s->ev[2], st));
@@ -1273,7 +1276,19 @@ bem_status bem_solve_multi(bem_solver_t s, int32_t R, const bem_frequency_desc *
             t->sys[r] = s->prsys(n_pts, s->pts, s->pot + 2 * (size_t)n_pts * r, s->grad + 6 * (size_t)n_pts * r, r);
         bem::proj_batch_finish(*t);
         CU(bem::launch_fields(*t, st));
-        CU(bem::launch_project(*t, s->prec == BEM_PREC_FP64 ? 0 : 1, st));
+        // mixed precision: one kernel evaluation per (point, element) pair
+        // for up to 8 right-hand sides at a time
+        if (s->prec == BEM_PREC_MIXED && R >= 2) {
+            std::unique_ptr<bem::ProjBatch> u(new bem::ProjBatch());
+            for (int c0 = 0; c0 < R; c0 += 8) {
+                u->B = std::min(8, R - c0);
+                for (int r = 0; r < u->B; ++r) u->sys[r] = t->sys[c0 + r];
+                bem::proj_batch_finish(*u);
+                CU(bem::launch_project_multi(*u, st));
+            }
+        } else {
+            CU(bem::launch_project(*t, s->prec == BEM_PREC_FP64 ? 0 : 1, st));
+        }
     }
     CU(cudaEventRecord(s->ev[5], st));
     for (int r = 0; r < R && n_pts > 0; ++r) {

@@ -90,6 +90,8 @@ inline int pc_blocks(int n) { return ceil_div(n, kBlock); }
 
 // Process-wide count of kernel launches issued by the launch_* functions.
 void count_launches(long long k);
+// Sets the calling thread's error message (bem_last_error).
+void set_error(const char *msg);
 long long launches();
 
 // Device-memory cache for meshes, solvers and point buffers.  Released blocks
@@ -186,6 +188,10 @@ void proj_batch_finish(ProjBatch &t);
 // potential and gradient at the points.
 cudaError_t launch_fields(const ProjBatch &t, cudaStream_t st);
 cudaError_t launch_project(const ProjBatch &t, int prec, cudaStream_t st);
+// The right-hand sides (systems 0 .. B-1, 2 <= B <= 8) of one complex64
+// solver: kernel evaluations shared between them (falls back to
+// launch_project when they do not share mesh, points and slicing).
+cudaError_t launch_project_multi(const ProjBatch &t, cudaStream_t st);
 
 // ---------------------------------------------------------------- preconditioner
 struct PcSys {

@@ -1351,6 +1351,186 @@ __global__ void __launch_bounds__(256, 2) k_project_pts(const __grid_constant__ 
     if (err != kDevOk && lane == 0) atomicMax(S.status, err);
 }
 
+// Several right-hand sides of one matrix (bem_solve_multi): systems
+// 0 .. nr-1 of the batch share the mesh, the points and the slicing and
+// differ in their element data.  The pass over (32-point group, element
+// slice) items is the one of k_project_pts, but a far flat triangle whose
+// elements carry no velocity term in any right-hand side is evaluated once
+// (P, U, T of proj_tri_points, independent of phi) and applied to every
+// right-hand side's phi: the kernel evaluations, which dominate, are shared,
+// and each right-hand side adds 4 complex multiply-adds per element.  Other
+// pairs (velocity terms, quadrilaterals, subdivided near pairs) are evaluated
+// per right-hand side as in k_project_pts.  Each right-hand side's partial
+// sums go to its own scratch; k_project_sum finishes them.
+// acc[r] += a with every index known at compile time (a runtime index
+// would put the accumulators in local memory)
+template <int RMAX>
+__device__ __forceinline__ void acc_add(ProjAcc<float> (&acc)[RMAX], int r, const ProjAcc<float> &a) {
+#pragma unroll
+    for (int q = 0; q < RMAX; ++q)
+        if (q == r) {
+            acc[q].p += a.p;
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk) acc[q].g[kk] += a.g[kk];
+        }
+}
+
+template <int RMAX>
+__global__ void __launch_bounds__(256, RMAX <= 4 ? 2 : 1) k_project_pts_multi(const __grid_constant__ ProjBatch tb, int nr) {
+    __shared__ WarpScratch ws_all[8];
+    const ProjSys &S = tb.sys[0];
+    const DevMesh m = to_dev(S.m);
+    const DevFreq &f = S.f;
+    const int lane = threadIdx.x, w = threadIdx.y, n = m.n, npts = S.npts;
+    const int G = (npts + 31) >> 5, nsl = S.nslice;
+    const int item = blockIdx.x * 8 + w;
+    if (item >= G * nsl) return;
+    const int g = item % G, sl = item / G;
+    const int per = (n + nsl - 1) / nsl;
+    const int j0 = sl * per, j1 = min(n, j0 + per);
+    const int p = g * 32 + lane;
+    const bool pv = p < npts;
+    const int pp = pv ? p : g * 32;
+    WarpScratch &ws = ws_all[w];
+    float xhi[3], xlo[3];
+    for (int c = 0; c < 3; ++c) {
+        const double xv = S.pts[3 * pp + c];
+        xhi[c] = (float)xv;
+        xlo[c] = (float)(xv - (double)xhi[c]);
+        asm volatile("" : "+f"(xhi[c]), "+f"(xlo[c]));
+    }
+    ProjAcc<float> acc[RMAX];
+#pragma unroll
+    for (int r = 0; r < RMAX; ++r) acc[r].p = acc[r].g[0] = acc[r].g[1] = acc[r].g[2] = cmk(0.f, 0.f);
+    float k = (float)f.k, wr = (float)f.wr;
+    asm volatile("" : "+f"(k), "+f"(wr));
+    const float k2 = k * k;
+    int err = kDevOk;
+    for (int kref = 0; kref < m.sym.nref; ++kref) {
+        const DevMesh mk = image_mesh(m, kref);
+        const bool neg = image_negated(m, kref);
+        for (int j = j0; j < j1; ++j) {
+            bool iv_any = false;
+#pragma unroll
+            for (int r = 0; r < RMAX; ++r)
+                if (r < nr && tb.sys[r].ivi[j] != 0) iv_any = true;
+            const int nv = m.nvert[j];
+            Elem32 e;
+            load_elem32(mk, j, xhi, xlo, e);
+            const float isq = m.isqa32[j];
+            const float q2 = (e.D[0] * e.D[0] + e.D[1] * e.D[1] + e.D[2] * e.D[2]) * (isq * isq);
+            bool near = false;
+            int order = 2;
+            if (q2 <= c_quad.far2_sq && !classify_fast(sqrtf(q2), near, order)) {
+                const double xp[3] = {S.pts[3 * pp], S.pts[3 * pp + 1], S.pts[3 * pp + 2]};
+                const double rd = ratio0_exact(mk, j, xp);
+                near = rd < kTolf;
+                if (!near) order = gauss_order(rd);
+            }
+            if (!near && e.nv == 3 && !iv_any) {
+                float2 P = make_float2(0.f, 0.f), U[3], Tn = make_float2(0.f, 0.f);
+                U[0] = U[1] = U[2] = make_float2(0.f, 0.f);
+                const float dny = e.D[0] * e.n[0] + e.D[1] * e.n[1] + e.D[2] * e.n[2];
+                if (order <= 2) proj_tri_points<4, 0>(e, dny, k2, wr, P, U, Tn);
+                else if (order == 3) proj_tri_points<7, 4>(e, dny, k2, wr, P, U, Tn);
+                else proj_tri_points<13, 11>(e, dny, k2, wr, P, U, Tn);
+                cplx<float> gk[3];
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk) gk[kk] = cplx<float>{fmaf(Tn.x, e.n[kk], U[kk].x), fmaf(Tn.y, e.n[kk], U[kk].y)};
+#pragma unroll
+                for (int r = 0; r < RMAX; ++r) {
+                    if (r >= nr) break;
+                    const float2 p2 = ((const float2 *)tb.sys[r].phi32)[j];
+                    const cplx<float> ph = neg ? cplx<float>{-p2.x, -p2.y} : cplx<float>{p2.x, p2.y};
+                    const cplx<float> pq = ph * cplx<float>{P.x, P.y};
+                    acc[r].p.re += pq.re;
+                    acc[r].p.im += pq.im;
+#pragma unroll
+                    for (int kk = 0; kk < 3; ++kk) {
+                        const cplx<float> gg = ph * gk[kk];
+                        acc[r].g[kk].re += gg.re;
+                        acc[r].g[kk].im += gg.im;
+                    }
+                }
+            } else if (!near) {
+                const int np = e.nv == 3 ? tri_count(order) : quad_count(order);
+#pragma unroll 1
+                for (int r = 0; r < RMAX; ++r) {
+                    if (r >= nr) break;
+                    const ProjSys &Sr = tb.sys[r];
+                    const bool iv = Sr.ivi[j] != 0;
+                    cplx<float> ph, vl[4];
+                    proj_elem_data<float>((const double2 *)Sr.phi, (const double2 *)Sr.vel, (const float2 *)Sr.phi32,
+                                          (const float2 *)Sr.vel32, n, j, nv, iv, kref, neg, ph, vl);
+                    ProjAcc<float> tmp;
+                    tmp.p = tmp.g[0] = tmp.g[1] = tmp.g[2] = cmk(0.f, 0.f);
+                    for (int gq = 0; gq < np; ++gq) {
+                        float s, t, wq;
+                        if (e.nv == 3) {
+                            const int o = tri_offset(order) + gq;
+                            s = c_trif[o][0]; t = c_trif[o][1]; wq = c_trif[o][2];
+                        } else {
+                            const int a = gq / order, b = gq - a * order;
+                            s = c_glxf[order][a]; t = c_glxf[order][b];
+                            wq = c_glwf[order][a] * c_glwf[order][b];
+                        }
+                        QPoint<float> q;
+                        map_point(e, s, t, wq, q);
+                        proj_point(q, ph, vl, e.nv, iv, k, wr, tmp);
+                    }
+                    acc_add<RMAX>(acc, r, tmp);
+                }
+            }
+            // near pairs: the whole warp subdivides for one lane's point at a
+            // time, once per right-hand side
+            unsigned todo = __ballot_sync(0xffffffffu, pv && near);
+            if (todo) {
+                Elem64 e64;
+                load_elem64(mk, j, e64);
+                while (todo) {
+                    const int L = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    double xl[3];
+                    float lh[3], ll[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        xl[c] = S.pts[3 * (g * 32 + L) + c];
+                        lh[c] = __shfl_sync(0xffffffffu, xhi[c], L);
+                        ll[c] = __shfl_sync(0xffffffffu, xlo[c], L);
+                    }
+                    Elem32 e32;
+                    load_elem32(mk, j, lh, ll, e32);
+#pragma unroll 1
+                    for (int r = 0; r < RMAX; ++r) {
+                        if (r >= nr) break;
+                        const ProjSys &Sr = tb.sys[r];
+                        const bool iv = Sr.ivi[j] != 0;
+                        cplx<float> phn, vln[4];
+                        proj_elem_data<float>((const double2 *)Sr.phi, (const double2 *)Sr.vel,
+                                              (const float2 *)Sr.phi32, (const float2 *)Sr.vel32, n, j, nv, true, kref,
+                                              neg, phn, vln);
+                        ProjSink<float> sink;
+                        sink.e = &e32; sink.phi = phn; sink.vel = vln; sink.ivi = iv; sink.k = k; sink.wr = wr;
+                        sink.init();
+                        const int rc = warp_subdivide(e64, m.area64[j], xl, ws, sink, &e32, isq);
+                        if (rc != kDevOk) err = rc;
+                        const ProjAcc<float> rs = sink.reduce();
+                        if (lane == L) acc_add<RMAX>(acc, r, rs);
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < RMAX; ++r) {
+        if (r >= nr) break;
+        float4 *out = tb.sys[r].part + 2 * ((size_t)(sl * G + g) * 32 + lane);
+        out[0] = make_float4(acc[r].p.re, acc[r].p.im, acc[r].g[0].re, acc[r].g[0].im);
+        out[1] = make_float4(acc[r].g[1].re, acc[r].g[1].im, acc[r].g[2].re, acc[r].g[2].im);
+    }
+    if (err != kDevOk && lane == 0) atomicMax(S.status, err);
+}
+
 // Thread per point: the slices' partial sums in slice order (FP64), then the
 // point's tau factor and incident field.
 __global__ void __launch_bounds__(256) k_project_sum(const __grid_constant__ ProjBatch tb) {
@@ -1622,6 +1802,25 @@ cudaError_t launch_fields(const ProjBatch &t, cudaStream_t st) {
     if (t.B <= 0 || t.fld_off[t.B] == 0) return cudaSuccess;
     count_launches(1);
     k_fields<<<t.fld_off[t.B], 256, 0, st>>>(t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_project_multi(const ProjBatch &t, cudaStream_t st) {
+    // the right-hand sides of one solver: same mesh, points and slicing
+    bool shared = t.B >= 2 && t.B <= 8 && t.sys[0].nslice > 0;
+    for (int b = 1; b < t.B && shared; ++b)
+        shared = t.sys[b].npts == t.sys[0].npts && t.sys[b].pts == t.sys[0].pts &&
+                 t.sys[b].nslice == t.sys[0].nslice && t.sys[b].m.n == t.sys[0].m.n;
+    if (!shared) return launch_project(t, 1, st);
+    if (t.sys[0].npts == 0) return cudaSuccess;
+    dim3 block(32, 8);
+    const int items = ((t.sys[0].npts + 31) / 32) * t.sys[0].nslice;
+    const int grid = (items + 7) / 8;
+    count_launches(2);
+    if (t.B <= 2) k_project_pts_multi<2><<<grid, block, 0, st>>>(t, t.B);
+    else if (t.B <= 4) k_project_pts_multi<4><<<grid, block, 0, st>>>(t, t.B);
+    else k_project_pts_multi<8><<<grid, block, 0, st>>>(t, t.B);
+    k_project_sum<<<t.ps_off[t.B], 256, 0, st>>>(t);
     return cudaGetLastError();
 }
 

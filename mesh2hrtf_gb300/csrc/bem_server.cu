@@ -300,6 +300,7 @@ void bem_server_s::run() {
                 }
                 s->have_precond = pc_st == 0;
                 s->have_freq = true;
+                s->factored = false;
                 r->t_join = Clock::now();
                 active.push_back(r);
                 states.push_back(s->kinit());

@@ -116,6 +116,7 @@ struct bem_solver_s {
     double *src_extra = nullptr;
     bem::DevFreq freq{};
     bool have_freq = false;
+    bool factored = false;    // A holds LU factors (bem_solve_direct) until the next assembly
     bool solved = false;
     double *pts = nullptr, *pot = nullptr, *grad = nullptr;
     int pts_cap = 0;

@@ -334,7 +334,11 @@ int run(int istart, int iend, bool estimate_ram, bool check_normals, int niterma
         // 500 matrix-vector products; GMRES spends one product per iteration
         lim.max_iter = nitermax_given ? nitermax : 500;
         bool limited = false;
-        if (nitermax_given && nitermax <= 0) {
+        if (p.solver == 4) {
+            // ISOLVER 4: the direct solver alone, no CGS line (NC_Main.cpp:833-866)
+            st = bem_solve_direct(gpu.solver, &info);
+            if (st != BEM_OK) gpu_fail(out, "direct solve", st);
+        } else if (nitermax_given && nitermax <= 0) {
             limited = true;
             info.iterations = 0;
             info.rel_residual = 1.0;
@@ -348,17 +352,15 @@ int run(int istart, int iend, bool estimate_ram, bool check_normals, int niterma
             std::cout << "Warning: Maximum number of iterations is reached!\n" << std::endl;
             out << "Warning: Maximum number of iterations is reached!\n" << std::endl;
         }
-        out << "\nCGS solver: number of iterations = " << info.iterations << ", relative error = "
-            << info.rel_residual << std::endl;
+        if (p.solver != 4)
+            out << "\nCGS solver: number of iterations = " << info.iterations << ", relative error = "
+                << info.rel_residual << std::endl;
         if (limited) {
-            // NumCalc falls back to a direct solve here (NC_CommonFunctions.cpp:1181-1191);
-            // the GPU path continues GMRES without the limit instead.
-            std::cout << "Iteration limit reached, GMRES continues without the limit!\n" << std::endl;
-            out << "Iteration limit reached, GMRES continues without the limit!\n" << std::endl;
-            lim.max_iter = 100000;
-            bem_solver_set_params(gpu.solver, &lim);
-            st = bem_solve(gpu.solver, &info);
-            if (st != BEM_OK) gpu_fail(out, "solve", st);
+            // as NumCalc after a failed CGS (NC_CommonFunctions.cpp:1181-1191)
+            std::cout << "Iteration method CGS failed, direct method is used!\n" << std::endl;
+            out << "Iteration method CGS failed, direct method is used!\n" << std::endl;
+            st = bem_solve_direct(gpu.solver, &info);
+            if (st != BEM_OK) gpu_fail(out, "direct solve", st);
         }
         st = bem_get_solution(gpu.solver, reinterpret_cast<double *>(x.data()));
         if (st != BEM_OK) gpu_fail(out, "solution", st);

@@ -29,9 +29,10 @@ SEED_STREAM = 20261206
 SEED_HEAD = 20261204
 
 
-def head_workload(seed=SEED_HEAD):
-    """(nodes, elems, source, points, frequencies in a seeded order)."""
-    v, f, info = meshes.head_like(32, seed=seed)
+def head_workload(seed=SEED_HEAD, mesh_n=32):
+    """(nodes, elems, source, points, frequencies in a seeded order); mesh_n
+    = 32 gives the 20480-triangle mesh (20 mesh_n^2 triangles)."""
+    v, f, info = meshes.head_like(mesh_n, seed=seed)
     pts = meshes.equal_angle_grid(1.2, 5.0, 24)
     freqs = np.arange(1, 201) * 100.0
     order = np.random.default_rng(seed).permutation(len(freqs))

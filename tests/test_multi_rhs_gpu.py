@@ -54,3 +54,40 @@ def test_multi_rhs_footprint_and_limit():
     fr = [workloads.frequency(capi, len(f), 1000.0, [1.0, 0, 0])] * 3
     with pytest.raises(capi.BemError):
         s.solve_multi(fr, np.zeros((0, 3)))
+
+
+def test_multi_rhs_projection_shares_kernel_evaluations():
+    """Mixed precision projects all right-hand sides in one pass that
+    evaluates each far flat-triangle kernel once (k_project_pts_multi); pairs
+    with velocity terms (a vibrating patch in one right-hand side) and
+    subdivided near pairs (points 1 mm off the surface) take the per-right-
+    hand-side path.  Each field equals the single-right-hand-side solve's to
+    the solutions' own agreement (1e-7 relative, 1e-6 for near points)."""
+    v, f = meshes.perturbed_ellipsoid(6, 78)   # 720 triangles
+    n = len(f)
+    m = capi.Mesh(v, f)
+    far = meshes.random_sphere_points(48, 1.2, 5)
+    near = np.array([meshes.surface_point_with_normal(v, f, 300 + q) for q in range(6)])
+    pts = np.vstack([far, near])
+    k = 2 * np.pi * 5000.0 / workloads.C0
+    amp = 0.1 / (1j * workloads.RHO * 2 * np.pi * 5000.0)
+    srcs = [meshes.surface_point_with_normal(v, f, 200 + r) * 1.5 for r in range(3)]
+    bcv = np.zeros((n, 4), np.complex128)
+    bcv[:12, :3] = 1e-4 + 2e-5j
+    freqs = [capi.Frequency(k, n, point_sources=srcs[0], point_amps=[amp]),
+             capi.Frequency(k, n, bc_value=bcv, point_sources=srcs[1], point_amps=[amp]),
+             capi.Frequency(k, n, plane_dirs=[0.0, 0.6, 0.8], plane_amps=[amp])]
+    s = capi.Solver(m, precision=capi.PREC_MIXED, tol=1e-10, n_rhs=3)
+    xs, pots, grads, infos = s.solve_multi(freqs, pts)
+    one = capi.Solver(m, precision=capi.PREC_MIXED, tol=1e-10)
+    for r in range(3):
+        x0, p0, g0 = one.solve_frequency(freqs[r], pts)
+        assert np.linalg.norm(xs[r] - x0) <= 1e-7 * np.linalg.norm(x0)
+        nf = len(far)
+        assert np.linalg.norm(pots[r][:nf] - p0[:nf]) <= 1e-7 * np.linalg.norm(p0[:nf])
+        assert np.linalg.norm(grads[r][:nf] - g0[:nf]) <= 1e-7 * np.linalg.norm(g0[:nf])
+        assert np.linalg.norm(pots[r][nf:] - p0[nf:]) <= 1e-6 * np.linalg.norm(p0[nf:])
+        assert np.linalg.norm(grads[r][nf:] - g0[nf:]) <= 1e-6 * np.linalg.norm(g0[nf:])
+    s.close()
+    one.close()
+    m.close()

@@ -67,7 +67,9 @@ def test_nitermax_reports_limit(numcalc, tmp_path, nitermax):
     out = open(os.path.join(wd, "NC.out")).read()
     assert "CGS solver: number of iterations = %d" % nitermax in out
     assert "Warning: Maximum number of iterations is reached!" in out
-    # the step still ends with a converged solution
+    # then, as NumCalc (NC_CommonFunctions.cpp:1181-1191), the direct solver
+    assert "Iteration method CGS failed, direct method is used!" in out
+    # the step still ends with the system's solution
     ids, vals = project.read_result(os.path.join(wd, "be.out", "be.1", "pEvalGrid"))
     assert gc.rel_err(vals, c["s1_pEvalGrid"]) < 1e-5
 
