@@ -479,6 +479,7 @@ def main():
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "wall_s": wall,
+        "tuned": capi.tune_info(n, capi.PREC_MIXED, 1),
     }
 
     if rank == 0:

@@ -146,6 +146,20 @@ int64_t bem_kernel_launches(void);
  * they are the denominators of the compute-bound stages' rooflines.
  * Diagnostic with no counterpart in the reference.  Sets the device. */
 bem_status bem_measure_issue_peaks(int32_t device, double *rates);
+/* The launch shapes the tuner holds for a system size, precision and
+ * right-hand-side count on the current device, as a JSON object written to
+ * buf (len bytes): the assembly's persistent grids (k_far / k_near resident
+ * blocks per SM), the complex64 product's strip height (rows per work item),
+ * whether each was tuned, the time of the chosen candidate, and the
+ * defaults.  The library times the candidates with CUDA events on the first
+ * assembly and the first solve of each (device model, size bucket,
+ * precision, right-hand sides), keeps the fastest in memory and appends it
+ * to a cache file ($BEM_GB300_TUNE_CACHE, else
+ * $XDG_CACHE_HOME/mesh2hrtf_gb300/tune.txt, else
+ * ~/.cache/mesh2hrtf_gb300/tune.txt); BEM_GB300_TUNE=0 keeps the defaults.
+ * Only shapes that leave every result bit unchanged are tuned.  No
+ * counterpart in the reference. */
+bem_status bem_tune_info(int32_t n_elem, int32_t precision, int32_t n_rhs, char *buf, int32_t len);
 /* Select the CUDA device for this thread's subsequent calls. */
 bem_status bem_set_device(int32_t device);
 /* Bytes a solver for n_elem unknowns holds on the device (matrix, Krylov

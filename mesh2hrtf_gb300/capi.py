@@ -34,7 +34,7 @@ EXPORTED = [
     "bem_solve_frequency", "bem_project_static", "bem_solve_batch", "bem_solve_multi", "bem_footprint_multi",
     "bem_server_create", "bem_server_submit", "bem_server_wait", "bem_server_destroy",
     "bem_mesh_footprint_bytes", "bem_device_memory", "bem_release_cached_memory", "bem_measure_issue_peaks",
-    "bem_solve_direct",
+    "bem_solve_direct", "bem_tune_info",
 ]
 STATIC_MAX_ELEMENTS = 32768
 
@@ -133,6 +133,7 @@ def load(build_if_missing: bool = True):
     lib.bem_server_destroy.argtypes = [vp]
     lib.bem_measure_issue_peaks.argtypes = [i32, dp]
     lib.bem_solve_direct.argtypes = [vp, C.POINTER(SolveInfo)]
+    lib.bem_tune_info.argtypes = [i32, i32, i32, C.c_char_p, i32]
     for name in EXPORTED:
         if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes", "bem_footprint_multi",
                         "bem_kernel_launches", "bem_mesh_footprint_bytes"):
@@ -409,6 +410,15 @@ def issue_peaks(device=0):
     r = np.zeros(3)
     _check(load().bem_measure_issue_peaks(device, r.ctypes.data_as(C.POINTER(C.c_double))))
     return {"fp32_fma_per_s": float(r[0]), "sfu_per_s": float(r[1]), "fp64_fma_per_s": float(r[2])}
+
+
+def tune_info(n_elem, precision=PREC_MIXED, n_rhs=1):
+    """bem_tune_info: the launch shapes the tuner holds for this key (dict)."""
+    import json
+
+    buf = C.create_string_buffer(1024)
+    _check(load().bem_tune_info(n_elem, precision, n_rhs, buf, len(buf)))
+    return json.loads(buf.value.decode())
 
 
 def footprint_bytes(n_elem, precision=PREC_MIXED, restart=0):

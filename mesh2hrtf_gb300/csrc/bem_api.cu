@@ -488,10 +488,61 @@ namespace bem {
 
 // ---- group operations shared by the single-solver and batched entry points
 
+// The assembly's launch shape for a group: the tuned choice for its largest
+// system.  On the first assembly of an untuned key every candidate shape
+// assembles the group once (each run writes the same bits), timed with CUDA
+// events, and the fastest is kept.
+bem_status tuned_asm_shape(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned *ctr, bem::AsmShape *out) {
+    const int prec = ss[0]->prec;
+    int big = 0;
+    for (int i = 1; i < cnt; ++i)
+        if (ss[i]->n > ss[big]->n) big = i;
+    const bem::TuneChoice tc = bem::tune_lookup(ss[big]->n, prec, ss[big]->n_rhs);
+    *out = tc.asm_shape;
+    if (!bem::tune_enabled() || tc.asm_tuned) return BEM_OK;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    for (auto &e : ev) CU(cudaEventCreate(&e));
+    std::unique_ptr<bem::AsmBatch> t(new bem::AsmBatch());
+    float best = 1e30f;
+    bem::AsmShape pick = tc.asm_shape;
+    cudaError_t err = cudaSuccess;
+    for (int fa = 1; fa <= bem::kFarPerSmMax && err == cudaSuccess; ++fa) {
+        for (int ne = 1; ne <= 2 && err == cudaSuccess; ++ne) {
+            bem::AsmShape sh;
+            sh.far_per_sm = fa;
+            sh.near_per_sm = ne;
+            err = cudaEventRecord(ev[0], st);
+            for (int c0 = 0; c0 < cnt && err == cudaSuccess; c0 += bem::kMaxAsm) {
+                const int k = std::min(bem::kMaxAsm, cnt - c0);
+                t->B = k;
+                for (int i = 0; i < k; ++i) t->sys[i] = ss[c0 + i]->asys();
+                bem::asm_batch_finish(*t);
+                err = bem::launch_assemble(*t, prec, ctr, st, sh);
+            }
+            if (err == cudaSuccess) err = cudaEventRecord(ev[1], st);
+            if (err == cudaSuccess) err = cudaEventSynchronize(ev[1]);
+            float ms = 0.f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            if (err == cudaSuccess && ms < best) {
+                best = ms;
+                pick = sh;
+            }
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    CU(err);
+    bem::tune_store_asm(ss[big]->n, prec, ss[big]->n_rhs, pick, best);
+    *out = pick;
+    return BEM_OK;
+}
+
 bem_status assemble_group(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned *ctr, cudaEvent_t e0,
                           cudaEvent_t e1, bem_status *rcs) {
     const int prec = ss[0]->prec;
     for (int i = 0; i < cnt; ++i) CU(cudaMemsetAsync(ss[i]->d.status, 0, sizeof(int), st));
+    bem::AsmShape shape;
+    bem_status trc = tuned_asm_shape(ss, cnt, st, ctr, &shape);
+    if (trc != BEM_OK) return trc;
     CU(cudaEventRecord(e0, st));
     std::unique_ptr<bem::AsmBatch> t(new bem::AsmBatch());
     for (int c0 = 0; c0 < cnt; c0 += bem::kMaxAsm) {
@@ -499,7 +550,7 @@ bem_status assemble_group(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned *
         t->B = k;
         for (int i = 0; i < k; ++i) t->sys[i] = ss[c0 + i]->asys();
         bem::asm_batch_finish(*t);
-        CU(bem::launch_assemble(*t, prec, ctr, st));
+        CU(bem::launch_assemble(*t, prec, ctr, st, shape));
         CU(bem::launch_rhs(*t, st));
     }
     CU(cudaEventRecord(e1, st));
@@ -585,10 +636,46 @@ bem_status precond_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
 
 // Restarted GMRES of every solver in ss on the engine: preconditioner set-up,
 // then iteration bodies until every system has finished.
+// The complex64 product's strip height of every solver in ss: the tuned
+// choice of its key; on the first solve of an untuned key every candidate
+// height times one product of that system (the products write only scratch
+// partials, and every height gives the same partials).
+bem_status tuned_strips(bem_solver_t *ss, int cnt, bem::Engine *eng) {
+    for (int i = 0; i < cnt; ++i) {
+        bem_solver_t s = ss[i];
+        if (s->prec != BEM_PREC_MIXED || s->n_rhs > 1) continue;   // grouped products have fixed strips
+        const bem::TuneChoice tc = bem::tune_lookup(s->n, s->prec, 1);
+        s->mv_strip = tc.mv_strip;
+        if (!bem::tune_enabled() || tc.mv_tuned) continue;
+        static const int kCand[4] = {16, 32, 64, 128};
+        float best = 1e30f;
+        int pick = tc.mv_strip;
+        for (int c : kCand) {
+            s->mv_strip = c;
+            float ms = 0.f;
+            const cudaError_t e = eng->time_product(s->ksys(), &ms);
+            if (e == cudaErrorLaunchTimeout)
+                return fail(BEM_ERR_DEVICE_TIMEOUT, "matrix-vector product: a bounded device wait gave up");
+            CU(e);
+            if (ms < best) {
+                best = ms;
+                pick = c;
+            }
+        }
+        bem::tune_store_mv(s->n, s->prec, 1, pick, best);
+        for (int j = i; j < cnt; ++j)   // the same key further on
+            if (ss[j]->prec == s->prec && ss[j]->n_rhs <= 1 && bem::tune_bucket(ss[j]->n) == bem::tune_bucket(s->n))
+                ss[j]->mv_strip = pick;
+    }
+    return BEM_OK;
+}
+
 bem_status solve_group(bem_solver_t *ss, int cnt, bem::Engine *eng, cudaStream_t st, cudaEvent_t e0,
                        cudaEvent_t e1, bem_status *rcs) {
     CU(cudaEventRecord(e0, st));
     bem_status prc = precond_group(ss, cnt, st);
+    if (prc != BEM_OK) return prc;
+    prc = tuned_strips(ss, cnt, eng);
     if (prc != BEM_OK) return prc;
     bem_status first = BEM_OK;
     for (int c0 = 0; c0 < cnt; c0 += bem::kMaxSys) {

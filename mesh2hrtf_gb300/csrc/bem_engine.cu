@@ -5,11 +5,47 @@
 #include <cstdlib>
 #include <cstring>
 
+#include <cudaTypedefs.h>
+
 #include "bem_engine.h"
 
 namespace bem {
 
 namespace {
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// TMA map of a complex64 matrix viewed as n rows of 2 n floats (row pitch
+// 2 lda floats): boxes of 32 floats x kUmRows rows with the 128-byte swizzle,
+// zeros outside the matrix
+bool encode_group_map(CUtensorMap *map, const void *A, int n, long long lda) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)(2 * (long long)n), (cuuint64_t)n};
+    cuuint64_t strides[1] = {(cuuint64_t)(2 * lda * 4)};
+    cuuint32_t box[2] = {32, (cuuint32_t)kUmRows};
+    cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(A), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // BEM_GB300_TEST_WAIT_CYCLES: a bound (clock cycles) for the products'
 // mbarrier waits in place of the default of about 2 s.  Only for tests that
 // make a wait run out; read whenever a batch is set up.
@@ -23,7 +59,8 @@ long long test_wait_cycles() {
 
 Engine::~Engine() {
     if (st_) cudaStreamSynchronize(st_);
-    if (exec_) cudaGraphExecDestroy(exec_);
+    for (auto &x : exec_)
+        if (x) cudaGraphExecDestroy(x);
     for (auto &e : ev_)
         if (e) cudaEventDestroy(e);
     cudaFree(d_tab_);
@@ -106,6 +143,15 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
         b = e;
     }
     h_tab_->n_groups = ng;
+    groups_ = ng;
+    // the groups' Krylov products on the 5th-generation tensor cores need a
+    // TMA map of each group's matrix; without them the warp-level kernel runs
+    bool umma = ng > 0 && group_product_umma();
+    for (int q = 0; q < ng && umma; ++q) {
+        const KSys &g0 = h_tab_->sys[h_tab_->grp[q].first];
+        umma = encode_group_map(&h_tab_->gmap[q], g0.A, g0.n, g0.lda);
+    }
+    h_tab_->grp_umma = umma ? 1 : 0;
     e = cudaMemcpyAsync(d_tab_, h_tab_, sizeof(KTable), cudaMemcpyHostToDevice, st_);
     if (e == cudaSuccess && B > 0)
         e = cudaMemcpyAsync(d_st_, h_st_, sizeof(KState) * B, cudaMemcpyHostToDevice, st_);
@@ -118,31 +164,69 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
     return e;
 }
 
+cudaError_t Engine::time_product(const KSys &sys, float *ms) {
+    cudaError_t e = ensure_init();
+    if (e != cudaSuccess) return e;
+    std::memset(h_tab_, 0, sizeof(KTable));
+    h_tab_->B = 1;
+    h_tab_->prec = prec_;
+    h_tab_->vb_total = sys.nvb;
+    h_tab_->wait_cycles = test_wait_cycles();
+    h_tab_->sys[0] = sys;
+    h_tab_->sys[0].st = d_st_;
+    h_tab_->sys[0].shared = 0;
+    const int strip = sys.strip > 0 ? sys.strip : kTmaStrip;
+    KPlan &p = h_tab_->plan[0];
+    p.n = 1;
+    p.sys[0] = 0;
+    p.off[0] = 0;
+    p.off[1] = sys.A16 ? mv_items16(sys.n, strip) : mv_items_of(sys.n, prec_, strip);
+    e = cudaMemcpyAsync(d_tab_, h_tab_, sizeof(KTable), cudaMemcpyHostToDevice, st_);
+    float best = 1e30f;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+        e = cudaEventRecord(ev_[0], st_);
+        if (e == cudaSuccess) e = launch_product(d_tab_, prec_, st_);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_[1], st_);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev_[1]);
+        float t = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev_[0], ev_[1]);
+        if (e == cudaSuccess && rep > 0 && t < best) best = t;
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h_tab_->err, &d_tab_->err, sizeof(int), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e == cudaSuccess && h_tab_->err) e = cudaErrorLaunchTimeout;
+    count_launches(3);
+    *ms = best;
+    B_ = 0;   // the table no longer holds a batch
+    return e;
+}
+
 cudaError_t Engine::run_body() {
     cudaError_t e = ensure_init();
     if (e != cudaSuccess) return e;
-    if (!exec_) {
+    const int v = groups_ > 0 ? 1 : 0;
+    if (!exec_[v]) {
         cudaGraph_t g = nullptr;
         e = cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
-        cudaError_t le = launch_krylov_body(prec_, d_tab_, ev_, st_, &body_launches_);
+        cudaError_t le = launch_krylov_body(prec_, d_tab_, ev_, st_, &body_launches_[v], v == 1);
         e = cudaStreamEndCapture(st_, &g);
         if (le != cudaSuccess) e = le;
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec_, g, 0);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec_[v], g, 0);
         if (g) cudaGraphDestroy(g);
         if (e != cudaSuccess) {
-            exec_ = nullptr;
+            exec_[v] = nullptr;
             return e;
         }
     }
-    e = cudaGraphLaunch(exec_, st_);
+    e = cudaGraphLaunch(exec_[v], st_);
     if (e == cudaSuccess && B_ > 0)
         e = cudaMemcpyAsync(h_st_, d_st_, sizeof(KState) * B_, cudaMemcpyDeviceToHost, st_);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&h_tab_->err, &d_tab_->err, sizeof(int), cudaMemcpyDeviceToHost, st_);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return e;
     if (h_tab_->err) return cudaErrorLaunchTimeout;   // a bounded wait in the product gave up
-    count_launches(body_launches_);
+    count_launches(body_launches_[v]);
     ++bodies_;
     if (timing_ok_) {
         for (int q = 0; q <= kSteps; ++q) {

@@ -34,6 +34,10 @@ public:
     int size() const { return B_; }
     int precision() const { return prec_; }
     cudaStream_t stream() const { return st_; }
+    // Time (ms, best of two launches after one warm-up) of one Krylov product
+    // of a complex64 system alone, with the strip height in sys.strip; for
+    // the tuner, before set_batch (it overwrites the launch table).
+    cudaError_t time_product(const KSys &sys, float *ms);
     // device time of the matrix-vector products (ms) and body replays since set_batch
     double matvec_ms() const { return mv_ms_; }
     long long bodies() const { return bodies_; }
@@ -49,8 +53,11 @@ private:
     int2 *d_items_ = nullptr;
     size_t items_cap_ = 0;
     std::vector<int2> items_;
-    cudaGraphExec_t exec_ = nullptr;
-    int body_launches_ = 0;
+    // the iteration body without and with the shared-matrix (group) products,
+    // each captured at its first replay
+    cudaGraphExec_t exec_[2] = {nullptr, nullptr};
+    int body_launches_[2] = {0, 0};
+    int groups_ = 0;   // shared-matrix groups of the current batch
     cudaEvent_t ev_[2 * (kSteps + 1)] = {};
     double mv_ms_ = 0.0;
     long long bodies_ = 0;

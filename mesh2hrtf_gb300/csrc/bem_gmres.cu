@@ -52,10 +52,13 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 #include "bem_engine.h"
 #include "bem_internal.h"
+#include "bem_umma.h"
 
 namespace bem {
 namespace {
@@ -156,8 +159,10 @@ __device__ void plan_build(KTable *tb, int which) {
     int c = 0;
     if (t < tb->B) {
         const KSys &S = tb->sys[t];
-        if (!S.shared && mv_active(S.st, which, tb->prec))
-            c = (which == 0 && S.A16) ? mv_items16(S.n) : mv_items_of(S.n, tb->prec);
+        if (!S.shared && mv_active(S.st, which, tb->prec)) {
+            const int strip = S.strip > 0 ? S.strip : kTmaStrip;
+            c = (which == 0 && S.A16) ? mv_items16(S.n, strip) : mv_items_of(S.n, tb->prec, strip);
+        }
     }
     cnt[t] = c;
     act[t] = c > 0;
@@ -175,7 +180,8 @@ __device__ void plan_build(KTable *tb, int which) {
     __shared__ int wsum[kMaxSys / 32][4];
     const int lane = t & 31, wp = t >> 5;
     const int ga = gm[t] ? 1 : 0;
-    const int gc = ga ? ceil_div(tb->sys[tb->grp[t].first].n, which == 1 ? kGrpRowsExact : kGrpRowsInner) : 0;
+    const int grows = which == 1 ? kGrpRowsExact : (which == 0 && tb->grp_umma ? kUmRows : kGrpRowsInner);
+    const int gc = ga ? ceil_div(tb->sys[tb->grp[t].first].n, grows) : 0;
     int v[4] = {act[t], cnt[t], ga, gc};
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -442,9 +448,10 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
             const int blk = local % nblk, strip = local / nblk;
             const int chunk = h ? 2 * blk : blk;                       // first chunk of the item
             const int c0 = blk * span, len = min(span, n - c0), lenp = (len + 1) & ~1;
-            const int rbase = strip * kTmaStrip;
+            const int sh = S.strip > 0 ? S.strip : kTmaStrip;   // rows per item
+            const int rbase = strip * sh;
             const int rps = kTmaRows;
-            const int nst = min(kTmaStrip / rps, (n - rbase + rps - 1) / rps);
+            const int nst = min(sh / rps, (n - rbase + rps - 1) / rps);
             // bytes per row segment: fp16 copies move whole 16-byte groups of 4 entries
             const uint32_t seg = h ? (uint32_t)(((len + 3) & ~3) * 4) : (uint32_t)(lenp * 8);
             const uint32_t pitch = kMvChunk * 8;
@@ -750,8 +757,10 @@ __global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(
     // bound of the waits (the drains of in-flight copies keep the full bound)
     const long long lim = tb->wait_cycles > 0 ? tb->wait_cycles : kWaitCycles;
     if (warp == NW) {
-        // ---------------- producer (one lane)
-        if (lane != 0) return;
+        // ---------------- producer warp: lane 0 takes the strips and keeps the
+        // barriers; lane r < ROWS issues row r's copy, the other copies (the
+        // members' x chunks) go round the lanes
+        const unsigned kAll = 0xffffffffu;
         const int total = pl.off[pl.n];
         int stage = 0;
         uint32_t eph = 1;
@@ -760,7 +769,9 @@ __global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(
         for (int q = 0; q < NS; ++q) { issued[q] = 0; fph[q] = 0; }
         bool ok = true;
         while (ok && total > 0) {
-            const int item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+            int item = 0;
+            if (lane == 0) item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+            item = __shfl_sync(kAll, item, 0);
             if (item >= total) break;
             const int j = plan_find(pl.off, pl.n, item);
             const KGroup g = tb->grp[pl.sys[j]];
@@ -771,42 +782,36 @@ __global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(
             const int nck = (n + kGrpCols - 1) / kGrpCols;
             const float2 *A = (const float2 *)S0.A;
             const size_t lda = (size_t)S0.lda;
-            // the members' x arrays, read once per strip
-            const void *xsrc[kMaxGroup];
-            int nmem = 0;
-#pragma unroll
-            for (int q = 0; q < kMaxGroup; ++q) {
-                xsrc[q] = nullptr;
-                if (q < g.count && ((mask >> q) & 1)) {
-                    xsrc[q] = EXACT ? (const void *)tb->sys[g.first + q].xf : (const void *)tb->sys[g.first + q].xh;
-                    ++nmem;
-                }
-            }
+            const int nmem = __popc(mask & ((1u << g.count) - 1u));
+            constexpr int XPER = EXACT ? 2 : 1;   // copies per member and stage
             for (int ck = 0; ck < nck && ok; ++ck) {
-                if (!mbar_wait(empty0 + 8 * stage, eph, err, lim)) { ok = false; break; }
+                int w = 1;
+                if (lane == 0) w = mbar_wait(empty0 + 8 * stage, eph, err, lim);
+                if (!__shfl_sync(kAll, w, 0)) { ok = false; break; }
                 const int c0 = ck * kGrpCols, len = min(kGrpCols, n - c0), lenp = (len + 1) & ~1;
-                GrpMeta mt;
-                mt.first = g.first; mt.chunk = ck; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
-                mt.last = ck == nck - 1; mt.mask = (int)mask; mt.pad = 0;
-                meta[stage] = mt;
                 const uint32_t xbytes = EXACT ? (uint32_t)XB : (uint32_t)(lenp * 8);
                 const uint32_t fb = full0 + 8 * stage;
-                mbar_expect_tx(fb, (uint32_t)(nrows * lenp * 8) + nmem * xbytes);
+                if (lane == 0) {
+                    GrpMeta mt;
+                    mt.first = g.first; mt.chunk = ck; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
+                    mt.last = ck == nck - 1; mt.mask = (int)mask; mt.pad = 0;
+                    meta[stage] = mt;
+                    mbar_expect_tx(fb, (uint32_t)(nrows * lenp * 8) + nmem * xbytes);
+                }
+                __syncwarp();
                 const uint32_t dst = smem_u32(smem + stage * SB);
-                const float2 *Arow = A + (size_t)row0 * lda + c0;
-                for (int r = 0; r < nrows; ++r) bulk_g2s(dst + r * kGrpCols * 8, Arow + r * lda, lenp * 8, fb);
-#pragma unroll
-                for (int q = 0; q < kMaxGroup; ++q) {
-                    if (!xsrc[q]) continue;
+                if (lane < nrows) bulk_g2s(dst + lane * kGrpCols * 8, A + (size_t)(row0 + lane) * lda + c0, lenp * 8, fb);
+                for (int t = lane; t < kMaxGroup * XPER; t += 32) {
+                    const int q = t / XPER, h = t - q * XPER;
+                    if (q >= g.count || !((mask >> q) & 1)) continue;
                     const uint32_t xd = dst + ASTAGE + q * XB;
                     if (EXACT) {
                         // chunk-permuted (hi, lo) pairs: the stage's even entries, then its odd ones
-                        const float4 *base = (const float4 *)xsrc[q] + (size_t)(c0 & ~(kMvChunk - 1));
+                        const float4 *base = (const float4 *)tb->sys[g.first + q].xf + (size_t)(c0 & ~(kMvChunk - 1));
                         const int o = (c0 & (kMvChunk - 1)) >> 1;
-                        bulk_g2s(xd, base + o, kGrpCols * 8, fb);
-                        bulk_g2s(xd + kGrpCols * 8, base + kMvChunk / 2 + o, kGrpCols * 8, fb);
+                        bulk_g2s(xd + h * kGrpCols * 8, base + h * (kMvChunk / 2) + o, kGrpCols * 8, fb);
                     } else {
-                        bulk_g2s(xd, (const float2 *)xsrc[q] + c0, lenp * 8, fb);
+                        bulk_g2s(xd, (const float2 *)tb->sys[g.first + q].xh + c0, lenp * 8, fb);
                     }
                 }
                 issued[stage] = 1;
@@ -814,22 +819,24 @@ __global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(
                 if (++stage == NS) { stage = 0; eph ^= 1; }
             }
         }
-        if (ok) {
-            if (mbar_wait(empty0 + 8 * stage, eph, err, lim)) {
-                meta[stage].first = -1;
-                mbar_arrive(full0 + 8 * stage);
-            } else {
-                ok = false;
+        if (lane == 0) {
+            if (ok) {
+                if (mbar_wait(empty0 + 8 * stage, eph, err, lim)) {
+                    meta[stage].first = -1;
+                    mbar_arrive(full0 + 8 * stage);
+                } else {
+                    ok = false;
+                }
             }
-        }
-        if (!ok)
-            for (int s = 0; s < NS; ++s)
-                if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
-        __threadfence();
-        if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
-            tb->mv_ctr[0] = 0u;
-            tb->mv_ctr[1] = 0u;
+            if (!ok)
+                for (int s = 0; s < NS; ++s)
+                    if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
             __threadfence();
+            if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
+                tb->mv_ctr[0] = 0u;
+                tb->mv_ctr[1] = 0u;
+                __threadfence();
+            }
         }
         return;
     }
@@ -991,6 +998,7 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1
 }
 
 __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb, int kind) {
+    if (kind == 0 && tb->grp_umma) return;   // k_mv_grp_umma takes the Krylov products
     extern __shared__ __align__(128) unsigned char smem[];
     double *red = reinterpret_cast<double *>(smem + kTcStages * kTcStageBytes);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcStages * kTcStageBytes + kTcRedBytes);
@@ -1014,8 +1022,11 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
     // bound of the waits (the drains of in-flight copies keep the full bound)
     const long long lim = tb->wait_cycles > 0 ? tb->wait_cycles : kWaitCycles;
     if (warp == kTcWarps) {
-        // ---------------- producer (one lane)
-        if (lane != 0) return;
+        // ---------------- producer warp: lane 0 takes the strips and keeps the
+        // barriers; lane r issues the bulk copy of row r of a stage and lanes
+        // 0 .. 7 the members' x chunks (one lane issuing all 40 copies of a
+        // stage held the product at about half the HBM bandwidth)
+        const unsigned kAll = 0xffffffffu;
         const int total = pl.off[pl.n];
         int stage = 0;
         uint32_t eph = 1;
@@ -1023,7 +1034,9 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
         uint32_t fph[kTcStages] = {0, 0};
         bool ok = true;
         while (ok && total > 0) {
-            const int item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+            int item = 0;
+            if (lane == 0) item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+            item = __shfl_sync(kAll, item, 0);
             if (item >= total) break;
             const int j = plan_find(pl.off, pl.n, item);
             const KGroup g = tb->grp[pl.sys[j]];
@@ -1034,52 +1047,50 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
             const int nck = (n + kGrpCols - 1) / kGrpCols;
             const float2 *A = (const float2 *)S0.A;
             const size_t lda = (size_t)S0.lda;
-            const float2 *xsrc[kMaxGroup];
-            int nmem = 0;
-#pragma unroll
-            for (int q = 0; q < kMaxGroup; ++q) {
-                xsrc[q] = nullptr;
-                if (q < g.count && ((mask >> q) & 1)) {
-                    xsrc[q] = tb->sys[g.first + q].xh;
-                    ++nmem;
-                }
-            }
+            // this lane's member x array (lanes 0 .. 7), and the member count
+            const float2 *xsrc = (lane < g.count && ((mask >> lane) & 1)) ? tb->sys[g.first + lane].xh : nullptr;
+            const int nmem = __popc(mask & ((1u << g.count) - 1u));
             for (int ck = 0; ck < nck && ok; ++ck) {
-                if (!mbar_wait(empty0 + 8 * stage, eph, err, lim)) { ok = false; break; }
+                int w = 1;
+                if (lane == 0) w = mbar_wait(empty0 + 8 * stage, eph, err, lim);
+                if (!__shfl_sync(kAll, w, 0)) { ok = false; break; }
                 const int c0 = ck * kGrpCols, len = min(kGrpCols, n - c0), lenp = (len + 1) & ~1;
-                GrpMeta mt;
-                mt.first = g.first; mt.chunk = ck; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
-                mt.last = ck == nck - 1; mt.mask = (int)mask; mt.pad = 0;
-                meta[stage] = mt;
                 const uint32_t fb = full0 + 8 * stage;
-                mbar_expect_tx(fb, (uint32_t)((nrows + nmem) * lenp * 8));
+                if (lane == 0) {
+                    GrpMeta mt;
+                    mt.first = g.first; mt.chunk = ck; mt.row0 = row0; mt.nrows = nrows; mt.len = len;
+                    mt.last = ck == nck - 1; mt.mask = (int)mask; mt.pad = 0;
+                    meta[stage] = mt;
+                    mbar_expect_tx(fb, (uint32_t)((nrows + nmem) * lenp * 8));
+                }
+                __syncwarp();
                 const uint32_t dst = smem_u32(smem + stage * kTcStageBytes);
-                const float2 *Arow = A + (size_t)row0 * lda + c0;
-                for (int r = 0; r < nrows; ++r) bulk_g2s(dst + r * kTcRowStride, Arow + r * lda, lenp * 8, fb);
-#pragma unroll
-                for (int q = 0; q < kMaxGroup; ++q)
-                    if (xsrc[q]) bulk_g2s(dst + kTcABytes + q * kTcXStride, xsrc[q] + c0, lenp * 8, fb);
+                if (lane < nrows)
+                    bulk_g2s(dst + lane * kTcRowStride, A + (size_t)(row0 + lane) * lda + c0, lenp * 8, fb);
+                if (xsrc) bulk_g2s(dst + kTcABytes + lane * kTcXStride, xsrc + c0, lenp * 8, fb);
                 issued[stage] = 1;
                 fph[stage] ^= 1;
                 if (++stage == kTcStages) { stage = 0; eph ^= 1; }
             }
         }
-        if (ok) {
-            if (mbar_wait(empty0 + 8 * stage, eph, err, lim)) {
-                meta[stage].first = -1;
-                mbar_arrive(full0 + 8 * stage);
-            } else {
-                ok = false;
+        if (lane == 0) {
+            if (ok) {
+                if (mbar_wait(empty0 + 8 * stage, eph, err, lim)) {
+                    meta[stage].first = -1;
+                    mbar_arrive(full0 + 8 * stage);
+                } else {
+                    ok = false;
+                }
             }
-        }
-        if (!ok)
-            for (int s = 0; s < kTcStages; ++s)
-                if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
-        __threadfence();
-        if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
-            tb->mv_ctr[0] = 0u;
-            tb->mv_ctr[1] = 0u;
+            if (!ok)
+                for (int s = 0; s < kTcStages; ++s)
+                    if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
             __threadfence();
+            if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
+                tb->mv_ctr[0] = 0u;
+                tb->mv_ctr[1] = 0u;
+                __threadfence();
+            }
         }
         return;
     }
@@ -1198,6 +1209,277 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
             rph ^= 1;
         }
         if (++stage == kTcStages) { stage = 0; fph ^= 1; }
+    }
+}
+
+
+// ------------------------------------------------------------ tcgen05 product
+// Krylov product of the shared-matrix groups on the 5th-generation tensor
+// cores.  The real-ified product Y^ = A^ X^ (A^: rows of interleaved (re, im)
+// complex64 entries, K = 2 n floats; X^: 16 columns, (re, -im) and (im, re)
+// patterns of the 8 members' x) is one tcgen05.mma.kind::tf32 chain per
+// 128-row strip: M = 128 rows (TMEM lanes), N = 16, K = 8 per instruction,
+// FP32 accumulation in TMEM.  TF32 operands carry about 3 digits, the
+// accuracy an inner GMRES cycle needs (the refinement residuals keep the
+// FP32-accurate products).
+// Warp 0: TMA producer.  A comes through the group's tensor map as two
+//   32-float x 128-row boxes per stage (128-byte swizzle, the layout the
+//   MMA's K-major descriptors read); lanes 0-7 bulk-copy the members' x chunks.
+// Warp 1: owns the TMEM allocation; lane 0 issues the MMAs and commits them
+//   to the stage's empty barrier (and, at a strip's end, to dfull).
+// Warps 2-5: build X^ of each stage in shared memory (K-major, swizzled),
+//   and after a strip's last stage read D from TMEM (warp w reads lanes
+//   32 (w mod 4) ..) and write the members' row results.
+// Every wait is bounded; on expiry the error word is set, copies and MMAs in
+// flight are drained, and TMEM is released before the block exits.
+constexpr int kUmN = 16;
+constexpr int kUmKS = 64;                                  // floats of K per stage
+constexpr int kUmStages = 4;
+constexpr int kUmASub = kUmRows * 32 * 4;                  // one 128-byte column of A: 16 KB
+constexpr int kUmABytes = 2 * kUmASub;
+constexpr int kUmBSub = kUmN * 32 * 4;                     // 2 KB
+constexpr int kUmBBytes = 2 * kUmBSub;
+constexpr int kUmXBytes = kMaxGroup * (kUmKS / 2) * 8;     // 32 complex entries per member
+constexpr int kUmStageBytes = kUmABytes + kUmBBytes + kUmXBytes;
+constexpr int kUmWarps = 6;
+constexpr int kUmSmem = kUmStages * kUmStageBytes + 1024 + 1024;
+static_assert(kUmStageBytes % 1024 == 0 && kUmABytes % 1024 == 0, "stage buffers keep the 1024-byte swizzle alignment");
+static_assert(kUmSmem <= 227 * 1024, "shared memory");
+constexpr uint32_t kUmIdesc = umma::instr_desc(umma::kDF32, umma::kFmtTF32, umma::kFmtTF32, kUmRows, kUmN);
+
+struct UmMeta {
+    int first, row0, nrows, k0, len, flags;   // flags: 1 first stage of a strip, 2 last
+    unsigned mask;
+    int grp;
+};
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
+}
+__device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, int acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__global__ void __launch_bounds__(32 * kUmWarps, 1) k_mv_grp_umma(KTable *tb) {
+    if (!tb->grp_umma) return;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned stage buffers (the swizzle pattern's period)
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    unsigned char *smem = smem_raw + (base - raw);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kUmStages * kUmStageBytes);
+    // bars: full[4], bready[4], empty[4], dfull, done; then the stage metadata and the TMEM address
+    UmMeta *meta = reinterpret_cast<UmMeta *>(bars + 3 * kUmStages + 2);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(meta + kUmStages);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t full0 = smem_u32(bars), bready0 = full0 + 8 * kUmStages, empty0 = bready0 + 8 * kUmStages;
+    const uint32_t dfull = empty0 + 8 * kUmStages, done = dfull + 8;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kUmStages; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(bready0 + 8 * s, 4);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(dfull, 1);
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(smem_u32(tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __shared__ PlanSmem pl;
+    plan_load(tb->gplan[0], pl);   // includes a block barrier
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    int *err = &tb->err;
+    const long long lim = tb->wait_cycles > 0 ? tb->wait_cycles : kWaitCycles;
+    const unsigned kAll = 0xffffffffu;
+
+    if (warp == 0) {
+        // ---------------- producer
+        const int total = pl.off[pl.n];
+        int stage = 0;
+        uint32_t eph = 1;
+        int issued[kUmStages] = {0, 0, 0, 0};
+        uint32_t fph[kUmStages] = {0, 0, 0, 0};
+        bool ok = true;
+        while (ok && total > 0) {
+            int item = 0;
+            if (lane == 0) item = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+            item = __shfl_sync(kAll, item, 0);
+            if (item >= total) break;
+            const int j = plan_find(pl.off, pl.n, item);
+            const int gi = pl.sys[j];
+            const KGroup g = tb->grp[gi];
+            const unsigned mask = tb->gmask[0][j] & ((1u << g.count) - 1u);
+            const int n = tb->sys[g.first].n;
+            const int row0 = (item - pl.off[j]) * kUmRows, nrows = min(kUmRows, n - row0);
+            const int nks = (2 * n + kUmKS - 1) / kUmKS;
+            const float2 *xsrc = (lane < g.count && ((mask >> lane) & 1)) ? tb->sys[g.first + lane].xh : nullptr;
+            const int nmem = __popc(mask);
+            for (int ks = 0; ks < nks && ok; ++ks) {
+                int w = 1;
+                if (lane == 0) w = mbar_wait(empty0 + 8 * stage, eph, err, lim);
+                if (!__shfl_sync(kAll, w, 0)) { ok = false; break; }
+                const int k0 = ks * kUmKS, c0 = k0 >> 1;
+                const int len = min(kUmKS / 2, n - c0), lenp = (len + 1) & ~1;
+                const uint32_t fb = full0 + 8 * stage;
+                const uint32_t sb = base + stage * kUmStageBytes;
+                if (lane == 0) {
+                    UmMeta mt;
+                    mt.first = g.first; mt.row0 = row0; mt.nrows = nrows; mt.k0 = k0; mt.len = len;
+                    mt.flags = (ks == 0 ? 1 : 0) | (ks == nks - 1 ? 2 : 0);
+                    mt.mask = mask; mt.grp = gi;
+                    meta[stage] = mt;
+                    // the map was rewritten for this batch through ordinary memory
+                    if (ks == 0)
+                        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                                         reinterpret_cast<uint64_t>(&tb->gmap[gi]))
+                                     : "memory");
+                    mbar_expect_tx(fb, (uint32_t)kUmABytes + (uint32_t)(nmem * lenp * 8));
+                    // A: two 32-float columns; x is a multiple of 32 floats
+                    // (128 bytes), rows and columns past the matrix read zeros
+                    tma_load_2d(sb, &tb->gmap[gi], k0, row0, fb);
+                    tma_load_2d(sb + kUmASub, &tb->gmap[gi], k0 + 32, row0, fb);
+                }
+                __syncwarp();
+                if (xsrc) bulk_g2s(sb + kUmABytes + kUmBBytes + lane * (kUmKS / 2) * 8, xsrc + c0, lenp * 8, fb);
+                issued[stage] = 1;
+                fph[stage] ^= 1;
+                if (++stage == kUmStages) { stage = 0; eph ^= 1; }
+            }
+        }
+        if (lane == 0) {
+            if (ok) {
+                if (mbar_wait(empty0 + 8 * stage, eph, err, lim)) {
+                    meta[stage].first = -1;
+                    mbar_arrive(full0 + 8 * stage);
+                } else {
+                    ok = false;
+                }
+            }
+            if (!ok)
+                for (int s = 0; s < kUmStages; ++s)
+                    if (issued[s]) mbar_wait(full0 + 8 * s, fph[s] ^ 1, err);
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t fph = 0;
+            while (true) {
+                if (!mbar_wait(full0 + 8 * stage, fph, err, lim)) break;
+                const UmMeta mt = meta[stage];
+                if (mt.first < 0) break;
+                if (!mbar_wait(bready0 + 8 * stage, fph, err, lim)) break;
+                tc_fence_after();
+                const uint32_t sb = base + stage * kUmStageBytes;
+#pragma unroll
+                for (int sub = 0; sub < 2; ++sub) {
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const uint64_t ad = umma::smem_desc(sb + sub * kUmASub + kk * 32, 16, 1024, umma::kLayout128B);
+                        const uint64_t bd =
+                            umma::smem_desc(sb + kUmABytes + sub * kUmBSub + kk * 32, 16, 1024, umma::kLayout128B);
+                        umma_tf32(tmem, ad, bd, kUmIdesc, ((mt.flags & 1) && sub == 0 && kk == 0) ? 0 : 1);
+                    }
+                }
+                umma_commit(empty0 + 8 * stage);   // the stage's buffers are free once these MMAs finish
+                if (mt.flags & 2) umma_commit(dfull);
+                if (++stage == kUmStages) { stage = 0; fph ^= 1; }
+            }
+            // every MMA issued has finished before TMEM is released
+            umma_commit(done);
+            mbar_wait(done, 0, err);
+        }
+        __syncwarp();
+    } else {
+        // ---------------- X^ builders and epilogue (warps 2-5)
+        const int t = threadIdx.x - 64;               // 0 .. 127
+        const int q4 = warp & 3;                       // TMEM lane quarter of this warp
+        const int brow = t >> 3, bq = brow & 7;        // B row: member bq, Re (rows 0-7) or Im (8-15)
+        const bool bim = brow >= 8;
+        const int kf0 = (t & 7) * 8;                   // this thread's 8 floats of the row
+        int stage = 0;
+        uint32_t fph = 0, dph = 0;
+        while (true) {
+            // every lane waits (each acquires the stage), and the warp leaves
+            // together if any lane gave up: the epilogue's TMEM load needs
+            // the whole warp
+            if (!__all_sync(kAll, mbar_wait(full0 + 8 * stage, fph, err, lim))) break;
+            const UmMeta mt = meta[stage];
+            if (mt.first < 0) break;
+            const uint32_t sbo = (uint32_t)stage * kUmStageBytes;
+            const float2 *xq = reinterpret_cast<const float2 *>(smem + sbo + kUmABytes + kUmBBytes) + bq * (kUmKS / 2);
+            const bool on = (mt.mask >> bq) & 1;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int kf = kf0 + e, jc = kf >> 1, part = kf & 1;
+                float v = 0.f;
+                if (on && jc < mt.len) {
+                    const float2 x = xq[jc];
+                    v = bim ? (part ? x.x : x.y) : (part ? -x.y : x.x);
+                }
+                *reinterpret_cast<float *>(smem + sbo + kUmABytes + (kf >> 5) * kUmBSub +
+                                           umma::sw128_offset(brow, kf & 31)) = v;
+            }
+            // the tensor core reads X^ through the async proxy
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bready0 + 8 * stage);
+            if (mt.flags & 2) {
+                // the strip's result: lane l of this warp holds row 32 q4 + l
+                if (!__all_sync(kAll, mbar_wait(dfull, dph, err, lim))) break;
+                dph ^= 1;
+                tc_fence_after();
+                uint32_t r[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15}, [%16];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                      "=r"(r[15])
+                    : "r"(umma::tmem_addr(tmem, 32u * q4, 0)));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                const int row = 32 * q4 + lane;
+                if (row < mt.nrows) {
+#pragma unroll
+                    for (int q = 0; q < kMaxGroup; ++q)
+                        if ((mt.mask >> q) & 1)
+                            reinterpret_cast<float2 *>(tb->sys[mt.first + q].mvp)[mt.row0 + row] =
+                                make_float2(__uint_as_float(r[q]), __uint_as_float(r[8 + q]));
+                }
+                tc_fence_before();
+            }
+            if (++stage == kUmStages) { stage = 0; fph ^= 1; }
+        }
+    }
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem) : "memory");
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
+            tb->mv_ctr[0] = 0u;
+            tb->mv_ctr[1] = 0u;
+            __threadfence();
+        }
     }
 }
 
@@ -2026,6 +2308,8 @@ cudaError_t krylov_prepare() {
                                        grp_smem_bytes(true));
         if (err == cudaSuccess)
             err = cudaFuncSetAttribute(k_mv_grp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k_mv_grp_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmSmem);
         g_mv_grid[1] = sms;   // one bulk-copy block per SM
         if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mv64<false>, 256, 0);
         g_mv_grid[0] = sms * (per > 0 ? per : 1);
@@ -2040,6 +2324,19 @@ cudaError_t krylov_prepare() {
         g_pcw_grid = sms * (per > 0 ? per : 1);
     });
     return err;
+}
+
+bool group_product_umma() {
+    const char *v = std::getenv("BEM_GB300_GROUP_PRODUCT");
+    return v && std::strcmp(v, "tcgen05") == 0;
+}
+
+cudaError_t launch_product(KTable *d_tab, int prec, cudaStream_t st) {
+    if (!g_vec_grid) return cudaErrorNotReady;   // krylov_prepare() first
+    constexpr int kTmaThreads = 32 * (kTmaConsumers + 1);
+    if (prec == 0) k_mv64<false><<<g_mv_grid[0], 256, 0, st>>>(d_tab, 0);
+    else k_mv_tma<false><<<g_mv_grid[1], kTmaThreads, tma_smem_bytes(false), st>>>(d_tab, 0);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_plans(KTable *d_tab, cudaStream_t st) {
@@ -2060,7 +2357,7 @@ static void pc_window(bool c128, const KTable *d_tab, int mode, int gv, cudaStre
 }
 
 cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev, cudaStream_t st,
-                               int *launches_out) {
+                               int *launches_out, bool groups) {
     KTable *tb = const_cast<KTable *>(d_tab);
     const bool c128 = prec == 0;
     if (!g_vec_grid) return cudaErrorNotReady;   // krylov_prepare() first
@@ -2073,8 +2370,11 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
         if (c128) k_mv64<false><<<gmv, 256, 0, st>>>(tb, 0);
         else {
             k_mv_tma<false><<<gmv, kTmaThreads, tma_smem_bytes(false), st>>>(tb, 0);
-            k_mv_grp_tc<<<gmv, 32 * (kTcWarps + 1), kTcSmem, st>>>(tb, 0);
-            ++nl;
+            if (groups) {
+                k_mv_grp_tc<<<gmv, 32 * (kTcWarps + 1), kTcSmem, st>>>(tb, 0);
+                k_mv_grp_umma<<<gmv, 32 * kUmWarps, kUmSmem, st>>>(tb);
+                nl += 2;
+            }
         }
         if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q + 1], st, cudaEventRecordExternal);
         if (c128) {
@@ -2101,10 +2401,10 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
     else {
         // first-cycle residuals with error-free products, then the recursive updates
         k_mv_tma<true><<<gmv, kTmaThreads, tma_smem_bytes(true), st>>>(tb, 1);
-        k_mv_grp<true><<<gmv, 32 * (GrpCfg<true>::kWarps + 1), grp_smem_bytes(true), st>>>(tb, 1);
+        if (groups) k_mv_grp<true><<<gmv, 32 * (GrpCfg<true>::kWarps + 1), grp_smem_bytes(true), st>>>(tb, 1);
         k_mv_tma<false><<<gmv, kTmaThreads, tma_smem_bytes(false), st>>>(tb, 2);
-        k_mv_grp_tc<<<gmv, 32 * (kTcWarps + 1), kTcSmem, st>>>(tb, 2);
-        nl += 3;
+        if (groups) k_mv_grp_tc<<<gmv, 32 * (kTcWarps + 1), kTcSmem, st>>>(tb, 2);
+        nl += groups ? 3 : 1;
     }
     if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * kSteps + 1], st, cudaEventRecordExternal);
     k_resid<<<gv, kThreads, 0, st>>>(d_tab);

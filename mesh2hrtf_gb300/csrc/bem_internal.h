@@ -10,6 +10,7 @@
 // batch.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -154,7 +155,17 @@ inline size_t image_table_bytes(int n, int nref) {
 // (prec 1): regular pairs (persistent k_far), then the near lists (persistent
 // k_near).  ctr: 4 device words, zero before the first use; the kernels leave
 // them zero.
-cudaError_t launch_assemble(const AsmBatch &t, int prec, unsigned *ctr, cudaStream_t st);
+// Launch shapes of the assembly (persistent grids: resident blocks per SM of
+// k_far, at most kFarPerSmMax, and of k_near, at most 2); the results do not
+// depend on them.
+struct AsmShape {
+    int far_per_sm = 3;
+    int near_per_sm = 2;
+};
+constexpr int kFarPerSmMax = 3;
+cudaError_t launch_assemble(const AsmBatch &t, int prec, unsigned *ctr, cudaStream_t st,
+                            AsmShape shape = AsmShape());
+
 // b = free terms + incident waves + columns with prescribed values (FP64).
 cudaError_t launch_rhs(const AsmBatch &t, cudaStream_t st);
 
@@ -282,6 +293,7 @@ struct KSys {
     int pcw;                // window correction of the preconditioner (needs pc)
     void *pcy, *pcz;        // its vectors X v and A_w X v: float2 for complex64
                             // systems, double2 for complex128
+    int strip;              // rows per item of the TMA product (0: kTmaStrip)
     KState *st;
 };
 
@@ -317,8 +329,20 @@ struct KTable {
     KPlan gplan[3];         // plans of the shared-matrix products (entries = groups)
     unsigned gmask[3][kMaxSys];   // per plan entry: members taking part
     const int2 *vb_items;   // (system, block)
+    int grp_umma;           // 1: the groups' Krylov products run on the 5th-generation
+                            // tensor cores (k_mv_grp_umma; 128-row strips),
+                            // 0: on the warp-level ones (k_mv_grp_tc; 32-row strips)
     KSys sys[kMaxSys];
+    // TMA tensor maps of the groups' matrices (complex64 rows viewed as
+    // 2 n floats; boxes of 32 floats x 128 rows, 128-byte swizzle)
+    alignas(64) CUtensorMap gmap[kMaxSys / 2];
 };
+// The grouped Krylov product on the 5th-generation tensor cores
+// (BEM_GB300_GROUP_PRODUCT=tcgen05; otherwise the warp-level kernel): TF32
+// operands, so an inner GMRES cycle of a group member stops at 3e-4 of its
+// starting residual, like the fp16 copy.
+bool group_product_umma();
+constexpr int kUmRows = 128;
 
 // Shared-matrix product: items are strips of rows over all columns (32 rows
 // for the Krylov product, 16 for the refinement residual), stages of 256
@@ -332,21 +356,45 @@ constexpr int kSteps = 8;
 // Enqueues one iteration body for the systems of *d_tab (device memory) on
 // st.  mv_ev: 2 * (kSteps + 1) events recorded around the matrix-vector
 // products (may be nullptr).  prec: 0 complex128, 1 complex64 matrices.
-// Returns the number of kernel launches enqueued through *launches_out.
+// groups: include the shared-matrix (group) products, for batches that have
+// groups.  Returns the number of kernel launches enqueued through
+// *launches_out.
 cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev, cudaStream_t st,
-                               int *launches_out);
+                               int *launches_out, bool groups);
 // complex64 matrices: the product streams row segments with bulk copies
-// (TMA) in strips of kTmaStrip rows; complex128: tiles of kMvRows rows.
+// (TMA) in strips of `strip` rows (a multiple of kTmaRows, chosen per system
+// by the tuner; kTmaStrip by default); complex128: tiles of kMvRows rows.
 constexpr int kTmaRows = 8;
 constexpr int kTmaStrip = 64;
-__host__ __device__ inline int mv_items_of(int n, int prec) {
-    return ceil_div(n, prec == 0 ? kMvRows : kTmaStrip) * mv_chunks(n);
+constexpr int kTmaStripMax = 256;
+__host__ __device__ inline int mv_items_of(int n, int prec, int strip = kTmaStrip) {
+    return ceil_div(n, prec == 0 ? kMvRows : strip) * mv_chunks(n);
 }
 // Krylov products from the fp16 copy of A: items span two column chunks
 // (8 KB row segments, the size the complex64 items move).
-__host__ __device__ inline int mv_items16(int n) {
-    return ceil_div(n, kTmaStrip) * ceil_div(mv_chunks(n), 2);
+__host__ __device__ inline int mv_items16(int n, int strip = kTmaStrip) {
+    return ceil_div(n, strip) * ceil_div(mv_chunks(n), 2);
 }
+
+// ---------------------------------------------------------------- tuner
+// Launch shapes chosen by timing candidates with CUDA events on the first
+// call per (device model, size bucket, precision, right-hand sides), kept in
+// memory and in a cache file (bem_tune.cu).  Only shapes that leave every
+// result bit unchanged are tuned.
+struct TuneChoice {
+    AsmShape asm_shape;
+    int mv_strip = kTmaStrip;   // rows per item of the complex64 product
+    bool asm_tuned = false, mv_tuned = false;
+    double asm_ms = 0.0, mv_ms = 0.0;   // time of the chosen candidate
+};
+bool tune_enabled();
+int tune_bucket(int n);
+TuneChoice tune_lookup(int n, int prec, int n_rhs);
+void tune_store_asm(int n, int prec, int n_rhs, AsmShape s, double ms);
+void tune_store_mv(int n, int prec, int n_rhs, int strip, double ms);
+// One Krylov product (kind 0) of the systems in plan[0] of *d_tab, outside
+// any iteration body (the tuner times it).
+cudaError_t launch_product(KTable *d_tab, int prec, cudaStream_t st);
 // Rebuilds both launch plans of *d_tab from the systems' current phases.
 cudaError_t launch_plans(KTable *d_tab, cudaStream_t st);
 // Scratch sizes of one system (complex entries).

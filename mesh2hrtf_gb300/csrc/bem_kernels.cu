@@ -635,7 +635,7 @@ __device__ __forceinline__ void far_tile_img(const DevMeshView &mv, const DevFre
     }
 }
 
-constexpr int kFarPerSm = 3;   // resident k_far blocks per SM (launch bounds and persistent grid)
+constexpr int kFarPerSm = kFarPerSmMax;   // resident k_far blocks per SM allowed by the launch bounds
 
 // ONE: the batch holds a single system, whose table then stays in constant
 // operands instead of registers.  IMG: some mesh of the batch has symmetry
@@ -1736,19 +1736,22 @@ int sm_count() {
 }
 }  // namespace
 
-cudaError_t launch_assemble(const AsmBatch &t, int prec, unsigned *ctr, cudaStream_t st) {
+cudaError_t launch_assemble(const AsmBatch &t, int prec, unsigned *ctr, cudaStream_t st, AsmShape shape) {
     if (t.B <= 0) return cudaSuccess;
     dim3 block(32, 8);
     const int far_items = t.far_off[t.B], near_items = t.near_off[t.B];
-    // persistent grids: kFarPerSm resident blocks of k_far per SM (launch bounds), 4 of k_near
-    const int gfar = std::max(1, std::min(far_items, kFarPerSm * sm_count()));
-    const int gnear = std::max(1, std::min((near_items + 7) / 8, 4 * sm_count()));
+    // persistent grids: far_per_sm resident blocks of k_far per SM (launch
+    // bounds allow kFarPerSm), near_per_sm of k_near (launch bounds allow 2)
+    const int fps = std::max(1, std::min(shape.far_per_sm, kFarPerSm));
+    const int nps = std::max(1, std::min(shape.near_per_sm, 2));
+    const int gfar = std::max(1, std::min(far_items, fps * sm_count()));
+    const int gnear = std::max(1, std::min((near_items + 7) / 8, nps * sm_count()));
     // Systems that fill the GPU on their own take one single-system launch
     // each: the single-system kernel keeps the table in constant operands
     // (fewer registers, no spills), which beat the shared work queue.
     bool split = t.B > 1;
     for (int b = 0; b < t.B && split; ++b)
-        if (t.far_off[b + 1] - t.far_off[b] < kFarPerSm * sm_count()) split = false;
+        if (t.far_off[b + 1] - t.far_off[b] < fps * sm_count()) split = false;
     std::unique_ptr<AsmBatch> one_sys;
     if (split) one_sys.reset(new AsmBatch());
     count_launches((split ? t.B : 1) + (near_items ? 1 : 0));
@@ -1778,7 +1781,7 @@ cudaError_t launch_assemble(const AsmBatch &t, int prec, unsigned *ctr, cudaStre
             one_sys->B = 1;
             one_sys->sys[0] = t.sys[b];
             asm_batch_finish(*one_sys);
-            far(*one_sys, std::max(1, std::min(one_sys->far_off[1], kFarPerSm * sm_count())));
+            far(*one_sys, std::max(1, std::min(one_sys->far_off[1], fps * sm_count())));
         }
     } else {
         far(t, gfar);

@@ -241,12 +241,19 @@ void bem_server_s::run() {
                     if (e == cudaSuccess) e = cudaMemsetAsync(ss[i]->d.status, 0, sizeof(int), st_a);
                     if (e == cudaSuccess) e = cudaMemsetAsync(ss[i]->d.x, 0, sizeof(double2) * ss[i]->n, st_a);
                 }
+                // launch shapes the tuner chose earlier for these sizes (the
+                // serving loop looks them up; it does not tune)
+                int big = 0;
+                for (int i = 1; i < cnt; ++i)
+                    if (ss[i]->n > ss[big]->n) big = i;
+                const bem::AsmShape shape = bem::tune_lookup(ss[big]->n, ss[big]->prec, 1).asm_shape;
+                for (int i = 0; i < cnt; ++i) ss[i]->mv_strip = bem::tune_lookup(ss[i]->n, ss[i]->prec, 1).mv_strip;
                 for (int c0 = 0; c0 < cnt && e == cudaSuccess; c0 += bem::kMaxAsm) {
                     const int k = std::min(bem::kMaxAsm, cnt - c0);
                     at->B = k;
                     for (int i = 0; i < k; ++i) at->sys[i] = ss[c0 + i]->asys();
                     bem::asm_batch_finish(*at);
-                    e = bem::launch_assemble(*at, prec01, ctr, st_a);
+                    e = bem::launch_assemble(*at, prec01, ctr, st_a, shape);
                     if (e == cudaSuccess) e = bem::launch_rhs(*at, st_a);
                 }
                 for (int i = 0; i < cnt && e == cudaSuccess; ++i) {

@@ -117,6 +117,7 @@ struct bem_solver_s {
     bem::DevFreq freq{};
     bool have_freq = false;
     bool factored = false;    // A holds LU factors (bem_solve_direct) until the next assembly
+    int mv_strip = 0;         // rows per item of the complex64 product (0: default; tuner's choice)
     bool solved = false;
     double *pts = nullptr, *pot = nullptr, *grad = nullptr;
     int pts_cap = 0;
@@ -158,6 +159,7 @@ struct bem_solver_s {
         k.ldv = n;
         k.mvp = d.mvp; k.dpa = d.dpa; k.dpb = d.dpb; k.nrmp = d.nrmp;
         k.H = d.H; k.cs = d.cs; k.sn = d.sn; k.g = d.g; k.y = d.y; k.hsum = d.hsum;
+        k.strip = mv_strip;
         return k;
     }
     bem::KState kinit() const {
@@ -170,7 +172,10 @@ struct bem_solver_s {
         // with the fp16 Krylov copy (perturbation ~5e-4 relative) a cycle
         // gains about three digits on the complex64 system; 3e-4 rather than
         // 1e-3 saves a refinement cycle now and then for a few more steps
-        q.floor_rel = prec == BEM_PREC_MIXED ? (d.A16 ? 3e-4 : 1e-5) : 0.0;
+        // (the right-hand sides of a solver with several share TF32 tensor-core
+        // products of about the same accuracy)
+        const bool tf32 = n_rhs > 1 && bem::group_product_umma();
+        q.floor_rel = prec == BEM_PREC_MIXED ? ((d.A16 || tf32) ? 3e-4 : 1e-5) : 0.0;
         return q;
     }
     bem::AsmSys asys(int r = 0) const {

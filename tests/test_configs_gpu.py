@@ -75,6 +75,11 @@ def test_batched_uneven_full_size():
     for r in res:
         assert r[4] == capi.BEM_OK
         assert r[3]["rel_residual"] <= 1e-9
+    # the launch shapes the tuner chose for the batch (its largest system sets
+    # the assembly's; every system has its own product strip)
+    sizes = sorted({len(i["elems"]) for i in insts})
+    for n in (sizes[0], sizes[len(sizes) // 2], sizes[-1]):
+        print("tuned", n, capi.tune_info(n))
     for s in ss:
         s.close()
     pick = list(range(0, 64, 8))

@@ -91,3 +91,34 @@ def test_multi_rhs_projection_shares_kernel_evaluations():
     s.close()
     one.close()
     m.close()
+
+
+def test_grouped_product_tensor_core_paths_agree(monkeypatch):
+    """The right-hand sides' shared Krylov product on the 5th-generation
+    tensor cores (tcgen05, TF32 operands, k_mv_grp_umma;
+    BEM_GB300_GROUP_PRODUCT=tcgen05) and on the warp-level ones (mma.sync
+    3xTF32, k_mv_grp_tc; the default)
+    reach the same solutions: both refine to a 1e-9 residual of the same
+    complex64 system with FP32-accurate residual products."""
+    v, f = meshes.perturbed_ellipsoid(14, 79)   # 3920 triangles: several 128-row strips, a ragged last one
+    n = len(f)
+    m = capi.Mesh(v, f)
+    pts = meshes.random_sphere_points(40, 1.2, 6)
+    srcs = [meshes.surface_point_with_normal(v, f, 400 + r) for r in range(8)]
+    freqs = [workloads.frequency(capi, n, 9000.0, s) for s in srcs]
+    out = {}
+    for mode in ("mma", "tcgen05"):
+        monkeypatch.setenv("BEM_GB300_GROUP_PRODUCT", mode)
+        s = capi.Solver(m, precision=capi.PREC_MIXED, tol=1e-9, n_rhs=8)
+        xs, pots, grads, infos = s.solve_multi(freqs, pts)
+        assert all(i["rel_residual"] <= 1e-9 for i in infos)
+        out[mode] = (xs, pots, [i["iterations"] for i in infos])
+        s.close()
+    for r in range(8):
+        xa, xb = out["mma"][0][r], out["tcgen05"][0][r]
+        assert np.linalg.norm(xa - xb) <= 1e-7 * np.linalg.norm(xa), r
+        pa, pb = out["mma"][1][r], out["tcgen05"][1][r]
+        assert np.linalg.norm(pa - pb) <= 1e-7 * np.linalg.norm(pa), r
+    # TF32 inner products: a few more Krylov steps at most
+    assert max(out["tcgen05"][2]) <= 2 * max(out["mma"][2]) + 10
+    m.close()
