@@ -2328,7 +2328,7 @@ cudaError_t krylov_prepare() {
 
 bool group_product_umma() {
     const char *v = std::getenv("BEM_GB300_GROUP_PRODUCT");
-    return v && std::strcmp(v, "tcgen05") == 0;
+    return !(v && std::strcmp(v, "mma") == 0);
 }
 
 cudaError_t launch_product(KTable *d_tab, int prec, cudaStream_t st) {

@@ -337,10 +337,10 @@ struct KTable {
     // 2 n floats; boxes of 32 floats x 128 rows, 128-byte swizzle)
     alignas(64) CUtensorMap gmap[kMaxSys / 2];
 };
-// The grouped Krylov product on the 5th-generation tensor cores
-// (BEM_GB300_GROUP_PRODUCT=tcgen05; otherwise the warp-level kernel): TF32
-// operands, so an inner GMRES cycle of a group member stops at 3e-4 of its
-// starting residual, like the fp16 copy.
+// The grouped Krylov product on the 5th-generation tensor cores (unless
+// BEM_GB300_GROUP_PRODUCT=mma selects the warp-level kernel): TF32 operands,
+// so an inner GMRES cycle of a group member stops at 3e-4 of its starting
+// residual, like the fp16 copy.
 bool group_product_umma();
 constexpr int kUmRows = 128;
 

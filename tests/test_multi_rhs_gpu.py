@@ -35,7 +35,9 @@ def test_multi_rhs_equals_single(prec):
             assert np.array_equal(pots[r], p0)
             assert np.array_equal(grads[r], g0)
         else:
-            assert abs(infos[r]["iterations"] - one.info.iterations) <= 2
+            # the shared products differ from the single solve's (TF32 operands
+            # on the tcgen05 path): at most one more refinement cycle's steps
+            assert -2 <= infos[r]["iterations"] - one.info.iterations <= 8
             assert np.linalg.norm(xs[r] - x0) <= 1e-7 * np.linalg.norm(x0)
             assert np.linalg.norm(pots[r] - p0) <= 1e-7 * np.linalg.norm(p0)
     # the right-hand sides really differ
@@ -95,9 +97,9 @@ def test_multi_rhs_projection_shares_kernel_evaluations():
 
 def test_grouped_product_tensor_core_paths_agree(monkeypatch):
     """The right-hand sides' shared Krylov product on the 5th-generation
-    tensor cores (tcgen05, TF32 operands, k_mv_grp_umma;
-    BEM_GB300_GROUP_PRODUCT=tcgen05) and on the warp-level ones (mma.sync
-    3xTF32, k_mv_grp_tc; the default)
+    tensor cores (tcgen05, TF32 operands, k_mv_grp_umma; the default) and on
+    the warp-level ones (mma.sync 3xTF32, k_mv_grp_tc;
+    BEM_GB300_GROUP_PRODUCT=mma)
     reach the same solutions: both refine to a 1e-9 residual of the same
     complex64 system with FP32-accurate residual products."""
     v, f = meshes.perturbed_ellipsoid(14, 79)   # 3920 triangles: several 128-row strips, a ragged last one
