@@ -506,11 +506,21 @@ bem_status tuned_asm_shape(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned 
     float best = 1e30f;
     bem::AsmShape pick = tc.asm_shape;
     cudaError_t err = cudaSuccess;
-    for (int fa = 1; fa <= bem::kFarPerSmMax && err == cudaSuccess; ++fa) {
-        for (int ne = 1; ne <= 2 && err == cudaSuccess; ++ne) {
+    // the default shape first; when one assembly of the group takes longer
+    // than kTuneAsmMaxMs (large FP64 systems) the default is kept without
+    // running the other candidates
+    constexpr float kTuneAsmMaxMs = 100.f;
+    std::vector<bem::AsmShape> cand(1, bem::AsmShape());
+    for (int fa = 1; fa <= bem::kFarPerSmMax; ++fa)
+        for (int ne = 1; ne <= 2; ++ne) {
             bem::AsmShape sh;
             sh.far_per_sm = fa;
             sh.near_per_sm = ne;
+            if (sh.far_per_sm != cand[0].far_per_sm || sh.near_per_sm != cand[0].near_per_sm) cand.push_back(sh);
+        }
+    for (size_t ci = 0; ci < cand.size() && err == cudaSuccess; ++ci) {
+        {
+            const bem::AsmShape sh = cand[ci];
             err = cudaEventRecord(ev[0], st);
             for (int c0 = 0; c0 < cnt && err == cudaSuccess; c0 += bem::kMaxAsm) {
                 const int k = std::min(bem::kMaxAsm, cnt - c0);
@@ -527,6 +537,7 @@ bem_status tuned_asm_shape(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned 
                 best = ms;
                 pick = sh;
             }
+            if (ci == 0 && ms > kTuneAsmMaxMs) break;
         }
     }
     for (auto &e : ev) cudaEventDestroy(e);

@@ -49,6 +49,14 @@ bool encode_group_map(CUtensorMap *map, const void *A, int n, long long lda) {
 // BEM_GB300_TEST_WAIT_CYCLES: a bound (clock cycles) for the products'
 // mbarrier waits in place of the default of about 2 s.  Only for tests that
 // make a wait run out; read whenever a batch is set up.
+// BEM_GB300_TEST_WAIT_KINDS: the product kinds the bound applies to (bit k:
+// kind k; 0 Krylov products, 1 first refinement residuals, 2 residual
+// updates); all by default.
+int test_wait_kinds() {
+    const char *v = std::getenv("BEM_GB300_TEST_WAIT_KINDS");
+    return (v && *v) ? std::atoi(v) : 7;
+}
+
 long long test_wait_cycles() {
     const char *v = std::getenv("BEM_GB300_TEST_WAIT_CYCLES");
     if (!v || !*v) return 0;
@@ -118,6 +126,7 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
     h_tab_->vb_total = vb_total;
     h_tab_->vb_items = d_items_;
     h_tab_->wait_cycles = test_wait_cycles();
+    h_tab_->wait_kinds = test_wait_kinds();
     for (int b = 0; b < B; ++b) {
         h_tab_->sys[b] = sys[b];
         h_tab_->sys[b].st = d_st_ + b;
@@ -172,6 +181,7 @@ cudaError_t Engine::time_product(const KSys &sys, float *ms) {
     h_tab_->prec = prec_;
     h_tab_->vb_total = sys.nvb;
     h_tab_->wait_cycles = test_wait_cycles();
+    h_tab_->wait_kinds = test_wait_kinds();
     h_tab_->sys[0] = sys;
     h_tab_->sys[0].st = d_st_;
     h_tab_->sys[0].shared = 0;

@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(32 * (kTmaConsumers + 1), 1) k_mv_tma(KTable *
     plan_load(tb->plan[kind], pl);   // includes a block barrier
     int *err = &tb->err;
     // bound of the waits (the drains of in-flight copies keep the full bound)
-    const long long lim = tb->wait_cycles > 0 ? tb->wait_cycles : kWaitCycles;
+    const long long lim = (tb->wait_cycles > 0 && ((tb->wait_kinds >> kind) & 1)) ? tb->wait_cycles : kWaitCycles;
     if (warp == kTmaConsumers) {
         // ---------------- producer warp: lane 0 takes the items and keeps the
         // barriers, lane r issues the bulk copy of row r of a stage (one
@@ -755,7 +755,7 @@ __global__ void __launch_bounds__(32 * (GrpCfg<EXACT>::kWarps + 1), 1) k_mv_grp(
     plan_load(tb->gplan[kind], pl);   // includes a block barrier
     int *err = &tb->err;
     // bound of the waits (the drains of in-flight copies keep the full bound)
-    const long long lim = tb->wait_cycles > 0 ? tb->wait_cycles : kWaitCycles;
+    const long long lim = (tb->wait_cycles > 0 && ((tb->wait_kinds >> kind) & 1)) ? tb->wait_cycles : kWaitCycles;
     if (warp == NW) {
         // ---------------- producer warp: lane 0 takes the strips and keeps the
         // barriers; lane r < ROWS issues row r's copy, the other copies (the
@@ -1020,7 +1020,7 @@ __global__ void __launch_bounds__(32 * (kTcWarps + 1), 1) k_mv_grp_tc(KTable *tb
     plan_load(tb->gplan[kind], pl);   // includes a block barrier
     int *err = &tb->err;
     // bound of the waits (the drains of in-flight copies keep the full bound)
-    const long long lim = tb->wait_cycles > 0 ? tb->wait_cycles : kWaitCycles;
+    const long long lim = (tb->wait_cycles > 0 && ((tb->wait_kinds >> kind) & 1)) ? tb->wait_cycles : kWaitCycles;
     if (warp == kTcWarps) {
         // ---------------- producer warp: lane 0 takes the strips and keeps the
         // barriers; lane r issues the bulk copy of row r of a stage and lanes
@@ -1307,7 +1307,7 @@ __global__ void __launch_bounds__(32 * kUmWarps, 1) k_mv_grp_umma(KTable *tb) {
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     int *err = &tb->err;
-    const long long lim = tb->wait_cycles > 0 ? tb->wait_cycles : kWaitCycles;
+    const long long lim = (tb->wait_cycles > 0 && ((tb->wait_kinds >> 0) & 1)) ? tb->wait_cycles : kWaitCycles;
     const unsigned kAll = 0xffffffffu;
 
     if (warp == 0) {

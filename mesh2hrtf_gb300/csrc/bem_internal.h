@@ -321,6 +321,7 @@ struct KTable {
     long long wait_cycles;  // bound of the products' mbarrier waits in clock
                             // cycles (0: the default of about 2 s); a test
                             // sets it low to make a wait run out
+    int wait_kinds;         // product kinds (bit k: kind k) the bound applies to
     unsigned mv_ctr[2];     // work queue of the persistent matvec
     KPlan plan[3];          // [0] Krylov product, [1] refinement residual with
                             // error-free products, [2] recursive residual update

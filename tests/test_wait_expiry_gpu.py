@@ -55,3 +55,42 @@ def test_product_wait_runs_out_and_context_survives(monkeypatch):
     s2.close()
     m.close()
     assert "BEM_GB300_TEST_WAIT_CYCLES" not in os.environ
+
+
+def test_grouped_tensor_core_product_wait_runs_out(monkeypatch):
+    """The same for the tcgen05 product of several right-hand sides sharing
+    one matrix (k_mv_grp_umma).  BEM_GB300_TEST_WAIT_KINDS=1 shortens only
+    the Krylov products' waits, so the first iteration body's residual
+    products finish and the tensor-core product of the next body gives up:
+    its producer drains the copies in flight, its MMA warp waits for the MMAs
+    it issued, and the block releases its tensor memory before it exits.  A
+    later grouped solve allocates tensor memory again and reproduces the
+    earlier solutions bit for bit."""
+    v, f, fr = _case()
+    n = len(f)
+    m = capi.Mesh(v, f)
+    pts = meshes.random_sphere_points(8, 1.2, 2)
+    k = fr.desc.wave_number
+    freqs = [capi.Frequency(k, n, point_sources=[0.4, 0.05 * r, 0.0], point_amps=[1e-3 + 0j]) for r in range(4)]
+    monkeypatch.delenv("BEM_GB300_GROUP_PRODUCT", raising=False)
+    s0 = capi.Solver(m, precision=capi.PREC_MIXED, tol=1e-9, n_rhs=4)
+    xs0, _, _, _ = s0.solve_multi(freqs, pts)
+    s0.close()
+
+    monkeypatch.setenv("BEM_GB300_TEST_WAIT_CYCLES", "200")
+    monkeypatch.setenv("BEM_GB300_TEST_WAIT_KINDS", "1")
+    s1 = capi.Solver(m, precision=capi.PREC_MIXED, tol=1e-9, n_rhs=4)
+    with pytest.raises(capi.BemError) as e:
+        s1.solve_multi(freqs, pts)
+    assert e.value.status == capi.BEM_ERR_DEVICE_TIMEOUT
+    s1.close()
+
+    monkeypatch.delenv("BEM_GB300_TEST_WAIT_CYCLES")
+    monkeypatch.delenv("BEM_GB300_TEST_WAIT_KINDS")
+    s2 = capi.Solver(m, precision=capi.PREC_MIXED, tol=1e-9, n_rhs=4)
+    xs2, _, _, infos = s2.solve_multi(freqs, pts)
+    assert all(i["rel_residual"] <= 1e-9 for i in infos)
+    for a, b in zip(xs0, xs2):
+        assert np.array_equal(a, b)
+    s2.close()
+    m.close()
