@@ -10,12 +10,15 @@ taken from a seeded permutation of the 200, so K steps sample the band.
 
 value     mixed-precision solves/s with the mesh resident on the device; a
           step is one bem_solve_batch call over its frequencies (one solver
-          per frequency on the shared mesh).
+          per frequency on the shared mesh).  The Krylov products read the
+          block low-rank copy of A by default (--krylov-copy blr; fp16 and
+          complex64 select the other copies).
 e2e       the same K steps through the C ABI with host buffers: every step
           uploads the mesh and evaluation points, creates the solvers, runs
           bem_solve_batch and copies unknowns and fields back.
 latency   p50/p99 of the same frequencies solved one at a time
-          (bem_solve_frequency).
+          (bem_solve_frequency) with the library's default fp16 Krylov copy,
+          the faster one for a single solve.
 fp64_gpu  the plain FP64 GPU path on the first timed batch (the same 16
           frequencies, also one bem_solve_batch), against the mixed time of
           that batch, and the mixed path's relative L2 error against it.
@@ -58,9 +61,20 @@ RHO, C0 = 1.21, 343.0
 N_TRI = 20480
 SEED = 20261204
 METRIC = "freq solves/s at <=1e-4 rel err, mixed vs plain FP64 GPU BEM; p50/p99 latency"
-# DRAM bytes (read + write) of one Krylov product from the fp16 copy at
-# N = 20480, measured by ncu on this workload (k_mv_tma launch list)
-MV_TRAFFIC = 1.6863e9
+# DRAM bytes (read + write) of one Krylov product at N = 20480 measured by
+# ncu on this workload, the algorithmic bytes of the same launch, and the
+# capture it comes from, per Krylov copy
+MV_TRAFFIC = {
+    "fp16": (1.6863e9, 1.6784e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum per Krylov k_mv_tma<0> launch "
+                                 "from the fp16 copy, 5 kHz (profiles/k_mv_tma_fp16_head20480.md)"),
+    "blr": (None, None, "not captured"),
+    "complex64": (None, None, "not captured"),
+}
+COPY_DESC = {"blr": "a block low-rank Krylov copy (fp16 factors and fp16 dense blocks)",
+             "fp16": "an fp16 Krylov copy", "complex64": "no Krylov copy"}
+ROOF_KERNEL = {"blr": "k_mv_blr (Krylov products from the block low-rank copy) + k_mv_tma (complex64 residuals)",
+               "fp16": "k_mv_tma (batched A x: fp16 Krylov copy, complex64 residuals)",
+               "complex64": "k_mv_tma (batched A x from the complex64 matrix)"}
 # Fixed work accounting of one kernel evaluation (one quadrature point of one
 # (collocation point, element) pair, NC_RegularIntegration,
 # NC_EquationSystem.cpp:1600-1728): r, 1/r and the phase (sin, cos, rsqrt:
@@ -195,7 +209,7 @@ PORT_SAMPLE = ("FP64 C restatement of NumCalc's TBEM path (oracle/bem_oracle.c):
 
 
 # ------------------------------------------------------------- rooflines
-def stage_rooflines(n, m_pts, peaks, hbm, info_steps, value):
+def stage_rooflines(n, m_pts, peaks, hbm, info_steps, value, copy="fp16"):
     """Roofline time per solve of every stage from its algorithmic work and
     the measured peaks, against the measured stage times (ms per solve)."""
     fp32, sfu = peaks["fp32_fma_per_s"], peaks["sfu_per_s"]
@@ -207,16 +221,19 @@ def stage_rooflines(n, m_pts, peaks, hbm, info_steps, value):
     act["nonproduct_ms"] = act["solve_ms"] - act["matvec_ms"]
     ev_asm = MIN_POINTS * float(n) * n
     t_asm = max(ev_asm * ASM_FP32_PER_EVAL / fp32, ev_asm * ASM_SFU_PER_EVAL / sfu, n * n * 8.0 / (hbm * 1e9))
-    by_kry = n * n * 4.0 + 2 * n * 16.0
     by_res = n * n * 8.0 + 2 * n * 16.0
-    t_mv = (it * by_kry + (nmv - it) * by_res) / (hbm * 1e9)
+    kry = sum(i["krylov_bytes"] * i["iterations"] for s in info_steps for i in s) / solves
+    t_mv = (kry + (nmv - it) * by_res) / (hbm * 1e9)
     # non-product solve work: the fp16 copy (read 8, write 4 bytes per entry),
     # block inverses (N/128 blocks, 8*128^3 FP32 operations each), per
     # preconditioner application the 1024-wide windows (fp16) and X twice,
     # and the Arnoldi passes (two Gram-Schmidt passes over the basis: reads
     # of (k+1) complex64 vectors for the dots and for the update)
     papp = it + cyc
-    by_np = n * n * 12.0 + papp * (n * 1024 * 4.0 + 2 * n * 128 * 8.0)
+    # the copies: fp16 split 12 B per entry; the block low-rank copy adds one
+    # full read of A by the probe check (8 B per entry)
+    copy_b = {"fp16": 12.0, "blr": 20.0, "complex64": 0.0}[copy]
+    by_np = n * n * copy_b + papp * (n * 1024 * 4.0 + 2 * n * 128 * 8.0)
     steps_per_cycle = it / max(cyc, 1.0)
     by_np += cyc * sum(4.0 * (k + 1) * n * 8.0 for k in range(int(round(steps_per_cycle))))
     t_np = by_np / (hbm * 1e9) + (n / 128.0) * 8 * 128.0 ** 3 / fp32
@@ -227,12 +244,16 @@ def stage_rooflines(n, m_pts, peaks, hbm, info_steps, value):
          "roof_ms": t_asm * 1e3, "actual_ms": act["assemble_ms"],
          "work": "%d-point rule on every pair (lower bound): %.3g evaluations x (%d FP32 + %d SFU); N^2*8 B written"
                  % (MIN_POINTS, ev_asm, ASM_FP32_PER_EVAL, ASM_SFU_PER_EVAL)},
-        {"stage": "Krylov products (k_mv_tma)", "bound": "hbm", "roof_ms": t_mv * 1e3, "actual_ms": act["matvec_ms"],
-         "work": "%.1f fp16 products (N^2*4 B) + %.1f complex64 residual products (N^2*8 B)" % (it, nmv - it)},
-        {"stage": "other solve work (fp16 split, block inverses, preconditioner, Arnoldi, cycle ends)",
+        {"stage": "products (%s)" % ROOF_KERNEL[copy], "bound": "hbm", "roof_ms": t_mv * 1e3,
+         "actual_ms": act["matvec_ms"],
+         "work": "%.1f Krylov products (%.3g B each, mean) + %.1f complex64 residual products (N^2*8 B)"
+                 % (it, kry / max(it, 1e-9), nmv - it)},
+        {"stage": "other solve work (Krylov copy, block inverses, preconditioner, Arnoldi, cycle ends)",
          "bound": "hbm", "roof_ms": t_np * 1e3, "actual_ms": act["nonproduct_ms"],
-         "work": "N^2*12 B split + %.1f preconditioner applications x (N*1024*4 + 2*N*128*8) B + Gram-Schmidt "
-                 "passes + N/128 x 8*128^3 FP32 operations" % papp},
+         "work": "N^2*%g B Krylov copy + %.1f preconditioner applications x (N*1024*4 + 2*N*128*8) B + "
+                 "Gram-Schmidt passes + N/128 x 8*128^3 FP32 operations%s"
+                 % (copy_b, papp, "; the cross approximation's row and column reads are not counted"
+                    if copy == "blr" else "")},
         {"stage": "projection (k_fields, k_project_pts, k_project_sum)", "bound": "fp32 issue",
          "roof_ms": t_proj * 1e3, "actual_ms": act["project_ms"],
          "work": "%.3g evaluations x (%d FP32 + %d SFU)" % (ev_proj, PROJ_FP32_PER_EVAL, PROJ_SFU_PER_EVAL)},
@@ -292,6 +313,8 @@ def main():
     ap.add_argument("--ref-budget-s", type=float, default=150.0,
                     help="reference arm: complete solves are timed while their total stays within this")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--krylov-copy", default="blr", choices=["blr", "fp16", "complex64"],
+                    help="the copy of A the Krylov products of the batched solves read (complex64_krylov)")
     ap.add_argument("--mesh-n", type=int, default=32,
                     help="head mesh of 20 n^2 triangles (32: the 20480-triangle workload; smaller for tests)")
     args = ap.parse_args()
@@ -359,7 +382,9 @@ def main():
     # one solver per frequency of a step, all on the resident mesh; a step is
     # one bem_solve_batch call (assembly, lockstep GMRES and projection of the
     # B frequencies together)
-    solvers = [capi.Solver(mesh, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000) for _ in range(B)]
+    kcopy = {"blr": capi.KRYLOV_BLR, "fp16": False, "complex64": True}[args.krylov_copy]
+    solvers = [capi.Solver(mesh, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000, complex64_krylov=kcopy)
+               for _ in range(B)]
 
     # each rank takes its own slice of the permuted frequency list
     def batch_freqs(step):
@@ -367,6 +392,10 @@ def main():
         return [float(freqs[(base + b) % len(freqs)]) for b in range(B)]
 
     infos, step_s, first_res = [], [], None
+    # bytes one Krylov product reads, per system: the block low-rank copy's
+    # own count (bem_krylov_copy_info, a 25 KB read-back per system and step,
+    # inside the timed region), else the fp16 or complex64 matrix
+    by_fp16, by_c64 = n * n * 4.0 + 2 * n * 16.0, n * n * 8.0 + 2 * n * 16.0
 
     def run_step(step, record):
         nonlocal first_res
@@ -375,7 +404,11 @@ def main():
         res = capi.solve_batch(solvers, Fs, [pts] * B)
         if record:
             step_s.append(time.perf_counter() - t1)
-            infos.append([r[3] for r in res])
+            inf = [dict(r[3]) for r in res]
+            for i, sv in zip(inf, solvers):
+                i["krylov_bytes"] = (sv.krylov_copy_info()["bytes_per_product"] if args.krylov_copy == "blr"
+                                     else by_fp16 if args.krylov_copy == "fp16" else by_c64)
+            infos.append(inf)
             if first_res is None:
                 first_res = res
 
@@ -411,12 +444,13 @@ def main():
     # copy, N^2*4 + 2*N*16; refinement residuals the complex64 matrix,
     # N^2*8 + 2*N*16), its time is the CUDA-event time of the launches inside
     # the iteration bodies (events on the engine's stream).
-    bytes_krylov = n * n * 4.0 + 2 * n * 16.0
-    bytes_resid = n * n * 8.0 + 2 * n * 16.0
+    bytes_resid = by_c64
     mv_ms = sum(step[0]["matvec_ms"] for step in infos)
     n_mv = sum(i["n_matvec"] for step in infos for i in step)
     n_kry = sum(i["iterations"] for step in infos for i in step)
-    mv_bytes = bytes_krylov * n_kry + bytes_resid * (n_mv - n_kry)
+    kry_bytes = sum(i["krylov_bytes"] * i["iterations"] for step in infos for i in step)
+    bytes_krylov = kry_bytes / max(n_kry, 1)   # mean over the timed products
+    mv_bytes = kry_bytes + bytes_resid * (n_mv - n_kry)
     achieved = mv_bytes / (mv_ms / 1000.0) / 1e9 if mv_ms > 0 else None
     asm_ms = sum(step[0]["assemble_ms"] for step in infos)
     solve_ms = sum(step[0]["solve_ms"] for step in infos)
@@ -439,7 +473,8 @@ def main():
     t0 = time.perf_counter()
     for s in range(args.warmup, args.warmup + args.steps):
         m2 = capi.Mesh(v, f, device=dev)
-        s2 = [capi.Solver(m2, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000) for _ in range(B)]
+        s2 = [capi.Solver(m2, precision=capi.PREC_MIXED, tol=1e-9, max_iter=3000, complex64_krylov=kcopy)
+              for _ in range(B)]
         capi.solve_batch(s2, [freq_desc(capi, n, fr, src) for fr in batch_freqs(s)], [pts] * B)
         for sv in s2:
             sv.close()
@@ -461,18 +496,19 @@ def main():
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1000.0, "solves_per_step": B,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32 (FP32 assembly, complex64 matrix with an fp16 Krylov copy; refinement residuals from "
-                 "the complex64 matrix, about twice-FP32 accurate; FP64 solution, Hessenberg and Givens)",
+        "dtype": "fp32 (FP32 assembly, complex64 matrix with %s; refinement residuals from "
+                 "the complex64 matrix, about twice-FP32 accurate; FP64 solution, Hessenberg and Givens)"
+                 % COPY_DESC[args.krylov_copy],
         "data": "synthetic", "config": cfg,
         "stage_ms_per_solve": {"assemble": asm_ms / n_solves, "solve": solve_ms / n_solves,
                                "project": proj_ms / n_solves, "matvec": mv_ms / n_solves,
                                "iterations": float(np.mean(iters))},
-        "roofline": {"bound": "hbm", "kernel": "k_mv_tma (batched A x: fp16 Krylov copy, complex64 residuals)",
+        "roofline": {"bound": "hbm", "kernel": ROOF_KERNEL[args.krylov_copy],
                      "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if achieved else None,
-                     "traffic": MV_TRAFFIC if n == N_TRI else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per Krylov k_mv_tma<0> "
-                                       "launch from the fp16 copy, same N (profiles/k_mv_tma_fp16_head20480.md)",
+                     "traffic": MV_TRAFFIC[args.krylov_copy][0] if n == N_TRI else None,
+                     "traffic_algorithmic_bytes_same_launch": MV_TRAFFIC[args.krylov_copy][1] if n == N_TRI else None,
+                     "traffic_source": MV_TRAFFIC[args.krylov_copy][2],
                      "bytes_per_krylov_product": bytes_krylov, "bytes_per_residual_product": bytes_resid,
                      "krylov_products": n_kry, "residual_products": n_mv - n_kry,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
@@ -487,7 +523,7 @@ def main():
     if rank == 0:
         # measured issue peaks and every stage's roofline
         ip = capi.issue_peaks(dev)
-        stages, e2e_roof = stage_rooflines(n, len(pts), ip, hbm, infos, value)
+        stages, e2e_roof = stage_rooflines(n, len(pts), ip, hbm, infos, value, args.krylov_copy)
         line["roofline"]["stages"] = stages
         line["roofline"]["end_to_end"] = e2e_roof
         line["roofline"]["issue_peaks"] = dict(ip, source="bem_measure_issue_peaks (micro-kernels, CUDA events)")

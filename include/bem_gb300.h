@@ -117,7 +117,16 @@ typedef struct {
                                   copy of A (row-scaled; 4 bytes per entry,
                                   +50 % matrix memory) and the refinement
                                   residuals the complex64 matrix; 1 every
-                                  product reads the complex64 matrix          */
+                                  product reads the complex64 matrix; 2 the
+                                  Krylov products read a block low-rank copy
+                                  over the fp16 one (off-diagonal 256 x 256
+                                  blocks compressed by adaptive cross
+                                  approximation, checked to 2e-4 with random
+                                  probes, fp16 factors; the other blocks from
+                                  the fp16 copy; about +100 % matrix memory):
+                                  fewer bytes per product, but the compression
+                                  costs about as much as 10-20 products, so it
+                                  pays off in batches and long solves        */
 } bem_solver_params;
 
 typedef struct {
@@ -228,6 +237,17 @@ bem_status bem_solve(bem_solver_t solver, bem_solve_info *info);
  * the factors (L unit lower, U upper).  info gets no iterations and a
  * residual of 0 (not computed); a zero pivot gives BEM_ERR_INVALID. */
 bem_status bem_solve_direct(bem_solver_t solver, bem_solve_info *info);
+
+/* The block low-rank Krylov copy of a solver created with
+ * complex64_krylov = 2, as of its last assembly: blocks per block row,
+ * blocks read from the fp16 copy (the diagonal ones and those whose cross
+ * approximation needed more than 48 terms or failed the probe check), the
+ * mean rank of the compressed ones, and the bytes one Krylov product moves
+ * (fp16 factors and scales, fp16 dense blocks, the input vector and row
+ * scales per item, and the partial sums it writes).  Synchronous.  A solver
+ * without that copy gives BEM_ERR_INVALID.  No counterpart in NumCalc. */
+bem_status bem_krylov_copy_info(bem_solver_t solver, int32_t *blocks_per_row, int32_t *dense_blocks,
+                                double *mean_rank, double *bytes_per_product);
 
 /* Copy the solution (complex, n_elem) to host memory. */
 bem_status bem_get_solution(bem_solver_t solver, double *x_host);

@@ -20,7 +20,7 @@ NUMCALC_DIR = os.path.join(PKG, "numcalc")
 NUMCALC_BIN = os.path.join(NUMCALC_DIR, "bin", "NumCalc")
 NUMCALC_SRC = os.path.join(NUMCALC_DIR, "src")
 
-CU_SOURCES = ["bem_api.cu", "bem_engine.cu", "bem_gmres.cu", "bem_kernels.cu", "bem_precond.cu", "bem_server.cu", "bem_static.cu", "bem_peaks.cu", "bem_direct.cu", "bem_tune.cu"]
+CU_SOURCES = ["bem_api.cu", "bem_engine.cu", "bem_gmres.cu", "bem_kernels.cu", "bem_precond.cu", "bem_server.cu", "bem_static.cu", "bem_peaks.cu", "bem_direct.cu", "bem_tune.cu", "bem_blr.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

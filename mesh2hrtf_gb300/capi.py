@@ -26,6 +26,7 @@ BEM_ERR_SUBDIVISION = 6
 BEM_ERR_PENDING = 7
 PREC_FP64 = 0
 PREC_MIXED = 1
+KRYLOV_BLR = 2   # Solver(complex64_krylov=KRYLOV_BLR): block low-rank Krylov copy
 
 EXPORTED = [
     "bem_last_error", "bem_version", "bem_kernel_launches", "bem_set_device", "bem_footprint_bytes",
@@ -34,7 +35,7 @@ EXPORTED = [
     "bem_solve_frequency", "bem_project_static", "bem_solve_batch", "bem_solve_multi", "bem_footprint_multi",
     "bem_server_create", "bem_server_submit", "bem_server_wait", "bem_server_destroy",
     "bem_mesh_footprint_bytes", "bem_device_memory", "bem_release_cached_memory", "bem_measure_issue_peaks",
-    "bem_solve_direct", "bem_tune_info",
+    "bem_solve_direct", "bem_tune_info", "bem_krylov_copy_info",
 ]
 STATIC_MAX_ELEMENTS = 32768
 
@@ -134,6 +135,8 @@ def load(build_if_missing: bool = True):
     lib.bem_measure_issue_peaks.argtypes = [i32, dp]
     lib.bem_solve_direct.argtypes = [vp, C.POINTER(SolveInfo)]
     lib.bem_tune_info.argtypes = [i32, i32, i32, C.c_char_p, i32]
+    lib.bem_krylov_copy_info.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double)]
     for name in EXPORTED:
         if name not in ("bem_last_error", "bem_version", "bem_footprint_bytes", "bem_footprint_multi",
                         "bem_kernel_launches", "bem_mesh_footprint_bytes"):
@@ -220,7 +223,9 @@ class Solver:
 
     def __init__(self, mesh: Mesh, precision=PREC_FP64, restart=0, max_iter=0, tol=0.0, hbm_budget=0.0,
                  precond=True, n_rhs=1, complex64_krylov=False):
-        """complex64_krylov: mixed precision without the fp16 Krylov copy of A.
+        """complex64_krylov: the copy of A that the Krylov products of a mixed
+        precision solver with one right-hand side read: False (the fp16 copy),
+        True (none: they read A) or KRYLOV_BLR (the block low-rank copy).
         precond: True (block-Jacobi with its window correction), "block-jacobi"
         (block-Jacobi alone) or False (none)."""
         lib = load()
@@ -232,8 +237,8 @@ class Solver:
             npc = 0 if precond else 1
         else:
             raise ValueError("precond must be True, False or 'block-jacobi', not %r" % (precond,))
-        p = SolverParams(precision, restart, max_iter, tol, hbm_budget, npc, n_rhs,
-                         1 if complex64_krylov else 0)
+        kc = KRYLOV_BLR if complex64_krylov == KRYLOV_BLR else (1 if complex64_krylov else 0)
+        p = SolverParams(precision, restart, max_iter, tol, hbm_budget, npc, n_rhs, kc)
         h = C.c_void_p()
         _check(lib.bem_solver_create(mesh.handle, C.byref(p), C.byref(h)))
         self.handle = h
@@ -256,6 +261,14 @@ class Solver:
         consumed until the next assemble)."""
         _check(load().bem_solve_direct(self.handle, C.byref(self.info)))
         return self.info.as_dict()
+
+    def krylov_copy_info(self):
+        """bem_krylov_copy_info: the block low-rank Krylov copy (dict)."""
+        nb, nd = C.c_int32(), C.c_int32()
+        mr, by = C.c_double(), C.c_double()
+        _check(load().bem_krylov_copy_info(self.handle, C.byref(nb), C.byref(nd), C.byref(mr), C.byref(by)))
+        return {"blocks_per_row": nb.value, "dense_blocks": nd.value, "mean_rank": mr.value,
+                "bytes_per_product": by.value}
 
     def solution(self):
         x = np.zeros(self.n, np.complex128)

@@ -243,7 +243,7 @@ void dev_release_cached(int device) {
 }
 
 size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, SolverBufs *o, int n_rhs,
-                     SolverBufs *extra, bool half_copy) {
+                     SolverBufs *extra, int krylov_copy) {
     size_t off = 0;
     auto take = [&](size_t bytes) -> void * {
         void *p = base ? (void *)(base + off) : nullptr;
@@ -254,9 +254,19 @@ size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, Solve
     const size_t esz = prec == 0 ? 16 : 8;
     SolverBufs d;
     d.A = take(N * lda * esz);
-    if (prec != 0 && n_rhs == 1 && half_copy) {
+    if (prec != 0 && n_rhs == 1 && (krylov_copy == 0 || krylov_copy == 2)) {
         d.A16 = take(N * lda * 4);
         d.rs = (float *)take(N * (size_t)mv_chunks(n) * 4);
+    }
+    if (prec != 0 && n_rhs == 1 && krylov_copy == 2) {
+        const size_t nb = (size_t)blr_blocks(n), terms = nb * nb * kBlrMaxRank * kBlrB;
+        d.blr_nb = (int)nb;
+        d.blr_rank = (int *)take(nb * nb * 4);
+        d.blr_U = (float2 *)take(terms * 8);
+        d.blr_V = (float2 *)take(terms * 8);
+        d.blr_U16 = (unsigned *)take(terms * 4);
+        d.blr_V16 = (unsigned *)take(terms * 4);
+        d.blr_scale = (float *)take(nb * nb * kBlrMaxRank * 4);
     }
     if (pc) {
         const size_t pb = precond_bytes(n, prec);
@@ -588,7 +598,8 @@ bem_status assemble_group(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned *
     return first;
 }
 
-// fp16 copies of the complex64 matrices that have one (SplitBatch).
+// fp16 copies (SplitBatch) and then block low-rank copies (BlrBatch, over
+// the fp16 copies) of the complex64 matrices that have one.
 cudaError_t split_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
     std::unique_ptr<bem::SplitBatch> t(new bem::SplitBatch());
     t->B = 0;
@@ -611,6 +622,31 @@ cudaError_t split_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
     if (e == cudaSuccess && t->B > 0) {
         bem::split_batch_finish(*t);
         e = bem::launch_split16(*t, st);
+    }
+    std::unique_ptr<bem::BlrBatch> bt(new bem::BlrBatch());
+    bt->B = 0;
+    for (int i = 0; i < cnt && e == cudaSuccess; ++i) {
+        const bem::SolverBufs &d = ss[i]->d;
+        if (d.blr_nb <= 0) continue;
+        bem::BlrSys &q = bt->sys[bt->B++];
+        q.A = d.A;
+        q.lda = ss[i]->lda;
+        q.n = ss[i]->n;
+        q.rank = d.blr_rank;
+        q.U = d.blr_U;
+        q.V = d.blr_V;
+        q.U16 = d.blr_U16;
+        q.V16 = d.blr_V16;
+        q.scale = d.blr_scale;
+        if (bt->B == bem::kMaxAsm) {
+            bem::blr_batch_finish(*bt);
+            e = bem::launch_blr_compress(*bt, st);
+            bt->B = 0;
+        }
+    }
+    if (e == cudaSuccess && bt->B > 0) {
+        bem::blr_batch_finish(*bt);
+        e = bem::launch_blr_compress(*bt, st);
     }
     return e;
 }
@@ -1137,8 +1173,10 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     const int prec = prm.precision == BEM_PREC_FP64 ? 0 : 1;
     const int n_rhs = prm.n_rhs > 0 ? prm.n_rhs : 1;
     if (n_rhs > bem::kMaxRhs) return fail(BEM_ERR_INVALID, "n_rhs %d above the limit %d", n_rhs, bem::kMaxRhs);
-    const bool half = prm.complex64_krylov == 0;
-    const size_t need = bem::solver_layout(n, prec, m, pc, nullptr, nullptr, n_rhs, nullptr, half);
+    if (prm.complex64_krylov < 0 || prm.complex64_krylov > 2)
+        return fail(BEM_ERR_INVALID, "complex64_krylov %d is not 0, 1 or 2", prm.complex64_krylov);
+    const int kcopy = prm.complex64_krylov;
+    const size_t need = bem::solver_layout(n, prec, m, pc, nullptr, nullptr, n_rhs, nullptr, kcopy);
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
     int dev = 0;
@@ -1167,13 +1205,52 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
         s->n_rhs = n_rhs;
         s->xr.resize(n_rhs - 1);
         s->xfreq.resize(n_rhs - 1);
-        bem::solver_layout(n, prec, m, pc, s->block, &s->d, n_rhs, s->xr.data(), half);
+        bem::solver_layout(n, prec, m, pc, s->block, &s->d, n_rhs, s->xr.data(), kcopy);
         e = cudaMemset(s->d.ctr, 0, 4 * sizeof(unsigned));
     }
     if (e != cudaSuccess)
         return fail(e == cudaErrorMemoryAllocation ? BEM_ERR_OUT_OF_HBM : BEM_ERR_CUDA, "solver allocation: %s",
                     cudaGetErrorString(e));
     *out = s.release();
+    return BEM_OK;
+}
+
+bem_status bem_krylov_copy_info(bem_solver_t s, int32_t *blocks_per_row, int32_t *dense_blocks, double *mean_rank,
+                                double *bytes_per_product) {
+    if (!s) return fail(BEM_ERR_INVALID, "null argument");
+    const int nb = s->d.blr_nb;
+    if (nb <= 0) return fail(BEM_ERR_INVALID, "the solver has no block low-rank Krylov copy");
+    std::vector<int> rk((size_t)nb * nb);
+    CU(cudaStreamSynchronize(s->st));
+    CU(cudaMemcpy(rk.data(), s->d.blr_rank, rk.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    const int n = s->n, nchunk = bem::mv_chunks(n);
+    long long dense = 0, lr = 0, rsum = 0;
+    double bytes = 0.0;
+    std::vector<char> item_dense((size_t)nb * nchunk, 0);
+    for (int I = 0; I < nb; ++I)
+        for (int J = 0; J < nb; ++J) {
+            const int r = rk[(size_t)I * nb + J];
+            const double m = std::min(bem::kBlrB, n - I * bem::kBlrB), c = std::min(bem::kBlrB, n - J * bem::kBlrB);
+            if (r < 0) {
+                ++dense;
+                bytes += m * c * 4.0;   // fp16 pairs of the fp16 copy
+                item_dense[(size_t)I * nchunk + J * bem::kBlrB / bem::kMvChunk] = 1;
+            } else {
+                ++lr;
+                rsum += r;
+                bytes += (double)r * (2.0 * bem::kBlrB * 4.0 + 4.0);   // fp16 U_l, V_l and the scale
+            }
+        }
+    // per item (block row x column chunk): its chunk of the input and, with a
+    // dense block, the rows' scales; per row and chunk: one float partial
+    for (int I = 0; I < nb; ++I)
+        for (int c = 0; c < nchunk; ++c)
+            bytes += bem::kMvChunk * 8.0 + (item_dense[(size_t)I * nchunk + c] ? bem::kBlrB * 4.0 : 0.0);
+    bytes += (double)n * nchunk * 8.0;
+    if (blocks_per_row) *blocks_per_row = nb;
+    if (dense_blocks) *dense_blocks = (int32_t)dense;
+    if (mean_rank) *mean_rank = lr > 0 ? (double)rsum / (double)lr : 0.0;
+    if (bytes_per_product) *bytes_per_product = bytes;
     return BEM_OK;
 }
 

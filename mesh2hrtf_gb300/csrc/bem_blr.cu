@@ -1,0 +1,385 @@
+// bem_blr.cu - the block low-rank Krylov copy of a complex64 matrix.
+//
+// After assembly and the fp16 copy, every off-diagonal kBlrB x kBlrB block
+// of A (in the unknowns' Morton order) is approximated by adaptive cross
+// approximation with partial pivoting, in FP32, from A's own entries: take a
+// row's residual against the terms so far, pivot on its largest entry, take
+// that column's residual and add the rank-one term; the next row is the
+// column residual's largest entry among the rows not used yet.  The
+// approximation stops when the new term's Frobenius norm is below kBlrStop
+// times the norm of the sum so far (sum of the terms' squared norms).
+//
+// That stopping rule only looks at the rows and columns it has visited, and
+// on blocks of neighbouring element patches it stops early now and then.  So
+// a second pass over the whole block checks the result: with kBlrSketch
+// Rademacher probes w_p (signs from a hash of the row), sum_p |w_p^T R|^2 /
+// kBlrSketch is an unbiased estimate of |R|_F^2 for the residual R = B - U V^T,
+// computed as w^T B - (w^T U) V^T.  A block whose estimate is within kBlrTol
+// of |B|_F keeps its terms, as fp16 factors with a power-of-two scale per
+// term; any other block, and every diagonal block, is read from the fp16
+// copy of A.  One warp per block; lane l holds entries l, l + 32, ... of the
+// block's rows and columns.
+//
+// Boundary-element matrices have numerically low-rank off-diagonal blocks
+// (the kernels are smooth between separated element patches): on the
+// 5120-triangle head-like mesh 60-80 % of the off-diagonal blocks of 256
+// unknowns compress to 25-30 terms at 0.5-4 kHz, so the copy holds about
+// 1.7 bytes per matrix entry against the fp16 copy's 4.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "bem_internal.h"
+
+namespace bem {
+namespace {
+
+constexpr int kBlrWarps = 2;   // small blocks: a slow warp holds few others back
+
+__device__ __forceinline__ float2 cmul2(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// largest value over the warp and its index (the smaller index on ties)
+__device__ __forceinline__ void warp_argmax(float &v, int &idx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (ov > v || (ov == v && oi < idx)) {
+            v = ov;
+            idx = oi;
+        }
+    }
+}
+// smallest index over the warp whose row is unused (kBlrB if none)
+__device__ __forceinline__ int first_unused(unsigned used, int lane) {
+    int cand = kBlrB;
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        if (!((used >> q) & 1u)) {
+            cand = lane + 32 * q;
+            break;
+        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cand = min(cand, __shfl_xor_sync(0xffffffffu, cand, o));
+    return cand;
+}
+
+// Rademacher probe signs of a row: bit p is the sign of probe p (integer
+// hash lowbias32 by C. Wellons)
+__device__ __forceinline__ unsigned probe_bits(unsigned x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ float psign(unsigned bits, int p) { return ((bits >> p) & 1u) ? -1.f : 1.f; }
+
+// fp16 pairs of v * 2^(15 - e), e the exponent of the largest component of
+// the warp's 256 entries (m = f 2^e, 0.5 <= f < 1); returns e
+__device__ __forceinline__ int store_half(const float2 *v, unsigned *out, int lane) {
+    float2 a[kBlrB / 32];
+    float m = 0.f;
+#pragma unroll
+    for (int q = 0; q < kBlrB / 32; ++q) {
+        a[q] = v[lane + 32 * q];
+        m = fmaxf(m, fmaxf(fabsf(a[q].x), fabsf(a[q].y)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    int e = 0;
+    if (m > 0.f) frexpf(m, &e);
+    const float sc = ldexpf(1.f, 15 - e);
+#pragma unroll
+    for (int q = 0; q < kBlrB / 32; ++q) {
+        const __half2 h = __floats2half2_rn(a[q].x * sc, a[q].y * sc);
+        out[lane + 32 * q] = *reinterpret_cast<const unsigned *>(&h);
+    }
+    return e;
+}
+
+__global__ void __launch_bounds__(32 * kBlrWarps) k_blr_aca(const __grid_constant__ BlrBatch tb) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long gb = (long long)blockIdx.x * kBlrWarps + warp;
+    if (gb >= tb.off[tb.B]) return;
+    int sb = 0;
+    while (gb >= tb.off[sb + 1]) ++sb;
+    const BlrSys &S = tb.sys[sb];
+    const int nb = blr_blocks(S.n);
+    const int b = (int)(gb - tb.off[sb]);
+    const int I = b / nb, J = b - (b / nb) * nb;
+    if (I == J) {
+        if (lane == 0) S.rank[b] = -1;
+        return;
+    }
+    const int I0 = I * kBlrB, J0 = J * kBlrB;
+    const int m = min(kBlrB, S.n - I0), nc = min(kBlrB, S.n - J0);
+    const float2 *A = reinterpret_cast<const float2 *>(S.A);
+    const size_t lda = S.lda;
+    float2 *U = S.U + (size_t)b * kBlrMaxRank * kBlrB;
+    float2 *V = S.V + (size_t)b * kBlrMaxRank * kBlrB;
+    unsigned used = 0;   // bit q: row lane + 32 q taken as a pivot row, or past the block
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        if (lane + 32 * q >= m) used |= 1u << q;
+    const float stop2 = kBlrStop * kBlrStop;
+    int istar = 0, k = 0;
+    float norm2 = 0.f;
+    bool ok = false;
+    for (int step = 0; step < kBlrMaxRank + kBlrB && k < kBlrMaxRank; ++step) {
+        // residual of row istar
+        float2 r[8];
+        const float2 *arow = A + (size_t)(I0 + istar) * lda + J0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int j = lane + 32 * q;
+            r[q] = j < nc ? arow[j] : make_float2(0.f, 0.f);
+        }
+#pragma unroll 4
+        for (int l = 0; l < k; ++l) {
+            const float2 ul = U[(size_t)l * kBlrB + istar];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float2 p = cmul2(ul, V[(size_t)l * kBlrB + lane + 32 * q]);
+                r[q].x -= p.x;
+                r[q].y -= p.y;
+            }
+        }
+        if (lane == (istar & 31)) used |= 1u << (istar >> 5);
+        float best = -1.f;
+        int bj = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int j = lane + 32 * q;
+            const float a = r[q].x * r[q].x + r[q].y * r[q].y;
+            if (j < nc && a > best) {
+                best = a;
+                bj = j;
+            }
+        }
+        warp_argmax(best, bj);
+        if (!(best > 1e-30f)) {
+            // the row is already represented: try the next unused row
+            const int nx = first_unused(used, lane);
+            if (nx >= kBlrB) {
+                ok = true;
+                break;
+            }
+            istar = nx;
+            continue;
+        }
+        // the pivot entry r[bj], from the lane that holds it
+        const int sel = bj >> 5;
+        float2 piv = r[0];
+#pragma unroll
+        for (int q = 1; q < 8; ++q) {
+            piv.x = sel == q ? r[q].x : piv.x;
+            piv.y = sel == q ? r[q].y : piv.y;
+        }
+        piv.x = __shfl_sync(0xffffffffu, piv.x, bj & 31);
+        piv.y = __shfl_sync(0xffffffffu, piv.y, bj & 31);
+        const float pd = 1.f / (piv.x * piv.x + piv.y * piv.y);
+        const float2 inv = make_float2(piv.x * pd, -piv.y * pd);
+        float nv2 = 0.f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int j = lane + 32 * q;
+            const float2 v = j < nc ? cmul2(r[q], inv) : make_float2(0.f, 0.f);
+            V[(size_t)k * kBlrB + j] = v;
+            nv2 += v.x * v.x + v.y * v.y;
+        }
+        // residual of column bj
+        float2 c[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = lane + 32 * q;
+            c[q] = i < m ? A[(size_t)(I0 + i) * lda + J0 + bj] : make_float2(0.f, 0.f);
+        }
+        __syncwarp();   // this step's V row is in memory for every lane
+#pragma unroll 4
+        for (int l = 0; l < k; ++l) {
+            const float2 vl = V[(size_t)l * kBlrB + bj];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float2 p = cmul2(U[(size_t)l * kBlrB + lane + 32 * q], vl);
+                c[q].x -= p.x;
+                c[q].y -= p.y;
+            }
+        }
+        float nu2 = 0.f, bu = -1.f;
+        int bi = kBlrB;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = lane + 32 * q;
+            U[(size_t)k * kBlrB + i] = c[q];
+            const float a = c[q].x * c[q].x + c[q].y * c[q].y;
+            nu2 += a;
+            if (!((used >> q) & 1u) && a > bu) {
+                bu = a;
+                bi = i;
+            }
+        }
+        nu2 = warp_sumf(nu2);
+        nv2 = warp_sumf(nv2);
+        const float t2 = nu2 * nv2;
+        norm2 += t2;
+        ++k;
+        __syncwarp();   // this step's U column is in memory for every lane
+        if (t2 <= stop2 * norm2) {
+            ok = true;
+            break;
+        }
+        warp_argmax(bu, bi);
+        if (bi >= kBlrB || bu < 0.f) {
+            ok = true;   // every row is a pivot row: the terms reproduce the block
+            break;
+        }
+        istar = bi;
+    }
+    if (lane == 0) S.rank[b] = ok ? k : -1;
+}
+
+
+// The probe check of k_blr_aca's approximations and their fp16 factors;
+// blocks it rejects become dense.  One block of 256 threads per matrix block:
+// the warps first form w_p^T U_l (warp w: terms w, w + 8, ...), then thread t
+// streams column t of the block (the warps together read whole rows) and
+// accumulates w_p^T B, and subtracts (w_p^T U) V^T.
+constexpr int kChkThreads = kBlrB;
+
+__global__ void __launch_bounds__(kChkThreads, 4) k_blr_check(const __grid_constant__ BlrBatch tb) {
+    __shared__ float2 cw[kBlrSketch][kBlrMaxRank];   // w_p^T U_l
+    __shared__ float red[2][kChkThreads / 32];
+    __shared__ int keep;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const long long gb = blockIdx.x;
+    if (gb >= tb.off[tb.B]) return;
+    int sb = 0;
+    while (gb >= tb.off[sb + 1]) ++sb;
+    const BlrSys &S = tb.sys[sb];
+    const int nb = blr_blocks(S.n);
+    const int b = (int)(gb - tb.off[sb]);
+    const int k = S.rank[b];
+    if (k < 0) return;
+    const int I = b / nb, J = b - (b / nb) * nb;
+    const int I0 = I * kBlrB, J0 = J * kBlrB;
+    const int m = min(kBlrB, S.n - I0), nc = min(kBlrB, S.n - J0);
+    const float2 *A = reinterpret_cast<const float2 *>(S.A);
+    const size_t lda = S.lda;
+    const float2 *U = S.U + (size_t)b * kBlrMaxRank * kBlrB;
+    const float2 *V = S.V + (size_t)b * kBlrMaxRank * kBlrB;
+    const unsigned key0 = (unsigned)(gb * kBlrB);
+    {
+        unsigned hb[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) hb[q] = probe_bits(key0 + lane + 32 * q);
+        for (int l = warp; l < k; l += kChkThreads / 32) {
+            float pr[kBlrSketch], pi[kBlrSketch];
+#pragma unroll
+            for (int p = 0; p < kBlrSketch; ++p) pr[p] = pi[p] = 0.f;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float2 u = U[(size_t)l * kBlrB + lane + 32 * q];   // zero past the block
+#pragma unroll
+                for (int p = 0; p < kBlrSketch; ++p) {
+                    const float sg = psign(hb[q], p);
+                    pr[p] = fmaf(sg, u.x, pr[p]);
+                    pi[p] = fmaf(sg, u.y, pi[p]);
+                }
+            }
+#pragma unroll
+            for (int p = 0; p < kBlrSketch; ++p) {
+                pr[p] = warp_sumf(pr[p]);
+                pi[p] = warp_sumf(pi[p]);
+            }
+            if (lane == 0)
+#pragma unroll
+                for (int p = 0; p < kBlrSketch; ++p) cw[p][l] = make_float2(pr[p], pi[p]);
+        }
+    }
+    __syncthreads();
+    float2 acc[kBlrSketch];
+#pragma unroll
+    for (int p = 0; p < kBlrSketch; ++p) acc[p] = make_float2(0.f, 0.f);
+    float bn2 = 0.f;
+    if (t < nc) {
+        const float2 *col = A + (size_t)I0 * lda + J0 + t;
+#pragma unroll 8
+        for (int i = 0; i < m; ++i) {
+            const unsigned bits = probe_bits(key0 + i);
+            const float2 bv = __ldcs(col + (size_t)i * lda);
+            bn2 = fmaf(bv.x, bv.x, fmaf(bv.y, bv.y, bn2));
+#pragma unroll
+            for (int p = 0; p < kBlrSketch; ++p) {
+                const float sg = psign(bits, p);
+                acc[p].x = fmaf(sg, bv.x, acc[p].x);
+                acc[p].y = fmaf(sg, bv.y, acc[p].y);
+            }
+        }
+    }
+    for (int l = 0; l < k; ++l) {
+        const float2 v = V[(size_t)l * kBlrB + t];   // zero past the block
+#pragma unroll
+        for (int p = 0; p < kBlrSketch; ++p) {
+            const float2 w = cmul2(cw[p][l], v);
+            acc[p].x -= w.x;
+            acc[p].y -= w.y;
+        }
+    }
+    float est = 0.f;
+#pragma unroll
+    for (int p = 0; p < kBlrSketch; ++p) est = fmaf(acc[p].x, acc[p].x, fmaf(acc[p].y, acc[p].y, est));
+    est = warp_sumf(est);
+    bn2 = warp_sumf(bn2);
+    if (lane == 0) {
+        red[0][warp] = est;
+        red[1][warp] = bn2;
+    }
+    __syncthreads();
+    if (t == 0) {
+        float e = 0.f, bb = 0.f;
+        for (int w = 0; w < kChkThreads / 32; ++w) {
+            e += red[0][w];
+            bb += red[1][w];
+        }
+        keep = e / (float)kBlrSketch <= kBlrTol * kBlrTol * bb;
+        if (!keep) S.rank[b] = -1;
+    }
+    __syncthreads();
+    if (!keep) return;
+    // the kept terms as fp16 factors, scale 2^(eu - 15) 2^(ev - 15) per term
+    unsigned *U16 = S.U16 + (size_t)b * kBlrMaxRank * kBlrB;
+    unsigned *V16 = S.V16 + (size_t)b * kBlrMaxRank * kBlrB;
+    for (int l = warp; l < k; l += kChkThreads / 32) {
+        const int eu = store_half(U + (size_t)l * kBlrB, U16 + (size_t)l * kBlrB, lane);
+        const int ev = store_half(V + (size_t)l * kBlrB, V16 + (size_t)l * kBlrB, lane);
+        if (lane == 0) S.scale[(size_t)b * kBlrMaxRank + l] = ldexpf(1.f, eu + ev - 30);
+    }
+}
+
+}  // namespace
+
+void blr_batch_finish(BlrBatch &t) {
+    t.off[0] = 0;
+    for (int b = 0; b < t.B; ++b) {
+        const int nb = blr_blocks(t.sys[b].n);
+        t.off[b + 1] = t.off[b] + nb * nb;
+    }
+}
+
+cudaError_t launch_blr_compress(const BlrBatch &t, cudaStream_t st) {
+    if (t.B <= 0 || t.off[t.B] == 0) return cudaSuccess;
+    count_launches(2);
+    const int grid = (t.off[t.B] + kBlrWarps - 1) / kBlrWarps;
+    k_blr_aca<<<grid, 32 * kBlrWarps, 0, st>>>(t);
+    k_blr_check<<<t.off[t.B], kChkThreads, 0, st>>>(t);
+    return cudaGetLastError();
+}
+
+}  // namespace bem

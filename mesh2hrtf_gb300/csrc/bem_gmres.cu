@@ -156,12 +156,13 @@ __device__ void plan_build(KTable *tb, int which) {
     __shared__ int cnt[kMaxSys], act[kMaxSys];
     __shared__ unsigned gm[kMaxSys];
     const int t = threadIdx.x;
-    int c = 0;
+    int c = 0, cb = 0;
     if (t < tb->B) {
         const KSys &S = tb->sys[t];
         if (!S.shared && mv_active(S.st, which, tb->prec)) {
             const int strip = S.strip > 0 ? S.strip : kTmaStrip;
-            c = (which == 0 && S.A16) ? mv_items16(S.n, strip) : mv_items_of(S.n, tb->prec, strip);
+            if (which == 0 && S.blr_nb > 0) cb = S.blr_nb * S.nchunk;   // block low-rank copy
+            else c = (which == 0 && S.A16) ? mv_items16(S.n, strip) : mv_items_of(S.n, tb->prec, strip);
         }
     }
     cnt[t] = c;
@@ -177,14 +178,15 @@ __device__ void plan_build(KTable *tb, int which) {
     __syncthreads();
     // exclusive prefix sums over the kMaxSys slots (warp scans, then the
     // warps' totals in order): the plan entries in slot order
-    __shared__ int wsum[kMaxSys / 32][4];
+    __shared__ int wsum[kMaxSys / 32][6];
     const int lane = t & 31, wp = t >> 5;
     const int ga = gm[t] ? 1 : 0;
     const int grows = which == 1 ? kGrpRowsExact : (which == 0 && tb->grp_umma ? kUmRows : kGrpRowsInner);
     const int gc = ga ? ceil_div(tb->sys[tb->grp[t].first].n, grows) : 0;
-    int v[4] = {act[t], cnt[t], ga, gc};
+    const int ba = cb > 0 ? 1 : 0;
+    int v[6] = {act[t], cnt[t], ga, gc, ba, cb};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < 6; ++q) {
         for (int o = 1; o < 32; o <<= 1) {
             const int y = __shfl_up_sync(0xffffffffu, v[q], o);
             if (lane >= o) v[q] += y;
@@ -192,12 +194,13 @@ __device__ void plan_build(KTable *tb, int which) {
         if (lane == 31) wsum[wp][q] = v[q];
     }
     __syncthreads();
-    int base[4] = {0, 0, 0, 0};
+    int base[6] = {0, 0, 0, 0, 0, 0};
     for (int w = 0; w < wp; ++w)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) base[q] += wsum[w][q];
+        for (int q = 0; q < 6; ++q) base[q] += wsum[w][q];
     const int pos = base[0] + v[0] - act[t], off = base[1] + v[1] - cnt[t];
     const int gpos = base[2] + v[2] - ga, goff = base[3] + v[3] - gc;
+    const int bpos = base[4] + v[4] - ba, boff = base[5] + v[5] - cb;
     KPlan &p = tb->plan[which];
     KPlan &gp = tb->gplan[which];
     if (act[t]) {
@@ -209,11 +212,19 @@ __device__ void plan_build(KTable *tb, int which) {
         gp.off[gpos] = goff;
         tb->gmask[which][gpos] = gm[t];
     }
+    if (which == 0 && ba) {
+        tb->bplan.sys[bpos] = t;
+        tb->bplan.off[bpos] = boff;
+    }
     if (t == kMaxSys - 1) {
         p.n = base[0] + v[0];
         p.off[p.n] = base[1] + v[1];
         gp.n = base[2] + v[2];
         gp.off[gp.n] = base[3] + v[3];
+        if (which == 0) {
+            tb->bplan.n = base[4] + v[4];
+            tb->bplan.off[tb->bplan.n] = base[5] + v[5];
+        }
     }
     __syncthreads();
 }
@@ -1483,6 +1494,182 @@ __global__ void __launch_bounds__(32 * kUmWarps, 1) k_mv_grp_umma(KTable *tb) {
     }
 }
 
+// ------------------------------------------------------------ block low-rank product
+// Krylov products of systems with a block low-rank copy (KSys::blr_nb > 0,
+// compressed by k_blr_aca over the fp16 copy).  Persistent grid of 256-thread
+// blocks; items (system, block row I, chunk c of kMvChunk columns =
+// kBlrPerItem blocks) from the queue.  Phase 1: warp w takes the terms
+// w, w + 8, ... of the item's compressed blocks, t_l = s_l V_l . x (fp16
+// factors).  Phase 2: thread i takes row i: sum over the item's compressed
+// blocks of U_l[i] t_l, plus its fp16 row segments of the dense blocks (the
+// thread streams them: 32-byte loads, one sector each) times the row's scale
+// for the chunk.  Sums run in a fixed order; the partial is float, one per
+// row and chunk like k_mv_tma's, so k_dot1 sums them unchanged.
+constexpr int kBlrThreads = kBlrB;
+constexpr int kBlrPerItem = kMvChunk / kBlrB;
+static_assert(kMvChunk % kBlrB == 0, "a chunk holds whole blocks");
+
+// y += a x, a an fp16 pair
+__device__ __forceinline__ void cmac_h(float2 &y, unsigned a, float2 x) {
+    const float2 av = h2f(a);
+    y.x = fmaf(av.x, x.x, y.x);
+    y.x = fmaf(-av.y, x.y, y.x);
+    y.y = fmaf(av.x, x.y, y.y);
+    y.y = fmaf(av.y, x.x, y.y);
+}
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+__global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
+    __shared__ float2 xs[kMvChunk];
+    __shared__ float2 ts[kBlrPerItem][kBlrMaxRank];
+    __shared__ int rk[kBlrPerItem], tsk[kBlrPerItem + 1];
+    __shared__ int item_s;
+    __shared__ PlanSmem pl;
+    plan_load(tb->bplan, pl);   // includes a block barrier
+    const int total = pl.off[pl.n];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    while (total > 0) {
+        if (threadIdx.x == 0) item_s = (int)atomicAdd(&tb->mv_ctr[0], 1u);
+        __syncthreads();
+        const int item = item_s;
+        if (item >= total) break;
+        const int j = plan_find(pl.off, pl.n, item);
+        const KSys &S = tb->sys[pl.sys[j]];
+        const int local = item - pl.off[j];
+        const int n = S.n, nb = S.blr_nb;
+        const int I = local / S.nchunk, c = local - I * S.nchunk;
+        const int c0 = c * kMvChunk, row0 = I * kBlrB;
+        for (int q = threadIdx.x; q < kMvChunk; q += kBlrThreads)
+            xs[q] = c0 + q < n ? S.xh[c0 + q] : make_float2(0.f, 0.f);
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int q = 0; q < kBlrPerItem; ++q) {
+                const int J = c * kBlrPerItem + q;
+                const int r = J < nb ? S.blr_rank[(size_t)I * nb + J] : 0;
+                rk[q] = r;
+                tsk[q] = acc;
+                acc += r > 0 ? r : 0;
+            }
+            tsk[kBlrPerItem] = acc;
+        }
+        __syncthreads();
+        // phase 1: t_l of the compressed blocks, two terms per warp at a time
+        const int nt = tsk[kBlrPerItem];
+        for (int t0 = warp; t0 < nt; t0 += 2 * (kBlrThreads / 32)) {
+            unsigned a[2][kBlrB / 32];
+            size_t bl[2];
+            int qq[2], ll[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int t = min(t0 + h * (kBlrThreads / 32), nt - 1);
+                int q = 0;
+                while (t >= tsk[q + 1]) ++q;
+                qq[h] = q;
+                ll[h] = t - tsk[q];
+                bl[h] = ((size_t)I * nb + c * kBlrPerItem + q) * kBlrMaxRank + ll[h];
+                const unsigned *v = S.blr_V16 + bl[h] * kBlrB;
+#pragma unroll
+                for (int e = 0; e < kBlrB / 32; ++e) a[h][e] = v[lane + 32 * e];
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const float2 *xq = xs + qq[h] * kBlrB;
+                float sr = 0.f, si = 0.f;
+#pragma unroll
+                for (int e = 0; e < kBlrB / 32; ++e) {
+                    const float2 av = h2f(a[h][e]), x = xq[lane + 32 * e];
+                    sr = fmaf(av.x, x.x, sr);
+                    sr = fmaf(-av.y, x.y, sr);
+                    si = fmaf(av.x, x.y, si);
+                    si = fmaf(av.y, x.x, si);
+                }
+                sr = warp_sum_f(sr);
+                si = warp_sum_f(si);
+                if (lane == 0 && (h == 0 || t0 + h * (kBlrThreads / 32) < nt)) {
+                    const float sc = S.blr_scale[bl[h]];
+                    ts[qq[h]][ll[h]] = make_float2(sr * sc, si * sc);
+                }
+            }
+        }
+        __syncthreads();
+        // phase 2: row i
+        const int i = threadIdx.x, row = row0 + i;
+        if (row < n) {
+            float2 y = make_float2(0.f, 0.f), yd = make_float2(0.f, 0.f);
+            bool dense = false;
+#pragma unroll 1
+            for (int q = 0; q < kBlrPerItem; ++q) {
+                const int r = rk[q], J = c * kBlrPerItem + q;
+                if (J >= nb) break;
+                if (r < 0) {
+                    // fp16 row segment of the dense block
+                    dense = true;
+                    const int nc = min(kBlrB, n - J * kBlrB);
+                    const unsigned *h = reinterpret_cast<const unsigned *>(S.A16) + (size_t)row * S.lda +
+                                        (size_t)J * kBlrB;
+                    const float2 *xq = xs + q * kBlrB;
+                    if (nc == kBlrB) {
+                        const uint4 *h4 = reinterpret_cast<const uint4 *>(h);
+#pragma unroll 4
+                        for (int g = 0; g < kBlrB / 8; ++g) {
+                            const uint4 p0 = h4[2 * g], p1 = h4[2 * g + 1];
+                            cmac_h(yd, p0.x, xq[8 * g + 0]);
+                            cmac_h(yd, p0.y, xq[8 * g + 1]);
+                            cmac_h(yd, p0.z, xq[8 * g + 2]);
+                            cmac_h(yd, p0.w, xq[8 * g + 3]);
+                            cmac_h(yd, p1.x, xq[8 * g + 4]);
+                            cmac_h(yd, p1.y, xq[8 * g + 5]);
+                            cmac_h(yd, p1.z, xq[8 * g + 6]);
+                            cmac_h(yd, p1.w, xq[8 * g + 7]);
+                        }
+                    } else {
+                        for (int e = 0; e < nc; ++e) cmac_h(yd, h[e], xq[e]);
+                    }
+                    continue;
+                }
+                const unsigned *u = S.blr_U16 + ((size_t)I * nb + J) * kBlrMaxRank * kBlrB + i;
+                int l = 0;
+                for (; l + 8 <= r; l += 8) {
+                    unsigned w[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) w[e] = u[(size_t)(l + e) * kBlrB];
+                    float2 p = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const float2 pe = cmulf(h2f(w[e]), ts[q][l + e]);
+                        p.x += pe.x;
+                        p.y += pe.y;
+                    }
+                    y.x += p.x;
+                    y.y += p.y;
+                }
+                for (; l < r; ++l) {
+                    const float2 p = cmulf(h2f(u[(size_t)l * kBlrB]), ts[q][l]);
+                    y.x += p.x;
+                    y.y += p.y;
+                }
+            }
+            if (dense) {
+                const float sc = S.rs[(size_t)row * S.nchunk + c];
+                y.x = fmaf(yd.x, sc, y.x);
+                y.y = fmaf(yd.y, sc, y.y);
+            }
+            reinterpret_cast<float2 *>(S.mvp)[(size_t)c * n + row] = y;
+        }
+        __syncthreads();   // shared buffers are rewritten by the next item
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&tb->mv_ctr[1], 1u) == gridDim.x - 1) {
+            tb->mv_ctr[0] = 0u;
+            tb->mv_ctr[1] = 0u;
+            __threadfence();
+        }
+    }
+}
+
 // ------------------------------------------------------------ block helpers
 // dp[l * nvb + blk] = sum over the block's rows of conj(V_l[row]) w[row], l < nv.
 __device__ void block_dots(const double2 *__restrict__ V, long long ldv, int nv, double2 wv, bool ok, int row,
@@ -2279,6 +2466,7 @@ __global__ void __launch_bounds__(kMaxSys) k_plans(KTable *tb) {
 int g_mv_grid[2] = {0, 0};
 int g_vec_grid = 0;
 int g_pcw_grid = 0;   // k_pcwin: every block it can keep resident (loads in flight)
+int g_blr_grid = 0;   // k_mv_blr: every block it can keep resident
 std::atomic<long long> g_launches{0};
 
 }  // namespace
@@ -2322,6 +2510,9 @@ cudaError_t krylov_prepare() {
         per = 0;
         if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcwin<false>, kThreads, 0);
         g_pcw_grid = sms * (per > 0 ? per : 1);
+        per = 0;
+        if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mv_blr, kBlrThreads, 0);
+        g_blr_grid = sms * (per > 0 ? per : 1);
     });
     return err;
 }
@@ -2357,7 +2548,7 @@ static void pc_window(bool c128, const KTable *d_tab, int mode, int gv, cudaStre
 }
 
 cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev, cudaStream_t st,
-                               int *launches_out, bool groups) {
+                               int *launches_out, bool groups, bool blr) {
     KTable *tb = const_cast<KTable *>(d_tab);
     const bool c128 = prec == 0;
     if (!g_vec_grid) return cudaErrorNotReady;   // krylov_prepare() first
@@ -2374,6 +2565,10 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
                 k_mv_grp_tc<<<gmv, 32 * (kTcWarps + 1), kTcSmem, st>>>(tb, 0);
                 k_mv_grp_umma<<<gmv, 32 * kUmWarps, kUmSmem, st>>>(tb);
                 nl += 2;
+            }
+            if (blr) {
+                k_mv_blr<<<g_blr_grid, kBlrThreads, 0, st>>>(tb);
+                ++nl;
             }
         }
         if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q + 1], st, cudaEventRecordExternal);

@@ -245,6 +245,39 @@ struct SplitBatch {
 void split_batch_finish(SplitBatch &t);
 cudaError_t launch_split16(const SplitBatch &t, cudaStream_t st);
 
+// Block low-rank Krylov copy of a complex64 matrix (bem_blr.cu), on top of
+// its fp16 copy: blocks of kBlrB x kBlrB unknowns.  Every off-diagonal block
+// is approximated by adaptive cross approximation (stopping at kBlrStop);
+// when a randomized estimate of the approximation's error (kBlrSketch
+// Rademacher probes of the whole block) is within kBlrTol of the block's
+// Frobenius norm, and at most kBlrMaxRank terms were needed, the block is
+// kept as sum_l s_l U_l V_l^T with fp16 factors U_l, V_l and a power-of-two
+// scale s_l; every other block (the diagonal ones included) is read from the
+// fp16 copy.  The Krylov products read this copy; the refinement residuals
+// keep reading A, so its accuracy bounds only how much an inner cycle gains.
+constexpr int kBlrB = 256;
+constexpr int kBlrMaxRank = 48;
+constexpr float kBlrTol = 2e-4f;
+constexpr float kBlrStop = 4e-5f;
+constexpr int kBlrSketch = 8;
+__host__ __device__ inline int blr_blocks(int n) { return ceil_div(n, kBlrB); }
+struct BlrSys {
+    const void *A;          // complex64, leading dimension lda
+    size_t lda;
+    int n;
+    int *rank;              // [nb][nb] rank of block (I, J), -1: dense
+    float2 *U, *V;          // FP32 work terms [nb * nb][kBlrMaxRank][kBlrB]: U[b][l][i], V[b][l][j]
+    unsigned *U16, *V16;    // the kept factors as fp16 pairs, same layout
+    float *scale;           // [nb * nb][kBlrMaxRank]
+};
+struct BlrBatch {
+    int B;
+    int off[kMaxAsm + 1];   // prefix of blocks (one warp each)
+    BlrSys sys[kMaxAsm];
+};
+void blr_batch_finish(BlrBatch &t);
+cudaError_t launch_blr_compress(const BlrBatch &t, cudaStream_t st);
+
 // ---------------------------------------------------------------- Krylov engine
 // Restarted GMRES of one system as a state machine on the device.  An
 // iteration body (one captured graph) runs kSteps Arnoldi steps for every
@@ -294,6 +327,11 @@ struct KSys {
     void *pcy, *pcz;        // its vectors X v and A_w X v: float2 for complex64
                             // systems, double2 for complex128
     int strip;              // rows per item of the TMA product (0: kTmaStrip)
+    int blr_nb;             // > 0: the Krylov products read the block low-rank
+                            // copy (blr_nb block rows; BlrSys) over A16
+    const int *blr_rank;
+    const unsigned *blr_U16, *blr_V16;
+    const float *blr_scale;
     KState *st;
 };
 
@@ -328,6 +366,7 @@ struct KTable {
     int n_groups;           // shared-matrix groups
     KGroup grp[kMaxSys];
     KPlan gplan[3];         // plans of the shared-matrix products (entries = groups)
+    KPlan bplan;            // Krylov products from block low-rank copies (k_mv_blr)
     unsigned gmask[3][kMaxSys];   // per plan entry: members taking part
     const int2 *vb_items;   // (system, block)
     int grp_umma;           // 1: the groups' Krylov products run on the 5th-generation
@@ -358,10 +397,11 @@ constexpr int kSteps = 8;
 // st.  mv_ev: 2 * (kSteps + 1) events recorded around the matrix-vector
 // products (may be nullptr).  prec: 0 complex128, 1 complex64 matrices.
 // groups: include the shared-matrix (group) products, for batches that have
-// groups.  Returns the number of kernel launches enqueued through
-// *launches_out.
+// groups; blr: include the block low-rank product (k_mv_blr), for batches
+// with systems that have a block low-rank copy.  Returns the number of kernel
+// launches enqueued through *launches_out.
 cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev, cudaStream_t st,
-                               int *launches_out, bool groups);
+                               int *launches_out, bool groups, bool blr);
 // complex64 matrices: the product streams row segments with bulk copies
 // (TMA) in strips of `strip` rows (a multiple of kTmaRows, chosen per system
 // by the tuner; kTmaStrip by default); complex128: tiles of kMvRows rows.

@@ -69,6 +69,11 @@ struct SolverBufs {
     void *A = nullptr;
     void *A16 = nullptr;       // mixed precision, one right-hand side: fp16 copy of A
     float *rs = nullptr;       // its row scales
+    int blr_nb = 0;            // mixed precision, one right-hand side: block low-rank
+    int *blr_rank = nullptr;   // copy of A (kBlrB blocks, blr_nb per row; BlrSys)
+    float2 *blr_U = nullptr, *blr_V = nullptr;   // for the Krylov products
+    unsigned *blr_U16 = nullptr, *blr_V16 = nullptr;
+    float *blr_scale = nullptr;
     double2 *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *z = nullptr, *V = nullptr;
     double2 *mvp = nullptr, *dpa = nullptr, *dpb = nullptr;
     float2 *xh = nullptr;
@@ -88,10 +93,11 @@ struct SolverBufs {
 
 // Byte layout of a solver's block for n_rhs right-hand sides; base ==
 // nullptr only sizes it (bem_footprint_bytes is this size for one).
-// half_copy: complex64 solvers with one right-hand side keep the fp16 copy
-// of A that their Krylov products read.
+// krylov_copy: the copy of A that the Krylov products of complex64 solvers
+// with one right-hand side read: 0 fp16 (row-scaled), 1 none (they read A),
+// 2 block low-rank over the fp16 copy.
 size_t solver_layout(int n, int prec, int m, bool pc, unsigned char *base, SolverBufs *o, int n_rhs = 1,
-                     SolverBufs *extra = nullptr, bool half_copy = true);
+                     SolverBufs *extra = nullptr, int krylov_copy = 0);
 
 }  // namespace bem
 
@@ -160,6 +166,11 @@ struct bem_solver_s {
         k.mvp = d.mvp; k.dpa = d.dpa; k.dpb = d.dpb; k.nrmp = d.nrmp;
         k.H = d.H; k.cs = d.cs; k.sn = d.sn; k.g = d.g; k.y = d.y; k.hsum = d.hsum;
         k.strip = mv_strip;
+        k.blr_nb = d.blr_nb;
+        k.blr_rank = d.blr_rank;
+        k.blr_U16 = d.blr_U16;
+        k.blr_V16 = d.blr_V16;
+        k.blr_scale = d.blr_scale;
         return k;
     }
     bem::KState kinit() const {
@@ -175,7 +186,7 @@ struct bem_solver_s {
         // (the right-hand sides of a solver with several share TF32 tensor-core
         // products of about the same accuracy)
         const bool tf32 = n_rhs > 1 && bem::group_product_umma();
-        q.floor_rel = prec == BEM_PREC_MIXED ? ((d.A16 || tf32) ? 3e-4 : 1e-5) : 0.0;
+        q.floor_rel = prec == BEM_PREC_MIXED ? ((d.A16 || d.blr_nb > 0 || tf32) ? 3e-4 : 1e-5) : 0.0;
         return q;
     }
     bem::AsmSys asys(int r = 0) const {
