@@ -104,6 +104,46 @@ __device__ __forceinline__ int store_half(const float2 *v, unsigned *out, int la
     return e;
 }
 
+// entry q of a lane's 8 (q = idx >> 5), from lane idx & 31, on every lane
+__device__ __forceinline__ float2 pick8(const float2 (&v)[8], int idx) {
+    const int sel = idx >> 5;
+    float2 p = v[0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) {
+        p.x = sel == q ? v[q].x : p.x;
+        p.y = sel == q ? v[q].y : p.y;
+    }
+    p.x = __shfl_sync(0xffffffffu, p.x, idx & 31);
+    p.y = __shfl_sync(0xffffffffu, p.y, idx & 31);
+    return p;
+}
+// largest |v|^2 over the entries < lim and its index (kBlrB, -1 if none)
+__device__ __forceinline__ void argmax8(const float2 (&v)[8], int lim, int lane, float &best, int &idx) {
+    best = -1.f;
+    idx = kBlrB;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int j = lane + 32 * q;
+        const float a = v[q].x * v[q].x + v[q].y * v[q].y;
+        if (j < lim && a > best) {
+            best = a;
+            idx = j;
+        }
+    }
+    warp_argmax(best, idx);
+}
+__device__ __forceinline__ unsigned mark_row(unsigned used, int row, int lane) {
+    return (row >= 0 && row < kBlrB && lane == (row & 31)) ? used | (1u << (row >> 5)) : used;
+}
+
+// Cross approximation with two pivots per pass: rows i1, i2 (the two largest
+// entries of the last column residual among unused rows) are taken together,
+// so each pass reads the terms so far once for two new terms.  Term 1 pivots
+// on row i1's residual; row i2's residual is updated by term 1 and gives
+// term 2; the column of term 2 is updated by term 1 likewise.  The result is
+// the two-step cross approximation with these pivots; only the choice of i2
+// (from the column residual one term earlier) differs from the one-pivot
+// method.
 __global__ void __launch_bounds__(32 * kBlrWarps) k_blr_aca(const __grid_constant__ BlrBatch tb) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long gb = (long long)blockIdx.x * kBlrWarps + warp;
@@ -129,122 +169,193 @@ __global__ void __launch_bounds__(32 * kBlrWarps) k_blr_aca(const __grid_constan
     for (int q = 0; q < 8; ++q)
         if (lane + 32 * q >= m) used |= 1u << q;
     const float stop2 = kBlrStop * kBlrStop;
-    int istar = 0, k = 0;
+    int i1 = 0, i2 = m > 1 ? 1 : -1, k = 0;
     float norm2 = 0.f;
     bool ok = false;
-    for (int step = 0; step < kBlrMaxRank + kBlrB && k < kBlrMaxRank; ++step) {
-        // residual of row istar
-        float2 r[8];
-        const float2 *arow = A + (size_t)(I0 + istar) * lda + J0;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int j = lane + 32 * q;
-            r[q] = j < nc ? arow[j] : make_float2(0.f, 0.f);
-        }
-#pragma unroll 4
-        for (int l = 0; l < k; ++l) {
-            const float2 ul = U[(size_t)l * kBlrB + istar];
+    for (int pass = 0; pass < kBlrMaxRank + kBlrB && k + 2 <= kBlrMaxRank; ++pass) {
+        bool two = i2 >= 0;
+        // residuals of rows i1 and i2
+        float2 r1[8], r2[8];
+        {
+            const float2 *a1 = A + (size_t)(I0 + i1) * lda + J0;
+            const float2 *a2 = A + (size_t)(I0 + (two ? i2 : i1)) * lda + J0;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                const float2 p = cmul2(ul, V[(size_t)l * kBlrB + lane + 32 * q]);
-                r[q].x -= p.x;
-                r[q].y -= p.y;
+                const int j = lane + 32 * q;
+                r1[q] = j < nc ? a1[j] : make_float2(0.f, 0.f);
+                r2[q] = (two && j < nc) ? a2[j] : make_float2(0.f, 0.f);
             }
         }
-        if (lane == (istar & 31)) used |= 1u << (istar >> 5);
-        float best = -1.f;
-        int bj = 0;
+#pragma unroll 2
+        for (int l = 0; l < k; ++l) {
+            const float2 u1 = U[(size_t)l * kBlrB + i1];
+            const float2 u2 = two ? U[(size_t)l * kBlrB + i2] : make_float2(0.f, 0.f);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int j = lane + 32 * q;
-            const float a = r[q].x * r[q].x + r[q].y * r[q].y;
-            if (j < nc && a > best) {
-                best = a;
-                bj = j;
+            for (int q = 0; q < 8; ++q) {
+                const float2 v = V[(size_t)l * kBlrB + lane + 32 * q];
+                const float2 p1 = cmul2(u1, v), p2 = cmul2(u2, v);
+                r1[q].x -= p1.x;
+                r1[q].y -= p1.y;
+                r2[q].x -= p2.x;
+                r2[q].y -= p2.y;
             }
         }
-        warp_argmax(best, bj);
+        used = mark_row(mark_row(used, i1, lane), i2, lane);
+        float best;
+        int j1;
+        argmax8(r1, nc, lane, best, j1);
+        if (!(best > 1e-30f) && two) {
+            // row i1 is represented already: row i2 alone gives the term
+#pragma unroll
+            for (int q = 0; q < 8; ++q) r1[q] = r2[q];
+            two = false;
+            argmax8(r1, nc, lane, best, j1);
+        }
         if (!(best > 1e-30f)) {
-            // the row is already represented: try the next unused row
-            const int nx = first_unused(used, lane);
-            if (nx >= kBlrB) {
+            // both rows are represented: the next unused rows
+            i1 = first_unused(used, lane);
+            if (i1 >= kBlrB) {
                 ok = true;
                 break;
             }
-            istar = nx;
+            i2 = first_unused(mark_row(used, i1, lane), lane);
+            if (i2 >= kBlrB) i2 = -1;
             continue;
         }
-        // the pivot entry r[bj], from the lane that holds it
-        const int sel = bj >> 5;
-        float2 piv = r[0];
+        // term 1: v1 = r1 / r1[j1]
+        {
+            const float2 piv = pick8(r1, j1);
+            const float pd = 1.f / (piv.x * piv.x + piv.y * piv.y);
+            const float2 inv = make_float2(piv.x * pd, -piv.y * pd);
 #pragma unroll
-        for (int q = 1; q < 8; ++q) {
-            piv.x = sel == q ? r[q].x : piv.x;
-            piv.y = sel == q ? r[q].y : piv.y;
+            for (int q = 0; q < 8; ++q) r1[q] = lane + 32 * q < nc ? cmul2(r1[q], inv) : make_float2(0.f, 0.f);
         }
-        piv.x = __shfl_sync(0xffffffffu, piv.x, bj & 31);
-        piv.y = __shfl_sync(0xffffffffu, piv.y, bj & 31);
-        const float pd = 1.f / (piv.x * piv.x + piv.y * piv.y);
-        const float2 inv = make_float2(piv.x * pd, -piv.y * pd);
-        float nv2 = 0.f;
+        // term 2: row i2's residual after term 1, v2 = r2 / r2[j2]
+        int j2 = -1;
+        if (two) {
+            const float2 c21 = pick8(r2, j1);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float2 p = cmul2(c21, r1[q]);
+                r2[q].x -= p.x;
+                r2[q].y -= p.y;
+            }
+            argmax8(r2, nc, lane, best, j2);
+            if (best > 1e-30f) {
+                const float2 piv = pick8(r2, j2);
+                const float pd = 1.f / (piv.x * piv.x + piv.y * piv.y);
+                const float2 inv = make_float2(piv.x * pd, -piv.y * pd);
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    r2[q] = lane + 32 * q < nc ? cmul2(r2[q], inv) : make_float2(0.f, 0.f);
+            } else {
+                j2 = -1;
+            }
+        }
+        const bool t2ok = j2 >= 0 && j2 < kBlrB;
+        const float2 v1j2 = t2ok ? pick8(r1, j2) : make_float2(0.f, 0.f);
+        float nv1 = 0.f, nv2 = 0.f;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int j = lane + 32 * q;
-            const float2 v = j < nc ? cmul2(r[q], inv) : make_float2(0.f, 0.f);
-            V[(size_t)k * kBlrB + j] = v;
-            nv2 += v.x * v.x + v.y * v.y;
+            V[(size_t)k * kBlrB + j] = r1[q];
+            nv1 += r1[q].x * r1[q].x + r1[q].y * r1[q].y;
+            if (t2ok) {
+                V[(size_t)(k + 1) * kBlrB + j] = r2[q];
+                nv2 += r2[q].x * r2[q].x + r2[q].y * r2[q].y;
+            }
         }
-        // residual of column bj
-        float2 c[8];
+        // residuals of columns j1 and j2
+        float2 c1[8], c2[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int i = lane + 32 * q;
-            c[q] = i < m ? A[(size_t)(I0 + i) * lda + J0 + bj] : make_float2(0.f, 0.f);
+            const float2 *arow = A + (size_t)(I0 + min(i, m - 1)) * lda + J0;
+            c1[q] = i < m ? arow[j1] : make_float2(0.f, 0.f);
+            c2[q] = (t2ok && i < m) ? arow[j2] : make_float2(0.f, 0.f);
         }
-        __syncwarp();   // this step's V row is in memory for every lane
-#pragma unroll 4
+        __syncwarp();   // this pass's V rows are in memory for every lane
+#pragma unroll 2
         for (int l = 0; l < k; ++l) {
-            const float2 vl = V[(size_t)l * kBlrB + bj];
+            const float2 w1 = V[(size_t)l * kBlrB + j1];
+            const float2 w2 = t2ok ? V[(size_t)l * kBlrB + j2] : make_float2(0.f, 0.f);
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                const float2 p = cmul2(U[(size_t)l * kBlrB + lane + 32 * q], vl);
-                c[q].x -= p.x;
-                c[q].y -= p.y;
+                const float2 u = U[(size_t)l * kBlrB + lane + 32 * q];
+                const float2 p1 = cmul2(u, w1), p2 = cmul2(u, w2);
+                c1[q].x -= p1.x;
+                c1[q].y -= p1.y;
+                c2[q].x -= p2.x;
+                c2[q].y -= p2.y;
             }
         }
-        float nu2 = 0.f, bu = -1.f;
-        int bi = kBlrB;
+        float nu1 = 0.f, nu2 = 0.f;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int i = lane + 32 * q;
-            U[(size_t)k * kBlrB + i] = c[q];
-            const float a = c[q].x * c[q].x + c[q].y * c[q].y;
-            nu2 += a;
-            if (!((used >> q) & 1u) && a > bu) {
-                bu = a;
-                bi = i;
+            U[(size_t)k * kBlrB + i] = c1[q];
+            nu1 += c1[q].x * c1[q].x + c1[q].y * c1[q].y;
+            if (t2ok) {
+                const float2 p = cmul2(c1[q], v1j2);   // column j2 after term 1
+                c2[q].x -= p.x;
+                c2[q].y -= p.y;
+                U[(size_t)(k + 1) * kBlrB + i] = c2[q];
+                nu2 += c2[q].x * c2[q].x + c2[q].y * c2[q].y;
             }
         }
-        nu2 = warp_sumf(nu2);
-        nv2 = warp_sumf(nv2);
-        const float t2 = nu2 * nv2;
-        norm2 += t2;
-        ++k;
-        __syncwarp();   // this step's U column is in memory for every lane
-        if (t2 <= stop2 * norm2) {
+        nu1 = warp_sumf(nu1);
+        nv1 = warp_sumf(nv1);
+        float tl = nu1 * nv1;
+        norm2 += tl;
+        k += 1;
+        if (t2ok) {
+            nu2 = warp_sumf(nu2);
+            nv2 = warp_sumf(nv2);
+            tl = nu2 * nv2;
+            norm2 += tl;
+            k += 1;
+        }
+        __syncwarp();   // this pass's U columns are in memory for every lane
+        if (tl <= stop2 * norm2) {
             ok = true;
             break;
         }
-        warp_argmax(bu, bi);
-        if (bi >= kBlrB || bu < 0.f) {
+        // next rows: the two largest entries of the last column residual
+        // among the unused rows
+        float la[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            la[q] = t2ok ? c2[q].x * c2[q].x + c2[q].y * c2[q].y : c1[q].x * c1[q].x + c1[q].y * c1[q].y;
+        float ba = -1.f, bb = -1.f;
+        int ia = kBlrB, ib = kBlrB;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float a = la[q];
+            if (!((used >> q) & 1u) && a > ba) {
+                ba = a;
+                ia = lane + 32 * q;
+            }
+        }
+        warp_argmax(ba, ia);
+        if (ia >= kBlrB || ba < 0.f) {
             ok = true;   // every row is a pivot row: the terms reproduce the block
             break;
         }
-        istar = bi;
+        const unsigned used2 = mark_row(used, ia, lane);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float a = la[q];
+            if (!((used2 >> q) & 1u) && a > bb) {
+                bb = a;
+                ib = lane + 32 * q;
+            }
+        }
+        warp_argmax(bb, ib);
+        i1 = ia;
+        i2 = (ib < kBlrB && bb >= 0.f) ? ib : -1;
     }
     if (lane == 0) S.rank[b] = ok ? k : -1;
 }
-
 
 // The probe check of k_blr_aca's approximations and their fp16 factors;
 // blocks it rejects become dense.  One block of 256 threads per matrix block:
