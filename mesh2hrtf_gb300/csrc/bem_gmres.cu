@@ -1507,6 +1507,7 @@ __global__ void __launch_bounds__(32 * kUmWarps, 1) k_mv_grp_umma(KTable *tb) {
 // row and chunk like k_mv_tma's, so k_dot1 sums them unchanged.
 constexpr int kBlrThreads = kBlrB;
 constexpr int kBlrPerItem = kMvChunk / kBlrB;
+constexpr int kBlrTermsPerWarp = 4;   // V rows in flight per warp in phase 1
 static_assert(kMvChunk % kBlrB == 0, "a chunk holds whole blocks");
 
 // y += a x, a an fp16 pair
@@ -1522,8 +1523,8 @@ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
 }
 
 __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
-    __shared__ float2 xs[kMvChunk];
-    __shared__ float2 ts[kBlrPerItem][kBlrMaxRank];
+    __shared__ __align__(16) float2 xs[kMvChunk];
+    __shared__ __align__(16) float2 ts[kBlrPerItem][kBlrMaxRank];
     __shared__ int rk[kBlrPerItem], tsk[kBlrPerItem + 1];
     __shared__ int item_s;
     __shared__ PlanSmem pl;
@@ -1555,35 +1556,46 @@ __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
             tsk[kBlrPerItem] = acc;
         }
         __syncthreads();
-        // phase 1: t_l of the compressed blocks, two terms per warp at a time
+        // phase 1: t_l of the compressed blocks, kBlrTermsPerWarp terms per
+        // warp at a time
         const int nt = tsk[kBlrPerItem];
-        for (int t0 = warp; t0 < nt; t0 += 2 * (kBlrThreads / 32)) {
-            unsigned a[2][kBlrB / 32];
-            size_t bl[2];
-            int qq[2], ll[2];
+        for (int t0 = warp; t0 < nt; t0 += kBlrTermsPerWarp * (kBlrThreads / 32)) {
+            unsigned a[kBlrTermsPerWarp][kBlrB / 32];
+            size_t bl[kBlrTermsPerWarp];
+            int qq[kBlrTermsPerWarp], ll[kBlrTermsPerWarp];
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
+            for (int h = 0; h < kBlrTermsPerWarp; ++h) {
                 const int t = min(t0 + h * (kBlrThreads / 32), nt - 1);
                 int q = 0;
                 while (t >= tsk[q + 1]) ++q;
                 qq[h] = q;
                 ll[h] = t - tsk[q];
                 bl[h] = ((size_t)I * nb + c * kBlrPerItem + q) * kBlrMaxRank + ll[h];
-                const unsigned *v = S.blr_V16 + bl[h] * kBlrB;
+                // lane: entries 2 lane + 64 e' and the next, e' < 4
+                const uint2 *v = reinterpret_cast<const uint2 *>(S.blr_V16 + bl[h] * kBlrB);
 #pragma unroll
-                for (int e = 0; e < kBlrB / 32; ++e) a[h][e] = v[lane + 32 * e];
+                for (int e = 0; e < kBlrB / 64; ++e) {
+                    const uint2 pr = v[lane + 32 * e];
+                    a[h][2 * e] = pr.x;
+                    a[h][2 * e + 1] = pr.y;
+                }
             }
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const float2 *xq = xs + qq[h] * kBlrB;
+            for (int h = 0; h < kBlrTermsPerWarp; ++h) {
+                const float4 *xq4 = reinterpret_cast<const float4 *>(xs + qq[h] * kBlrB);
                 float sr = 0.f, si = 0.f;
 #pragma unroll
-                for (int e = 0; e < kBlrB / 32; ++e) {
-                    const float2 av = h2f(a[h][e]), x = xq[lane + 32 * e];
-                    sr = fmaf(av.x, x.x, sr);
-                    sr = fmaf(-av.y, x.y, sr);
-                    si = fmaf(av.x, x.y, si);
-                    si = fmaf(av.y, x.x, si);
+                for (int e = 0; e < kBlrB / 64; ++e) {
+                    const float4 x2 = xq4[lane + 32 * e];
+                    const float2 a0 = h2f(a[h][2 * e]), a1 = h2f(a[h][2 * e + 1]);
+                    sr = fmaf(a0.x, x2.x, sr);
+                    sr = fmaf(-a0.y, x2.y, sr);
+                    si = fmaf(a0.x, x2.y, si);
+                    si = fmaf(a0.y, x2.x, si);
+                    sr = fmaf(a1.x, x2.z, sr);
+                    sr = fmaf(-a1.y, x2.w, sr);
+                    si = fmaf(a1.x, x2.w, si);
+                    si = fmaf(a1.y, x2.z, si);
                 }
                 sr = warp_sum_f(sr);
                 si = warp_sum_f(si);
@@ -1615,14 +1627,18 @@ __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
 #pragma unroll 4
                         for (int g = 0; g < kBlrB / 8; ++g) {
                             const uint4 p0 = h4[2 * g], p1 = h4[2 * g + 1];
-                            cmac_h(yd, p0.x, xq[8 * g + 0]);
-                            cmac_h(yd, p0.y, xq[8 * g + 1]);
-                            cmac_h(yd, p0.z, xq[8 * g + 2]);
-                            cmac_h(yd, p0.w, xq[8 * g + 3]);
-                            cmac_h(yd, p1.x, xq[8 * g + 4]);
-                            cmac_h(yd, p1.y, xq[8 * g + 5]);
-                            cmac_h(yd, p1.z, xq[8 * g + 6]);
-                            cmac_h(yd, p1.w, xq[8 * g + 7]);
+                            // x in 16-byte shared loads (two entries each;
+                            // every thread reads the same address)
+                            const float4 *x4 = reinterpret_cast<const float4 *>(xq + 8 * g);
+                            const float4 xa = x4[0], xb = x4[1], xc = x4[2], xd = x4[3];
+                            cmac_h(yd, p0.x, make_float2(xa.x, xa.y));
+                            cmac_h(yd, p0.y, make_float2(xa.z, xa.w));
+                            cmac_h(yd, p0.z, make_float2(xb.x, xb.y));
+                            cmac_h(yd, p0.w, make_float2(xb.z, xb.w));
+                            cmac_h(yd, p1.x, make_float2(xc.x, xc.y));
+                            cmac_h(yd, p1.y, make_float2(xc.z, xc.w));
+                            cmac_h(yd, p1.z, make_float2(xd.x, xd.y));
+                            cmac_h(yd, p1.w, make_float2(xd.z, xd.w));
                         }
                     } else {
                         for (int e = 0; e < nc; ++e) cmac_h(yd, h[e], xq[e]);
@@ -1631,16 +1647,36 @@ __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
                 }
                 const unsigned *u = S.blr_U16 + ((size_t)I * nb + J) * kBlrMaxRank * kBlrB + i;
                 int l = 0;
+                for (; l + 16 <= r; l += 16) {
+                    unsigned w[16];
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) w[e] = u[(size_t)(l + e) * kBlrB];
+                    float2 p = make_float2(0.f, 0.f);
+                    const float4 *t4 = reinterpret_cast<const float4 *>(&ts[q][l]);   // l is even
+#pragma unroll
+                    for (int e = 0; e < 16; e += 2) {
+                        const float4 tt = t4[e >> 1];
+                        const float2 pa = cmulf(h2f(w[e]), make_float2(tt.x, tt.y));
+                        const float2 pb = cmulf(h2f(w[e + 1]), make_float2(tt.z, tt.w));
+                        p.x += pa.x + pb.x;
+                        p.y += pa.y + pb.y;
+                    }
+                    y.x += p.x;
+                    y.y += p.y;
+                }
                 for (; l + 8 <= r; l += 8) {
                     unsigned w[8];
 #pragma unroll
                     for (int e = 0; e < 8; ++e) w[e] = u[(size_t)(l + e) * kBlrB];
                     float2 p = make_float2(0.f, 0.f);
+                    const float4 *t4 = reinterpret_cast<const float4 *>(&ts[q][l]);   // l is even
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        const float2 pe = cmulf(h2f(w[e]), ts[q][l + e]);
-                        p.x += pe.x;
-                        p.y += pe.y;
+                    for (int e = 0; e < 8; e += 2) {
+                        const float4 tt = t4[e >> 1];
+                        const float2 pa = cmulf(h2f(w[e]), make_float2(tt.x, tt.y));
+                        const float2 pb = cmulf(h2f(w[e + 1]), make_float2(tt.z, tt.w));
+                        p.x += pa.x + pb.x;
+                        p.y += pa.y + pb.y;
                     }
                     y.x += p.x;
                     y.y += p.y;
