@@ -598,33 +598,15 @@ bem_status assemble_group(bem_solver_t *ss, int cnt, cudaStream_t st, unsigned *
     return first;
 }
 
-// fp16 copies (SplitBatch) and then block low-rank copies (BlrBatch, over
-// the fp16 copies) of the complex64 matrices that have one.
+// Block low-rank copies (BlrBatch) and fp16 copies (SplitBatch; for a
+// solver with a block low-rank copy only the segments that copy reads) of
+// the complex64 matrices that have them.
 cudaError_t split_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
-    std::unique_ptr<bem::SplitBatch> t(new bem::SplitBatch());
-    t->B = 0;
-    cudaError_t e = cudaSuccess;
-    for (int i = 0; i < cnt && e == cudaSuccess; ++i) {
-        const bem::SolverBufs &d = ss[i]->d;
-        if (!d.A16) continue;
-        bem::SplitSys &q = t->sys[t->B++];
-        q.A = d.A;
-        q.lda = ss[i]->lda;
-        q.n = ss[i]->n;
-        q.A16 = d.A16;
-        q.rs = d.rs;
-        if (t->B == bem::kMaxAsm) {
-            bem::split_batch_finish(*t);
-            e = bem::launch_split16(*t, st);
-            t->B = 0;
-        }
-    }
-    if (e == cudaSuccess && t->B > 0) {
-        bem::split_batch_finish(*t);
-        e = bem::launch_split16(*t, st);
-    }
+    // the block low-rank copies first: their ranks say which fp16 segments
+    // are read
     std::unique_ptr<bem::BlrBatch> bt(new bem::BlrBatch());
     bt->B = 0;
+    cudaError_t e = cudaSuccess;
     for (int i = 0; i < cnt && e == cudaSuccess; ++i) {
         const bem::SolverBufs &d = ss[i]->d;
         if (d.blr_nb <= 0) continue;
@@ -647,6 +629,29 @@ cudaError_t split_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
     if (e == cudaSuccess && bt->B > 0) {
         bem::blr_batch_finish(*bt);
         e = bem::launch_blr_compress(*bt, st);
+    }
+    std::unique_ptr<bem::SplitBatch> t(new bem::SplitBatch());
+    t->B = 0;
+    for (int i = 0; i < cnt && e == cudaSuccess; ++i) {
+        const bem::SolverBufs &d = ss[i]->d;
+        if (!d.A16) continue;
+        bem::SplitSys &q = t->sys[t->B++];
+        q.A = d.A;
+        q.lda = ss[i]->lda;
+        q.n = ss[i]->n;
+        q.A16 = d.A16;
+        q.rs = d.rs;
+        q.blr_rank = d.blr_nb > 0 ? d.blr_rank : nullptr;
+        q.blr_nb = d.blr_nb;
+        if (t->B == bem::kMaxAsm) {
+            bem::split_batch_finish(*t);
+            e = bem::launch_split16(*t, st);
+            t->B = 0;
+        }
+    }
+    if (e == cudaSuccess && t->B > 0) {
+        bem::split_batch_finish(*t);
+        e = bem::launch_split16(*t, st);
     }
     return e;
 }
@@ -700,7 +705,9 @@ bem_status tuned_strips(bem_solver_t *ss, int cnt, bem::Engine *eng) {
         for (int c : kCand) {
             s->mv_strip = c;
             float ms = 0.f;
-            const cudaError_t e = eng->time_product(s->ksys(), &ms);
+            bem::KSys k = s->ksys();
+            if (k.blr_nb > 0) k.A16 = nullptr;   // its fp16 copy is partial: time the residual product
+            const cudaError_t e = eng->time_product(k, &ms);
             if (e == cudaErrorLaunchTimeout)
                 return fail(BEM_ERR_DEVICE_TIMEOUT, "matrix-vector product: a bounded device wait gave up");
             CU(e);

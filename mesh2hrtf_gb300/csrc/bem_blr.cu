@@ -1,8 +1,8 @@
 // bem_blr.cu - the block low-rank Krylov copy of a complex64 matrix.
 //
-// After assembly and the fp16 copy, every off-diagonal kBlrB x kBlrB block
-// of A (in the unknowns' Morton order) is approximated by adaptive cross
-// approximation with partial pivoting, in FP32, from A's own entries: take a
+// After assembly, every off-diagonal kBlrB x kBlrB block of A (in the
+// unknowns' Morton order) is approximated by adaptive cross approximation
+// with partial pivoting, in FP32, from A's own entries: take a
 // row's residual against the terms so far, pivot on its largest entry, take
 // that column's residual and add the rank-one term; the next row is the
 // column residual's largest entry among the rows not used yet.  The
@@ -17,8 +17,9 @@
 // computed as w^T B - (w^T U) V^T.  A block whose estimate is within kBlrTol
 // of |B|_F keeps its terms, as fp16 factors with a power-of-two scale per
 // term; any other block, and every diagonal block, is read from the fp16
-// copy of A.  One warp per block; lane l holds entries l, l + 32, ... of the
-// block's rows and columns.
+// copy of A, which is made afterwards for those blocks' segments only.  One
+// warp per block; lane l holds entries l, l + 32, ... of the block's rows
+// and columns.
 //
 // Boundary-element matrices have numerically low-rank off-diagonal blocks
 // (the kernels are smooth between separated element patches): on the

@@ -236,6 +236,9 @@ struct SplitSys {
     void *A16;              // fp16 pairs, the same leading dimension
     float *rs;              // [n][mv_chunks(n)] segment scales:
                             // A[i][j] ~ rs[i * mv_chunks(n) + j / kMvChunk] * A16[i][j]
+    const int *blr_rank;    // block low-rank copy's ranks (BlrSys::rank) or nullptr:
+    int blr_nb;             // then only the segments read are converted: the
+                            // diagonal chunk and chunks with a dense block
 };
 struct SplitBatch {
     int B;
@@ -245,8 +248,8 @@ struct SplitBatch {
 void split_batch_finish(SplitBatch &t);
 cudaError_t launch_split16(const SplitBatch &t, cudaStream_t st);
 
-// Block low-rank Krylov copy of a complex64 matrix (bem_blr.cu), on top of
-// its fp16 copy: blocks of kBlrB x kBlrB unknowns.  Every off-diagonal block
+// Block low-rank Krylov copy of a complex64 matrix (bem_blr.cu), with its
+// fp16 copy for the blocks that stay dense: blocks of kBlrB x kBlrB unknowns.  Every off-diagonal block
 // is approximated by adaptive cross approximation (stopping at kBlrStop);
 // when a randomized estimate of the approximation's error (kBlrSketch
 // Rademacher probes of the whole block) is within kBlrTol of the block's

@@ -267,7 +267,8 @@ __global__ void __launch_bounds__(512) k_binv64(const __grid_constant__ PcBatch 
 }
 
 // fp16 copy of complex64 rows (SplitBatch): one warp per (row, column
-// chunk of kMvChunk entries).  The segment's largest component m sets the
+// chunk of kMvChunk entries; with a block low-rank copy only the segments it
+// reads).  The segment's largest component m sets the
 // scale 2^(15 - e) with m < 2^e; every component is scaled (exactly) and
 // rounded to nearest.  Power-of-two scales keep A16 * rs within one fp16
 // rounding of A.  The warp holds its 8 KB segment in registers, so A is
@@ -282,6 +283,18 @@ __global__ void __launch_bounds__(kSplitThreads) k_split16(const __grid_constant
     const long long item = (long long)(blockIdx.x - tb.off[sb]) * kSplitWarps + (threadIdx.x >> 5);
     if (item >= (long long)n * nch) return;
     const int i = (int)(item / nch), c = (int)(item - (long long)i * nch);
+    if (S.blr_rank && c != i / kMvChunk) {
+        // block low-rank copy: only the diagonal chunk (the preconditioner's
+        // window) and chunks with a dense block of this row's block row
+        const int I = i / kBlrB, nb = S.blr_nb;
+        bool need = false;
+#pragma unroll
+        for (int q = 0; q < kMvChunk / kBlrB; ++q) {
+            const int J = c * (kMvChunk / kBlrB) + q;
+            need |= J < nb && S.blr_rank[(size_t)I * nb + J] < 0;
+        }
+        if (!need) return;
+    }
     const int c0 = c * kMvChunk, len = min(kMvChunk, n - c0), len2 = len >> 1;
     const float2 *seg = (const float2 *)S.A + (size_t)i * S.lda + c0;   // 8 KB aligned within the row
     const float4 *seg4 = reinterpret_cast<const float4 *>(seg);
