@@ -359,15 +359,18 @@ __global__ void __launch_bounds__(32 * kBlrWarps) k_blr_aca(const __grid_constan
 }
 
 // The probe check of k_blr_aca's approximations and their fp16 factors;
-// blocks it rejects become dense.  One block of 256 threads per matrix block:
-// the warps first form w_p^T U_l (warp w: terms w, w + 8, ...), then thread t
-// streams column t of the block (the warps together read whole rows) and
-// accumulates w_p^T B, and subtracts (w_p^T U) V^T.
-constexpr int kChkThreads = kBlrB;
+// blocks it rejects become dense.  One block of 128 threads per matrix block:
+// the row's probe signs go to shared memory once, the warps form w_p^T U_l
+// (warp w: terms w, w + 4, ...), then thread t streams columns 2t and 2t + 1
+// of the block (16-byte loads; the warps together read whole rows),
+// accumulating w_p^T B and |B|^2, and subtracts (w_p^T U) V^T.
+constexpr int kChkThreads = kBlrB / 2;
+constexpr int kChkWarps = kChkThreads / 32;
 
-__global__ void __launch_bounds__(kChkThreads, 4) k_blr_check(const __grid_constant__ BlrBatch tb) {
+__global__ void __launch_bounds__(kChkThreads, 6) k_blr_check(const __grid_constant__ BlrBatch tb) {
     __shared__ float2 cw[kBlrSketch][kBlrMaxRank];   // w_p^T U_l
-    __shared__ float red[2][kChkThreads / 32];
+    __shared__ unsigned rbits[kBlrB];                 // probe signs per row
+    __shared__ float red[2][kChkWarps];
     __shared__ int keep;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const long long gb = blockIdx.x;
@@ -387,66 +390,81 @@ __global__ void __launch_bounds__(kChkThreads, 4) k_blr_check(const __grid_const
     const float2 *U = S.U + (size_t)b * kBlrMaxRank * kBlrB;
     const float2 *V = S.V + (size_t)b * kBlrMaxRank * kBlrB;
     const unsigned key0 = (unsigned)(gb * kBlrB);
-    {
-        unsigned hb[8];
+    for (int i = t; i < kBlrB; i += kChkThreads) rbits[i] = probe_bits(key0 + i);
+    __syncthreads();
+    for (int l = warp; l < k; l += kChkWarps) {
+        float pr[kBlrSketch], pi[kBlrSketch];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) hb[q] = probe_bits(key0 + lane + 32 * q);
-        for (int l = warp; l < k; l += kChkThreads / 32) {
-            float pr[kBlrSketch], pi[kBlrSketch];
+        for (int p = 0; p < kBlrSketch; ++p) pr[p] = pi[p] = 0.f;
 #pragma unroll
-            for (int p = 0; p < kBlrSketch; ++p) pr[p] = pi[p] = 0.f;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const float2 u = U[(size_t)l * kBlrB + lane + 32 * q];   // zero past the block
-#pragma unroll
-                for (int p = 0; p < kBlrSketch; ++p) {
-                    const float sg = psign(hb[q], p);
-                    pr[p] = fmaf(sg, u.x, pr[p]);
-                    pi[p] = fmaf(sg, u.y, pi[p]);
-                }
-            }
+        for (int q = 0; q < 8; ++q) {
+            const float2 u = U[(size_t)l * kBlrB + lane + 32 * q];   // zero past the block
+            const unsigned hb = rbits[lane + 32 * q];
 #pragma unroll
             for (int p = 0; p < kBlrSketch; ++p) {
-                pr[p] = warp_sumf(pr[p]);
-                pi[p] = warp_sumf(pi[p]);
+                const float sg = psign(hb, p);
+                pr[p] = fmaf(sg, u.x, pr[p]);
+                pi[p] = fmaf(sg, u.y, pi[p]);
             }
-            if (lane == 0)
-#pragma unroll
-                for (int p = 0; p < kBlrSketch; ++p) cw[p][l] = make_float2(pr[p], pi[p]);
         }
+#pragma unroll
+        for (int p = 0; p < kBlrSketch; ++p) {
+            pr[p] = warp_sumf(pr[p]);
+            pi[p] = warp_sumf(pi[p]);
+        }
+        if (lane == 0)
+#pragma unroll
+            for (int p = 0; p < kBlrSketch; ++p) cw[p][l] = make_float2(pr[p], pi[p]);
     }
     __syncthreads();
-    float2 acc[kBlrSketch];
+    float2 acc0[kBlrSketch], acc1[kBlrSketch];
 #pragma unroll
-    for (int p = 0; p < kBlrSketch; ++p) acc[p] = make_float2(0.f, 0.f);
+    for (int p = 0; p < kBlrSketch; ++p) acc0[p] = acc1[p] = make_float2(0.f, 0.f);
     float bn2 = 0.f;
-    if (t < nc) {
-        const float2 *col = A + (size_t)I0 * lda + J0 + t;
+    const int j = 2 * t;
+    if (j < nc) {
+        const float2 *col = A + (size_t)I0 * lda + J0 + j;
+        const bool pair = j + 1 < nc;
 #pragma unroll 8
         for (int i = 0; i < m; ++i) {
-            const unsigned bits = probe_bits(key0 + i);
-            const float2 bv = __ldcs(col + (size_t)i * lda);
+            const unsigned bits = rbits[i];
+            float4 bv;
+            if (pair) {
+                bv = __ldcs(reinterpret_cast<const float4 *>(col + (size_t)i * lda));
+            } else {
+                const float2 v = __ldcs(col + (size_t)i * lda);
+                bv = make_float4(v.x, v.y, 0.f, 0.f);
+            }
             bn2 = fmaf(bv.x, bv.x, fmaf(bv.y, bv.y, bn2));
+            bn2 = fmaf(bv.z, bv.z, fmaf(bv.w, bv.w, bn2));
 #pragma unroll
             for (int p = 0; p < kBlrSketch; ++p) {
                 const float sg = psign(bits, p);
-                acc[p].x = fmaf(sg, bv.x, acc[p].x);
-                acc[p].y = fmaf(sg, bv.y, acc[p].y);
+                acc0[p].x = fmaf(sg, bv.x, acc0[p].x);
+                acc0[p].y = fmaf(sg, bv.y, acc0[p].y);
+                acc1[p].x = fmaf(sg, bv.z, acc1[p].x);
+                acc1[p].y = fmaf(sg, bv.w, acc1[p].y);
             }
         }
     }
     for (int l = 0; l < k; ++l) {
-        const float2 v = V[(size_t)l * kBlrB + t];   // zero past the block
+        const float4 v = *reinterpret_cast<const float4 *>(V + (size_t)l * kBlrB + j);   // zero past the block
 #pragma unroll
         for (int p = 0; p < kBlrSketch; ++p) {
-            const float2 w = cmul2(cw[p][l], v);
-            acc[p].x -= w.x;
-            acc[p].y -= w.y;
+            const float2 w0 = cmul2(cw[p][l], make_float2(v.x, v.y));
+            const float2 w1 = cmul2(cw[p][l], make_float2(v.z, v.w));
+            acc0[p].x -= w0.x;
+            acc0[p].y -= w0.y;
+            acc1[p].x -= w1.x;
+            acc1[p].y -= w1.y;
         }
     }
     float est = 0.f;
 #pragma unroll
-    for (int p = 0; p < kBlrSketch; ++p) est = fmaf(acc[p].x, acc[p].x, fmaf(acc[p].y, acc[p].y, est));
+    for (int p = 0; p < kBlrSketch; ++p) {
+        est = fmaf(acc0[p].x, acc0[p].x, fmaf(acc0[p].y, acc0[p].y, est));
+        est = fmaf(acc1[p].x, acc1[p].x, fmaf(acc1[p].y, acc1[p].y, est));
+    }
     est = warp_sumf(est);
     bn2 = warp_sumf(bn2);
     if (lane == 0) {
@@ -456,7 +474,7 @@ __global__ void __launch_bounds__(kChkThreads, 4) k_blr_check(const __grid_const
     __syncthreads();
     if (t == 0) {
         float e = 0.f, bb = 0.f;
-        for (int w = 0; w < kChkThreads / 32; ++w) {
+        for (int w = 0; w < kChkWarps; ++w) {
             e += red[0][w];
             bb += red[1][w];
         }
@@ -468,7 +486,7 @@ __global__ void __launch_bounds__(kChkThreads, 4) k_blr_check(const __grid_const
     // the kept terms as fp16 factors, scale 2^(eu - 15) 2^(ev - 15) per term
     unsigned *U16 = S.U16 + (size_t)b * kBlrMaxRank * kBlrB;
     unsigned *V16 = S.V16 + (size_t)b * kBlrMaxRank * kBlrB;
-    for (int l = warp; l < k; l += kChkThreads / 32) {
+    for (int l = warp; l < k; l += kChkWarps) {
         const int eu = store_half(U + (size_t)l * kBlrB, U16 + (size_t)l * kBlrB, lane);
         const int ev = store_half(V + (size_t)l * kBlrB, V16 + (size_t)l * kBlrB, lane);
         if (lane == 0) S.scale[(size_t)b * kBlrMaxRank + l] = ldexpf(1.f, eu + ev - 30);
