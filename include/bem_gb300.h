@@ -109,7 +109,11 @@ typedef struct {
                                   128-unknown diagonal blocks with one
                                   correction step over 1024-unknown diagonal
                                   windows A_w, M = X (2 I - A_w X);
-                                  1: none; 2: block-Jacobi only (M = X)       */
+                                  1: none; 2: block-Jacobi only (M = X);
+                                  3: NumCalc's scaling preconditioner, the
+                                  diagonal d_i = sqrt(N / sum_j |a_ij|^2)
+                                  on the right (NC_ComputeScalingVector,
+                                  NC_CommonFunctions.cpp:1322-1351)           */
     int32_t n_rhs;             /* right-hand sides the solver can hold for
                                   bem_solve_multi (0 or 1: one; at most 16)    */
     int32_t complex64_krylov;  /* mixed precision with one right-hand side:

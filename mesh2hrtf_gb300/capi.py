@@ -227,16 +227,19 @@ class Solver:
         precision solver with one right-hand side read: False (the fp16 copy),
         True (none: they read A) or KRYLOV_BLR (the block low-rank copy).
         precond: True (block-Jacobi with its window correction), "block-jacobi"
-        (block-Jacobi alone) or False (none)."""
+        (block-Jacobi alone), "scaling" (NumCalc's diagonal scaling) or False
+        (none)."""
         lib = load()
         self.mesh = mesh
         self.n = mesh.n
         if precond == "block-jacobi":
             npc = 2
+        elif precond == "scaling":
+            npc = 3
         elif precond is True or precond is False:
             npc = 0 if precond else 1
         else:
-            raise ValueError("precond must be True, False or 'block-jacobi', not %r" % (precond,))
+            raise ValueError("precond must be True, False, 'block-jacobi' or 'scaling', not %r" % (precond,))
         kc = KRYLOV_BLR if complex64_krylov == KRYLOV_BLR else (1 if complex64_krylov else 0)
         p = SolverParams(precision, restart, max_iter, tol, hbm_budget, npc, n_rhs, kc)
         h = C.c_void_p()

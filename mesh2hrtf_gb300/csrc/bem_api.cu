@@ -666,12 +666,21 @@ bem_status precond_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
         if (ss[i]->precond) pcs.push_back(ss[i]);
         CU(cudaMemsetAsync(ss[i]->d.x, 0, sizeof(double2) * ss[i]->n, st));
     }
-    for (size_t c0 = 0; c0 < pcs.size(); c0 += bem::kMaxAsm) {
-        const int k = (int)std::min<size_t>(bem::kMaxAsm, pcs.size() - c0);
+    std::vector<bem_solver_t> bj;   // block-Jacobi; the scaling ones are set here
+    for (bem_solver_t s : pcs) {
+        if (!s->pc_scaling) {
+            bj.push_back(s);
+            continue;
+        }
+        CU(cudaMemsetAsync(s->d.status, 0, sizeof(int), st));
+        CU(bem::launch_pc_scaling(s->psys(), prec, st));
+    }
+    for (size_t c0 = 0; c0 < bj.size(); c0 += bem::kMaxAsm) {
+        const int k = (int)std::min<size_t>(bem::kMaxAsm, bj.size() - c0);
         pt->B = k;
         for (int i = 0; i < k; ++i) {
-            CU(cudaMemsetAsync(pcs[c0 + i]->d.status, 0, sizeof(int), st));
-            pt->sys[i] = pcs[c0 + i]->psys();
+            CU(cudaMemsetAsync(bj[c0 + i]->d.status, 0, sizeof(int), st));
+            pt->sys[i] = bj[c0 + i]->psys();
         }
         bem::pc_batch_finish(*pt);
         CU(bem::launch_block_inverse(*pt, prec, st));
@@ -1174,8 +1183,8 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     const int m = prm.restart > 0 ? prm.restart : 60;
     if (m > bem::kMaxRestart) return fail(BEM_ERR_INVALID, "restart length %d above the limit %d", m, bem::kMaxRestart);
     const int n = mesh->n;
-    if (prm.no_precond < 0 || prm.no_precond > 2)
-        return fail(BEM_ERR_INVALID, "no_precond %d is not 0, 1 or 2", prm.no_precond);
+    if (prm.no_precond < 0 || prm.no_precond > 3)
+        return fail(BEM_ERR_INVALID, "no_precond %d is not 0, 1, 2 or 3", prm.no_precond);
     const bool pc = prm.no_precond != 1;
     const int prec = prm.precision == BEM_PREC_FP64 ? 0 : 1;
     const int n_rhs = prm.n_rhs > 0 ? prm.n_rhs : 1;
@@ -1203,6 +1212,7 @@ bem_status bem_solver_create(bem_mesh_t mesh, const bem_solver_params *p, bem_so
     s->lda = round_up((size_t)n, 32);
     s->precond = pc;
     s->pc_window = prm.no_precond == 0;
+    s->pc_scaling = prm.no_precond == 3;
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     for (auto &ev : s->ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);

@@ -221,6 +221,9 @@ struct PcBatch {
 void pc_batch_finish(PcBatch &t);
 size_t precond_bytes(int n, int prec);
 cudaError_t launch_block_inverse(const PcBatch &t, int prec, cudaStream_t st);
+// NumCalc's scaling preconditioner in the block-Jacobi storage: Minv set to
+// the diagonal d_i = sqrt(n / sum_j |a_ij|^2) (a zero row sets *status)
+cudaError_t launch_pc_scaling(const PcSys &s, int prec, cudaStream_t st);
 
 // ---------------------------------------------------------------- fp16 Krylov copy
 // A complex64 system may also hold A in fp16 pairs, every row segment of

@@ -18,6 +18,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "bem_internal.h"
 
 namespace bem {
@@ -342,6 +344,53 @@ cudaError_t launch_split16(const SplitBatch &t, cudaStream_t st) {
     if (t.B <= 0 || t.off[t.B] == 0) return cudaSuccess;
     count_launches(1);
     k_split16<<<t.off[t.B], kSplitThreads, 0, st>>>(t);
+    return cudaGetLastError();
+}
+
+// NumCalc's scaling preconditioner (NC_ComputeScalingVector,
+// NC_CommonFunctions.cpp:1322-1351, TBEM branch): d_i = sqrt(N / sum_j
+// |a_ij|^2), applied to the multiplier vector before every product
+// (NC_MatrixVectorMultiplication, :1224-1232), i.e. on the right, and to the
+// result at the end (:1193-1203).  Here it is the diagonal of M^{-1} in the
+// block-Jacobi storage (the caller clears the blocks), so the Krylov kernels
+// apply it unchanged.  Warp per row; row sums in the matrix's precision.
+template <typename T>
+__global__ void __launch_bounds__(256) k_pc_scaling(const PcSys S) {
+    using C2 = typename std::conditional<std::is_same<T, double>::value, double2, float2>::type;
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (i >= S.n) return;
+    const C2 *row = reinterpret_cast<const C2 *>(S.A) + (size_t)i * S.lda;
+    T acc = 0;
+    for (int j = lane; j < S.n; j += 32) {
+        const C2 a = row[j];
+        acc += a.x * a.x + a.y * a.y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane != 0) return;
+    if (!(acc > 0)) {
+        atomicMax(S.status, 1);
+        return;
+    }
+    const double d = sqrt((double)S.n / (double)acc);
+    const int p = i / kBlock, r = i - p * kBlock;
+    C2 *M = reinterpret_cast<C2 *>(S.Minv) + (size_t)p * kBlock * kBlock;
+    C2 v;
+    v.x = (T)d;
+    v.y = 0;
+    M[(size_t)r * kBlock + r] = v;
+}
+
+cudaError_t launch_pc_scaling(const PcSys &s, int prec, cudaStream_t st) {
+    if (s.n <= 0) return cudaSuccess;
+    const size_t bytes = (size_t)pc_blocks(s.n) * kBlock * kBlock * (prec == 0 ? 16 : 8);
+    cudaError_t e = cudaMemsetAsync(s.Minv, 0, bytes, st);
+    if (e != cudaSuccess) return e;
+    count_launches(1);
+    const int grid = (s.n + 7) / 8;
+    if (prec == 0) k_pc_scaling<double><<<grid, 256, 0, st>>>(s);
+    else k_pc_scaling<float><<<grid, 256, 0, st>>>(s);
     return cudaGetLastError();
 }
 

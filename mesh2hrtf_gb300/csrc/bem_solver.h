@@ -111,6 +111,7 @@ struct bem_solver_s {
     size_t lda = 0;
     bool precond = true, have_precond = false;
     bool pc_window = true;   // block-Jacobi with the window correction step
+    bool pc_scaling = false; // NumCalc's diagonal scaling instead of block-Jacobi
     cudaStream_t st = nullptr;
     cudaEvent_t ev[8] = {};
     unsigned char *block = nullptr;

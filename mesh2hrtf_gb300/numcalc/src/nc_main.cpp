@@ -251,6 +251,11 @@ int run(int istart, int iend, bool estimate_ram, bool check_normals, int niterma
         bem_solver_params sp{};
         sp.precision = prec;
         sp.tol = 1e-9;   // ErroIterSols, NC_CommonFunctions.cpp:39
+        // NC.inp's preconditioner (Main Parameters II, token 4): the
+        // incomplete LU (0, any scanning degree) is stood in for by the
+        // block-Jacobi preconditioner with its window correction; scaling
+        // (1) and none (2) are NumCalc's own
+        sp.no_precond = p.precond == 1 ? 3 : p.precond == 2 ? 1 : 0;
         // HBM admission: wait while other NumCalc processes hold the memory
         const char *wait_env = std::getenv("NUMCALC_GB300_WAIT_S");
         const double wait_s = wait_env ? std::atof(wait_env) : 3600.0;

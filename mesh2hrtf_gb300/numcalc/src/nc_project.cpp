@@ -727,10 +727,19 @@ void read_project(FILE *inp, std::ofstream &out, bool check_normals, Project &p)
             else out << "methodPreconditioner_ = 2: no preconditioner" << std::endl;
             // the GPU path keeps the reference's solution and stopping rule but
             // not its iteration: say so next to the reference's choice
-            out << "GPU solver: restarted GMRES (relative residual 1e-9) with a block-Jacobi preconditioner "
-                   "(128-unknown blocks, one correction over 1024-unknown windows) in place of CGS with the "
-                   "preconditioner above; the direct solver runs when the iteration limit is reached"
-                << std::endl;
+            if (p.precond == 0)
+                out << "GPU solver: restarted GMRES (relative residual 1e-9) with a block-Jacobi preconditioner "
+                       "(128-unknown blocks, one correction over 1024-unknown windows) in place of CGS with the "
+                       "preconditioner above; the direct solver runs when the iteration limit is reached"
+                    << std::endl;
+            else if (p.precond == 1)
+                out << "GPU solver: restarted GMRES (relative residual 1e-9) with the scaling preconditioner above "
+                       "in place of CGS; the direct solver runs when the iteration limit is reached"
+                    << std::endl;
+            else
+                out << "GPU solver: restarted GMRES (relative residual 1e-9) without a preconditioner in place of "
+                       "CGS; the direct solver runs when the iteration limit is reached"
+                    << std::endl;
         } else {
             out << "GPU solver: LU factorisation without pivoting on the GPU (as Tfactor_usy / Tfbelim)" << std::endl;
         }

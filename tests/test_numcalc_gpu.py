@@ -20,14 +20,15 @@ def numcalc():
     return build.NUMCALC_BIN
 
 
-def _project(tmp_path, name="sphere80"):
+def _project(tmp_path, name="sphere80", precond=0):
     c = gc.load(name)
     if name == "sphere80":
         ps = c["point_sources"]
         sh = [c.pts[:24], c.pts[24:]]
         p = project.Project(root=str(tmp_path / "p"), nodes=c.nodes, elems=c.elems, eval_points=c.pts,
                             eval_elems=meshes.shells_triangles(sh), freqs=list(c.freqs),
-                            point_sources=[tuple(ps[0])], boundary=["ELEM 0 TO 79 VELO 0.0 -1 0.0 -1"])
+                            point_sources=[tuple(ps[0])], boundary=["ELEM 0 TO 79 VELO 0.0 -1 0.0 -1"],
+                            precond=precond)
     else:   # sphere320_adm_velo: admittance everywhere, velocity source on 3 elements
         p = project.Project(root=str(tmp_path / "p"), nodes=c.nodes, elems=c.elems, eval_points=c.pts,
                             eval_elems=meshes.grid_triangles(c.pts), freqs=list(c.freqs),
@@ -55,6 +56,21 @@ def test_be_out_matches_reference(numcalc, tmp_path, precision, tol, name):
                 assert np.abs(vals).max() == 0
             else:
                 assert gc.rel_err(vals, ref) < tol, (s, f, gc.rel_err(vals, ref))
+
+
+@pytest.mark.parametrize("precond", [1, 2])
+def test_scaling_and_no_preconditioner(numcalc, tmp_path, precond):
+    """NC.inp's scaling preconditioner (1) and none (2): the same results as
+    the reference's (ILU) run within the mixed path's bar."""
+    c, wd = _project(tmp_path, "sphere80", precond)
+    r = subprocess.run([numcalc], cwd=wd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:]
+    out = open(os.path.join(wd, "NC.out")).read()
+    assert ("with the scaling preconditioner above" if precond == 1 else "without a preconditioner") in out
+    for s in range(1, len(c.freqs) + 1):
+        for f in ("pBoundary", "pEvalGrid"):
+            ids, vals = project.read_result(os.path.join(wd, "be.out", "be.%d" % s, f))
+            assert gc.rel_err(vals, c["s%d_%s" % (s, f)]) < 1e-5, (s, f)
 
 
 @pytest.mark.parametrize("nitermax", [0, 1, 2])

@@ -5,6 +5,8 @@ It changes how GMRES gets there, not where: every preconditioner mode meets
 the same residual target on the same system, so the solutions agree to about
 the target times the condition number (bar: 1e-6 relative), and the
 corrected preconditioner needs fewer iterations than block-Jacobi alone.
+The modes include NumCalc's own scaling preconditioner (no_precond = 3,
+NC_ComputeScalingVector, NC_CommonFunctions.cpp:1322-1351) and none.
 
 Covers both matrix paths of the correction (complex128 for FP64, complex64
 and its fp16 copy for mixed precision), partial windows (n not a multiple of
@@ -18,7 +20,7 @@ from tests import golden_cases as gc
 
 pytestmark = pytest.mark.gpu
 
-MODES = (True, "block-jacobi", False)
+MODES = (True, "block-jacobi", "scaling", False)
 
 
 def _freq(c, step=1):
@@ -94,7 +96,7 @@ def test_invalid_preconditioner_mode_is_rejected():
     m = capi.Mesh(c.nodes, c.elems)
     with pytest.raises(ValueError):
         capi.Solver(m, precond="ilu")
-    p = capi.SolverParams(capi.PREC_MIXED, 0, 0, 0.0, 0.0, 3, 0, 0)
+    p = capi.SolverParams(capi.PREC_MIXED, 0, 0, 0.0, 0.0, 4, 0, 0)
     h = capi.C.c_void_p()
     rc = capi.load().bem_solver_create(m.handle, capi.C.byref(p), capi.C.byref(h))
     assert rc == capi.BEM_ERR_INVALID
