@@ -1525,6 +1525,7 @@ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
 __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
     __shared__ __align__(16) float2 xs[kMvChunk];
     __shared__ __align__(16) float2 ts[kBlrPerItem][kBlrMaxRank];
+    __shared__ __align__(16) float2 red[4][kBlrB];   // phase 2b: per term group and row
     __shared__ int rk[kBlrPerItem], tsk[kBlrPerItem + 1];
     __shared__ int item_s;
     __shared__ PlanSmem pl;
@@ -1606,86 +1607,97 @@ __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
             }
         }
         __syncthreads();
-        // phase 2: row i
+        // phase 2a: thread i streams its row of the dense blocks (fp16 row
+        // segments, 32-byte loads)
         const int i = threadIdx.x, row = row0 + i;
+        float2 yd = make_float2(0.f, 0.f);
+        bool dense = false;
         if (row < n) {
-            float2 y = make_float2(0.f, 0.f), yd = make_float2(0.f, 0.f);
-            bool dense = false;
+#pragma unroll 1
+            for (int q = 0; q < kBlrPerItem; ++q) {
+                const int J = c * kBlrPerItem + q;
+                if (J >= nb) break;
+                if (rk[q] >= 0) continue;
+                dense = true;
+                const int nc = min(kBlrB, n - J * kBlrB);
+                const unsigned *h = reinterpret_cast<const unsigned *>(S.A16) + (size_t)row * S.lda +
+                                    (size_t)J * kBlrB;
+                const float2 *xq = xs + q * kBlrB;
+                if (nc == kBlrB) {
+                    const uint4 *h4 = reinterpret_cast<const uint4 *>(h);
+#pragma unroll 4
+                    for (int g = 0; g < kBlrB / 8; ++g) {
+                        const uint4 p0 = h4[2 * g], p1 = h4[2 * g + 1];
+                        // x in 16-byte shared loads (two entries each;
+                        // every thread reads the same address)
+                        const float4 *x4 = reinterpret_cast<const float4 *>(xq + 8 * g);
+                        const float4 xa = x4[0], xb = x4[1], xc = x4[2], xd = x4[3];
+                        cmac_h(yd, p0.x, make_float2(xa.x, xa.y));
+                        cmac_h(yd, p0.y, make_float2(xa.z, xa.w));
+                        cmac_h(yd, p0.z, make_float2(xb.x, xb.y));
+                        cmac_h(yd, p0.w, make_float2(xb.z, xb.w));
+                        cmac_h(yd, p1.x, make_float2(xc.x, xc.y));
+                        cmac_h(yd, p1.y, make_float2(xc.z, xc.w));
+                        cmac_h(yd, p1.z, make_float2(xd.x, xd.y));
+                        cmac_h(yd, p1.w, make_float2(xd.z, xd.w));
+                    }
+                } else {
+                    for (int e = 0; e < nc; ++e) cmac_h(yd, h[e], xq[e]);
+                }
+            }
+        }
+        // phase 2b: the compressed blocks; thread t takes rows 4 (t & 63) ..
+        // + 3 (16-byte loads of U_l, four rows each) for the terms
+        // l = t >> 6 (mod 4), the four term groups meet in shared memory
+        {
+            const int rg = threadIdx.x & 63, tg = threadIdx.x >> 6;
+            float2 acc[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
+                             make_float2(0.f, 0.f)};
 #pragma unroll 1
             for (int q = 0; q < kBlrPerItem; ++q) {
                 const int r = rk[q], J = c * kBlrPerItem + q;
                 if (J >= nb) break;
-                if (r < 0) {
-                    // fp16 row segment of the dense block
-                    dense = true;
-                    const int nc = min(kBlrB, n - J * kBlrB);
-                    const unsigned *h = reinterpret_cast<const unsigned *>(S.A16) + (size_t)row * S.lda +
-                                        (size_t)J * kBlrB;
-                    const float2 *xq = xs + q * kBlrB;
-                    if (nc == kBlrB) {
-                        const uint4 *h4 = reinterpret_cast<const uint4 *>(h);
-#pragma unroll 4
-                        for (int g = 0; g < kBlrB / 8; ++g) {
-                            const uint4 p0 = h4[2 * g], p1 = h4[2 * g + 1];
-                            // x in 16-byte shared loads (two entries each;
-                            // every thread reads the same address)
-                            const float4 *x4 = reinterpret_cast<const float4 *>(xq + 8 * g);
-                            const float4 xa = x4[0], xb = x4[1], xc = x4[2], xd = x4[3];
-                            cmac_h(yd, p0.x, make_float2(xa.x, xa.y));
-                            cmac_h(yd, p0.y, make_float2(xa.z, xa.w));
-                            cmac_h(yd, p0.z, make_float2(xb.x, xb.y));
-                            cmac_h(yd, p0.w, make_float2(xb.z, xb.w));
-                            cmac_h(yd, p1.x, make_float2(xc.x, xc.y));
-                            cmac_h(yd, p1.y, make_float2(xc.z, xc.w));
-                            cmac_h(yd, p1.z, make_float2(xd.x, xd.y));
-                            cmac_h(yd, p1.w, make_float2(xd.z, xd.w));
-                        }
-                    } else {
-                        for (int e = 0; e < nc; ++e) cmac_h(yd, h[e], xq[e]);
+                if (r <= 0) continue;
+                const uint4 *u = reinterpret_cast<const uint4 *>(S.blr_U16 +
+                                                                 ((size_t)I * nb + J) * kBlrMaxRank * kBlrB) + rg;
+                int l = tg;
+                for (; l + 12 < r; l += 16) {
+                    uint4 w[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) w[e] = u[(size_t)(l + 4 * e) * (kBlrB / 4)];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const float2 t = ts[q][l + 4 * e];
+                        const float2 p0 = cmulf(h2f(w[e].x), t), p1 = cmulf(h2f(w[e].y), t);
+                        const float2 p2 = cmulf(h2f(w[e].z), t), p3 = cmulf(h2f(w[e].w), t);
+                        acc[0].x += p0.x; acc[0].y += p0.y;
+                        acc[1].x += p1.x; acc[1].y += p1.y;
+                        acc[2].x += p2.x; acc[2].y += p2.y;
+                        acc[3].x += p3.x; acc[3].y += p3.y;
                     }
-                    continue;
                 }
-                const unsigned *u = S.blr_U16 + ((size_t)I * nb + J) * kBlrMaxRank * kBlrB + i;
-                int l = 0;
-                for (; l + 16 <= r; l += 16) {
-                    unsigned w[16];
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) w[e] = u[(size_t)(l + e) * kBlrB];
-                    float2 p = make_float2(0.f, 0.f);
-                    const float4 *t4 = reinterpret_cast<const float4 *>(&ts[q][l]);   // l is even
-#pragma unroll
-                    for (int e = 0; e < 16; e += 2) {
-                        const float4 tt = t4[e >> 1];
-                        const float2 pa = cmulf(h2f(w[e]), make_float2(tt.x, tt.y));
-                        const float2 pb = cmulf(h2f(w[e + 1]), make_float2(tt.z, tt.w));
-                        p.x += pa.x + pb.x;
-                        p.y += pa.y + pb.y;
-                    }
-                    y.x += p.x;
-                    y.y += p.y;
+                for (; l < r; l += 4) {
+                    const uint4 w = u[(size_t)l * (kBlrB / 4)];
+                    const float2 t = ts[q][l];
+                    const float2 p0 = cmulf(h2f(w.x), t), p1 = cmulf(h2f(w.y), t);
+                    const float2 p2 = cmulf(h2f(w.z), t), p3 = cmulf(h2f(w.w), t);
+                    acc[0].x += p0.x; acc[0].y += p0.y;
+                    acc[1].x += p1.x; acc[1].y += p1.y;
+                    acc[2].x += p2.x; acc[2].y += p2.y;
+                    acc[3].x += p3.x; acc[3].y += p3.y;
                 }
-                for (; l + 8 <= r; l += 8) {
-                    unsigned w[8];
+            }
+            float4 *rd = reinterpret_cast<float4 *>(red[tg] + 4 * rg);
+            rd[0] = make_float4(acc[0].x, acc[0].y, acc[1].x, acc[1].y);
+            rd[1] = make_float4(acc[2].x, acc[2].y, acc[3].x, acc[3].y);
+        }
+        __syncthreads();
+        if (row < n) {
+            float2 y = red[0][i];
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) w[e] = u[(size_t)(l + e) * kBlrB];
-                    float2 p = make_float2(0.f, 0.f);
-                    const float4 *t4 = reinterpret_cast<const float4 *>(&ts[q][l]);   // l is even
-#pragma unroll
-                    for (int e = 0; e < 8; e += 2) {
-                        const float4 tt = t4[e >> 1];
-                        const float2 pa = cmulf(h2f(w[e]), make_float2(tt.x, tt.y));
-                        const float2 pb = cmulf(h2f(w[e + 1]), make_float2(tt.z, tt.w));
-                        p.x += pa.x + pb.x;
-                        p.y += pa.y + pb.y;
-                    }
-                    y.x += p.x;
-                    y.y += p.y;
-                }
-                for (; l < r; ++l) {
-                    const float2 p = cmulf(h2f(u[(size_t)l * kBlrB]), ts[q][l]);
-                    y.x += p.x;
-                    y.y += p.y;
-                }
+            for (int g = 1; g < 4; ++g) {
+                y.x += red[g][i].x;
+                y.y += red[g][i].y;
             }
             if (dense) {
                 const float sc = S.rs[(size_t)row * S.nchunk + c];
