@@ -1505,7 +1505,9 @@ __global__ void __launch_bounds__(32 * kUmWarps, 1) k_mv_grp_umma(KTable *tb) {
 // thread streams them: 32-byte loads, one sector each) times the row's scale
 // for the chunk.  Sums run in a fixed order; the partial is float, one per
 // row and chunk like k_mv_tma's, so k_dot1 sums them unchanged.
-constexpr int kBlrThreads = kBlrB;
+constexpr int kBlrRowsPerThread = 2;   // dense rows per thread; more blocks resident per SM
+constexpr int kBlrThreads = kBlrB / kBlrRowsPerThread;
+constexpr int kBlrTermGroups = kBlrThreads / 64;   // phase 2b: 64 threads x 4 rows per term group
 constexpr int kBlrPerItem = kMvChunk / kBlrB;
 constexpr int kBlrTermsPerWarp = 4;   // V rows in flight per warp in phase 1
 static_assert(kMvChunk % kBlrB == 0, "a chunk holds whole blocks");
@@ -1522,10 +1524,10 @@ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 
-__global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
+__global__ void __launch_bounds__(kBlrThreads, 4 * kBlrRowsPerThread) k_mv_blr(KTable *tb) {
     __shared__ __align__(16) float2 xs[kMvChunk];
     __shared__ __align__(16) float2 ts[kBlrPerItem][kBlrMaxRank];
-    __shared__ __align__(16) float2 red[4][kBlrB];   // phase 2b: per term group and row
+    __shared__ __align__(16) float2 red[kBlrTermGroups][kBlrB];   // phase 2b: per term group and row
     __shared__ int rk[kBlrPerItem], tsk[kBlrPerItem + 1];
     __shared__ int item_s;
     __shared__ PlanSmem pl;
@@ -1607,22 +1609,26 @@ __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
             }
         }
         __syncthreads();
-        // phase 2a: thread i streams its row of the dense blocks (fp16 row
-        // segments, 32-byte loads)
-        const int i = threadIdx.x, row = row0 + i;
-        float2 yd = make_float2(0.f, 0.f);
+        // phase 2a: thread i streams rows i + kBlrThreads r of the dense
+        // blocks (fp16 row segments, 32-byte loads)
+        float2 yd[kBlrRowsPerThread];
         bool dense = false;
-        if (row < n) {
+#pragma unroll
+        for (int rr = 0; rr < kBlrRowsPerThread; ++rr) yd[rr] = make_float2(0.f, 0.f);
 #pragma unroll 1
-            for (int q = 0; q < kBlrPerItem; ++q) {
-                const int J = c * kBlrPerItem + q;
-                if (J >= nb) break;
-                if (rk[q] >= 0) continue;
-                dense = true;
-                const int nc = min(kBlrB, n - J * kBlrB);
+        for (int q = 0; q < kBlrPerItem; ++q) {
+            const int J = c * kBlrPerItem + q;
+            if (J >= nb) break;
+            if (rk[q] >= 0) continue;
+            dense = true;
+            const int nc = min(kBlrB, n - J * kBlrB);
+            const float2 *xq = xs + q * kBlrB;
+#pragma unroll
+            for (int rr = 0; rr < kBlrRowsPerThread; ++rr) {
+                const int row = row0 + threadIdx.x + rr * kBlrThreads;
+                if (row >= n) continue;
                 const unsigned *h = reinterpret_cast<const unsigned *>(S.A16) + (size_t)row * S.lda +
                                     (size_t)J * kBlrB;
-                const float2 *xq = xs + q * kBlrB;
                 if (nc == kBlrB) {
                     const uint4 *h4 = reinterpret_cast<const uint4 *>(h);
 #pragma unroll 4
@@ -1632,24 +1638,26 @@ __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
                         // every thread reads the same address)
                         const float4 *x4 = reinterpret_cast<const float4 *>(xq + 8 * g);
                         const float4 xa = x4[0], xb = x4[1], xc = x4[2], xd = x4[3];
-                        cmac_h(yd, p0.x, make_float2(xa.x, xa.y));
-                        cmac_h(yd, p0.y, make_float2(xa.z, xa.w));
-                        cmac_h(yd, p0.z, make_float2(xb.x, xb.y));
-                        cmac_h(yd, p0.w, make_float2(xb.z, xb.w));
-                        cmac_h(yd, p1.x, make_float2(xc.x, xc.y));
-                        cmac_h(yd, p1.y, make_float2(xc.z, xc.w));
-                        cmac_h(yd, p1.z, make_float2(xd.x, xd.y));
-                        cmac_h(yd, p1.w, make_float2(xd.z, xd.w));
+                        cmac_h(yd[rr], p0.x, make_float2(xa.x, xa.y));
+                        cmac_h(yd[rr], p0.y, make_float2(xa.z, xa.w));
+                        cmac_h(yd[rr], p0.z, make_float2(xb.x, xb.y));
+                        cmac_h(yd[rr], p0.w, make_float2(xb.z, xb.w));
+                        cmac_h(yd[rr], p1.x, make_float2(xc.x, xc.y));
+                        cmac_h(yd[rr], p1.y, make_float2(xc.z, xc.w));
+                        cmac_h(yd[rr], p1.z, make_float2(xd.x, xd.y));
+                        cmac_h(yd[rr], p1.w, make_float2(xd.z, xd.w));
                     }
                 } else {
-                    for (int e = 0; e < nc; ++e) cmac_h(yd, h[e], xq[e]);
+                    for (int e = 0; e < nc; ++e) cmac_h(yd[rr], h[e], xq[e]);
                 }
             }
         }
         // phase 2b: the compressed blocks; thread t takes rows 4 (t & 63) ..
         // + 3 (16-byte loads of U_l, four rows each) for the terms
-        // l = t >> 6 (mod 4), the four term groups meet in shared memory
+        // l = t >> 6 (mod kBlrTermGroups); the term groups meet in shared
+        // memory
         {
+            constexpr int G = kBlrTermGroups;
             const int rg = threadIdx.x & 63, tg = threadIdx.x >> 6;
             float2 acc[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
                              make_float2(0.f, 0.f)};
@@ -1661,13 +1669,13 @@ __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
                 const uint4 *u = reinterpret_cast<const uint4 *>(S.blr_U16 +
                                                                  ((size_t)I * nb + J) * kBlrMaxRank * kBlrB) + rg;
                 int l = tg;
-                for (; l + 12 < r; l += 16) {
+                for (; l + 3 * G < r; l += 4 * G) {
                     uint4 w[4];
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) w[e] = u[(size_t)(l + 4 * e) * (kBlrB / 4)];
+                    for (int e = 0; e < 4; ++e) w[e] = u[(size_t)(l + G * e) * (kBlrB / 4)];
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
-                        const float2 t = ts[q][l + 4 * e];
+                        const float2 t = ts[q][l + G * e];
                         const float2 p0 = cmulf(h2f(w[e].x), t), p1 = cmulf(h2f(w[e].y), t);
                         const float2 p2 = cmulf(h2f(w[e].z), t), p3 = cmulf(h2f(w[e].w), t);
                         acc[0].x += p0.x; acc[0].y += p0.y;
@@ -1676,7 +1684,7 @@ __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
                         acc[3].x += p3.x; acc[3].y += p3.y;
                     }
                 }
-                for (; l < r; l += 4) {
+                for (; l < r; l += G) {
                     const uint4 w = u[(size_t)l * (kBlrB / 4)];
                     const float2 t = ts[q][l];
                     const float2 p0 = cmulf(h2f(w.x), t), p1 = cmulf(h2f(w.y), t);
@@ -1692,17 +1700,20 @@ __global__ void __launch_bounds__(kBlrThreads, 4) k_mv_blr(KTable *tb) {
             rd[1] = make_float4(acc[2].x, acc[2].y, acc[3].x, acc[3].y);
         }
         __syncthreads();
-        if (row < n) {
-            float2 y = red[0][i];
 #pragma unroll
-            for (int g = 1; g < 4; ++g) {
-                y.x += red[g][i].x;
-                y.y += red[g][i].y;
+        for (int rr = 0; rr < kBlrRowsPerThread; ++rr) {
+            const int il = threadIdx.x + rr * kBlrThreads, row = row0 + il;
+            if (row >= n) continue;
+            float2 y = red[0][il];
+#pragma unroll
+            for (int g = 1; g < kBlrTermGroups; ++g) {
+                y.x += red[g][il].x;
+                y.y += red[g][il].y;
             }
             if (dense) {
                 const float sc = S.rs[(size_t)row * S.nchunk + c];
-                y.x = fmaf(yd.x, sc, y.x);
-                y.y = fmaf(yd.y, sc, y.y);
+                y.x = fmaf(yd[rr].x, sc, y.x);
+                y.y = fmaf(yd[rr].y, sc, y.y);
             }
             reinterpret_cast<float2 *>(S.mvp)[(size_t)c * n + row] = y;
         }
