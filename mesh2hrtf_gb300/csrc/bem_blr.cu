@@ -2,12 +2,13 @@
 //
 // After assembly, every off-diagonal kBlrB x kBlrB block of A (in the
 // unknowns' Morton order) is approximated by adaptive cross approximation
-// with partial pivoting, in FP32, from A's own entries: take a
-// row's residual against the terms so far, pivot on its largest entry, take
-// that column's residual and add the rank-one term; the next row is the
-// column residual's largest entry among the rows not used yet.  The
-// approximation stops when the new term's Frobenius norm is below kBlrStop
-// times the norm of the sum so far (sum of the terms' squared norms).
+// with partial pivoting, in FP32, from A's own entries: take a row's
+// residual against the terms so far, pivot on its largest entry, take that
+// column's residual and add the rank-one term; the next row is the column
+// residual's largest entry among the rows not used yet (k_blr_aca takes two
+// such rows per pass, see there).  The approximation stops when the new
+// term's Frobenius norm is below kBlrStop times the norm of the sum so far
+// (sum of the terms' squared norms).
 //
 // That stopping rule only looks at the rows and columns it has visited, and
 // on blocks of neighbouring element patches it stops early now and then.  So
@@ -17,9 +18,9 @@
 // computed as w^T B - (w^T U) V^T.  A block whose estimate is within kBlrTol
 // of |B|_F keeps its terms, as fp16 factors with a power-of-two scale per
 // term; any other block, and every diagonal block, is read from the fp16
-// copy of A, which is made afterwards for those blocks' segments only.  One
-// warp per block; lane l holds entries l, l + 32, ... of the block's rows
-// and columns.
+// copy of A, which is made afterwards for those blocks' segments only.  The
+// approximation runs one warp per block (lane l holds entries l, l + 32, ...
+// of the block's rows and columns), the check one block of 128 threads.
 //
 // Boundary-element matrices have numerically low-rank off-diagonal blocks
 // (the kernels are smooth between separated element patches): on the
