@@ -13,7 +13,6 @@
 #include <mutex>
 #include <unordered_map>
 #include <memory>
-#include <mutex>
 #include <string>
 #include <vector>
 
@@ -656,9 +655,29 @@ cudaError_t split_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
     return e;
 }
 
+// A second stream per device for the preconditioner's set-up, so that the
+// block inverses (latency bound: a barrier per pivot) run beside the Krylov
+// copies (bound by DRAM traffic); both only read A.  nullptr if it cannot be
+// had (then everything runs on the caller's stream).
+cudaStream_t aux_stream(cudaStream_t st) {
+    static std::mutex mu;
+    static cudaStream_t streams[64] = {};
+    int dev = -1, sdev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (cudaStreamGetDevice(st, &sdev) != cudaSuccess || sdev != dev) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!streams[dev] && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        streams[dev] = nullptr;
+    }
+    return streams[dev];
+}
+
 bem_status precond_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
     const int prec = ss[0]->prec;
-    CU(split_group(ss, cnt, st));
     std::unique_ptr<bem::PcBatch> pt(new bem::PcBatch());
     std::vector<bem_solver_t> pcs;
     for (int i = 0; i < cnt; ++i) {
@@ -666,25 +685,49 @@ bem_status precond_group(bem_solver_t *ss, int cnt, cudaStream_t st) {
         if (ss[i]->precond) pcs.push_back(ss[i]);
         CU(cudaMemsetAsync(ss[i]->d.x, 0, sizeof(double2) * ss[i]->n, st));
     }
+    // the inverses on the second stream, from the assembled A
+    cudaStream_t ps = st;
+    struct Events {
+        cudaEvent_t e[2] = {nullptr, nullptr};
+        ~Events() {
+            for (cudaEvent_t x : e)
+                if (x) cudaEventDestroy(x);
+        }
+    } evs;
+    cudaEvent_t *ev = evs.e;
+    cudaStream_t aux = pcs.empty() ? nullptr : aux_stream(st);
+    if (aux && cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming) == cudaSuccess &&
+        cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming) == cudaSuccess) {
+        CU(cudaEventRecord(ev[0], st));
+        CU(cudaStreamWaitEvent(aux, ev[0], 0));
+        ps = aux;
+    } else {
+        cudaGetLastError();
+    }
     std::vector<bem_solver_t> bj;   // block-Jacobi; the scaling ones are set here
     for (bem_solver_t s : pcs) {
         if (!s->pc_scaling) {
             bj.push_back(s);
             continue;
         }
-        CU(cudaMemsetAsync(s->d.status, 0, sizeof(int), st));
-        CU(bem::launch_pc_scaling(s->psys(), prec, st));
+        CU(cudaMemsetAsync(s->d.status, 0, sizeof(int), ps));
+        CU(bem::launch_pc_scaling(s->psys(), prec, ps));
     }
     for (size_t c0 = 0; c0 < bj.size(); c0 += bem::kMaxAsm) {
         const int k = (int)std::min<size_t>(bem::kMaxAsm, bj.size() - c0);
         pt->B = k;
         for (int i = 0; i < k; ++i) {
-            CU(cudaMemsetAsync(bj[c0 + i]->d.status, 0, sizeof(int), st));
+            CU(cudaMemsetAsync(bj[c0 + i]->d.status, 0, sizeof(int), ps));
             pt->sys[i] = bj[c0 + i]->psys();
         }
         bem::pc_batch_finish(*pt);
-        CU(bem::launch_block_inverse(*pt, prec, st));
+        CU(bem::launch_block_inverse(*pt, prec, ps));
     }
+    if (ps != st) CU(cudaEventRecord(ev[1], ps));
+    // the Krylov copies on the caller's stream meanwhile
+    const cudaError_t se = split_group(ss, cnt, st);
+    if (ps != st) CU(cudaStreamWaitEvent(st, ev[1], 0));
+    CU(se);
     if (!pcs.empty()) {
         std::vector<int> sing(pcs.size(), 0);
         for (size_t i = 0; i < pcs.size(); ++i)
