@@ -67,7 +67,7 @@ METRIC = "freq solves/s at <=1e-4 rel err, mixed vs plain FP64 GPU BEM; p50/p99 
 MV_TRAFFIC = {
     "fp16": (1.6863e9, 1.6784e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum per Krylov k_mv_tma<0> launch "
                                  "from the fp16 copy, 5 kHz (profiles/k_mv_tma_fp16_head20480.md)"),
-    "blr": (4.0455e9, 4.1127e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum per busy k_mv_blr launch of the "
+    "blr": (4.0315e9, 4.1127e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum per busy k_mv_blr launch of the "
                                 "bench's first batch of 16, against that batch's algorithmic bytes per launch "
                                 "(bem_krylov_copy_info bytes x Krylov steps / 48 launches; "
                                 "profiles/k_mv_blr_head20480.md)"),
