@@ -87,3 +87,23 @@ def test_batch_same_mesh_many_frequencies():
         assert st == capi.BEM_OK
         assert np.array_equal(x, x0) and np.array_equal(pot, p0)
         assert info["rel_residual"] <= 1e-9
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_MIXED, capi.PREC_FP64])
+def test_large_batch_equals_alone(prec):
+    """A batch of 20 instances of one mesh (the engine's launch tables and
+    plans hold them all at once): the same bits as alone."""
+    pts = meshes.random_sphere_points(64, 1.2, 9)
+    v, f = meshes.icosphere(320, 0.1)
+    m = capi.Mesh(v, f)
+    freqs = [_freq(len(f), 300.0 + 350.0 * i, [1.0, 0.05 * i, 0.0]) for i in range(20)]
+    s = capi.Solver(m, precision=prec, tol=1e-9)
+    alone = [s.solve_frequency(fr, pts)[:2] for fr in freqs[:3]]
+    s.close()
+    solvers = [capi.Solver(m, precision=prec, tol=1e-9) for _ in freqs]
+    res = capi.solve_batch(solvers, freqs, [pts] * len(freqs))
+    for (x0, p0), r in zip(alone, res):
+        assert np.array_equal(r[0], x0) and np.array_equal(r[1], p0)
+    for sv in solvers:
+        sv.close()
+    m.close()
