@@ -177,9 +177,12 @@ bem_status bem_tune_info(int32_t n_elem, int32_t precision, int32_t n_rhs, char 
 bem_status bem_set_device(int32_t device);
 /* Bytes a solver for n_elem unknowns holds on the device (matrix, Krylov
  * basis, preconditioner, work vectors) at the given precision and restart
- * length: the HBM
+ * length, with the default Krylov copy: the HBM
  * admission footprint (NumCalc's host RAM estimate, NC_Main.cpp:524-541,
- * counts (N + N^2) * 16 bytes for the same data). */
+ * counts (N + N^2) * 16 bytes for the same data).  The block low-rank copy
+ * (complex64_krylov = 2) adds about 295 KB per block of 256 x 256 unknowns,
+ * ceil(N / 256)^2 blocks (1.9 GB at N = 20480); bem_solver_create checks
+ * the whole footprint against the budget. */
 double bem_footprint_bytes(int32_t n_elem, int32_t precision, int32_t restart);
 /* The same for a solver holding n_rhs right-hand sides (bem_solve_multi). */
 double bem_footprint_multi(int32_t n_elem, int32_t precision, int32_t restart, int32_t n_rhs);
