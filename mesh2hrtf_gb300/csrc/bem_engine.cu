@@ -154,8 +154,12 @@ cudaError_t Engine::set_batch(const std::vector<KSys> &sys, const std::vector<KS
     h_tab_->n_groups = ng;
     groups_ = ng;
     blr_ = 0;
-    for (int b = 0; b < B; ++b)
-        if (h_tab_->sys[b].blr_nb > 0 && !h_tab_->sys[b].shared) ++blr_;
+    dense_ = 0;
+    for (int b = 0; b < B; ++b) {
+        if (h_tab_->sys[b].shared) continue;
+        if (h_tab_->sys[b].blr_nb > 0) ++blr_;
+        else ++dense_;
+    }
     // the groups' Krylov products on the 5th-generation tensor cores need a
     // TMA map of each group's matrix; without them the warp-level kernel runs
     bool umma = ng > 0 && group_product_umma();
@@ -217,13 +221,13 @@ cudaError_t Engine::time_product(const KSys &sys, float *ms) {
 cudaError_t Engine::run_body() {
     cudaError_t e = ensure_init();
     if (e != cudaSuccess) return e;
-    const int v = (groups_ > 0 ? 1 : 0) | (blr_ > 0 ? 2 : 0);
+    const int v = (groups_ > 0 ? 1 : 0) | (blr_ > 0 ? 2 : 0) | (dense_ > 0 ? 4 : 0);
     if (!exec_[v]) {
         cudaGraph_t g = nullptr;
         e = cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
         cudaError_t le = launch_krylov_body(prec_, d_tab_, ev_, st_, &body_launches_[v], (v & 1) != 0,
-                                                   (v & 2) != 0);
+                                                   (v & 2) != 0, (v & 4) != 0);
         e = cudaStreamEndCapture(st_, &g);
         if (le != cudaSuccess) e = le;
         if (e == cudaSuccess) e = cudaGraphInstantiate(&exec_[v], g, 0);

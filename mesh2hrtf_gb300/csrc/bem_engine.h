@@ -53,13 +53,15 @@ private:
     int2 *d_items_ = nullptr;
     size_t items_cap_ = 0;
     std::vector<int2> items_;
-    // the iteration body without and with the shared-matrix (group) products
-    // (bit 0) and the block low-rank product (bit 1), each variant captured
-    // at its first replay
-    cudaGraphExec_t exec_[4] = {nullptr, nullptr, nullptr, nullptr};
-    int body_launches_[4] = {0, 0, 0, 0};
+    // the iteration body's variants: with the shared-matrix (group) products
+    // (bit 0), with the block low-rank product (bit 1), with the product of
+    // single systems from A or its fp16 copy (bit 2); each captured at its
+    // first replay
+    cudaGraphExec_t exec_[8] = {};
+    int body_launches_[8] = {};
     int groups_ = 0;   // shared-matrix groups of the current batch
     int blr_ = 0;      // systems of the current batch with a block low-rank copy
+    int dense_ = 0;    // single systems whose Krylov products read A or its fp16 copy
     cudaEvent_t ev_[2 * (kSteps + 1)] = {};
     double mv_ms_ = 0.0;
     long long bodies_ = 0;

@@ -2607,7 +2607,7 @@ static void pc_window(bool c128, const KTable *d_tab, int mode, int gv, cudaStre
 }
 
 cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev, cudaStream_t st,
-                               int *launches_out, bool groups, bool blr) {
+                               int *launches_out, bool groups, bool blr, bool dense) {
     KTable *tb = const_cast<KTable *>(d_tab);
     const bool c128 = prec == 0;
     if (!g_vec_grid) return cudaErrorNotReady;   // krylov_prepare() first
@@ -2619,7 +2619,8 @@ cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev
         if (mv_ev) cudaEventRecordWithFlags(mv_ev[2 * q], st, cudaEventRecordExternal);
         if (c128) k_mv64<false><<<gmv, 256, 0, st>>>(tb, 0);
         else {
-            k_mv_tma<false><<<gmv, kTmaThreads, tma_smem_bytes(false), st>>>(tb, 0);
+            if (dense) k_mv_tma<false><<<gmv, kTmaThreads, tma_smem_bytes(false), st>>>(tb, 0);
+            else --nl;   // counted with the step's 8 below
             if (groups) {
                 k_mv_grp_tc<<<gmv, 32 * (kTcWarps + 1), kTcSmem, st>>>(tb, 0);
                 k_mv_grp_umma<<<gmv, 32 * kUmWarps, kUmSmem, st>>>(tb);

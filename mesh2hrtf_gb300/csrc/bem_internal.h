@@ -404,10 +404,12 @@ constexpr int kSteps = 8;
 // products (may be nullptr).  prec: 0 complex128, 1 complex64 matrices.
 // groups: include the shared-matrix (group) products, for batches that have
 // groups; blr: include the block low-rank product (k_mv_blr), for batches
-// with systems that have a block low-rank copy.  Returns the number of kernel
-// launches enqueued through *launches_out.
+// with systems that have a block low-rank copy; dense: include the Krylov
+// product from A or its fp16 copy (k_mv_tma / k_mv64), for batches with
+// single systems without one (always for complex128).  Returns the number of
+// kernel launches enqueued through *launches_out.
 cudaError_t launch_krylov_body(int prec, const KTable *d_tab, cudaEvent_t *mv_ev, cudaStream_t st,
-                               int *launches_out, bool groups, bool blr);
+                               int *launches_out, bool groups, bool blr, bool dense);
 // complex64 matrices: the product streams row segments with bulk copies
 // (TMA) in strips of `strip` rows (a multiple of kTmaRows, chosen per system
 // by the tuner; kTmaStrip by default); complex128: tiles of kMvRows rows.
