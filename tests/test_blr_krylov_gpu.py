@@ -16,10 +16,11 @@ from tests import golden_cases as gc
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", ["sphere1280_1k", "sphere320_adm_velo", "quad96_soft_plane"])
+@pytest.mark.parametrize("name", ["pspw2412_4k", "sphere1280_1k", "sphere320_adm_velo", "quad96_soft_plane"])
 def test_blr_krylov_matches_complex64_krylov(name):
-    """Golden cases of the reference: 1280, 320 and 96 unknowns (five, two and
-    one block rows, the last ones ragged)."""
+    """Golden cases of the reference: 2412, 1280, 320 and 96 unknowns (ten,
+    five, two and one block rows, the last ones ragged; plane and point
+    sources, admittance and velocity boundary conditions, quadrilaterals)."""
     c = gc.load(name)
     st = c.step(1)
     f = capi.Frequency(st["k"], c.n, bc_type=st["bc_type"], bc_value=st["bc_value"],
