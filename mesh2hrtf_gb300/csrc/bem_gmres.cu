@@ -1496,13 +1496,16 @@ __global__ void __launch_bounds__(32 * kUmWarps, 1) k_mv_grp_umma(KTable *tb) {
 
 // ------------------------------------------------------------ block low-rank product
 // Krylov products of systems with a block low-rank copy (KSys::blr_nb > 0,
-// compressed by k_blr_aca over the fp16 copy).  Persistent grid of 256-thread
-// blocks; items (system, block row I, chunk c of kMvChunk columns =
-// kBlrPerItem blocks) from the queue.  Phase 1: warp w takes the terms
-// w, w + 8, ... of the item's compressed blocks, t_l = s_l V_l . x (fp16
-// factors).  Phase 2: thread i takes row i: sum over the item's compressed
-// blocks of U_l[i] t_l, plus its fp16 row segments of the dense blocks (the
-// thread streams them: 32-byte loads, one sector each) times the row's scale
+// compressed by k_blr_aca / k_blr_check; dense blocks in the fp16 copy).
+// Persistent grid of 128-thread blocks (8 resident per SM); items (system,
+// block row I, chunk c of kMvChunk columns = kBlrPerItem blocks) from the
+// queue.  Phase 1: warp w takes the terms w, w + 4, ... of the item's
+// compressed blocks, t_l = s_l V_l . x (fp16 factors, x chunk in shared
+// memory).  Phase 2a: thread i streams rows i and i + 128 of the dense
+// blocks (fp16 row segments, 32-byte loads, one sector each).  Phase 2b:
+// thread t takes rows 4 (t & 63) .. + 3 of the compressed blocks with
+// 16-byte loads of U_l for every other term; the two term groups are added
+// in order through shared memory, then the dense part times the row's scale
 // for the chunk.  Sums run in a fixed order; the partial is float, one per
 // row and chunk like k_mv_tma's, so k_dot1 sums them unchanged.
 constexpr int kBlrRowsPerThread = 2;   // dense rows per thread; more blocks resident per SM
