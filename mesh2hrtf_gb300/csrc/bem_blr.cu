@@ -372,7 +372,8 @@ __global__ void __launch_bounds__(kChkThreads, 6) k_blr_check(const __grid_const
     __shared__ float2 cw[kBlrSketch][kBlrMaxRank];   // w_p^T U_l
     __shared__ unsigned rbits[kBlrB];                 // probe signs per row
     __shared__ float red[2][kChkWarps];
-    __shared__ int keep;
+    __shared__ float tn[kBlrMaxRank];   // term norms
+    __shared__ int keep, kept;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const long long gb = blockIdx.x;
     if (gb >= tb.off[tb.B]) return;
@@ -472,6 +473,19 @@ __global__ void __launch_bounds__(kChkThreads, 6) k_blr_check(const __grid_const
         red[0][warp] = est;
         red[1][warp] = bn2;
     }
+    // Frobenius norms of the terms, |U_l| |V_l| (warp w: terms w, w + 4, ...)
+    for (int l = warp; l < k; l += kChkWarps) {
+        float nu = 0.f, nv = 0.f;
+#pragma unroll
+        for (int q = 0; q < kBlrB / 32; ++q) {
+            const float2 u = U[(size_t)l * kBlrB + lane + 32 * q], v = V[(size_t)l * kBlrB + lane + 32 * q];
+            nu = fmaf(u.x, u.x, fmaf(u.y, u.y, nu));
+            nv = fmaf(v.x, v.x, fmaf(v.y, v.y, nv));
+        }
+        nu = warp_sumf(nu);
+        nv = warp_sumf(nv);
+        if (lane == 0) tn[l] = sqrtf(nu) * sqrtf(nv);
+    }
     __syncthreads();
     if (t == 0) {
         float e = 0.f, bb = 0.f;
@@ -479,15 +493,25 @@ __global__ void __launch_bounds__(kChkThreads, 6) k_blr_check(const __grid_const
             e += red[0][w];
             bb += red[1][w];
         }
-        keep = e / (float)kBlrSketch <= kBlrTol * kBlrTol * bb;
-        if (!keep) S.rank[b] = -1;
+        const float est = e / (float)kBlrSketch;
+        keep = est <= kBlrTol * kBlrTol * bb;
+        int kk = k;
+        if (keep) {
+            // drop trailing terms within half the tolerance left: by the
+            // triangle inequality the error grows by at most their norms
+            const float budget = 0.5f * (kBlrTol * sqrtf(bb) - sqrtf(est));
+            float dropped = 0.f;
+            while (kk > 0 && dropped + tn[kk - 1] <= budget) dropped += tn[--kk];
+        }
+        kept = kk;
+        S.rank[b] = keep ? kk : -1;
     }
     __syncthreads();
     if (!keep) return;
     // the kept terms as fp16 factors, scale 2^(eu - 15) 2^(ev - 15) per term
     unsigned *U16 = S.U16 + (size_t)b * kBlrMaxRank * kBlrB;
     unsigned *V16 = S.V16 + (size_t)b * kBlrMaxRank * kBlrB;
-    for (int l = warp; l < k; l += kChkWarps) {
+    for (int l = warp; l < kept; l += kChkWarps) {
         const int eu = store_half(U + (size_t)l * kBlrB, U16 + (size_t)l * kBlrB, lane);
         const int ev = store_half(V + (size_t)l * kBlrB, V16 + (size_t)l * kBlrB, lane);
         if (lane == 0) S.scale[(size_t)b * kBlrMaxRank + l] = ldexpf(1.f, eu + ev - 30);
