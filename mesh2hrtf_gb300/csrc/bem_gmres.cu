@@ -2152,15 +2152,24 @@ __device__ void givens_step(const KSys &S) {
 }
 
 // One block of kMaxSys threads, thread t = system t: the Givens step of every
-// system in phase ARNOLDI, then the plans of the next Krylov product and of
-// the refinement residual.
+// system in phase ARNOLDI, then, if a system's phase changed, the plans of
+// the next Krylov product and of the refinement residual.
 __global__ void __launch_bounds__(kMaxSys) k_givens(KTable *tb) {
+    __shared__ int changed;   // some system left phase ARNOLDI in this step
     const int b = threadIdx.x;
-    if (b < tb->B && tb->sys[b].st->phase == kPhaseArnoldi) givens_step(tb->sys[b]);
+    if (b == 0) changed = 0;
     __syncthreads();
-    plan_build(tb, 0);
-    plan_build(tb, 1);
-    plan_build(tb, 2);
+    if (b < tb->B && tb->sys[b].st->phase == kPhaseArnoldi) {
+        givens_step(tb->sys[b]);
+        if (tb->sys[b].st->phase != kPhaseArnoldi) atomicOr(&changed, 1);
+    }
+    __syncthreads();
+    // the plans depend only on the systems' phases
+    if (changed) {
+        plan_build(tb, 0);
+        plan_build(tb, 1);
+        plan_build(tb, 2);
+    }
 }
 
 // ------------------------------------------------------------ end of cycle
@@ -2510,12 +2519,15 @@ __device__ void decide_step(const KSys &S) {
 
 // One block of kMaxSys threads: convergence decision after a cycle (or the
 // initial residual) and the restart of every system in phase UPDATE, then the
-// plan of the next body's first Krylov product.
+// plans from the new phases (k_givens rebuilds them only when a phase changes
+// in its step).
 __global__ void __launch_bounds__(kMaxSys) k_decide(KTable *tb) {
     const int b = threadIdx.x;
     if (b < tb->B && tb->sys[b].st->phase == kPhaseUpdate) decide_step(tb->sys[b]);
     __syncthreads();
     plan_build(tb, 0);
+    plan_build(tb, 1);
+    plan_build(tb, 2);
 }
 
 // Both plans from the current phases (after the host rewrote the table).
