@@ -104,3 +104,12 @@ def test_copy_info_needs_the_copy():
         s.krylov_copy_info()
     s.close()
     m.close()
+
+
+def test_krylov_copy_mode_out_of_range_is_rejected():
+    v, f = meshes.icosphere(80, 0.1)
+    m = capi.Mesh(v, f)
+    p = capi.SolverParams(capi.PREC_MIXED, 0, 0, 0.0, 0.0, 0, 0, 3)
+    h = capi.C.c_void_p()
+    assert capi.load().bem_solver_create(m.handle, capi.C.byref(p), capi.C.byref(h)) == capi.BEM_ERR_INVALID
+    m.close()
