@@ -269,8 +269,8 @@ __global__ void __launch_bounds__(512) k_binv64(const __grid_constant__ PcBatch 
 }
 
 // fp16 copy of complex64 rows (SplitBatch): one warp per (row, column
-// chunk of kMvChunk entries; with a block low-rank copy only the segments it
-// reads).  The segment's largest component m sets the
+// chunk of kMvChunk entries; with a block low-rank copy a block per (block
+// row, chunk), only for the segments the copy reads).  The segment's largest component m sets the
 // scale 2^(15 - e) with m < 2^e; every component is scaled (exactly) and
 // rounded to nearest.  Power-of-two scales keep A16 * rs within one fp16
 // rounding of A.  The warp holds its 8 KB segment in registers, so A is
@@ -278,25 +278,9 @@ __global__ void __launch_bounds__(512) k_binv64(const __grid_constant__ PcBatch 
 constexpr int kSplitThreads = 256;
 constexpr int kSplitWarps = kSplitThreads / 32;
 
-__global__ void __launch_bounds__(kSplitThreads) k_split16(const __grid_constant__ SplitBatch tb) {
-    const int sb = find_blk(tb.off, tb.B, blockIdx.x);
-    const SplitSys &S = tb.sys[sb];
-    const int n = S.n, nch = mv_chunks(n), lane = threadIdx.x & 31;
-    const long long item = (long long)(blockIdx.x - tb.off[sb]) * kSplitWarps + (threadIdx.x >> 5);
-    if (item >= (long long)n * nch) return;
-    const int i = (int)(item / nch), c = (int)(item - (long long)i * nch);
-    if (S.blr_rank && c != i / kMvChunk) {
-        // block low-rank copy: only the diagonal chunk (the preconditioner's
-        // window) and chunks with a dense block of this row's block row
-        const int I = i / kBlrB, nb = S.blr_nb;
-        bool need = false;
-#pragma unroll
-        for (int q = 0; q < kMvChunk / kBlrB; ++q) {
-            const int J = c * (kMvChunk / kBlrB) + q;
-            need |= J < nb && S.blr_rank[(size_t)I * nb + J] < 0;
-        }
-        if (!need) return;
-    }
+// One row segment (row i, chunk c) by one warp.
+__device__ __forceinline__ void split_segment(const SplitSys &S, int i, int c, int lane) {
+    const int n = S.n, nch = mv_chunks(n);
     const int c0 = c * kMvChunk, len = min(kMvChunk, n - c0), len2 = len >> 1;
     const float2 *seg = (const float2 *)S.A + (size_t)i * S.lda + c0;   // 8 KB aligned within the row
     const float4 *seg4 = reinterpret_cast<const float4 *>(seg);
@@ -332,12 +316,46 @@ __global__ void __launch_bounds__(kSplitThreads) k_split16(const __grid_constant
     if ((len & 1) && lane == 0) h[len - 1] = __floats2half2_rn(last.x * scale, last.y * scale);
 }
 
+__global__ void __launch_bounds__(kSplitThreads) k_split16(const __grid_constant__ SplitBatch tb) {
+    const int sb = find_blk(tb.off, tb.B, blockIdx.x);
+    const SplitSys &S = tb.sys[sb];
+    const int n = S.n, nch = mv_chunks(n), lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (S.blr_rank) {
+        // block low-rank copy: a block per (block row I, chunk c), converted
+        // only for the diagonal chunk (the preconditioner's window) and
+        // chunks with a dense block of the block row; warp w takes rows w,
+        // w + kSplitWarps, ...
+        const int it = blockIdx.x - tb.off[sb], nb = S.blr_nb;
+        const int I = it / nch, c = it - (it / nch) * nch;
+        if (I >= nb) return;
+        bool need = c == I * kBlrB / kMvChunk;
+#pragma unroll
+        for (int q = 0; q < kMvChunk / kBlrB; ++q) {
+            const int J = c * (kMvChunk / kBlrB) + q;
+            need |= J < nb && S.blr_rank[(size_t)I * nb + J] < 0;
+        }
+        if (!need) return;
+        for (int r = warp; r < kBlrB; r += kSplitWarps) {
+            const int i = I * kBlrB + r;
+            if (i < n) split_segment(S, i, c, lane);
+        }
+        return;
+    }
+    const long long item = (long long)(blockIdx.x - tb.off[sb]) * kSplitWarps + warp;
+    if (item >= (long long)n * nch) return;
+    const int i = (int)(item / nch), c = (int)(item - (long long)i * nch);
+    split_segment(S, i, c, lane);
+}
+
 }  // namespace
 
 void split_batch_finish(SplitBatch &t) {
     t.off[0] = 0;
-    for (int b = 0; b < t.B; ++b)
-        t.off[b + 1] = t.off[b] + ceil_div((long long)t.sys[b].n * mv_chunks(t.sys[b].n), kSplitWarps);
+    for (int b = 0; b < t.B; ++b) {
+        const SplitSys &q = t.sys[b];
+        t.off[b + 1] = t.off[b] + (q.blr_rank ? q.blr_nb * mv_chunks(q.n)   // a block per (block row, chunk)
+                                              : ceil_div((long long)q.n * mv_chunks(q.n), kSplitWarps));
+    }
 }
 
 cudaError_t launch_split16(const SplitBatch &t, cudaStream_t st) {
