@@ -10,21 +10,25 @@ Restates, for the traditional-BEM results this build produces:
 * HRIRs by the inverse real FFT of the conjugated, referenced spectrum with a
   0 Hz bin of 1, a real Nyquist bin and a circular shift of 30 cm of travel
   (``compute_hrirs.py:6-109``, ``output2hrtf.py:118-128``);
-* the SOFA geometry conventions of ``_get_sofa_object``
-  (``output2hrtf.py:209-287``): evaluation points as spherical source
-  positions (azimuth, elevation in degrees, radius), the ear positions
-  (``sourceCenter``) as receivers.
+* the SOFA objects of ``_get_sofa_object`` (``output2hrtf.py:209-287``):
+  evaluation points as spherical source positions (azimuth, elevation in
+  degrees, radius), the ear positions (``sourceCenter``) as receivers,
+  SimpleFreeFieldHRTF / HRIR for two receivers, GeneralTF / FIR otherwise.
+
+The in-memory entry points (``hrtf_sofa``, ``write_hrtf_sofa``) take the
+evaluation-grid pressure as the solver returns it (``capi.Solver.
+solve_frequency``, ``capi.solve_batch``, ``capi.Server.wait``), so HRTFs come
+straight from the results with no result file in between; ``output2hrtf``
+reads a project's result files and calls them.
 
 Differences from the reference:
 
 * Results are read at full precision when the drop-in wrote them
   (``NUMCALC_GB300_NPY=1``: ``be.out/be.<k>/<name>.npy``); otherwise from the
   7-digit text files, as the reference does.
-* SOFA files need ``sofar`` (netCDF-4/HDF5), which this image does not have:
-  ``output2hrtf`` writes ``Output2HRTF/HRTF_<grid>.npz`` and
-  ``HRIR_<grid>.npz`` with the SOFA variable names instead (``Data_Real``,
-  ``Data_Imag``, ``N``, ``Data_IR``, ``Data_SamplingRate``,
-  ``SourcePosition``, ``ReceiverPosition``, ``GLOBAL_SOFAConventions``).
+* The SOFA files are written by ``mesh2hrtf_gb300.sofa`` in the netCDF
+  classic container (sofar, which writes netCDF-4/HDF5, is not installed);
+  the conventions' variables and attributes are sofar's.
 * Each grid's rows are selected by node id, not by the order of
   ``os.listdir(EvaluationGrids)``.
 
@@ -39,6 +43,7 @@ import sys
 import numpy as np
 
 from . import project as _project
+from . import sofa as _sofa
 
 
 def read_result(step_dir, name, full_precision=True):
@@ -141,52 +146,104 @@ def _grid_nodes(folder, grid):
     return nodes[:, 0].astype(np.int64), nodes[:, 1:4]
 
 
+def sofa_object(data, source_position, receiver_position, mode, mesh2hrtf_version, frequencies=None,
+                sampling_rate=None):
+    """The SOFA object of complex pressures or impulse responses of shape
+    (points, receivers, frequencies or samples), as _get_sofa_object builds
+    it (output2hrtf.py:209-287): the evaluation points (Cartesian) as
+    spherical source positions, the ear positions as receivers."""
+    data = np.asarray(data)
+    n_rec = data.shape[1]
+    if mode == "HRTF":
+        conv = "SimpleFreeFieldHRTF" if n_rec == 2 else "GeneralTF"
+    else:
+        conv = "SimpleFreeFieldHRIR" if n_rec == 2 else "GeneralFIR"
+    s = _sofa.new(conv)
+    s["GLOBAL_ApplicationName"] = "Mesh2HRTF"
+    s["GLOBAL_ApplicationVersion"] = str(mesh2hrtf_version)
+    s["GLOBAL_History"] = "numerically simulated data"
+    s["SourcePosition"] = cartesian_to_spherical(source_position)
+    s["SourcePosition_Units"] = "degree, degree, meter"
+    s["SourcePosition_Type"] = "spherical"
+    s["ReceiverPosition"] = np.asarray(receiver_position, float).reshape(-1, 3, 1)
+    s["ReceiverPosition_Units"] = "meter"
+    s["ReceiverPosition_Type"] = "cartesian"
+    if mode == "HRTF":
+        s["Data_Real"] = np.real(data)
+        s["Data_Imag"] = np.imag(data)
+        s["N"] = np.asarray(frequencies, float).flatten()
+    else:
+        s["Data_IR"] = np.asarray(data, float)
+        s["Data_SamplingRate"] = np.array([float(sampling_rate)])
+        s["Data_Delay"] = np.zeros((1, n_rec))
+    return s
+
+
+def hrtf_sofa(pressure, grid_xyz, params):
+    """(HRTF, HRIR) SOFA objects of one evaluation grid from its pressure
+    (points, sources, frequencies) as the solver returned it, without a
+    result file in between: the C ABI returns the potential, and the
+    pressure is i * rho * omega times it (what the drop-in prints).  The
+    HRIR object is None unless the project's ``computeHRIRs`` is set.
+    ``params`` holds the keys of a project's parameters.json that
+    Output2HRTF reads (output2hrtf.py:86-128)."""
+    freqs = np.asarray(params["frequencies"], float)
+    data = np.asarray(pressure, complex)
+    if data.ndim != 3 or data.shape[0] != len(grid_xyz) or data.shape[2] != len(freqs):
+        raise ValueError("pressure must have shape (points, sources, frequencies) = (%d, *, %d), not %s"
+                         % (len(grid_xyz), len(freqs), data.shape))
+    receivers = np.asarray(params["sourceCenter"], float).reshape(-1, 3)
+    hrtf = sofa_object(data, grid_xyz, receivers, "HRTF", params.get("Mesh2HRTF_Version", ""), frequencies=freqs)
+    if params.get("reference"):
+        radius = hrtf["SourcePosition"][:, 2]
+        data = reference_hrtfs(data, freqs, radius, params["sourceType"], params.get("sourceArea", []),
+                               params["speedOfSound"], params["densityOfMedium"], mode="min")
+        hrtf["Data_Real"], hrtf["Data_Imag"] = np.real(data), np.imag(data)
+    hrir = None
+    if params.get("computeHRIRs"):
+        if not params.get("reference"):
+            raise ValueError("Computing HRIRs requires prior referencing")
+        fs = round(2 * freqs[-1])
+        n_shift = int(np.round(.30 / (1 / fs * params["speedOfSound"])))
+        ir, fs = compute_hrirs(data, freqs, n_shift)
+        hrir = sofa_object(ir, grid_xyz, receivers, "HRIR", params.get("Mesh2HRTF_Version", ""),
+                           sampling_rate=fs)
+    return hrtf, hrir
+
+
+def write_hrtf_sofa(out_dir, grid, pressure, grid_xyz, params):
+    """Write ``HRTF_<grid>.sofa`` (and ``HRIR_<grid>.sofa`` with
+    computeHRIRs) to out_dir from in-memory pressure; returns the paths."""
+    os.makedirs(out_dir, exist_ok=True)
+    hrtf, hrir = hrtf_sofa(pressure, grid_xyz, params)
+    paths = [os.path.join(out_dir, "HRTF_%s.sofa" % grid)]
+    _sofa.write(paths[0], hrtf)
+    if hrir is not None:
+        paths.append(os.path.join(out_dir, "HRIR_%s.sofa" % grid))
+        _sofa.write(paths[1], hrir)
+    return paths
+
+
 def output2hrtf(folder, full_precision=True):
     """Process a project's NumCalc results (output2hrtf.py:15-128): per
-    evaluation grid the referenced HRTFs and, with computeHRIRs, the HRIRs.
-    Returns the paths written."""
+    evaluation grid the referenced HRTFs and, with computeHRIRs, the HRIRs,
+    written as SOFA files to <folder>/Output2HRTF.  Returns the paths
+    written."""
     params_path = os.path.join(folder, "parameters.json")
     if not os.path.isfile(params_path):
         raise ValueError("The folder %s is not a valid Mesh2HRTF project. It must contain the file "
                          "'parameters.json'" % folder)
     params = json.load(open(params_path))
     out_dir = os.path.join(folder, "Output2HRTF")
-    os.makedirs(out_dir, exist_ok=True)
     ids, pressure = read_pressure(folder, params["numSources"], params["numFrequencies"], "pEvalGrid",
                                   full_precision)
     row_of = {int(i): r for r, i in enumerate(ids)}
     grids = params.get("evaluationGrids") or sorted(os.listdir(os.path.join(folder, "EvaluationGrids")))
     written = []
-    freqs = np.asarray(params["frequencies"], float)
     for grid in grids:
         gid, xyz = _grid_nodes(folder, grid)
         rows = np.array([row_of[int(i)] for i in gid])
-        data = pressure[rows]
-        src = cartesian_to_spherical(xyz)
-        receivers = np.asarray(params["sourceCenter"], float).reshape(-1, 3)
-        conv = "SimpleFreeFieldHRTF" if data.shape[1] == 2 else "GeneralTF"
-        if params.get("reference"):
-            data = reference_hrtfs(data, freqs, src[:, 2], params["sourceType"], params.get("sourceArea", []),
-                                   params["speedOfSound"], params["densityOfMedium"], mode="min")
-        path = os.path.join(out_dir, "HRTF_%s.npz" % grid)
-        np.savez(path, Data_Real=data.real, Data_Imag=data.imag, N=freqs, SourcePosition=src,
-                 SourcePosition_Type="spherical", SourcePosition_Units="degree, degree, meter",
-                 ReceiverPosition=receivers, GLOBAL_SOFAConventions=conv,
-                 GLOBAL_ApplicationVersion=params.get("Mesh2HRTF_Version", ""))
-        written.append(path)
-        if params.get("computeHRIRs"):
-            if not params.get("reference"):
-                raise ValueError("Computing HRIRs requires prior referencing")
-            fs = round(2 * freqs[-1])
-            n_shift = int(np.round(.30 / (1 / fs * params["speedOfSound"])))
-            hrir, fs = compute_hrirs(data, freqs, n_shift)
-            path = os.path.join(out_dir, "HRIR_%s.npz" % grid)
-            np.savez(path, Data_IR=hrir, Data_SamplingRate=fs, Data_Delay=np.zeros((1, hrir.shape[1])),
-                     SourcePosition=src, SourcePosition_Type="spherical",
-                     SourcePosition_Units="degree, degree, meter", ReceiverPosition=receivers,
-                     GLOBAL_SOFAConventions="SimpleFreeFieldHRIR" if hrir.shape[1] == 2 else "GeneralFIR",
-                     GLOBAL_ApplicationVersion=params.get("Mesh2HRTF_Version", ""))
-            written.append(path)
+        written += write_hrtf_sofa(out_dir, grid, pressure[rows], xyz, params)
     return written
 
 

@@ -8,7 +8,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from mesh2hrtf_gb300 import build, meshes, project
+from mesh2hrtf_gb300 import build, capi, meshes, project, sofa
 from tests import golden_cases as gc
 
 pytestmark = pytest.mark.gpu
@@ -152,6 +152,23 @@ def test_full_precision_results_and_hrtfs(numcalc, tmp_path):
                "sourceCenter": [[0.5, 0.1, 0.0]], "sourceArea": [], "reference": True, "computeHRIRs": False,
                "numFrequencies": len(c.freqs), "frequencies": [float(v) for v in c.freqs]},
               open(os.path.join(root, "parameters.json"), "w"))
-    h = np.load(o2h.output2hrtf(root)[0])
+    h = sofa.read(o2h.output2hrtf(root)[0])
     hrtf = h["Data_Real"] + 1j * h["Data_Imag"]
     assert hrtf.shape == (len(c.pts), 1, len(c.freqs)) and np.all(np.isfinite(hrtf))
+    assert h["GLOBAL_SOFAConventions"] == "GeneralTF"
+    # the same HRTFs straight from the solver's results (no result file)
+    params = json.load(open(os.path.join(root, "parameters.json")))
+    m = capi.Mesh(c.nodes, c.elems)
+    sv = capi.Solver(m, precision=capi.PREC_FP64, tol=1e-9)   # the drop-in's tolerance
+    pres = []
+    for s in range(1, len(c.freqs) + 1):
+        st = c.step(s)
+        fr = capi.Frequency(st["k"], c.n, bc_type=st["bc_type"], bc_value=st["bc_value"],
+                            admittance=st["admittance"], point_sources=st["point_sources"],
+                            point_amps=st["point_amps"], plane_dirs=st["plane_dirs"], plane_amps=st["plane_amps"])
+        _, pot, _ = sv.solve_frequency(fr, c.pts, with_grad=False)
+        pres.append(1j * st["rpfact"] * pot)   # pressure = i rho omega potential
+    sv.close()
+    m.close()
+    mem, _ = o2h.hrtf_sofa(np.stack(pres, axis=-1)[:, None, :], c.pts, params)
+    assert gc.rel_err(mem["Data_Real"] + 1j * mem["Data_Imag"], hrtf) < 1e-6
