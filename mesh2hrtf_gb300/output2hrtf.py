@@ -39,9 +39,11 @@ from __future__ import annotations
 import json
 import os
 import sys
+import warnings
 
 import numpy as np
 
+from . import output_report as _report
 from . import project as _project
 from . import sofa as _sofa
 
@@ -224,17 +226,23 @@ def write_hrtf_sofa(out_dir, grid, pressure, grid_xyz, params):
     return paths
 
 
-def output2hrtf(folder, full_precision=True):
-    """Process a project's NumCalc results (output2hrtf.py:15-128): per
-    evaluation grid the referenced HRTFs and, with computeHRIRs, the HRIRs,
-    written as SOFA files to <folder>/Output2HRTF.  Returns the paths
-    written."""
+def output2hrtf(folder, full_precision=True, report=True):
+    """Process a project's NumCalc results (output2hrtf.py:15-128): the
+    project report from the NC*.out files (a warning lists the issues; see
+    output_report), then per evaluation grid the referenced HRTFs and, with
+    computeHRIRs, the HRIRs, written as SOFA files to <folder>/Output2HRTF.
+    Returns the SOFA paths written."""
     params_path = os.path.join(folder, "parameters.json")
     if not os.path.isfile(params_path):
         raise ValueError("The folder %s is not a valid Mesh2HRTF project. It must contain the file "
                          "'parameters.json'" % folder)
-    params = json.load(open(params_path))
+    with open(params_path) as fh:
+        params = json.load(fh)
     out_dir = os.path.join(folder, "Output2HRTF")
+    if report:
+        found, text = _report.write_output_report(folder)
+        if found:
+            warnings.warn(text)
     ids, pressure = read_pressure(folder, params["numSources"], params["numFrequencies"], "pEvalGrid",
                                   full_precision)
     row_of = {int(i): r for r, i in enumerate(ids)}

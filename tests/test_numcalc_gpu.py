@@ -8,7 +8,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from mesh2hrtf_gb300 import build, capi, meshes, project, sofa
+from mesh2hrtf_gb300 import build, capi, meshes, output_report, project, sofa
 from tests import golden_cases as gc
 
 pytestmark = pytest.mark.gpu
@@ -129,8 +129,10 @@ def test_manage_numcalc_runs_every_step_on_the_gpu(numcalc, tmp_path):
 
 def test_full_precision_results_and_hrtfs(numcalc, tmp_path):
     """NUMCALC_GB300_NPY=1: every result file also as .npy (the printed
-    values at full precision); Output2HRTF's referencing reads them
-    (mesh2hrtf_gb300/output2hrtf.py)."""
+    values at full precision); the project report parses the run's NC.out;
+    Output2HRTF's referencing reads the results and equals the same HRTFs
+    made from the solver's in-memory results (mesh2hrtf_gb300/output2hrtf.py,
+    output_report.py)."""
     import json
 
     from mesh2hrtf_gb300 import output2hrtf as o2h
@@ -152,12 +154,22 @@ def test_full_precision_results_and_hrtfs(numcalc, tmp_path):
                "sourceCenter": [[0.5, 0.1, 0.0]], "sourceArea": [], "reference": True, "computeHRIRs": False,
                "numFrequencies": len(c.freqs), "frequencies": [float(v) for v in c.freqs]},
               open(os.path.join(root, "parameters.json"), "w"))
+    # the drop-in's NC.out through the project report: every step found,
+    # converged, with its iterations and timings (no -1 anywhere)
+    issues, text = output_report.write_output_report(root)
+    assert not issues, text
+    rows = open(os.path.join(root, "Output2HRTF", "report_source_1.csv")).read().splitlines()[1:]
+    assert len(rows) == len(c.freqs)
+    for r, f in zip(rows, c.freqs):
+        v = [x.strip() for x in r.split(",")]
+        assert v[2] == "NC.out" and float(v[1]) == float("%g" % f) and int(v[5]) > 0 and 0 <= float(v[6]) <= 1e-9
     h = sofa.read(o2h.output2hrtf(root)[0])
     hrtf = h["Data_Real"] + 1j * h["Data_Imag"]
     assert hrtf.shape == (len(c.pts), 1, len(c.freqs)) and np.all(np.isfinite(hrtf))
     assert h["GLOBAL_SOFAConventions"] == "GeneralTF"
     # the same HRTFs straight from the solver's results (no result file)
-    params = json.load(open(os.path.join(root, "parameters.json")))
+    with open(os.path.join(root, "parameters.json")) as fh:
+        params = json.load(fh)
     m = capi.Mesh(c.nodes, c.elems)
     sv = capi.Solver(m, precision=capi.PREC_FP64, tol=1e-9)   # the drop-in's tolerance
     pres = []

@@ -64,7 +64,7 @@ def _project(root, source_type, freqs, areas=(), npy=True, radius=1.0, reference
 def test_free_field_of_the_reference_source_gives_unit_hrtf(tmp_path, source_type, areas):
     freqs = [1000.0, 2000.0, 3000.0, 4000.0]
     _project(tmp_path, source_type, freqs, areas)
-    paths = o2h.output2hrtf(str(tmp_path))
+    paths = o2h.output2hrtf(str(tmp_path), report=False)
     assert [os.path.basename(p) for p in paths] == ["HRTF_G.sofa", "HRIR_G.sofa"]
     h = sofa.read(paths[0])
     hrtf = h["Data_Real"] + 1j * h["Data_Imag"]
@@ -88,8 +88,8 @@ def test_text_results_lose_digits_npy_results_do_not(tmp_path):
     (tmp_path / "b").mkdir()
     _project(tmp_path / "a", "Point source", freqs, npy=True, hrirs=False)
     _project(tmp_path / "b", "Point source", freqs, npy=False, hrirs=False)
-    ha = sofa.read(o2h.output2hrtf(str(tmp_path / "a"))[0])
-    hb = sofa.read(o2h.output2hrtf(str(tmp_path / "b"))[0])
+    ha = sofa.read(o2h.output2hrtf(str(tmp_path / "a"), report=False)[0])
+    hb = sofa.read(o2h.output2hrtf(str(tmp_path / "b"), report=False)[0])
     ea = np.abs(ha["Data_Real"] + 1j * ha["Data_Imag"] - 1).max()
     eb = np.abs(hb["Data_Real"] + 1j * hb["Data_Imag"] - 1).max()
     assert ea < 1e-13 and 1e-9 < eb < 1e-5   # % E prints 7 significant digits
@@ -151,7 +151,7 @@ def test_shtf_matches_the_reference_sofa_files(tmp_path, kind):
     version and the dates)."""
     g = np.load(GOLDEN)
     grid = _shtf_project(tmp_path, g, _as_run(g))
-    paths = o2h.output2hrtf(str(tmp_path))
+    paths = o2h.output2hrtf(str(tmp_path), report=False)
     ours = sofa.read(paths[0 if kind == "HRTF" else 1])
     ref = {k[len(kind) + 2:]: g[k] for k in g.files if k.startswith(kind + "__") and "___dim_" not in k}
     assert set(ours) == set(ref)
@@ -174,7 +174,7 @@ def test_shtf_with_the_committed_parameters_differs_by_the_area_rounding(tmp_pat
     g = np.load(GOLDEN)
     params = json.loads(str(g["params_json"]))
     _shtf_project(tmp_path, g, params)
-    h = sofa.read(o2h.output2hrtf(str(tmp_path))[0])
+    h = sofa.read(o2h.output2hrtf(str(tmp_path), report=False)[0])
     ratio = (h["Data_Real"] + 1j * h["Data_Imag"]) / (g["HRTF__Data_Real"] + 1j * g["HRTF__Data_Imag"])
     expect = np.array([float("%.6g" % a) / a for a in params["sourceArea"]])
     np.testing.assert_allclose(ratio, np.broadcast_to(expect[None, :, None], ratio.shape), rtol=1e-13)
@@ -187,7 +187,7 @@ def test_in_memory_pressure_equals_the_file_path(tmp_path):
     xyz = _project(tmp_path, "Both ears", freqs, (3.2e-5, 3.7e-5))
     params = json.loads((tmp_path / "parameters.json").read_text())
     ids, pressure = o2h.read_pressure(str(tmp_path), 2, len(freqs))
-    files = [sofa.read(p) for p in o2h.output2hrtf(str(tmp_path))]
+    files = [sofa.read(p) for p in o2h.output2hrtf(str(tmp_path), report=False)]
     mem = o2h.hrtf_sofa(pressure, xyz, params)
     for a, b in zip(mem, files):
         for k, v in a.items():
@@ -228,3 +228,30 @@ def test_sofa_round_trip_and_checks(tmp_path):
         sofa.write(str(tmp_path / "d.sofa"), dict(s, Bogus_Units="m"))
     with pytest.raises(ValueError):
         sofa.new("FreeFieldDirectivityTF")
+
+
+def test_shtf_output2hrtf_writes_the_reference_reports(tmp_path):
+    """The whole of Output2HRTF on the SHTF project with its NC*.out files:
+    the reports equal the reference's (no issues, so no warning) and the
+    SOFA files are written."""
+    import warnings
+
+    g = np.load(GOLDEN)
+    _shtf_project(tmp_path, g, _as_run(g))
+    rep = json.loads(str(np.load(os.path.join(os.path.dirname(__file__), "golden", "output_report.npz"))["doc"]))
+    for s, files in enumerate(rep["SHTF"]["files"]):
+        for name, text in files.items():
+            (tmp_path / "NumCalc" / ("source_%d" % (s + 1)) / name).write_text(text)
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        paths = o2h.output2hrtf(str(tmp_path))
+    assert len(paths) == 2
+    for s, ref in enumerate(rep["SHTF"]["csv"]):
+        assert (tmp_path / "Output2HRTF" / ("report_source_%d.csv" % (s + 1))).read_text() == ref
+    assert not (tmp_path / "Output2HRTF" / "report_issues.txt").exists()
+
+
+def test_missing_steps_warn(tmp_path):
+    _project(tmp_path, "Point source", [500.0, 1000.0], hrirs=False)
+    with pytest.warns(UserWarning, match="Frequency steps that were not calculated:\n1, 2"):
+        o2h.output2hrtf(str(tmp_path))
