@@ -3,7 +3,9 @@ SHTF test project (mesh2hrtf tests/resources/SHTF: 2 ear sources, 60
 frequencies, evaluation grid FourPointHorPlane_r100cm) and the HRTF / HRIR
 SOFA files the reference's output2hrtf wrote for it.
 
-    python tests/golden/make_output2hrtf_golden.py [reference root]
+    python tests/golden/make_output2hrtf_golden.py
+
+with MESH2HRTF_REFERENCE set to the root of a Mesh2HRTF checkout.
 
 Writes tests/golden/shtf_output2hrtf.npz: the project's parameters, the grid
 nodes, the pEvalGrid text lines of every source and step (as the reference
@@ -476,4 +478,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = os.environ.get("MESH2HRTF_REFERENCE", "")
+    if not os.path.isdir(root):
+        sys.exit("set MESH2HRTF_REFERENCE to the root of a Mesh2HRTF checkout")
+    main(root)

@@ -4,7 +4,9 @@ the SHTF project's NC1-20/21-40/41-60.out of both sources) and what the
 reference's own write_output_report makes of them (report_source_*.csv, the
 issue flag and report_issues.txt).
 
-    python tests/golden/make_output_report_golden.py [reference root]
+    python tests/golden/make_output_report_golden.py
+
+with MESH2HRTF_REFERENCE set to the root of a Mesh2HRTF checkout.
 
 The reference module is loaded from its file (it needs only numpy; the
 mesh2hrtf package itself imports sofar, which is not installed) and run on
@@ -74,4 +76,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = os.environ.get("MESH2HRTF_REFERENCE", "")
+    if not os.path.isdir(root):
+        sys.exit("set MESH2HRTF_REFERENCE to the root of a Mesh2HRTF checkout")
+    main(root)
