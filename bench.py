@@ -462,7 +462,8 @@ def main():
     iters = [i["iterations"] for step in infos for i in step]
     peaks = {}
     try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
     except OSError:
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)

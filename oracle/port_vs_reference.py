@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import argparse
 import os
+import pathlib
 import re
 import subprocess
 import sys
@@ -44,7 +45,7 @@ def reference_run(wd):
     wall = time.perf_counter() - t0
     if r.returncode != 0:
         raise RuntimeError(r.stdout[-2000:] + r.stderr)
-    out = open(os.path.join(wd, "NC.out")).read()
+    out = pathlib.Path(os.path.join(wd, "NC.out")).read_text()
     st = {}
     for key, name in (("Assembling the equation system", "assemble"), ("Solving the equation system", "solve"),
                       ("Post processing", "post")):

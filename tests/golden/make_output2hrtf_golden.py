@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import json
 import os
+import pathlib
 import struct
 import sys
 import zlib
@@ -36,7 +37,7 @@ UNDEF = 0xFFFFFFFFFFFFFFFF
 
 class H5:
     def __init__(self, path):
-        self.d = open(path, "rb").read()
+        self.d = pathlib.Path(path).read_bytes()
         d = self.d
         if d[:8] != b"\x89HDF\r\n\x1a\n":
             raise ValueError("not an HDF5 file")
@@ -450,14 +451,14 @@ def read_sofa(path):
 
 def main(ref_root):
     shtf = os.path.join(ref_root, "tests", "resources", "SHTF")
-    params = json.load(open(os.path.join(shtf, "parameters.json")))
+    params = json.loads(pathlib.Path(os.path.join(shtf, "parameters.json")).read_text())
     grid = params["evaluationGrids"][0]
     nodes = np.loadtxt(os.path.join(shtf, "EvaluationGrids", grid, "Nodes.txt"), skiprows=1, ndmin=2)
     lines = []
     for s in range(params["numSources"]):
         for k in range(params["numFrequencies"]):
             p = os.path.join(shtf, "NumCalc", "source_%d" % (s + 1), "be.out", "be.%d" % (k + 1), "pEvalGrid")
-            lines.append(open(p).read())
+            lines.append(pathlib.Path(p).read_text())
     keep = {"Mesh2HRTF_Version", "speedOfSound", "densityOfMedium", "evaluationGrids", "sourceType",
             "numSources", "sourceCenter", "sourceArea", "reference", "computeHRIRs", "numFrequencies",
             "frequencies"}

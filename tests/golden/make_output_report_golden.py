@@ -19,6 +19,7 @@ from __future__ import annotations
 import importlib.util
 import json
 import os
+import pathlib
 import shutil
 import sys
 import tempfile
@@ -59,15 +60,15 @@ def main(ref_root):
                 for f in sorted(os.listdir(src)):
                     if f.startswith("NC") and f.endswith(".out"):
                         shutil.copyfile(os.path.join(src, f), os.path.join(dst, f))
-                        texts[f] = open(os.path.join(src, f)).read()
+                        texts[f] = pathlib.Path(os.path.join(src, f)).read_text()
                 files.append(texts)
             issues, report = ref.write_output_report(tmp)
-            csv = [open(os.path.join(tmp, "Output2HRTF", "report_source_%d.csv" % (s + 1))).read()
+            csv = [pathlib.Path(os.path.join(tmp, "Output2HRTF", "report_source_%d.csv" % (s + 1))).read_text()
                    for s in range(len(srcs))]
             issues_txt = os.path.join(tmp, "Output2HRTF", "report_issues.txt")
-            out[name] = {"parameters": json.load(open(params)), "files": files, "issues": bool(issues),
+            out[name] = {"parameters": json.loads(pathlib.Path(params).read_text()), "files": files, "issues": bool(issues),
                          "report": report or "", "csv": csv,
-                         "issues_txt": open(issues_txt).read() if os.path.isfile(issues_txt) else None}
+                         "issues_txt": pathlib.Path(issues_txt).read_text() if os.path.isfile(issues_txt) else None}
         finally:
             shutil.rmtree(tmp)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "output_report.npz")

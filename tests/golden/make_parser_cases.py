@@ -15,6 +15,7 @@ from __future__ import annotations
 import hashlib
 import json
 import os
+import pathlib
 import shutil
 import subprocess
 import sys
@@ -87,7 +88,7 @@ def case_dialect():
 
     def mutate(root, wd):
         inp = os.path.join(wd, "NC.inp")
-        txt = open(inp).read().split("\n")
+        txt = pathlib.Path(inp).read_text().split("\n")
         out = []
         for ln in txt:
             if ln.startswith("BOUNDARY"):
@@ -96,11 +97,11 @@ def case_dialect():
                 out.append(ln.replace(" ", "   ") + "   ")
             else:
                 out.append(ln)
-        open(inp, "w").write("\n".join(out).rstrip("\n") + "\nEND\n")
+        pathlib.Path(inp).write_text("\n".join(out).rstrip("\n") + "\nEND\n")
         nodes = os.path.join(root, "ObjectMeshes", "Reference", "Nodes.txt")
-        lines = open(nodes).read().split("\n")
+        lines = pathlib.Path(nodes).read_text().split("\n")
         lines[3] = lines[3].replace(" ", "  ")
-        open(nodes, "w").write("\n".join(lines).rstrip("\n") + " ")   # no newline at the end
+        pathlib.Path(nodes).write_text("\n".join(lines).rstrip("\n") + " ")   # no newline at the end
     return _write(p, "dialect", mutate)
 
 
@@ -115,10 +116,10 @@ def case_dup_node():
 
     def mutate(root, wd):
         nodes = os.path.join(root, "ObjectMeshes", "Reference", "Nodes.txt")
-        lines = open(nodes).read().split("\n")
+        lines = pathlib.Path(nodes).read_text().split("\n")
         tok = lines[4].split(" ")
         lines[4] = " ".join(["1"] + tok[1:])       # node id 3 becomes a second id 1
-        open(nodes, "w").write("\n".join(lines))
+        pathlib.Path(nodes).write_text("\n".join(lines))
     return _write(p, "dup_node", mutate)
 
 
@@ -139,17 +140,17 @@ def case_quads_groups():
 
     def mutate(root, wd):
         el = os.path.join(root, "ObjectMeshes", "Reference", "Elements.txt")
-        lines = open(el).read().strip("\n").split("\n")
+        lines = pathlib.Path(el).read_text().strip("\n").split("\n")
         out = [lines[0]]
         for i, ln in enumerate(lines[1:]):
             tok = ln.split()
             ids = [t for t in tok[1:5] if int(t) >= 0]
             grp = str(i % 3)
             out.append(" ".join([tok[0]] + ids + ["0", "0", grp]))
-        open(el, "w").write("\n".join(out) + "\n")
+        pathlib.Path(el).write_text("\n".join(out) + "\n")
         inp = os.path.join(wd, "NC.inp")
-        s = open(inp).read().replace("2 %d" % (len(elems) + len(pts) * 2 - 4), "4 %d" % (len(elems) + len(pts) * 2 - 4), 1)
-        open(inp, "w").write(s)
+        s = pathlib.Path(inp).read_text().replace("2 %d" % (len(elems) + len(pts) * 2 - 4), "4 %d" % (len(elems) + len(pts) * 2 - 4), 1)
+        pathlib.Path(inp).write_text(s)
     return _write(p, "quads_groups", mutate)
 
 
@@ -163,8 +164,8 @@ def case_crlf():
 
     def mutate(root, wd):
         inp = os.path.join(wd, "NC.inp")
-        s = open(inp).read().replace("\n", "\r\n")
-        open(inp, "w", newline="").write(s)
+        s = pathlib.Path(inp).read_text().replace("\n", "\r\n")
+        pathlib.Path(inp).write_text(s, newline="")
     return _write(p, "crlf", mutate)
 
 
@@ -183,7 +184,7 @@ def reference_result(wd):
     shutil.rmtree(tmp)
     est = subprocess.run([refdump.REF_NUMCALC, "-estimate_ram"], cwd=wd, capture_output=True, text=True)
     if est.returncode == 0 and os.path.exists(os.path.join(wd, "Memory.txt")):
-        res["memory_txt"] = open(os.path.join(wd, "Memory.txt")).read()
+        res["memory_txt"] = pathlib.Path(os.path.join(wd, "Memory.txt")).read_text()
     for junk in ("NC.out", "Memory.txt", "NCuntil1.out"):
         if os.path.exists(os.path.join(wd, junk)):
             os.remove(os.path.join(wd, junk))
@@ -200,4 +201,5 @@ if __name__ == "__main__":
         wd = fn()
         allres[name] = reference_result(wd)
         print(name, allres[name].get("returncode"), allres[name].get("stdout_tail"))
-    json.dump(allres, open(os.path.join(OUT, "digests.json"), "w"), indent=1, sort_keys=True)
+    with open(os.path.join(OUT, "digests.json"), "w") as fh:
+        json.dump(allres, fh, indent=1, sort_keys=True)

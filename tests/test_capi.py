@@ -2,6 +2,7 @@
 include/bem_gb300.h declares (no GPU needed: no compute calls)."""
 import ctypes
 import os
+import pathlib
 import re
 
 from mesh2hrtf_gb300 import build, capi
@@ -10,7 +11,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _declared():
-    src = open(os.path.join(ROOT, "include", "bem_gb300.h")).read()
+    src = pathlib.Path(os.path.join(ROOT, "include", "bem_gb300.h")).read_text()
     return sorted(set(re.findall(r"\b(bem_[a-z_0-9]+)\s*\(", src)))
 
 

@@ -10,6 +10,7 @@ last line of stdout and of NC.out.  Where the reference build is present the
 test also runs it live and compares.
 """
 import os
+import pathlib
 import subprocess
 
 import pytest
@@ -49,7 +50,7 @@ def test_flipped_element_is_reported_as_the_reference_does(numcalc, tmp_path):
     wd = _project(tmp_path, flip=True)
     rc, last, err = _run(numcalc, wd)
     assert rc == 1 and last == MESSAGE and err == REF_STDERR
-    assert open(os.path.join(wd, "NC.out")).read().strip().split("\n")[-1] == MESSAGE
+    assert pathlib.Path(os.path.join(wd, "NC.out")).read_text().strip().split("\n")[-1] == MESSAGE
     if refdump.available():
         wd2 = _project(tmp_path / "ref", flip=True)
         assert _run(refdump.REF_NUMCALC, wd2) == (rc, last, err)

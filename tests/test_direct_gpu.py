@@ -9,6 +9,7 @@ mixed precision (complex64 factors, FP64 substitutions) within the metric's
 7-digit print bar (2e-6 FP64, 1e-5 mixed).
 """
 import os
+import pathlib
 import subprocess
 
 import numpy as np
@@ -79,7 +80,7 @@ def test_numcalc_isolver4(tmp_path, precision, tol):
     env = dict(os.environ, NUMCALC_GB300_PRECISION=precision)
     r = subprocess.run([numcalc], cwd=wd, env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:]
-    out = open(os.path.join(wd, "NC.out")).read()
+    out = pathlib.Path(os.path.join(wd, "NC.out")).read_text()
     assert "methodSolver_  = 4: Gaussean elimination (direct) solver" in out
     assert "CGS solver:" not in out and "End time:" in out
     for s in range(1, len(c.freqs) + 1):

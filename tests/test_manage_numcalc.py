@@ -69,7 +69,7 @@ def fake(tmp_path, monkeypatch):
 
 
 def _runs(log):
-    return [json.loads(line) for line in open(log)] if os.path.exists(log) else []
+    return [json.loads(line) for line in log.read_text().splitlines()] if os.path.exists(log) else []
 
 
 def _max_concurrent_gb(runs, dev):

@@ -3,6 +3,7 @@ reference NumCalc on the same project (reference results from
 tests/golden/sphere80.npz, printed there with 17 digits, here with NumCalc's
 7-digit format)."""
 import os
+import pathlib
 import subprocess
 
 import numpy as np
@@ -43,7 +44,7 @@ def test_be_out_matches_reference(numcalc, tmp_path, precision, tol, name):
     env = dict(os.environ, NUMCALC_GB300_PRECISION=precision)
     r = subprocess.run([numcalc], cwd=wd, env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:]
-    out = open(os.path.join(wd, "NC.out")).read()
+    out = pathlib.Path(os.path.join(wd, "NC.out")).read_text()
     assert out.count(">> S T E P   N U M B E R   A N D   F R E Q U E N C Y <<") == len(c.freqs)
     assert "CGS solver: number of iterations = " in out and "End time:" in out
     assert "Assembling the equation system         : " in out
@@ -65,7 +66,7 @@ def test_scaling_and_no_preconditioner(numcalc, tmp_path, precond):
     c, wd = _project(tmp_path, "sphere80", precond)
     r = subprocess.run([numcalc], cwd=wd, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:]
-    out = open(os.path.join(wd, "NC.out")).read()
+    out = pathlib.Path(os.path.join(wd, "NC.out")).read_text()
     assert ("with the scaling preconditioner above" if precond == 1 else "without a preconditioner") in out
     for s in range(1, len(c.freqs) + 1):
         for f in ("pBoundary", "pEvalGrid"):
@@ -80,7 +81,7 @@ def test_nitermax_reports_limit(numcalc, tmp_path, nitermax):
     c, wd = _project(tmp_path, "sphere320_adm_velo")
     r = subprocess.run([numcalc, "-nitermax", str(nitermax)], cwd=wd, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:]
-    out = open(os.path.join(wd, "NC.out")).read()
+    out = pathlib.Path(os.path.join(wd, "NC.out")).read_text()
     assert "CGS solver: number of iterations = %d" % nitermax in out
     assert "Warning: Maximum number of iterations is reached!" in out
     # then, as NumCalc (NC_CommonFunctions.cpp:1181-1191), the direct solver
@@ -98,7 +99,7 @@ def test_istart_iend_keeps_other_steps(numcalc, tmp_path):
     assert not os.path.exists(os.path.join(wd, "be.out", "be.1"))
     assert subprocess.run([numcalc, "-istart", "1", "-iend", "1"], cwd=wd, capture_output=True).returncode == 0
     assert os.path.exists(os.path.join(wd, "be.out", "be.2", "pEvalGrid"))
-    out = open(os.path.join(wd, "NC1-1.out")).read()
+    out = pathlib.Path(os.path.join(wd, "NC1-1.out")).read_text()
     assert "Step 1," in out and "Step 2," not in out
 
 
@@ -116,11 +117,11 @@ def test_manage_numcalc_runs_every_step_on_the_gpu(numcalc, tmp_path):
     project.write_project(p, "source_1")
     p.point_sources = [(-0.4, 0.2, 0.1, 1.0, 0.0)]
     wd2 = project.write_project(p, "source_2")
-    open(os.path.join(str(tmp_path / "p"), "parameters.json"), "w").write("{}")
+    pathlib.Path(os.path.join(str(tmp_path / "p"), "parameters.json")).write_text("{}")
     mn.manage_numcalc(str(tmp_path / "p"), numcalc, max_hbm_load=20.0, steps_per_instance=1, wait_time=0.05)
     wd1 = os.path.join(str(tmp_path / "p"), "NumCalc", "source_1")
     for s in range(1, len(c.freqs) + 1):
-        assert "End time:" in open(os.path.join(wd1, "NC%d-%d.out" % (s, s))).read()
+        assert "End time:" in pathlib.Path(os.path.join(wd1, "NC%d-%d.out" % (s, s))).read_text()
         ids, vals = project.read_result(os.path.join(wd1, "be.out", "be.%d" % s, "pEvalGrid"))
         assert gc.rel_err(vals, c["s%d_pEvalGrid" % s]) < 1e-5
         assert os.path.isfile(os.path.join(wd2, "be.out", "be.%d" % s, "pEvalGrid"))
@@ -149,16 +150,16 @@ def test_full_precision_results_and_hrtfs(numcalc, tmp_path):
             assert gc.rel_err(full, txt) < 1e-6                     # 7 printed digits
             assert gc.rel_err(full, c["s%d_%s" % (s, f)]) < 2e-6     # the reference, 17 digits
     root = str(tmp_path / "p")
-    json.dump({"Mesh2HRTF_Version": "1.0.0", "speedOfSound": 343.0, "densityOfMedium": 1.21,
-               "evaluationGrids": ["Grid"], "sourceType": "Point source", "numSources": 1,
-               "sourceCenter": [[0.5, 0.1, 0.0]], "sourceArea": [], "reference": True, "computeHRIRs": False,
-               "numFrequencies": len(c.freqs), "frequencies": [float(v) for v in c.freqs]},
-              open(os.path.join(root, "parameters.json"), "w"))
+    pathlib.Path(os.path.join(root, "parameters.json")).write_text(json.dumps({
+        "Mesh2HRTF_Version": "1.0.0", "speedOfSound": 343.0, "densityOfMedium": 1.21,
+        "evaluationGrids": ["Grid"], "sourceType": "Point source", "numSources": 1,
+        "sourceCenter": [[0.5, 0.1, 0.0]], "sourceArea": [], "reference": True, "computeHRIRs": False,
+        "numFrequencies": len(c.freqs), "frequencies": [float(v) for v in c.freqs]}))
     # the drop-in's NC.out through the project report: every step found,
     # converged, with its iterations and timings (no -1 anywhere)
     issues, text = output_report.write_output_report(root)
     assert not issues, text
-    rows = open(os.path.join(root, "Output2HRTF", "report_source_1.csv")).read().splitlines()[1:]
+    rows = pathlib.Path(os.path.join(root, "Output2HRTF", "report_source_1.csv")).read_text().splitlines()[1:]
     assert len(rows) == len(c.freqs)
     for r, f in zip(rows, c.freqs):
         v = [x.strip() for x in r.split(",")]

@@ -3,6 +3,7 @@ reference (table digests from tests/golden/parser/digests.json), error exits,
 command line, output naming and -estimate_ram for traditional-BEM projects."""
 import json
 import os
+import pathlib
 import shutil
 import subprocess
 import sys
@@ -18,7 +19,7 @@ PARSER = os.path.join(HERE, "golden", "parser")
 sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_parser_cases as mpc  # noqa: E402
 
-REF = json.load(open(os.path.join(PARSER, "digests.json")))
+REF = json.loads(pathlib.Path(os.path.join(PARSER, "digests.json")).read_text())
 
 
 @pytest.fixture(scope="module")
@@ -52,7 +53,7 @@ def test_estimate_ram_matches_reference(case, numcalc, tmp_path):
     wd = _copy(case, tmp_path)
     r = subprocess.run([numcalc, "-estimate_ram"], cwd=wd, capture_output=True, text=True)
     assert r.returncode == 0, r.stdout[-500:]
-    assert open(os.path.join(wd, "Memory.txt")).read() == REF[case]["memory_txt"]
+    assert pathlib.Path(os.path.join(wd, "Memory.txt")).read_text() == REF[case]["memory_txt"]
     assert not os.path.exists(os.path.join(wd, "be.out", "be.1"))
 
 
@@ -80,7 +81,7 @@ def test_output_naming_estimate_mode(args, name, numcalc, tmp_path):
     r = subprocess.run([numcalc, "-estimate_ram", *args], cwd=wd, capture_output=True, text=True)
     assert r.returncode == 0
     assert os.path.exists(os.path.join(wd, name))
-    mem = open(os.path.join(wd, "Memory.txt")).read().strip().split("\n")
+    mem = pathlib.Path(os.path.join(wd, "Memory.txt")).read_text().strip().split("\n")
     first = int(args[args.index("-istart") + 1]) if "-istart" in args else 1
     last = int(args[args.index("-iend") + 1]) if "-iend" in args else 3
     assert [int(l.split()[0]) for l in mem] == list(range(first, last + 1))

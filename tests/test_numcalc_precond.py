@@ -9,6 +9,7 @@ option itself (bem_solver_params.no_precond) is covered on the GPU by
 tests/test_precond_gpu.py.
 """
 import os
+import pathlib
 import subprocess
 
 import pytest
@@ -33,7 +34,7 @@ def _nc_out(exe, tmp_path, precond):
     env = dict(os.environ, NUMCALC_GB300_DUMP_TABLES=str(tmp_path / ("tables%d.bin" % precond)))
     r = subprocess.run([exe], cwd=wd, capture_output=True, text=True, env=env, timeout=120)
     assert r.returncode == 0, r.stderr[-2000:]
-    return open(os.path.join(wd, "NC.out")).read()
+    return pathlib.Path(os.path.join(wd, "NC.out")).read_text()
 
 
 @pytest.mark.parametrize("precond,echo,gpu", [

@@ -7,6 +7,7 @@ SHTF test project against the SOFA files the reference wrote for it
 (tests/golden/shtf_output2hrtf.npz, made by make_output2hrtf_golden.py)."""
 import json
 import os
+import pathlib
 
 import numpy as np
 import pytest
@@ -210,7 +211,7 @@ def test_sofa_round_trip_and_checks(tmp_path):
              SourcePosition_Type="spherical", GLOBAL_Comment="x")
     path = str(tmp_path / "a.sofa")
     sofa.write(path, s)
-    assert open(path, "rb").read(4) == b"CDF\x02"          # netCDF classic, 64-bit offsets
+    assert pathlib.Path(path).read_bytes()[:4] == b"CDF\x02"          # netCDF classic, 64-bit offsets
     r = sofa.read(path)
     assert set(r) == set(s)
     for k, v in s.items():
