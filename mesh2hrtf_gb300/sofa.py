@@ -160,10 +160,10 @@ def write(path, sofa):
     with netcdf_file(path, "w", version=2) as f:
         for k in _GLOBAL_ORDER:
             if "GLOBAL_" + k in sofa:
-                setattr(f, k, str(sofa["GLOBAL_" + k]))
+                setattr(f, k, _chars(sofa["GLOBAL_" + k]))
         for k, v in sofa.items():
             if k.startswith("GLOBAL_") and k[7:] not in _GLOBAL_ORDER:
-                setattr(f, k[7:], str(v))
+                setattr(f, k[7:], _chars(v))
         for d in ("M", "R", "E", "N", "I", "C"):
             if d in dims:
                 f.createDimension(d, dims[d])
@@ -175,7 +175,13 @@ def write(path, sofa):
             if k.startswith("GLOBAL_") or k in _DIMS:
                 continue
             var, attr = _owner(k, variables)
-            setattr(ncv[var], attr, str(v))
+            setattr(ncv[var], attr, _chars(v))
+
+
+def _chars(v):
+    """A text attribute as netCDF characters: UTF-8 bytes, which the netCDF
+    library reads back as the same string."""
+    return str(v).encode("utf-8")
 
 
 def _text(v):

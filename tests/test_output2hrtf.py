@@ -208,7 +208,7 @@ def test_sofa_round_trip_and_checks(tmp_path):
     rng = np.random.default_rng(1)
     s.update(Data_Real=rng.normal(size=(5, 1, 3)), Data_Imag=rng.normal(size=(5, 1, 3)), N=[1.0, 2.0, 3.0],
              SourcePosition=rng.normal(size=(5, 3)), ReceiverPosition=np.zeros((1, 3, 1)),
-             SourcePosition_Type="spherical", GLOBAL_Comment="x")
+             SourcePosition_Type="spherical", GLOBAL_Comment="x", GLOBAL_AuthorContact="Jörg Müller")
     path = str(tmp_path / "a.sofa")
     sofa.write(path, s)
     assert pathlib.Path(path).read_bytes()[:4] == b"CDF\x02"          # netCDF classic, 64-bit offsets
