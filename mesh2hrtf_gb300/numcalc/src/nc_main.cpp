@@ -28,11 +28,13 @@
 #include <ctime>
 #include <iomanip>
 #include <iostream>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
 
 #include "bem_gb300.h"
+#include "nc_fmm_plan.h"
 #include "nc_project.h"
 
 using nc::cd;
@@ -272,13 +274,17 @@ int run(int istart, int iend, bool estimate_ram, bool check_normals, int niterma
     if (iend == 0) iend = p.n_freq;
     if (istart > 0) istart--;
     std::vector<cd> x(N), pot(ev_nodes.size()), grad(3 * ev_nodes.size());
+    // -estimate_ram of an SL-/ML-FMM project reports the reference's FMM
+    // estimate; projects with symmetry planes keep the dense one
+    std::unique_ptr<nc::FmmPlan> fmm;
+    if (estimate_ram && p.method_bem != 0 && p.n_reflections == 1) fmm.reset(new nc::FmmPlan(p));
     for (int step = istart; step < iend; ++step) {
         time(&ltim[3]);
         const double f = p.freqs[step];
         std::cout << "\nStep " << step + 1 << ", Frequency = " << f << " Hz" << std::endl;
         out << "\n\n\n>> S T E P   N U M B E R   A N D   F R E Q U E N C Y <<\n" << std::endl;
         out << "Step " << step + 1 << ", Frequency = " << f << " Hz" << std::endl;
-        if (step == istart) {
+        if (step == istart && !fmm) {
             // NC_DeclareArrays / NC_FrequencyInformations for a TBEM step
             const int ncomp = (int)((unsigned)N * (unsigned)N);
             for (std::ostream *o : {(std::ostream *)&std::cout, (std::ostream *)&out}) {
@@ -288,16 +294,39 @@ int run(int istart, int iend, bool estimate_ram, bool check_normals, int niterma
             }
         }
         if (estimate_ram) {
-            // NC_Main.cpp:524-541,717-733: TBEM count, unsigned 32-bit like the reference
-            unsigned nint = 0, ncmplx = (unsigned)N;
-            std::cout << "TBEM: \n";
-            std::cout << "Number of entries right hand side: " << ncmplx << "\n";
-            std::cout << "Number of Matrix entries: " << ncmplx * ncmplx << "\n";
-            ncmplx += (unsigned)N * (unsigned)N;
-            std::cout << "Total Nr. of Integers: " << nint << "\n";
-            std::cout << "Total Nr. of Cmplxdble: " << ncmplx << "\n";
-            const double gb = (double)(nint * sizeof(int) + ncmplx * 16) / 1000.0 / 1000.0 / 1000.0;
-            std::cout << "RAM Estimation: " << gb << " GByte\n";
+            double gb;
+            if (fmm) {
+                // an SL-/ML-FMM project: the reference's cluster set-up and
+                // FMM matrix counts for this step (nc_fmm_plan.cpp)
+                if (fmm->declare(step, istart, f)) {
+                    // the method lines of NC_FrequencyInformations (NC_Main.cpp:1051-1080)
+                    const char *name = fmm->method() == 0   ? "Traditional BEM"
+                                       : fmm->method() == 1 ? "Single level fast multipole BEM"
+                                                            : "Direct multilevel fast multipole BEM";
+                    for (std::ostream *o : {(std::ostream *)&std::cout, (std::ostream *)&out}) {
+                        *o << "\n" << name << std::endl;
+                        if (step == istart) {
+                            *o << "\nNumber of equations = " << N << std::endl;
+                            if (fmm->method() == 0)
+                                *o << "Number of entries of the coefficient matrix = " << (int)((unsigned)N * (unsigned)N)
+                                   << std::endl;
+                        }
+                    }
+                }
+                fmm->expansion(2.0 * nc::kPI * f / p.c);
+                gb = fmm->ram_estimate_gb(std::cout);
+            } else {
+                // NC_Main.cpp:524-541,717-733: TBEM count, unsigned 32-bit like the reference
+                unsigned nint = 0, ncmplx = (unsigned)N;
+                std::cout << "TBEM: \n";
+                std::cout << "Number of entries right hand side: " << ncmplx << "\n";
+                std::cout << "Number of Matrix entries: " << ncmplx * ncmplx << "\n";
+                ncmplx += (unsigned)N * (unsigned)N;
+                std::cout << "Total Nr. of Integers: " << nint << "\n";
+                std::cout << "Total Nr. of Cmplxdble: " << ncmplx << "\n";
+                gb = (double)(nint * sizeof(int) + ncmplx * 16) / 1000.0 / 1000.0 / 1000.0;
+                std::cout << "RAM Estimation: " << gb << " GByte\n";
+            }
             est << step + 1 << " " << f << " " << gb << "\n";
             // device: solver + mesh + evaluation points + a CUDA context
             const double dev = bem_footprint_bytes(N, prec, 0) + bem_mesh_footprint_bytes(N, p.n_sym) +
