@@ -6,6 +6,7 @@
 // drop-in's host code).
 #include "nc_fmm_plan.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <iostream>
@@ -208,7 +209,51 @@ void FmmPlan::clusters_of(int lev, const std::vector<std::vector<int>> &groups, 
             out.cl.push_back(std::move(c));
         }
     }
-    for (FmmCluster &c : out.cl) cluster_geometry(c);
+    out.n_orig = (int)out.cl.size();
+    for (int i = 0; i < out.n_orig; ++i) {
+        out.cl[i].orig = i;
+        cluster_geometry(out.cl[i]);
+    }
+}
+
+// Images of the level's clusters in the symmetry planes: the same radius,
+// the centre mirrored in every plane an odd number of the reflection steps
+// cross; an image's father is the same reflection of its original's father
+// (NC_ClusterReflectionsSLFMM :508-626, NC_ClusterReflectionsAtLevelMLFMM
+// :1317-1475).
+void FmmPlan::reflect(FmmLevel &L, const FmmLevel *father) const {
+    const int nref = p_.n_reflections;
+    if (nref <= 1) return;
+    // axis of each reflection step (the order NC_ReflectPointVector uses)
+    static const int kStepAxis[8] = {0, 0, 1, 0, 2, 0, 1, 0};
+    int first_free = 0, first_plane = 0;
+    for (int k = 0; k < 3; ++k)
+        if (p_.sym_planes[k] == 0) { first_free = k + 1; break; }
+    for (int k = 0; k < 3; ++k)
+        if (p_.sym_planes[k] != 0) { first_plane = k; break; }
+    const int n = L.n_orig;
+    L.cl.reserve((size_t)n * nref);
+    for (int icl = 0; icl < n; ++icl) {
+        int crossings[3] = {0, 0, 0};
+        for (int kref = 1; kref < nref; ++kref) {
+            int dir;
+            if (nref == 8) dir = kStepAxis[kref];
+            else if (nref == 4) {
+                dir = first_free + kStepAxis[kref];
+                if (dir >= 3) dir -= 3;
+            } else dir = first_plane;
+            ++crossings[dir];
+            const FmmCluster &o = L.cl[icl];
+            FmmCluster c;
+            c.elems = o.elems;
+            c.radius = o.radius;
+            c.orig = icl;
+            for (int k = 0; k < 3; ++k)
+                c.center[k] = crossings[k] % 2 ? 2.0 * p_.sym_coords[k] - o.center[k] : o.center[k];
+            if (father) c.father = father->n_orig + (nref - 1) * o.father + (kref - 1);
+            L.cl.push_back(std::move(c));
+        }
+    }
 }
 
 // radii statistics and the near/far split of one level
@@ -218,12 +263,13 @@ void FmmPlan::near_far(FmmLevel &L, int) {
     const int n = (int)L.cl.size();
     L.r_max = L.r_avg = 0.0;
     L.r_min = 1.0e40;
-    for (const FmmCluster &c : L.cl) {
-        if (c.radius > L.r_max) L.r_max = c.radius;
-        if (c.radius < L.r_min) L.r_min = c.radius;
-        L.r_avg += c.radius;
+    for (int i = 0; i < L.n_orig; ++i) {
+        const double r = L.cl[i].radius;
+        if (r > L.r_max) L.r_max = r;
+        if (r < L.r_min) L.r_min = r;
+        L.r_avg += r;
     }
-    L.r_avg /= (double)n;
+    L.r_avg /= (double)L.n_orig;
     L.pairs_canceled = L.pairs_far = 0;
     std::vector<char> far((size_t)n * n, 0);
     for (int i = 0; i < n; ++i)
@@ -282,6 +328,7 @@ void FmmPlan::build_single() {
     }
     lv_.assign(1, FmmLevel());
     clusters_of(0, be_groups(), lv_[0]);
+    reflect(lv_[0], nullptr);
     near_far(lv_[0], 0);
 }
 
@@ -291,8 +338,9 @@ void FmmPlan::build_tree() {
         std::vector<std::vector<int>> groups;
         if (l == 0) groups = be_groups();
         else
-            for (const FmmCluster &c : lv_[l - 1].cl) groups.push_back(c.elems);
+            for (int i = 0; i < lv_[l - 1].n_orig; ++i) groups.push_back(lv_[l - 1].cl[i].elems);
         clusters_of(l, groups, lv_[l]);
+        reflect(lv_[l], l > 0 ? &lv_[l - 1] : nullptr);
         near_far(lv_[l], l);
     }
 }
@@ -383,14 +431,25 @@ double FmmPlan::ram_estimate_gb(std::ostream &log) const {
     using u32 = uint32_t;
     const u32 N = (u32)n_rows_;
     u32 nint = 0, ncmplx = N;   // the right-hand side
+    // near-field entries: each original cluster's elements times the
+    // elements of the original clusters whose images or selves are near it
     auto nearfield = [&](const FmmLevel &L) {
         u32 nnz = 0;
-        for (const FmmCluster &c : L.cl) {
+        std::vector<char> seen(L.n_orig);
+        for (int i = 0; i < L.n_orig; ++i) {
+            std::fill(seen.begin(), seen.end(), 0);
+            for (int j : L.cl[i].near) seen[L.cl[j].orig] = 1;
             u32 nij = 0;
-            for (int j : c.near) nij += (u32)L.cl[j].elems.size();
-            nnz += (u32)c.elems.size() * nij;
+            for (int j = 0; j < L.n_orig; ++j)
+                if (seen[j]) nij += (u32)L.cl[j].elems.size();
+            nnz += (u32)L.cl[i].elems.size() * nij;
         }
         return nnz;
+    };
+    auto all_elems = [](const FmmLevel &L) {
+        u32 n = 0;
+        for (const FmmCluster &c : L.cl) n += (u32)c.elems.size();
+        return n;
     };
     if (method_ == 0) {
         log << "TBEM: \n";
@@ -399,23 +458,21 @@ double FmmPlan::ram_estimate_gb(std::ostream &log) const {
         ncmplx += N * N;
     } else if (method_ == 1) {
         const FmmLevel &L = lv_[0];
-        const u32 ns = (u32)L.n_sphere, ncl = (u32)L.cl.size();
+        const u32 ns = (u32)L.n_sphere, nall = (u32)L.cl.size(), norig = (u32)L.n_orig;
         ncmplx += ns * 2u;
         u32 nnz = nearfield(L);
         log << "SLFMM:\n";
         log << "Nearfield: " << (int)nnz << "\n";
         nint += nnz + N + 1u;
         ncmplx += nnz;
-        nnz = 0;
-        for (const FmmCluster &c : L.cl) nnz += (u32)c.elems.size();
-        nnz *= ns;
+        nnz = all_elems(L) * ns;
         ncmplx += nnz;
-        nint += nnz + ns * ncl + 1u;
+        nint += nnz + ns * nall + 1u;
         log << "T Matrix: " << (int)nnz << "\n";
         nnz = 0;
-        for (const FmmCluster &c : L.cl) nnz += (u32)c.n_far;
+        for (int i = 0; i < L.n_orig; ++i) nnz += (u32)L.cl[i].n_far;
         nnz *= ns;
-        nint += nnz + ncl * ns;
+        nint += nnz + norig * ns;
         ncmplx += nnz;
         log << "D Matrix: " << (int)nnz << "\n";
         nnz = N * ns;
@@ -432,9 +489,7 @@ double FmmPlan::ram_estimate_gb(std::ostream &log) const {
         log << "Nearfield " << (int)nnz << "\n";
         for (size_t l = 0; l < lv_.size(); ++l) {
             const FmmLevel &L = lv_[l];
-            nnz = 0;
-            for (const FmmCluster &c : L.cl) nnz += (u32)c.elems.size();
-            nnz *= (u32)L.n_sphere;
+            nnz = all_elems(L) * (u32)L.n_sphere;
             log << "Tmatrix level " << l << ": " << (int)nnz << "\n";
             nint += nnz + (u32)L.cl.size() * (u32)L.n_sphere + 1u;
             ncmplx += nnz;
@@ -443,16 +498,17 @@ double FmmPlan::ram_estimate_gb(std::ostream &log) const {
             const FmmLevel &L = lv_[l];
             nnz = 0;
             if (l == 0) {
-                for (const FmmCluster &c : L.cl) nnz += (u32)c.n_far * (u32)L.n_sphere;
+                for (int i = 0; i < L.n_orig; ++i) nnz += (u32)L.cl[i].n_far * (u32)L.n_sphere;
             } else {
                 // far clusters whose father is in the near field of the
                 // cluster's own father (the interactions this level adds)
                 const FmmLevel &F = lv_[l - 1];
                 const size_t nf = F.cl.size();
-                std::vector<char> near(nf * nf, 0);
-                for (size_t i = 0; i < nf; ++i)
-                    for (int j : F.cl[i].near) near[i * nf + j] = 1;
-                for (const FmmCluster &c : L.cl) {
+                std::vector<char> near((size_t)F.n_orig * nf, 0);
+                for (int i = 0; i < F.n_orig; ++i)
+                    for (int j : F.cl[i].near) near[(size_t)i * nf + j] = 1;
+                for (int i = 0; i < L.n_orig; ++i) {
+                    const FmmCluster &c = L.cl[i];
                     u32 m = 0;
                     for (int j : c.far)
                         if (near[(size_t)c.father * nf + L.cl[j].father]) ++m;
@@ -460,7 +516,7 @@ double FmmPlan::ram_estimate_gb(std::ostream &log) const {
                 }
             }
             log << "D Matrix level " << l << ": " << (int)nnz << "\n";
-            nint += nnz + (u32)L.cl.size() * (u32)L.n_sphere + 1u;
+            nint += nnz + (u32)L.n_orig * (u32)L.n_sphere + 1u;
             ncmplx += nnz;
         }
         for (size_t l = 0; l < lv_.size(); ++l) {

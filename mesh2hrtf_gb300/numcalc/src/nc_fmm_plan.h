@@ -19,6 +19,7 @@ struct FmmCluster {
     std::vector<int> elems;   // internal element numbers, in the order the clustering found them
     double center[3] = {0.0, 0.0, 0.0};
     double radius = 0.0;
+    int orig = 0;             // the original cluster (itself, or the one this image mirrors)
     int father = -1;          // cluster on the level above (multilevel)
     std::vector<int> near;    // same-level clusters in the near field (itself included)
     int n_far = 0;            // same-level clusters in the far field
@@ -26,7 +27,10 @@ struct FmmCluster {
 };
 
 struct FmmLevel {
+    // the original clusters, then with symmetry planes their images: for
+    // each original in turn its reflections 1 .. n_reflections - 1
     std::vector<FmmCluster> cl;
+    int n_orig = 0;
     double r_max = 0.0, r_avg = 0.0, r_min = 0.0;
     int pairs_canceled = 0;   // geometric far pairs closer than the Hankel-argument limit
     int pairs_far = 0;        // geometric far pairs
@@ -59,6 +63,7 @@ private:
     void merge_small(std::vector<std::vector<int>> &cells) const;
     void cluster_geometry(FmmCluster &c) const;
     void near_far(FmmLevel &L, int lev);
+    void reflect(FmmLevel &L, const FmmLevel *father) const;
     int estimate_levels();
     void build_single();
     void build_tree();

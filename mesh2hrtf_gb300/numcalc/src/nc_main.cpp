@@ -275,9 +275,9 @@ int run(int istart, int iend, bool estimate_ram, bool check_normals, int niterma
     if (istart > 0) istart--;
     std::vector<cd> x(N), pot(ev_nodes.size()), grad(3 * ev_nodes.size());
     // -estimate_ram of an SL-/ML-FMM project reports the reference's FMM
-    // estimate; projects with symmetry planes keep the dense one
+    // estimate
     std::unique_ptr<nc::FmmPlan> fmm;
-    if (estimate_ram && p.method_bem != 0 && p.n_reflections == 1) fmm.reset(new nc::FmmPlan(p));
+    if (estimate_ram && p.method_bem != 0) fmm.reset(new nc::FmmPlan(p));
     for (int step = istart; step < iend; ++step) {
         time(&ltim[3]);
         const double f = p.freqs[step];

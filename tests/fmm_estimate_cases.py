@@ -13,12 +13,12 @@ import numpy as np
 from mesh2hrtf_gb300 import meshes, project
 
 
-def _project(root, v, f, freqs, method, n_pts=40):
-    pts = meshes.random_sphere_points(n_pts, 1.0, 7)
+def _project(root, v, f, freqs, method, n_pts=40, **sym):
+    pts = meshes.random_sphere_points(n_pts, 1.0, 7) + np.asarray(sym.get("sym_coords", (0.0, 0.0, 0.0)))
     return project.Project(root=str(root), nodes=v, elems=f, eval_points=pts,
                            eval_elems=meshes.grid_triangles(pts), freqs=list(freqs),
-                           point_sources=[(0.0, 0.3, 0.0, 0.1, 0.0)],
-                           boundary=["ELEM 0 TO %d VELO 0.0 -1 0.0 -1" % (len(f) - 1)], method=method)
+                           point_sources=[(0.31, 0.27, 0.22, 0.1, 0.0)],
+                           boundary=["ELEM 0 TO %d VELO 0.0 -1 0.0 -1" % (len(f) - 1)], method=method, **sym)
 
 
 def _main1(wd, token, value):
@@ -96,11 +96,24 @@ def write(name, root):
         wd = project.write_project(_project(root, v, f, [2000.0, 9000.0, 18000.0], 4))
         _main2(wd, 3, 0.04)
         return wd
+    if name == "half3456_sl":       # one symmetric plane x = 0
+        v, f = meshes.sphere_sector(24, 0.1, (0,), triangles=True)
+        return project.write_project(_project(root, v, f, [500.0, 2000.0, 8000.0, 16000.0], 1,
+                                              nsym=1, sym_planes=(1, 0, 0)))
+    if name == "quarter2400_ml":    # antisymmetric y = 0, symmetric z = 0
+        v, q = meshes.sphere_sector(40, 0.1, (1, 2))
+        return project.write_project(_project(root, v, q, [1000.0, 6000.0, 12000.0, 20000.0], 4,
+                                              nsym=2, sym_planes=(0, 2, 1)))
+    if name == "octant2400_ml":     # three planes through an off-origin point
+        c = (0.01, -0.02, 0.03)
+        v, f = meshes.sphere_sector(40, 0.1, (0, 1, 2), center=c, triangles=True)
+        return project.write_project(_project(root, v, f, [3000.0, 9000.0, 20000.0], 4,
+                                              nsym=3, sym_planes=(1, 2, 3), sym_coords=c))
     raise KeyError(name)
 
 
 CASES = ("sphere1280_ml", "head5120_ml", "head5120_sl", "head5120_descending", "quads2400_ml", "groups3_ml",
-         "min_terms5_ml", "min_terms10_sl", "cluster_edge_ml")
+         "min_terms5_ml", "min_terms10_sl", "cluster_edge_ml", "half3456_sl", "quarter2400_ml", "octant2400_ml")
 
 COUNT_PREFIXES = ("TBEM:", "SLFMM:", "MLFMM:", "Nearfield", "T Matrix", "D Matrix", "S Matrix", "Tmatrix",
                   "Total Nr", "RAM Est", "Number of entries right hand side", "Number of Matrix entries")

@@ -4,8 +4,9 @@ for byte, and prints the same matrix counts, on the reference's SHTF test
 project (the file its test_numcalc_commandline_estimate_ram compares) and
 on projects that exercise traditional-BEM steps, single- and multilevel
 FMM, the fall-back between them, frequencies in falling order,
-quadrilaterals, several element groups, the minimum expansion order and a
-prescribed cluster edge length (tests/fmm_estimate_cases.py; golden files
+quadrilaterals, several element groups, the minimum expansion order, a
+prescribed cluster edge length and one to three symmetry planes (the
+clusters' images) (tests/fmm_estimate_cases.py; golden files
 from the reference built here, tests/golden/make_fmm_estimate_golden.py).
 No GPU: -estimate_ram makes no device call."""
 import json
